@@ -1,0 +1,332 @@
+"""Benchmark: batched lnL + gradient of 1024 MBHB samples on one GB300.
+
+Workload (the adjoint configuration): one LISA-like heliocentric detector
+(L = 2.5e9 m, trailing 20 deg), first-generation ("1.5") TDI A/E/T,
+T = 2^22 s, dt = 8 s, dense grid 1e-4..0.03 Hz (125 410 bins x 3 channels),
+data = IMRPhenomD injection (m1 = 1e6, m2 = 5e5 Msun, chi = 0.5/-0.3,
+10 Gpc, ...) + seeded noise; 1024 prior samples (seed 2026 + rank) with the
+per-sample cutoff 1.2 f_RD; lnL and its gradient w.r.t. the 11 parameters
+(ln Mc, q, chi1, chi2, ln D_L, cos i, lambda, sin beta, psi, phi_c, t_c).
+
+One step = one call of the batched lnL+gradient over the 1024 samples.
+`value` times steps with inputs resident in HBM (CUDA events around each
+step; the L2 is flushed between steps by writing a 512 MB buffer outside the
+timed events); `e2e` times the same call through the public API with the
+parameters copied from pinned host memory and lnL/gradient copied back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+    python bench.py --impl reference   # the reference's CPU path (oracle port)
+
+Multi-GPU (torchrun): replicas; every rank evaluates its own 1024 samples
+(weak scaling); rank 0 prints the line with the max-over-ranks step time.
+"""
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DUR, DT, FMIN, FMAX = 2.0 ** 22, 8.0, 1e-4, 0.03
+BATCH = 1024
+METRIC = "lnL+grad evals/s, 1024 MBHB samples, 1 GB300: mixed vs FP64, |dlnL|<=1e-2"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--precision", default=os.environ.get("PES_BENCH_PRECISION", "mixed"),
+                    choices=["mixed", "fp64"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def fp64_peak_tflops(torch):
+    """FP64 throughput denominator: cuBLAS DGEMM 8192^3 (best of 5)."""
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = math.inf
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b
+    return 2 * 8192 ** 3 / best / 1e12
+
+
+def cpu_baseline_run(n_samples, threads, precision_note):
+    """The reference's CPU path (oracle port, FP64 dense, OpenMP over samples)."""
+    from oracle import fdpath as oracle
+    from pespace_gb300.workloads import config0_theta, prior_samples
+
+    oracle.build()
+    g = oracle.grid(DUR, DT, FMIN, FMAX)
+    th0 = config0_theta(DUR - 86400.0)
+    orb = oracle.heliocentric(2.5e9, 0.0, -math.pi / 9)
+    psd = oracle.psd(g["freqs"], "AET", False, "1.5", **oracle.PSD_PRESETS["LISA_SciRDv1"])
+    noise = oracle.noise_realization(g, psd, "AET", 2026)
+    data = np.stack([noise[c] for c in "AET"])
+    psd_arr = np.stack([psd[c] for c in "AET"])
+    plan = oracle.Plan(g, [(orb, "1.5", data, psd_arr)], 1e-4, cut_factor=1.2)
+    data = data + plan.model_tdi(0, th0)
+    plan = oracle.Plan(g, [(orb, "1.5", data, psd_arr)], 1e-4, cut_factor=1.2)
+    thetas = prior_samples(np.random.default_rng(2026), n_samples, th0[10])
+    t0 = time.perf_counter()
+    plan.lnl(thetas, grad=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return n_samples / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = max(threads, 16)
+    rates = []
+    for _ in range(args.warmup):
+        cpu_baseline_run(threads, threads, "")
+    for _ in range(args.steps):
+        r, _ = cpu_baseline_run(n, threads, "")
+        rates.append(r)
+    v = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "lnL+grad evals/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "adjoint: 1024-sample prior batch, LISA TDI1.5 AET, T=2^22 s, dt=8 s, 125410 bins",
+                   "global_batch": BATCH, "sample_per_step": n},
+        "cpu_baseline": {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} prior samples per step, full 125410-bin grid, FP64 dense with "
+                                   "forward-mode gradient; taichi/jax absent on this host"},
+        "e2e": {"value": v, "unit": "lnL+grad evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_native(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pespace_gb300 import _lib
+    from pespace_gb300.inference import WhittleLikelihood
+    from pespace_gb300.workloads import config0_theta, lisa_dataset, prior_samples
+
+    B = args.batch
+    th0 = config0_theta(DUR - 86400.0)
+    det = lisa_dataset(DUR, DT, FMIN, FMAX, th0, "1.5", seed=2026)
+    eng = WhittleLikelihood(det, precision=args.precision, reference_frequency=1e-4, cut_factor=1.2, max_batch=B)
+    theta_host = torch.as_tensor(prior_samples(np.random.default_rng(2026 + rank), B, th0[10])).pin_memory()
+    theta = theta_host.to("cuda")
+    lib = _lib.load()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_device():
+        return eng.log_likelihood_and_grad(theta)
+
+    for _ in range(max(3, args.warmup)):
+        step_device()
+    torch.cuda.synchronize()
+    lib.pes_plan_profile(eng._plan, 1)
+    n_cls = _lib.KERNEL_CLASSES
+    launches = (ctypes_i64 := __import__("ctypes").c_int64 * n_cls)()
+    dev_ms = (__import__("ctypes").c_double * n_cls)()
+    lib.pes_plan_stats(eng._plan, launches, dev_ms)  # reset
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    step_ms = []
+    with clocks:
+        barrier()
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            step_device()
+            e.record()
+            step_ms.append((s, e))
+        barrier()
+    times = [s.elapsed_time(e) for s, e in step_ms]
+    lib.pes_plan_stats(eng._plan, launches, dev_ms)
+    lib.pes_plan_profile(eng._plan, 0)
+    kern = {lib.pes_kernel_class_name(k).decode(): (int(launches[k]), float(dev_ms[k])) for k in range(n_cls)
+            if launches[k]}
+    gpu_launches = sum(v[0] for v in kern.values())
+    mean_ms = float(np.mean(times))
+    t_local = torch.tensor([mean_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    mean_ms = float(t_local.item())
+    value = world * B / (mean_ms / 1e3)
+
+    # ---------------- e2e through host buffers
+    lnl_host = torch.empty(B, dtype=torch.float64).pin_memory()
+    grad_host = torch.empty((B, 11), dtype=torch.float64).pin_memory()
+    e2e_ms = []
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        th_dev = theta_host.to("cuda", non_blocking=True)
+        lnl, grad = eng.log_likelihood_and_grad(th_dev)
+        lnl_host.copy_(lnl, non_blocking=True)
+        grad_host.copy_(grad, non_blocking=True)
+        e.record()
+        e.synchronize()
+        e2e_ms.append(s.elapsed_time(e))
+    t_e2e = torch.tensor([float(np.mean(e2e_ms))], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_e2e, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world * B / (float(t_e2e.item()) / 1e3)
+
+    # ---------------- accuracy against the FP64 path on this workload
+    err = None
+    if args.precision == "mixed":
+        ref = WhittleLikelihood(det, precision="fp64", reference_frequency=1e-4, cut_factor=1.2, max_batch=B)
+        a, _ = eng.log_likelihood_and_grad(theta)
+        b = ref.log_likelihood_batch(theta)
+        err = float((a - b).abs().max().item())
+        del ref
+
+    # ---------------- roofline of the dominant kernel
+    dom = max(kern.items(), key=lambda kv: kv[1][1])
+    peaks = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch) if rank == 0 else None
+    roofline = None
+    if rank == 0:
+        from pespace_gb300 import census
+
+        roofline = census.roofline(dom[0], dom[1], eng, theta, fp64_peak, peaks)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "lnL+grad evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": "adjoint: 1024-sample prior batch, LISA TDI1.5 AET, T=2^22 s, dt=8 s, "
+                                   "125410 bins, cutoff 1.2 f_RD", "precision": args.precision,
+                       "global_batch": B * world, "per_gpu_batch": B, "nbins": int(eng.desc.nbins),
+                       "l2": "flushed between steps (512 MB write outside the timed events)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "lnL+grad evals/s", "h2d_bytes_per_step": int(B * 11 * 8),
+                    "d2h_bytes_per_step": int(B * 12 * 8)},
+            "gpu_launches": int(gpu_launches),
+            "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in kern.items()},
+            "roofline": roofline,
+            "clocks": clocks.summary(),
+        }
+        if err is not None:
+            line["max_abs_dlnl_vs_fp64"] = err
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            n = max(threads, 16)
+            v, dt = cpu_baseline_run(n, threads, "")
+            line["cpu_baseline"] = {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
+                                    "sample": f"{n} prior samples, full grid, FP64 dense + forward-mode gradient "
+                                              f"({dt:.1f} s)"}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_native(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+"""TDI data container and FD TDI combination (pespace/detector/tdi.py) on CUDA.
+
+Storage is channel-major: ``fd_data`` is a (C, N) complex128 CUDA tensor and
+``fd_noise_power_density`` a (C, N) float64 CUDA tensor, C = len(channels).
+"""
+
+import warnings
+from collections import namedtuple
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .noise import FrequencyDomainNoiseModel, available_noise_models
+
+
+@dataclass(frozen=True)
+class DataInformation:
+    """tdi.py:64-159: the dense frequency grid of a dataset.
+
+    ``frequency_samples_array`` = rfftfreq(int(duration // delta_time + 1),
+    delta_time) masked to [minimum_frequency, maximum_frequency]; its spacing is
+    1/(Nt dt).  The likelihood weight is ``delta_frequency`` = 1/duration.
+    """
+
+    channels: tuple
+    duration: float
+    delta_time: float
+    start_time: float
+    minimum_frequency: float
+    maximum_frequency: float
+    sampling_frequency: float = field(init=False)
+    delta_frequency: float = field(init=False)
+    time_series_length: int = field(init=False)
+    full_frequency_series_length: int = field(init=False)
+    frequency_mask_array: np.ndarray = field(init=False)
+    frequency_samples_array: np.ndarray = field(init=False)
+    frequency_series_length: int = field(init=False)
+    first_index: int = field(init=False)
+    frequency_step: float = field(init=False)
+
+    def __post_init__(self):
+        nt = int(self.duration // self.delta_time + 1)
+        full = np.fft.rfftfreq(nt, self.delta_time)
+        mask = (full >= self.minimum_frequency) * (full <= self.maximum_frequency)
+        idx = np.nonzero(mask)[0]
+        for k, v in dict(
+            sampling_frequency=1 / self.delta_time,
+            delta_frequency=1 / self.duration,
+            time_series_length=nt,
+            full_frequency_series_length=int(full.size),
+            frequency_mask_array=mask,
+            frequency_samples_array=full[mask],
+            frequency_series_length=int(idx.size),
+            first_index=int(idx[0]) if idx.size else 0,
+            frequency_step=1.0 / (nt * self.delta_time),
+        ).items():
+            object.__setattr__(self, k, v)
+
+    @property
+    def time_samples_array(self):
+        return np.arange(self.time_series_length) * self.delta_time + self.start_time
+
+
+class TDIChannelData:
+    """tdi.py:162-1376 (frequency-domain part) with CUDA tensors."""
+
+    def __init__(self, scaling=False, backend="cuda"):
+        if backend != "cuda":
+            raise ValueError(f"Invalid backend: {backend}")
+        self.scaling = scaling
+        self.backend = backend
+        self._reset()
+
+    def _reset(self):
+        self.frequency_samples = None
+        self.fd_data = None
+        self.fd_noise_power_density = None
+        self._data_info = None
+        self._reset_flag = False
+
+    @property
+    def data_info(self):
+        return self._data_info
+
+    def set_data_info(self, channels, duration, delta_time, start_time, minimum_frequency, maximum_frequency):
+        if self._reset_flag:
+            warnings.warn("You are setting `data_info`, but you have set TDI data of current instance previously.")
+        self._data_info = DataInformation(tuple(channels), duration, delta_time, start_time, minimum_frequency,
+                                          maximum_frequency)
+
+    def set_fd_data_from_zero(self, channels, duration, delta_time, start_time=0.0, minimum_frequency=1e-5,
+                              maximum_frequency=0.1):
+        if self._reset_flag:
+            warnings.warn("You are setting `fd_data` with zero value; the instance is reset.")
+            self._reset()
+        self.set_data_info(channels, duration, delta_time, start_time, minimum_frequency, maximum_frequency)
+        n = self.data_info.frequency_series_length
+        self.frequency_samples = torch.as_tensor(self.data_info.frequency_samples_array, dtype=torch.float64,
+                                                 device="cuda")
+        self.fd_data = torch.zeros((len(channels), n), dtype=torch.complex128, device="cuda")
+        self._reset_flag = True
+
+    def set_fd_data_from_input(self, channels, duration, delta_time, tdi_data_array, start_time=0.0,
+                               minimum_frequency=1e-5, maximum_frequency=0.1):
+        self.set_fd_data_from_zero(channels, duration, delta_time, start_time, minimum_frequency, maximum_frequency)
+        arr = torch.as_tensor(np.asarray(tdi_data_array), dtype=torch.complex128, device="cuda")
+        if tuple(arr.shape) != tuple(self.fd_data.shape):
+            raise ValueError(f"tdi_data_array must have shape {tuple(self.fd_data.shape)}, got {tuple(arr.shape)}; "
+                             "crop it with `data_info.frequency_mask_array` first")
+        self.fd_data.copy_(arr)
+
+    def set_fd_noise_power_density_from_model(self, noise_model, **model_kwargs):
+        if isinstance(noise_model, str):
+            if noise_model not in available_noise_models:
+                raise ValueError(f"{noise_model} is not an implemented noise model. \n"
+                                 f"Current available noise models include {[*available_noise_models.keys()]}.")
+            psd = available_noise_models[noise_model]
+        elif isinstance(noise_model, FrequencyDomainNoiseModel):
+            psd = noise_model
+        else:
+            raise TypeError(f"unsupported noise model {type(noise_model).__name__}")
+        if self.data_info is None:
+            raise ValueError("The `data_info` has not yet set.")
+        if self.fd_noise_power_density is not None:
+            warnings.warn("`fd_noise_power_density` has been set previously; it is replaced.")
+        d = psd(self.data_info.frequency_samples_array, self.data_info.channels, self.scaling, **model_kwargs)
+        arr = np.stack([np.asarray(d[c], dtype=np.float64) for c in self.data_info.channels])
+        self.fd_noise_power_density = torch.as_tensor(arr, device="cuda")
+
+    def get_fd_noise_realization(self, seed=None, output_type="cuda"):
+        """tdi.py:896-916: seeded white noise coloured by sqrt(PSD) (host RNG)."""
+        if self.fd_noise_power_density is None:
+            raise ValueError("Setting `fd_noise_power_density` before generating noise realization.")
+        info = self.data_info
+        rng = np.random.default_rng(seed=seed)
+        var = 0.5 / (info.delta_frequency) ** 0.5
+        psd = self.fd_noise_power_density.cpu().numpy()
+        out = []
+        for c_i, _ in enumerate(info.channels):
+            re, im = rng.normal(0, var, (2, info.full_frequency_series_length))
+            re[0] = 0.0
+            im[0] = 0.0
+            if np.mod(info.time_series_length, 2) == 0:
+                im[-1] = 0.0
+                re[-1] = 0.0
+            out.append((re + 1j * im)[info.frequency_mask_array] * psd[c_i] ** 0.5)
+        arr = np.stack(out)
+        if output_type == "numpy":
+            return namedtuple("DataContent", info.channels)(*arr)
+        if output_type == "cuda":
+            return torch.as_tensor(arr, dtype=torch.complex128, device="cuda")
+        raise ValueError(f"Unknown output_type: {output_type}")
+
+    def add_into_fd_data(self, input):
+        arr = input if torch.is_tensor(input) else torch.as_tensor(np.stack(list(input)), device="cuda")
+        if tuple(arr.shape) != tuple(self.fd_data.shape):
+            raise ValueError("Cannot add the input into the `fd_data`: shape differs from the TDI data")
+        self.fd_data += arr.to(self.fd_data.dtype)
+
+    @property
+    def fd_data_numpy(self):
+        if self.fd_data is None:
+            return None
+        return namedtuple("DataContent", self.data_info.channels)(*self.fd_data.cpu().numpy())
+
+    @property
+    def fd_noise_power_density_numpy(self):
+        if self.fd_noise_power_density is None:
+            return None
+        return namedtuple("DataContent", self.data_info.channels)(*self.fd_noise_power_density.cpu().numpy())
+
+
+class FDMichelsonConstantEqualArm:
+    """tdi.py:1603-1793: FD Michelson TDI with constant equal arms."""
+
+    domain = "fd"
+
+    def __init__(self, generation="1.5", orthogonal=True, backend="cuda"):
+        self.generation = str(generation)
+        if self.generation not in ("1.5", "2.0"):
+            raise ValueError(f"Unsupported generation {self.generation}.")
+        if backend != "cuda":
+            raise ValueError(f"Unknown backend: {backend}")
+        self.orthogonal = bool(orthogonal)
+        self.labels = ("A", "E", "T") if self.orthogonal else ("X", "Y", "Z")
+        self.backend = backend
+        self.detector = None
+
+    @property
+    def generation_code(self):
+        return 15 if self.generation == "1.5" else 20
+
+    def init_tdi_combination_model(self, detector):
+        self.detector = detector
+        n = detector.tdi_data.data_info.frequency_series_length
+        detector.tdi_response = torch.zeros((3, n), dtype=torch.complex128, device="cuda")
+
+    def update_tdi_response(self):
+        det = self.detector
+        freqs = det.tdi_data.frequency_samples
+        n = freqs.numel()
+        _lib.check(_lib.load().pes_tdi_combination(
+            _lib.ptr(freqs), n, det.orbit_model.arm_length_sec(0.0), self.generation_code, int(self.orthogonal),
+            _lib.ptr(det.single_link_response), _lib.ptr(det.tdi_response), _lib.stream_handle()))

@@ -1,0 +1,222 @@
+"""Whittle likelihoods on CUDA.
+
+* ``compute_whittle_likelihood`` replaces ``compute_whittle_likelihood_ti``
+  (pespace/inference/likelihood_ti.py:17-69) and ``noise_weighted_inner_product``
+  replaces the JAX kernel (likelihood_jax.py:21-42).
+* ``LikelihoodBilbyInterface`` keeps ``LikelihoodBilbyInterfaceTaichi``'s
+  constructor and ``log_likelihood(parameters)`` (interface_bilby.py:31-116),
+  one sample at a time through the plugin kernels.
+* ``WhittleLikelihood`` is the batched engine: one plan, many samples per call,
+  lnL and its 11-parameter gradient (behind ``torch.autograd``).
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..waveform.phenomd import theta_from_parameters
+
+
+def _rows(data, labels, channels):
+    idx = [labels.index(c) for c in channels]
+    return data[idx].contiguous()
+
+
+def noise_weighted_inner_product(observed_data, response_data, psd, df):
+    """-2 df sum |d - h|^2 / S over (C, N) (or (N,)) CUDA tensors; returns a float."""
+    d = torch.as_tensor(observed_data, dtype=torch.complex128, device="cuda")
+    h = torch.as_tensor(response_data, dtype=torch.complex128, device="cuda")
+    s = torch.as_tensor(psd, dtype=torch.float64, device="cuda")
+    if d.dim() == 1:
+        d, h, s = d[None], h[None], s[None]
+    d, h, s = d.contiguous(), h.contiguous(), s.contiguous()
+    if not (d.shape == h.shape == s.shape):
+        raise ValueError(f"shape mismatch: data {tuple(d.shape)}, response {tuple(h.shape)}, psd {tuple(s.shape)}")
+    C, N = d.shape
+    lib = _lib.load()
+    ws = torch.empty(int(lib.pes_whittle_workspace_len(N)), dtype=torch.float64, device="cuda")
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    _lib.check(lib.pes_whittle_lnl(_lib.ptr(d), _lib.ptr(h), _lib.ptr(s), C, N, float(df), _lib.ptr(ws),
+                                   ws.numel(), _lib.ptr(out), _lib.stream_handle()))
+    return float(out.item())
+
+
+def compute_whittle_likelihood(channels, observed_data, response_data, psd, df, labels=("A", "E", "T")):
+    """likelihood_ti.py:17-69 over the listed channels of (C, N) tensors."""
+    return noise_weighted_inner_product(_rows(observed_data, labels, channels), _rows(response_data, labels, channels),
+                                        _rows(psd, labels, channels), df)
+
+
+class LikelihoodBilbyInterface:
+    """interface_bilby.py:21-116 without the bilby base class (bilby is optional)."""
+
+    def __init__(self, waveform, detector, channels):
+        self.waveform = waveform
+        if not isinstance(detector, tuple):
+            detector = (detector,)
+        self.detector = detector
+        unsupported = [c for c in channels if c not in ("A", "E", "T")]
+        if any(unsupported):
+            raise ValueError("The likelihood compution only support TDI channels of ('A','E','T'). "
+                             f"{unsupported} are not supported currently.")
+        self.channels = tuple(channels)
+        self.parameters = {}
+
+    def log_likelihood(self, parameters=None):
+        parameters = self.parameters if parameters is None else parameters
+        self.waveform.update_waveform(parameters)
+        logl = 0.0
+        for det in self.detector:
+            det.update_detector_response(self.waveform.waveform_container, parameters["ecliptic_longitude"],
+                                         parameters["ecliptic_latitude"], parameters["polarization"],
+                                         parameters["coalescence_time"])
+            logl += compute_whittle_likelihood(self.channels, det.tdi_data.fd_data, det.tdi_response,
+                                               det.tdi_data.fd_noise_power_density,
+                                               det.tdi_data.data_info.delta_frequency,
+                                               labels=det.tdi_combination.labels)
+        return logl
+
+
+class WhittleLikelihood:
+    """Batched lnL / lnL+gradient over parameter samples on one GPU.
+
+    Parameters
+    ----------
+    detector : InterferometerAntenna or tuple of them (same frequency grid,
+        orthogonal A/E/T combination).  Their ``tdi_data`` must hold
+        ``fd_data`` and ``fd_noise_power_density``.
+    channels : subset of ("A", "E", "T").
+    precision : "fp64" (dense FP64, every bin) or "mixed" (FP64 sparse grid,
+        FP32 dense bulk).
+    cut_factor : per-sample model cutoff in units of the ringdown frequency
+        (0 keeps the IMRPhenomD Mf = 0.2 cut only).
+    """
+
+    def __init__(self, detector, channels=("A", "E", "T"), precision="fp64", reference_frequency=None,
+                 cut_factor=0.0, max_batch=1024, n_sparse=1024):
+        if not isinstance(detector, tuple):
+            detector = (detector,)
+        if len(detector) > _lib.MAX_DETECTORS:
+            raise ValueError(f"at most {_lib.MAX_DETECTORS} detectors")
+        unsupported = [c for c in channels if c not in ("A", "E", "T")]
+        if any(unsupported):
+            raise ValueError(f"The likelihood computation only supports orthogonal channels ('A', 'E', 'T'). "
+                             f"{unsupported} are not supported currently.")
+        info0 = detector[0].tdi_data.data_info
+        for det in detector:
+            if det.tdi_combination.labels != ("A", "E", "T"):
+                raise ValueError(f"detector {det.name} must use the orthogonal (A, E, T) combination")
+            info = det.tdi_data.data_info
+            if (info.frequency_series_length, info.first_index, info.frequency_step) != (
+                    info0.frequency_series_length, info0.first_index, info0.frequency_step):
+                raise ValueError("all detectors must share one frequency grid")
+            if det.tdi_data.fd_data is None or det.tdi_data.fd_noise_power_density is None:
+                raise ValueError(f"fd_data and fd_noise_power_density must be set for detector={det.name}")
+        self.detector = detector
+        self.channels = tuple(channels)
+        self.precision = precision
+        self.max_batch = int(max_batch)
+        desc = _lib.PesPlanDesc()
+        desc.nbins = info0.frequency_series_length
+        desc.k0 = info0.first_index
+        desc.f_step = info0.frequency_step
+        desc.df = info0.delta_frequency
+        desc.f_ref = float(reference_frequency if reference_frequency is not None else info0.minimum_frequency)
+        desc.cut_factor = float(cut_factor)
+        desc.n_det = len(detector)
+        desc.chan_mask = sum(1 << "AET".index(c) for c in self.channels)
+        desc.precision = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
+        desc.n_sparse = int(n_sparse)
+        desc.max_batch = self.max_batch
+        for i, det in enumerate(detector):
+            desc.det[i].orbit = det.orbit_model.to_c()
+            desc.det[i].generation = det.tdi_combination.generation_code
+        self.desc = desc
+        lib = _lib.load()
+        handle = ctypes.c_void_p()
+        _lib.check(lib.pes_plan_create(ctypes.byref(desc), ctypes.byref(handle)))
+        self._plan = handle
+        for i, det in enumerate(detector):
+            data = det.tdi_data.fd_data.to(torch.complex128).contiguous()
+            psd = det.tdi_data.fd_noise_power_density.to(torch.float64).contiguous()
+            _lib.check(lib.pes_plan_set_data(self._plan, i, _lib.ptr(data), _lib.ptr(psd), _lib.stream_handle()))
+        self.last_status = None
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and plan.value:
+            try:
+                _lib.load().pes_plan_destroy(plan)
+            except Exception:
+                pass
+            self._plan = None
+
+    def _prep(self, theta):
+        theta = torch.as_tensor(theta, dtype=torch.float64, device="cuda")
+        if theta.dim() == 1:
+            theta = theta[None]
+        if theta.shape[-1] != 11:
+            raise ValueError(f"theta must have 11 columns, got {tuple(theta.shape)}")
+        return theta.contiguous()
+
+    def log_likelihood_batch(self, theta):
+        """lnL for a (B, 11) parameter tensor; returns a (B,) CUDA tensor."""
+        theta = self._prep(theta)
+        B = theta.shape[0]
+        out = torch.empty(B, dtype=torch.float64, device="cuda")
+        status = torch.empty(B, dtype=torch.int32, device="cuda")
+        for lo in range(0, B, self.max_batch):
+            hi = min(B, lo + self.max_batch)
+            _lib.check(_lib.load().pes_lnl_batch(self._plan, _lib.ptr(theta[lo:hi]), hi - lo, _lib.ptr(out[lo:hi]),
+                                                 _lib.ptr(status[lo:hi]), _lib.stream_handle()))
+        self.last_status = status
+        return out
+
+    def log_likelihood_and_grad(self, theta):
+        """(lnL (B,), dlnL/dtheta (B, 11)) for a (B, 11) parameter tensor."""
+        theta = self._prep(theta)
+        B = theta.shape[0]
+        out = torch.empty(B, dtype=torch.float64, device="cuda")
+        grad = torch.empty((B, 11), dtype=torch.float64, device="cuda")
+        status = torch.empty(B, dtype=torch.int32, device="cuda")
+        for lo in range(0, B, self.max_batch):
+            hi = min(B, lo + self.max_batch)
+            _lib.check(_lib.load().pes_lnl_grad_batch(self._plan, _lib.ptr(theta[lo:hi]), hi - lo,
+                                                      _lib.ptr(out[lo:hi]), _lib.ptr(grad[lo:hi]),
+                                                      _lib.ptr(status[lo:hi]), _lib.stream_handle()))
+        self.last_status = status
+        return out, grad
+
+    def log_likelihood(self, params):
+        """Single parameter set (dict / namedtuple with reference names); returns a float."""
+        return float(self.log_likelihood_batch(theta_from_parameters(params)).item())
+
+    def model_tdi(self, theta, det=0, orthogonal=True):
+        """Dense A/E/T model of one detector (parity / debugging)."""
+        theta = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(11))
+        out = torch.empty((3, int(self.desc.nbins)), dtype=torch.complex128, device="cuda")
+        _lib.check(_lib.load().pes_plan_model_tdi(self._plan, det, int(orthogonal), _lib.ptr(theta), _lib.ptr(out),
+                                                  _lib.stream_handle()))
+        return out
+
+
+class _LogLikelihoodFn(torch.autograd.Function):
+    """lnL(theta) with the gradient from the plan's derivative kernels."""
+
+    @staticmethod
+    def forward(ctx, theta, engine):
+        lnl, grad = engine.log_likelihood_and_grad(theta)
+        ctx.save_for_backward(grad)
+        return lnl
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return g[:, None] * grad, None
+
+
+def log_likelihood(theta, engine):
+    """Differentiable batched lnL: ``log_likelihood(theta, engine).sum().backward()``."""
+    return _LogLikelihoodFn.apply(theta, engine)
