@@ -1,22 +1,769 @@
-// Mixed-precision batched path (sparse FP64 grid + FP32 dense spline bulk).
+// Mixed-precision batched path.
+//
+//  1. sparse stage (FP64): at n_sparse log-spaced nodes f_j shared by all
+//     samples, the phase Phi_s = Psi + 2 pi f k.x0(t_f) and the three TDI
+//     channel transfers G_c (response of the unit-phase waveform with the
+//     constellation-centre delay factored out), per (sample, detector);
+//  2. not-a-knot cubic splines through the nodes (FP64 solve; phase
+//     coefficients kept in FP64, transfer coefficients stored in FP32);
+//  3. dense stage (FP32 bulk): for every bin, h_c = G_c(f) exp(-i (Phi_s(f) +
+//     2 pi f t_c)); the phase of each run of <= 32 bins is anchored in FP64 at
+//     the run start and advanced in FP32 with exact split products; the
+//     residual |d - h|^2 / S is accumulated with compensation, per-block
+//     partials are summed in FP64 in a fixed order;
+//  4. gradient: the dense stage also accumulates the adjoint moments
+//     sum_bins A_q(f) t^p of each spline interval; a transposed spline solve
+//     turns them into node adjoints, and the sparse stage is recomputed with
+//     dual numbers and contracted with those adjoints (no dense residuals are
+//     stored).
+#include <cmath>
+#include <vector>
+
 #include "pes_plan.cuh"
 
 namespace pes {
 
-struct MixedBuffers {
-  int unused;
+constexpr int kNodeQ = 7;         // Phi_s, Re/Im G_A, G_E, G_T
+constexpr int kChunkMax = 32;     // bins per phase-anchored run (one warp)
+constexpr int kMixThreads = 128;  // 4 warps; each warp owns 32 consecutive runs
+constexpr int kMoments = 4;       // t^0..t^3
+constexpr int kSparseThreads = 128;
+constexpr int kScratchRows = 5;   // doubles per node in the per-(sample, det, q) spline scratch
+
+struct MixedDev {
+  int32_t J;                // nodes
+  int32_t nchunks;
+  int32_t n_det;
+  int32_t nblk_dense;
+  int32_t nblk_sparse;
+  int32_t pad;
+  double scale;             // FP32 storage scale of data and model
+  const double* node_f;     // [J]
+  const int32_t* ch_begin;  // [nchunks] first bin of the run
+  const int32_t* ch_len;    // [nchunks]
+  const int32_t* ch_iv;     // [nchunks] spline interval of the run
+  const float* bin_t;       // [nbins] f_i - f_iv(i)
+  float2* dat;              // [n_det][3][nbins] scaled data
+  float* wgt;               // [n_det][3][nbins] inverse scaled PSD (0 off the channel mask)
+  int32_t* nsp;             // [B] spline intervals of the sample (nodes 0..nsp)
+  int32_t* nch;             // [B] runs with a live bin
+  double* yv;               // [B][n_det][7][J] node values
+  double* scr;              // [B][n_det][7][5 J] spline scratch
+  double* cphi;             // [B][n_det][J][4] phase spline coefficients (FP64)
+  float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32)
+  double* mom;              // [B][n_det][J][7][4] adjoint moments
+  double* ybar;             // [B][n_det][7][J] node adjoints
+  double* part;             // [B][nblk_dense] lnL partials
+  double* gpart;            // [B][n_det][nblk_sparse][kGradTangents] gradient partials
+  double* gdir;             // [B][n_det] direct t_c term of the gradient
 };
 
-int mixed_create(PesPlan* p) {
-  (void)p;
-  set_error("mixed precision plans are not available in this build");
-  return PES_EINVAL;
+struct GenArg {
+  int32_t gen20[PES_MAX_DETECTORS];
+};
+
+struct MixedBuffers {
+  MixedDev dev;
+  GenArg gen;
+  std::vector<void*> allocs;
+};
+
+// ------------------------------------------------------------------ sparse stage
+template <class T>
+__device__ __forceinline__ void node_eval(const PlanDev& P, const MixedDev& M, const SampleBlock<T>& b, int d,
+                                          int gen20, double f, T y[kNodeQ]) {
+  T Mf = b.wf.Msec * f;
+  T amp, psi, tf;
+  phenomd_eval<T>(b.wf, Mf, amp, psi, tf);
+  amp = amp * M.scale;
+  const T zero = lift<T>(0.0);
+  Cx<T> hp = cx(b.wf.pfac * amp, zero);
+  Cx<T> hc = cx(zero, -(b.wf.cfac * amp));
+  Cx<T> L[6], C[3];
+  T kx0;
+  single_links_impl<true, T>(P.orbit[d], f, hp, hc, tf + b.tc, b.pol, L, &kx0);
+  Cx<double> D, Pf;
+  tdi_factors(f, P.orbit[d].arm_sec, gen20, D, Pf);
+  tdi_channels<T>(D, Pf, 1, L, C);
+  y[0] = psi + (2.0 * kPi * f) * kx0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    y[1 + 2 * c] = C[c].re;
+    y[2 + 2 * c] = C[c].im;
+  }
 }
-void mixed_destroy(PesPlan* p) { delete p->mixed; p->mixed = nullptr; }
-int mixed_set_data(PesPlan*, cudaStream_t) { return PES_OK; }
-int mixed_lnl(PesPlan*, const double*, int64_t, double*, double*, int32_t*, cudaStream_t) {
-  set_error("mixed precision plans are not available in this build");
-  return PES_EINVAL;
+
+template <class T>
+__device__ __forceinline__ void load_block(const SampleBlock<T>* blocks, int s, SampleBlock<T>& sb) {
+  const int n8 = sizeof(SampleBlock<T>) / 8;
+  const double* src = reinterpret_cast<const double*>(&blocks[s]);
+  double* dst = reinterpret_cast<double*>(&sb);
+  for (int j = threadIdx.x; j < n8; j += blockDim.x) dst[j] = src[j];
+}
+
+// Forward: node values in FP64.  grid (ceil(J/128), n_det, B)
+__global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedDev M, GenArg G,
+                                                               const SampleBlock<double>* __restrict__ blocks) {
+  __shared__ SampleBlock<double> sb;
+  const int s = blockIdx.z, d = blockIdx.y;
+  load_block(blocks, s, sb);
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ns = M.nsp[s];
+  if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J) return;
+  double y[kNodeQ];
+  node_eval<double>(P, M, sb, d, G.gen20[d], M.node_f[j], y);
+  double* out = M.yv + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
+#pragma unroll
+  for (int q = 0; q < kNodeQ; ++q) out[(size_t)q * M.J + j] = y[q];
+}
+
+// Backward: recompute node values with NT tangents and contract with the node adjoints.
+template <int NT>
+__global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G,
+                                                               const SampleBlock<Dual<NT>>* __restrict__ blocks) {
+  __shared__ SampleBlock<Dual<NT>> sb;
+  __shared__ double red[kSparseThreads / 32][NT];
+  const int s = blockIdx.z, d = blockIdx.y;
+  load_block(blocks, s, sb);
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ns = M.nsp[s];
+  double acc[NT];
+#pragma unroll
+  for (int k = 0; k < NT; ++k) acc[k] = 0.0;
+  if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
+    Dual<NT> y[kNodeQ];
+    node_eval<Dual<NT>>(P, M, sb, d, G.gen20[d], M.node_f[j], y);
+    const double* yb = M.ybar + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
+#pragma unroll
+    for (int q = 0; q < kNodeQ; ++q) {
+      const double w = yb[(size_t)q * M.J + j];
+#pragma unroll
+      for (int k = 0; k < NT; ++k) acc[k] += w * y[q].d[k];
+    }
+  }
+  const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < NT; ++k) {
+    double x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (l == 0) red[wid][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NT) {
+    double x = 0.0;
+#pragma unroll
+    for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
+    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * kGradTangents + threadIdx.x] = x;
+  }
+}
+
+// ------------------------------------------------------------------ per-sample ranges
+// nsp: intervals 0..nsp-1 cover every live bin (nodes 0..nsp); nch: runs with a live bin.
+__global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  const SampleBlock<double>& b = blocks[s];
+  int ns = 0, nc = 0;
+  if (b.status == kSampleOk && b.kcut > 0) {
+    const int64_t last = b.kcut - 1;
+    int lo = 0, hi = M.nchunks - 1;  // last run whose first bin is <= last
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (M.ch_begin[mid] <= last) lo = mid; else hi = mid - 1;
+    }
+    nc = lo + 1;
+    ns = M.ch_iv[lo] + 1;
+    if (ns < 3) ns = 3;
+    if (ns > M.J - 1) ns = M.J - 1;
+  }
+  M.nsp[s] = ns;
+  M.nch[s] = nc;
+}
+
+// ------------------------------------------------------------------ splines
+// Not-a-knot cubic spline through nodes 0..n (n >= 3).  Unknowns: second
+// derivatives m_1..m_{n-1} (m_0 and m_n eliminated with the not-a-knot
+// conditions).  Row i: lo_i m_{i-1} + di_i m_i + up_i m_{i+1} = 6 (D_i - D_{i-1}).
+__device__ __forceinline__ void nak_row(const double* f, int n, int i, double& lo, double& di, double& up) {
+  const double h0 = f[i] - f[i - 1], h1 = f[i + 1] - f[i];
+  lo = h0;
+  di = 2.0 * (h0 + h1);
+  up = h1;
+  if (i == 1) {  // m_0 = ((h0 + h1) m_1 - h0 m_2) / h1
+    di += h0 * (h0 + h1) / h1;
+    up -= h0 * h0 / h1;
+    lo = 0.0;
+  }
+  if (i == n - 1) {  // m_n = ((h_{n-2} + h_{n-1}) m_{n-1} - h_{n-1} m_{n-2}) / h_{n-2}
+    di += h1 * (h0 + h1) / h0;
+    lo -= h1 * h1 / h0;
+    up = 0.0;
+  }
+}
+
+__device__ __forceinline__ void nak_ends(const double* f, int n, const double* m, double& m0, double& mn) {
+  const double h0 = f[1] - f[0], h1 = f[2] - f[1];
+  m0 = ((h0 + h1) * m[1] - h0 * m[2]) / h1;
+  const double ha = f[n - 1] - f[n - 2], hb = f[n] - f[n - 1];
+  mn = ((ha + hb) * m[n - 1] - hb * m[n - 2]) / ha;
+}
+
+// Thread per (sample, detector, quantity): fit and store interval coefficients.
+__global__ void k_spline_fit(MixedDev M, int64_t B) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int q = (int)(tid % kNodeQ);
+  const int64_t sd = tid / kNodeQ;
+  if (sd >= B * (int64_t)M.n_det) return;
+  const int64_t s = sd / M.n_det;
+  const int n = M.nsp[s];
+  if (n < 3) return;
+  const double* f = M.node_f;
+  const double* y = M.yv + ((size_t)sd * kNodeQ + q) * M.J;
+  double* cpr = M.scr + ((size_t)sd * kNodeQ + q) * kScratchRows * M.J;  // c'
+  double* dpr = cpr + M.J;                                                 // d'
+  double* m = dpr + M.J;                                                   // m_0..m_n
+  double cprev = 0.0, dprev = 0.0;
+  double slope_prev = (y[1] - y[0]) / (f[1] - f[0]);
+  for (int i = 1; i <= n - 1; ++i) {
+    double lo, di, up;
+    nak_row(f, n, i, lo, di, up);
+    const double slope = (y[i + 1] - y[i]) / (f[i + 1] - f[i]);
+    const double r = 6.0 * (slope - slope_prev);
+    slope_prev = slope;
+    const double den = di - lo * cprev;
+    cprev = up / den;
+    dprev = (r - lo * dprev) / den;
+    cpr[i] = cprev;
+    dpr[i] = dprev;
+  }
+  double mnext = 0.0;
+  for (int i = n - 1; i >= 1; --i) {
+    const double mi = dpr[i] - cpr[i] * mnext;
+    m[i] = mi;
+    mnext = mi;
+  }
+  nak_ends(f, n, m, m[0], m[n]);
+  for (int i = 0; i < n; ++i) {
+    const double h = f[i + 1] - f[i];
+    const double a = y[i];
+    const double bc = (y[i + 1] - y[i]) / h - h * (2.0 * m[i] + m[i + 1]) / 6.0;
+    const double cc = 0.5 * m[i];
+    const double dc = (m[i + 1] - m[i]) / (6.0 * h);
+    if (q == 0) {
+      double* o = M.cphi + ((size_t)sd * M.J + i) * 4;
+      o[0] = a;
+      o[1] = bc;
+      o[2] = cc;
+      o[3] = dc;
+    } else {
+      M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4((float)a, (float)bc, (float)cc, (float)dc);
+    }
+  }
+}
+
+// Transpose of the fit: interval coefficient adjoints (the dense moments,
+// times wscale) -> node adjoints ybar.  Also the direct t_c term (q == 0).
+__global__ void k_spline_adjoint(MixedDev M, int64_t B, double wscale) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int q = (int)(tid % kNodeQ);
+  const int64_t sd = tid / kNodeQ;
+  if (sd >= B * (int64_t)M.n_det) return;
+  const int64_t s = sd / M.n_det;
+  const int n = M.nsp[s];
+  double* yb = M.ybar + ((size_t)sd * kNodeQ + q) * M.J;
+  for (int i = 0; i < M.J; ++i) yb[i] = 0.0;
+  if (q == 0) M.gdir[sd] = 0.0;
+  if (n < 3) return;
+  const double* f = M.node_f;
+  const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments;
+  double* mb = M.scr + ((size_t)sd * kNodeQ + q) * kScratchRows * M.J;  // mbar_0..mbar_n
+  double* Db = mb + M.J;                                                 // Dbar_0..Dbar_{n-1}
+  double* cpt = Db + M.J;                                                // transposed-solve c'
+  double* dpt = cpt + M.J;                                               // transposed-solve d'
+  for (int i = 0; i <= n; ++i) mb[i] = 0.0;
+  double gd = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double h = f[i + 1] - f[i];
+    const double* mm = mom + ((size_t)i * kNodeQ + q) * kMoments;
+    const double ab = wscale * mm[0], bb = wscale * mm[1], cb = wscale * mm[2], db = wscale * mm[3];
+    if (q == 0) gd += 2.0 * kPi * (f[i] * mm[0] + mm[1]);  // sum_bins A_phi 2 pi f
+    yb[i] += ab;
+    Db[i] = bb;
+    mb[i] += -h * bb / 3.0 + 0.5 * cb - db / (6.0 * h);
+    mb[i + 1] += -h * bb / 6.0 + db / (6.0 * h);
+  }
+  if (q == 0) M.gdir[sd] = wscale * gd;
+  {  // eliminated end second derivatives
+    const double h0 = f[1] - f[0], h1 = f[2] - f[1];
+    mb[1] += mb[0] * (h0 + h1) / h1;
+    mb[2] -= mb[0] * h0 / h1;
+    const double ha = f[n - 1] - f[n - 2], hb = f[n] - f[n - 1];
+    mb[n - 1] += mb[n] * (ha + hb) / ha;
+    mb[n - 2] -= mb[n] * hb / ha;
+  }
+  // rbar = A^{-T} mbar over rows 1..n-1; A^T row i: sub = up_{i-1}, diag = di_i, super = lo_{i+1}
+  double cprev = 0.0, dprev = 0.0;
+  for (int i = 1; i <= n - 1; ++i) {
+    double lo, di, up, lo_n = 0.0, di_n, up_n, lo_p, di_p, up_p = 0.0;
+    nak_row(f, n, i, lo, di, up);
+    if (i > 1) nak_row(f, n, i - 1, lo_p, di_p, up_p);
+    if (i < n - 1) nak_row(f, n, i + 1, lo_n, di_n, up_n);
+    const double sub = (i > 1) ? up_p : 0.0;
+    const double sup = (i < n - 1) ? lo_n : 0.0;
+    const double den = di - sub * cprev;
+    cprev = sup / den;
+    dprev = (mb[i] - sub * dprev) / den;
+    cpt[i] = cprev;
+    dpt[i] = dprev;
+  }
+  double rnext = 0.0;
+  for (int i = n - 1; i >= 1; --i) {
+    const double ri = dpt[i] - cpt[i] * rnext;
+    rnext = ri;
+    // r_i = 6 (D_i - D_{i-1})
+    Db[i] += 6.0 * ri;
+    Db[i - 1] -= 6.0 * ri;
+  }
+  for (int i = 0; i < n; ++i) {
+    const double h = f[i + 1] - f[i];
+    yb[i + 1] += Db[i] / h;
+    yb[i] -= Db[i] / h;
+  }
+}
+
+// ------------------------------------------------------------------ dense stage
+// 2 pi split into a 12-bit head and two tails for exact FP32 reduction of
+// exactly-representable arguments up to ~2^11 turns.
+constexpr float kTwoPiHi = 6.28125f;                // 8 significant bits: k * hi exact for |k| < 2^16
+constexpr float kTwoPiMid = 0.0019353071693331003f;   // float(2 pi - hi)
+constexpr float kTwoPiLo = 1.0253131677018246e-11f;   // float(2 pi - hi - mid)
+constexpr float kInvTwoPi = 0.159154943091895336f;
+
+__device__ __forceinline__ float reduce_exact(float x) {
+  const float k = rintf(x * kInvTwoPi);
+  float r = fmaf(-k, kTwoPiHi, x);
+  r = fmaf(-k, kTwoPiMid, r);
+  r = fmaf(-k, kTwoPiLo, r);
+  return r;
+}
+
+// head of x truncated to `bits` significant bits (so that head * small integer is exact in FP32)
+__device__ __forceinline__ float head_bits(double x, int bits) {
+  const long long m = ~((1LL << (53 - bits)) - 1);
+  return (float)__longlong_as_double(__double_as_longlong(x) & m);
+}
+
+__device__ __forceinline__ double wrap_2pi(double x) {
+  return x - (2.0 * kPi) * rint(x * (1.0 / (2.0 * kPi)));
+}
+
+struct RunPhase {
+  float c0, s0;           // cos, sin of the anchored phase at the run start
+  float p1h, p1l;         // per-bin increment (wrapped), head/tail
+  float p2h, p2l;         // quadratic coefficient, head/tail
+  float p3h, p3l;         // cubic coefficient, head/tail
+};
+
+template <bool kGrad>
+__global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev M,
+                                                             const SampleBlock<double>* __restrict__ blocks) {
+  __shared__ double red[kMixThreads / 32];
+  const int s = blockIdx.y;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int g = blockIdx.x * (kMixThreads / 32) + wid;  // run group
+  const int nc = M.nch[s];
+  const int64_t kcut = blocks[s].kcut;
+  const double tc = blocks[s].tc;
+  const int first = g * kChunkMax;
+  float acc = 0.0f, comp = 0.0f;
+  if (blocks[s].status == kSampleOk && first < nc) {
+    const int cl = first + lane;
+    for (int d = 0; d < M.n_det; ++d) {
+      const size_t sd = (size_t)s * M.n_det + d;
+      // ---- per-run phase anchors, one run per lane (FP64)
+      RunPhase rp = {1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      if (cl < nc) {
+        const int j = M.ch_iv[cl];
+        const int kb = M.ch_begin[cl];
+        const double fb = (double)(P.k0 + kb) * P.f_step;
+        const double t = fb - M.node_f[j];
+        const double* co = M.cphi + (sd * M.J + j) * 4;
+        const double a = co[0], b = co[1], c = co[2], dd = co[3];
+        const double S0 = a + t * (b + t * (c + t * dd));
+        const double S1 = b + t * (2.0 * c + 3.0 * dd * t);
+        const double S2 = c + 3.0 * dd * t;
+        const double D = P.f_step;
+        const double ph0 = wrap_2pi(S0 + (2.0 * kPi * fb) * tc);
+        const double ph1 = wrap_2pi(D * (S1 + 2.0 * kPi * tc));
+        const double ph2 = D * D * S2;
+        const double ph3 = D * D * D * dd;
+        float s0f, c0f;
+        sincosf((float)ph0, &s0f, &c0f);
+        rp.c0 = c0f;
+        rp.s0 = s0f;
+        rp.p1h = head_bits(ph1, 12);
+        rp.p1l = (float)(ph1 - (double)rp.p1h);
+        rp.p2h = head_bits(ph2, 13);
+        rp.p2l = (float)(ph2 - (double)rp.p2h);
+        rp.p3h = head_bits(ph3, 8);
+        rp.p3l = (float)(ph3 - (double)rp.p3h);
+      }
+      // ---- runs of the group, one bin per lane
+      float mq[kNodeQ * kMoments];
+      int cur_iv = -1;
+      if (kGrad) {
+#pragma unroll
+        for (int k = 0; k < kNodeQ * kMoments; ++k) mq[k] = 0.0f;
+      }
+      const int last = min(nc, first + kChunkMax);
+      for (int c = first; c < last; ++c) {
+        const int src = c - first;
+        RunPhase r;
+        r.c0 = __shfl_sync(0xffffffffu, rp.c0, src);
+        r.s0 = __shfl_sync(0xffffffffu, rp.s0, src);
+        r.p1h = __shfl_sync(0xffffffffu, rp.p1h, src);
+        r.p1l = __shfl_sync(0xffffffffu, rp.p1l, src);
+        r.p2h = __shfl_sync(0xffffffffu, rp.p2h, src);
+        r.p2l = __shfl_sync(0xffffffffu, rp.p2l, src);
+        r.p3h = __shfl_sync(0xffffffffu, rp.p3h, src);
+        r.p3l = __shfl_sync(0xffffffffu, rp.p3l, src);
+        const int j = M.ch_iv[c];
+        const int kb = M.ch_begin[c];
+        const int len = M.ch_len[c];
+        if (kGrad && j != cur_iv) {
+          if (cur_iv >= 0) {
+            // flush the previous interval's moments
+#pragma unroll
+            for (int k = 0; k < kNodeQ * kMoments; ++k) {
+              float x = mq[k];
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+              if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, (double)x);
+              mq[k] = 0.0f;
+            }
+          }
+          cur_iv = j;
+        }
+        const int64_t i = (int64_t)kb + lane;
+        if (lane < len && i < kcut) {
+          const float t = M.bin_t[i];
+          const float u = (float)lane;
+          const float u2 = u * u, u3 = u2 * u;
+          const float del = reduce_exact(r.p1h * u) + reduce_exact(r.p2h * u2) + reduce_exact(r.p3h * u3) +
+                            (r.p1l * u + r.p2l * u2 + r.p3l * u3);
+          float sd_, cd_;
+          sincosf(del, &sd_, &cd_);
+          const float cph = r.c0 * cd_ - r.s0 * sd_;
+          const float sph = r.s0 * cd_ + r.c0 * sd_;
+          const float4* G = M.cg + (sd * M.J + j) * 6;
+          float term = 0.0f;
+          float aphi = 0.0f;
+          float ag[6];
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
+            const float gr = cr.x + t * (cr.y + t * (cr.z + t * cr.w));
+            const float gi = ci.x + t * (ci.y + t * (ci.z + t * ci.w));
+            const float hr = gr * cph + gi * sph;
+            const float hi = gi * cph - gr * sph;
+            const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
+            const float2 dv = M.dat[off];
+            const float w = M.wgt[off];
+            const float er = dv.x - hr, ei = dv.y - hi;
+            term = fmaf(er * er + ei * ei, w, term);
+            if (kGrad) {
+              ag[2 * ch] = w * (er * cph - ei * sph);
+              ag[2 * ch + 1] = w * (er * sph + ei * cph);
+              aphi = fmaf(w, dv.x * hi - dv.y * hr, aphi);
+            }
+          }
+          // compensated accumulation
+          const float yk = term - comp;
+          const float tk = acc + yk;
+          comp = (tk - acc) - yk;
+          acc = tk;
+          if (kGrad) {
+            const float tp[kMoments] = {1.0f, t, t * t, t * t * t};
+#pragma unroll
+            for (int p = 0; p < kMoments; ++p) {
+              mq[0 * kMoments + p] = fmaf(aphi, tp[p], mq[0 * kMoments + p]);
+#pragma unroll
+              for (int qq = 0; qq < 6; ++qq) mq[(1 + qq) * kMoments + p] = fmaf(ag[qq], tp[p], mq[(1 + qq) * kMoments + p]);
+            }
+          }
+        }
+      }
+      if (kGrad && cur_iv >= 0) {
+#pragma unroll
+        for (int k = 0; k < kNodeQ * kMoments; ++k) {
+          float x = mq[k];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+          if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, (double)x);
+        }
+      }
+    }
+  }
+  // deterministic reduction: lanes (FP64) -> warps -> block partial
+  double v = (double)acc - (double)comp;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0.0;
+#pragma unroll
+    for (int w = 0; w < kMixThreads / 32; ++w) x += red[w];
+    M.part[(size_t)s * M.nblk_dense + blockIdx.x] = x;
+  }
+}
+
+__global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B,
+                                 double* __restrict__ lnl, int32_t* __restrict__ status) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  const SampleBlock<double>& b = blocks[s];
+  if (b.status != kSampleOk) {
+    lnl[s] = -INFINITY;
+    if (status) status[s] = b.status;
+    return;
+  }
+  double acc = 0.0;
+  for (int k = 0; k < M.nblk_dense; ++k) acc += M.part[(size_t)s * M.nblk_dense + k];
+  const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
+  lnl[s] = v;
+  if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
+}
+
+__global__ void k_mixed_grad_finalize(MixedDev M, const SampleBlock<Dual<kGradTangents>>* __restrict__ blocks,
+                                      int64_t B, int pass, double* __restrict__ grad) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  constexpr int NT = kGradTangents;
+  const bool ok = blocks[s].status == kSampleOk;
+  for (int k = 0; k < NT; ++k) {
+    const int pidx = pass * NT + k;
+    if (pidx >= 11) break;
+    double acc = 0.0;
+    if (ok) {
+      for (int d = 0; d < M.n_det; ++d) {
+        for (int b = 0; b < M.nblk_sparse; ++b)
+          acc += M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + b) * NT + k];
+        if (pidx == 10) acc += M.gdir[(size_t)s * M.n_det + d];
+      }
+    }
+    grad[11 * s + pidx] = acc;
+  }
+}
+
+// ------------------------------------------------------------------ data ingestion
+__global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __restrict__ data,
+                               const double* __restrict__ psd) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.nbins) return;
+  for (int ch = 0; ch < 3; ++ch) {
+    const size_t off = ((size_t)det * 3 + ch) * P.nbins + i;
+    const double2 v = data[ch * P.nbins + i];
+    M.dat[off] = make_float2((float)(v.x * M.scale), (float)(v.y * M.scale));
+    const double w = ((P.chan_mask >> ch) & 1) ? 1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale) : 0.0;
+    M.wgt[off] = (float)w;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+template <class X>
+static int alloc(MixedBuffers* mb, X** ptr, size_t count) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, sizeof(X) * (count ? count : 1));
+  if (e != cudaSuccess) {
+    set_error("mixed plan: cudaMalloc of %zu bytes failed: %s", sizeof(X) * count, cudaGetErrorString(e));
+    return PES_ENOMEM;
+  }
+  mb->allocs.push_back(p);
+  *ptr = reinterpret_cast<X*>(p);
+  return PES_OK;
+}
+
+int mixed_create(PesPlan* p) {
+  const PesPlanDesc& d = p->desc;
+  PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
+  PES_REQUIRE(d.k0 >= 1, "mixed plan: the grid must start above 0 Hz (k0 >= 1)");
+  PES_REQUIRE(d.nbins >= 8, "mixed plan: needs at least 8 bins");
+  MixedBuffers* mb = new MixedBuffers();
+  p->mixed = mb;
+  MixedDev& M = mb->dev;
+  const int64_t n = d.nbins;
+  const int J = d.n_sparse;
+  const int nd = d.n_det;
+  const int64_t B = d.max_batch;
+  M.J = J;
+  M.n_det = nd;
+  M.scale = 3.085677581491367e16 / (1.476625038050124729627979840144936351e3 * 4.925490947641266978197229498498379006e-6);
+  for (int k = 0; k < nd; ++k) mb->gen.gen20[k] = d.det[k].generation == 20;
+  // shared sparse grid, bin -> interval map, runs
+  const double flo = (double)d.k0 * d.f_step, fhi = (double)(d.k0 + n - 1) * d.f_step;
+  std::vector<double> nf(J);
+  for (int j = 0; j < J; ++j) nf[j] = flo * std::pow(fhi / flo, (double)j / (J - 1));
+  nf[0] = flo;
+  nf[J - 1] = fhi;
+  std::vector<float> bt(n);
+  std::vector<int32_t> cb, cl, ci;
+  int j = 0;
+  int run_iv = -1, run_len = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double f = (double)(d.k0 + i) * d.f_step;
+    while (j + 1 < J - 1 && nf[j + 1] <= f) ++j;
+    bt[i] = (float)(f - nf[j]);
+    if (j != run_iv || run_len == kChunkMax) {
+      cb.push_back((int32_t)i);
+      cl.push_back(0);
+      ci.push_back(j);
+      run_iv = j;
+      run_len = 0;
+    }
+    cl.back() += 1;
+    run_len += 1;
+  }
+  M.nchunks = (int32_t)cb.size();
+  M.nblk_dense = (int32_t)ceil_div(M.nchunks, (long long)kChunkMax * (kMixThreads / 32));
+  M.nblk_sparse = (int32_t)ceil_div(J, kSparseThreads);
+  int rc = PES_OK;
+  double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
+  int32_t *chb, *chl, *chi, *nsp, *nch;
+  float* bin_t;
+  float2* dat;
+  float* wgt;
+  float4* cg;
+  const size_t sd = (size_t)B * nd;
+  if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
+      (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
+      (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
+      (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * kScratchRows * J)) ||
+      (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) ||
+      (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
+      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
+      (rc = alloc(mb, &gpart, sd * M.nblk_sparse * kGradTangents)) || (rc = alloc(mb, &gdir, sd)))
+    return rc;
+  PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+  PES_CHECK_CUDA(cudaMemcpy(chb, cb.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
+  PES_CHECK_CUDA(cudaMemcpy(chl, cl.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
+  PES_CHECK_CUDA(cudaMemcpy(chi, ci.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
+  PES_CHECK_CUDA(cudaMemcpy(bin_t, bt.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  PES_CHECK_CUDA(cudaMemset(dat, 0, sizeof(float2) * nd * 3 * n));
+  PES_CHECK_CUDA(cudaMemset(wgt, 0, sizeof(float) * nd * 3 * n));
+  M.node_f = node_f;
+  M.ch_begin = chb;
+  M.ch_len = chl;
+  M.ch_iv = chi;
+  M.bin_t = bin_t;
+  M.dat = dat;
+  M.wgt = wgt;
+  M.nsp = nsp;
+  M.nch = nch;
+  M.yv = yv;
+  M.scr = scr;
+  M.cphi = cphi;
+  M.cg = cg;
+  M.mom = mom;
+  M.ybar = ybar;
+  M.part = part;
+  M.gpart = gpart;
+  M.gdir = gdir;
+  // the dense-path partial buffer is not needed; gradient set-up blocks are shared
+  return PES_OK;
+}
+
+void mixed_destroy(PesPlan* p) {
+  if (!p->mixed) return;
+  for (void* a : p->mixed->allocs) cudaFree(a);
+  delete p->mixed;
+  p->mixed = nullptr;
+}
+
+}  // namespace pes
+
+// Called from pes_plan_set_data with the caller's FP64 arrays.
+namespace pes {
+int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cudaStream_t st) {
+  MixedDev& M = p->mixed->dev;
+  k_mixed_ingest<<<ceil_div(p->desc.nbins, 256), 256, 0, st>>>(p->dev, M, det,
+                                                               reinterpret_cast<const double2*>(data), psd);
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
+int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* grad, int32_t* status,
+              cudaStream_t st) {
+  MixedDev& M = p->mixed->dev;
+  const GenArg& G = p->mixed->gen;
+  SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
+  {
+    ProfScope ps(p, kKSetup, st);
+    k_setup<double><<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B, 0, blocks);
+  }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKOther, st);
+    k_mixed_ranges<<<ceil_div(B, 64), 64, 0, st>>>(M, blocks, B);
+  }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKSparse, st);
+    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
+    k_sparse_fwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
+  }
+  PES_CHECK_LAUNCH();
+  const int64_t nsd = B * (int64_t)M.n_det * kNodeQ;
+  {
+    ProfScope ps(p, kKSpline, st);
+    k_spline_fit<<<ceil_div(nsd, 64), 64, 0, st>>>(M, B);
+  }
+  PES_CHECK_LAUNCH();
+  if (grad) PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(double) * B * M.n_det * M.J * kNodeQ * kMoments, st));
+  {
+    ProfScope ps(p, kKDenseMixed, st);
+    dim3 grid(M.nblk_dense, (unsigned)B);
+    if (grad)
+      k_dense_mixed<true><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks);
+    else
+      k_dense_mixed<false><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks);
+  }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKFinalize, st);
+    k_mixed_finalize<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, M, blocks, B, lnl, status);
+  }
+  PES_CHECK_LAUNCH();
+  if (!grad) return PES_OK;
+  {
+    ProfScope ps(p, kKAdjoint, st);
+    k_spline_adjoint<<<ceil_div(nsd, 64), 64, 0, st>>>(M, B, 4.0 * p->dev.df);
+  }
+  PES_CHECK_LAUNCH();
+  constexpr int NT = kGradTangents;
+  SampleBlock<Dual<NT>>* dblocks = reinterpret_cast<SampleBlock<Dual<NT>>*>(p->blocks);
+  for (int pass = 0; pass * NT < 11; ++pass) {
+    {
+      ProfScope ps(p, kKSetup, st);
+      k_setup<Dual<NT>><<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B, pass, dblocks);
+    }
+    PES_CHECK_LAUNCH();
+    {
+      ProfScope ps(p, kKAdjoint, st);
+      dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
+      k_sparse_bwd<NT><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, dblocks);
+    }
+    PES_CHECK_LAUNCH();
+    {
+      ProfScope ps(p, kKFinalize, st);
+      k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, dblocks, B, pass, grad);
+    }
+    PES_CHECK_LAUNCH();
+  }
+  return PES_OK;
 }
 
 }  // namespace pes

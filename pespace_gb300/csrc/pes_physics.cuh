@@ -15,10 +15,10 @@
 namespace pes {
 
 // ------------------------------------------------------------------ orbits
-// n[i] = unit vector of link i+1 (n1: 2->3, n2: 3->1, n3: 1->2); x[i] = node i+1.
+// n[i] = unit vector of link i+1 (n1: 2->3, n2: 3->1, n3: 1->2); xd[i] = node
+// i+1 relative to the constellation centre x0 (light-seconds, SSB axes).
 template <class T>
-PES_HD void constellation(const PesOrbit& o, const T& t, T n[3][3], T x[3][3]) {
-  T xd[3][3];
+PES_HD void constellation_parts(const PesOrbit& o, const T& t, T n[3][3], T xd[3][3], T x0[3]) {
   T c0, s0;
   T alpha = o.omega_revolution * t + o.revolution_initial;
   dsincos(alpha, &s0, &c0);
@@ -53,15 +53,26 @@ PES_HD void constellation(const PesOrbit& o, const T& t, T n[3][3], T x[3][3]) {
     }
   }
   const double inv_arm = 1.0 / o.arm_sec;
-  T x0[3] = {c0 * kAUsec, s0 * kAUsec, lift<T>(0.0)};
+  x0[0] = c0 * kAUsec;
+  x0[1] = s0 * kAUsec;
+  x0[2] = lift<T>(0.0);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     n[0][j] = (xd[2][j] - xd[1][j]) * inv_arm;
     n[1][j] = (xd[0][j] - xd[2][j]) * inv_arm;
     n[2][j] = (xd[1][j] - xd[0][j]) * inv_arm;
+  }
+}
+
+// Node positions in the SSB frame: x = xd + x0.
+template <class T>
+PES_HD void constellation(const PesOrbit& o, const T& t, T n[3][3], T x[3][3]) {
+  T xd[3][3], x0[3];
+  constellation_parts(o, t, n, xd, x0);
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
 #pragma unroll
     for (int k = 0; k < 3; ++k) x[k][j] = xd[k][j] + x0[j];
-  }
 }
 
 // e+ = p p - q q, ex = p q + q p (symmetric: 6 independent entries each), k.
@@ -103,12 +114,15 @@ PES_HD T sinc_ref(const T& x) {
 }
 
 // Six single-link responses of one time-shifted mode (hp, hc at f; tf already
-// includes t_c).  Order: 12, 21, 23, 32, 31, 13.
-template <class T>
-PES_HD void single_links(const PesOrbit& o, double f, const Cx<T>& hp, const Cx<T>& hc, const T& tf,
-                         const Polar<T>& pol, Cx<T> out[6]) {
-  T n[3][3], x[3][3];
-  constellation(o, tf, n, x);
+// includes t_c).  Order: 12, 21, 23, 32, 31, 13.  With kFactorDoppler the
+// propagation delays use node positions relative to the constellation centre
+// and the centre's delay k.x0 is returned instead (the links then miss the
+// factor exp(-2 pi i f k.x0)); otherwise the links are those of antenna.py.
+template <bool kFactorDoppler, class T>
+PES_HD void single_links_impl(const PesOrbit& o, double f, const Cx<T>& hp, const Cx<T>& hc, const T& tf,
+                              const Polar<T>& pol, Cx<T> out[6], T* kx0_out) {
+  T n[3][3], xd[3][3], x0[3];
+  constellation_parts(o, tf, n, xd, x0);
   Cx<T> nh[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -118,12 +132,19 @@ PES_HD void single_links(const PesOrbit& o, double f, const Cx<T>& hp, const Cx<
   T kn[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) kn[i] = pol.k[0] * n[i][0] + pol.k[1] * n[i][1] + pol.k[2] * n[i][2];
-  T kx[3];  // k.(x1+x2), k.(x2+x3), k.(x3+x1)
+  T kx[3];  // k.(x1+x2), k.(x2+x3), k.(x3+x1)  (or with xd when factoring)
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const int a = i, b = (i + 1) % 3;
-    kx[i] = pol.k[0] * (x[a][0] + x[b][0]) + pol.k[1] * (x[a][1] + x[b][1]) + pol.k[2] * (x[a][2] + x[b][2]);
+    if (kFactorDoppler) {
+      kx[i] = pol.k[0] * (xd[a][0] + xd[b][0]) + pol.k[1] * (xd[a][1] + xd[b][1]) + pol.k[2] * (xd[a][2] + xd[b][2]);
+    } else {
+      kx[i] = pol.k[0] * ((xd[a][0] + x0[0]) + (xd[b][0] + x0[0])) +
+              pol.k[1] * ((xd[a][1] + x0[1]) + (xd[b][1] + x0[1])) +
+              pol.k[2] * ((xd[a][2] + x0[2]) + (xd[b][2] + x0[2]));
+    }
   }
+  if (kFactorDoppler) *kx0_out = pol.k[0] * x0[0] + pol.k[1] * x0[1];
   const double arm = o.arm_sec;
   const double pifL = kPi * f * arm;
   const double ce = -kPi * f;
@@ -141,12 +162,17 @@ PES_HD void single_links(const PesOrbit& o, double f, const Cx<T>& hp, const Cx<
     const int ni = nidx[pr];
     Cx<T> pre = cx(pifL * nh[ni].im, -(pifL * nh[ni].re));
     Cx<T> b = cmul(pre, e[pr]);
-    // sinc arguments: pair 0 (12: 1+kn3, 21: 1-kn3); pair 1 (23: 1+kn1, 32: 1-kn1); pair 2 (31: 1+kn2, 13: 1-kn2)
     T sp = sinc_ref(pifL * (1.0 + kn[ni]));
     T sm = sinc_ref(pifL * (1.0 - kn[ni]));
     out[2 * pr] = cscale(sp, b);
     out[2 * pr + 1] = cscale(sm, b);
   }
+}
+
+template <class T>
+PES_HD void single_links(const PesOrbit& o, double f, const Cx<T>& hp, const Cx<T>& hc, const T& tf,
+                         const Polar<T>& pol, Cx<T> out[6]) {
+  single_links_impl<false, T>(o, f, hp, hc, tf, pol, out, nullptr);
 }
 
 // TDI delay factor D = exp(-2 pi i f L) and generation prefactor.

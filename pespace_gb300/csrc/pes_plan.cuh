@@ -121,9 +121,90 @@ struct ProfScope {
 }  // namespace pes
 
 namespace pes {
+
+constexpr int kGradTangents = 4;  // tangents per gradient pass (3 passes for 11 parameters)
+
+// ------------------------------------------------------------------ scalar helpers
+template <class T> struct Seed;
+template <> struct Seed<double> {
+  PES_HD static double make(double v, int) { return v; }
+  static constexpr int N = 0;
+};
+template <int N> struct Seed<Dual<N>> {
+  PES_HD static Dual<N> make(double v, int slot) {
+    Dual<N> r = mkdual<N>(v);
+    if (slot >= 0 && slot < N) r.d[slot] = 1.0;
+    return r;
+  }
+  static constexpr int NT = N;
+};
+template <class T> struct NumTangents { static constexpr int value = 0; };
+template <int N> struct NumTangents<Dual<N>> { static constexpr int value = N; };
+
+template <class T> PES_HD void scalar_to(const T& x, double* out);
+template <> PES_HD void scalar_to<double>(const double& x, double* out) { out[0] = x; }
+template <int N> PES_HD void scalar_to(const Dual<N>& x, double* out) {
+  out[0] = x.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) out[1 + i] = x.d[i];
+}
+
+// true when parameters are in the model's domain
+PES_HD bool theta_in_domain(const double* t) {
+  for (int j = 0; j < 11; ++j)
+    if (!isfinite(t[j])) return false;
+  return t[1] >= 1.0 && t[1] <= 1000.0 && fabs(t[2]) < 1.0 && fabs(t[3]) < 1.0 && fabs(t[5]) <= 1.0 &&
+         fabs(t[7]) <= 1.0;
+}
+
+// bins [0, kcut) satisfy f <= fcut and Msec f <= 0.2 (both monotone in f)
+PES_HD int64_t find_kcut(const PlanDev& P, double Msec, double fcut) {
+  int64_t lo = 0, hi = P.nbins;  // invariant: live(i) for i < lo, !live(i) for i >= hi
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    double f = (double)(P.k0 + mid) * P.f_step;
+    bool live = (f <= fcut) && (Msec * f <= kMfCut);
+    if (live) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------------ kernels
+template <class T>
+__global__ void k_setup(PlanDev P, const double* __restrict__ theta, int64_t B, int pass,
+                        SampleBlock<T>* __restrict__ blocks) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  constexpr int NT = NumTangents<T>::value;
+  double raw[11];
+  for (int j = 0; j < 11; ++j) raw[j] = theta[11 * s + j];
+  SampleBlock<T>& b = blocks[s];
+  if (!theta_in_domain(raw)) {
+    b.status = kSampleOutOfDomain;
+    b.kcut = 0;
+    b.fcut = 0.0;
+    return;
+  }
+  T th[11];
+  for (int j = 0; j < 11; ++j) th[j] = Seed<T>::make(raw[j], NT > 0 ? j - pass * NT : -1);
+  phenomd_setup<T>(th, P.f_ref, b.wf);
+  T sb = th[7];
+  T cb = dsqrt((1.0 - sb) * (1.0 + sb));
+  make_polar<T>(th[6], sb, cb, th[8], b.pol);
+  b.tc = th[10];
+  const double Msec = val(b.wf.Msec);
+  const double fmax = (double)(P.k0 + P.nbins - 1) * P.f_step + 1.0;
+  double fcut = fmax;
+  if (P.cut_factor > 0.0) fcut = fmin(fmax, P.cut_factor * val(b.wf.fRD) / Msec);
+  b.fcut = fcut;
+  b.kcut = find_kcut(P, Msec, fcut);
+  b.status = kSampleOk;
+}
+
+
 int mixed_create(PesPlan* p);
 void mixed_destroy(PesPlan* p);
-int mixed_set_data(PesPlan* p, cudaStream_t st);
+int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cudaStream_t st);
 int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* grad, int32_t* status,
               cudaStream_t st);
 }  // namespace pes
