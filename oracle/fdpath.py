@@ -101,7 +101,7 @@ def lib():
         L.oracle_tdi.argtypes = [vp, i64, d, ctypes.c_int, ctypes.c_int, vp, vp]
         L.oracle_whittle.argtypes = [vp, vp, vp, ctypes.c_int, i64, d]
         L.oracle_whittle.restype = d
-        L.oracle_phenomd.argtypes = [vp, vp, i64, d, d, vp, vp, vp, vp]
+        L.oracle_phenomd.argtypes = [vp, vp, i64, d, d, vp, vp, vp, vp, vp]
         L.oracle_model_tdi.argtypes = [P(OraclePlan), ctypes.c_int, ctypes.c_int, vp, vp]
         L.oracle_lnl_batch.argtypes = [P(OraclePlan), vp, i64, vp, vp, ctypes.c_int]
         _lib = L
@@ -193,17 +193,22 @@ def whittle(d, h, S, df):
     return lib().oracle_whittle(_p(d), _p(h), _p(S), d.shape[0], d.shape[1], df)
 
 
-def phenomd(theta, freqs, f_ref, f_cut_hz=np.inf):
+def phenomd(theta, freqs, f_ref, f_cut_hz=np.inf, amp_psi=False):
+    """IMRPhenomD container (hp, hc, tf) and set-up info; with amp_psi also the
+    (2,2) amplitude and unwrapped phase Psi (h22 = A exp(-i Psi)) per frequency."""
     theta = np.ascontiguousarray(theta, dtype=np.float64)
     freqs = np.ascontiguousarray(freqs, dtype=np.float64)
     hp = np.zeros(freqs.size, dtype=np.complex128)
     hc = np.zeros(freqs.size, dtype=np.complex128)
     tf = np.zeros(freqs.size)
     info = np.zeros(18)
+    ap = np.zeros((freqs.size, 2)) if amp_psi else None
     lib().oracle_phenomd(_p(theta), _p(freqs), freqs.size, f_ref, float(min(f_cut_hz, 1e300)), _p(hp), _p(hc),
-                         _p(tf), _p(info))
+                         _p(tf), _p(info), _p(ap) if amp_psi else None)
     keys = ["M_sec", "fRD", "fDM", "fpeak", "t0", "eta", "gamma1", "gamma2", "gamma3",
             "d0", "d1", "d2", "d3", "d4", "C1Int", "C2Int", "C1MRD", "C2MRD"]
+    if amp_psi:
+        return hp, hc, tf, dict(zip(keys, info)), ap[:, 0], ap[:, 1]
     return hp, hc, tf, dict(zip(keys, info))
 
 

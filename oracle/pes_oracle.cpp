@@ -623,7 +623,8 @@ void phenomd_setup(const T* th, double f_ref, PhenomD<T>& p) {
 // Plus/cross polarisations and t(f) of the (2,2) waveform at frequency f [Hz];
 // zero above f_cut_hz.  Returns false when the bin is cut.
 template <class T>
-bool phenomd_eval(const PhenomD<T>& p, double f, double f_cut_hz, Cx<T>& hp, Cx<T>& hc, T& tf) {
+bool phenomd_eval(const PhenomD<T>& p, double f, double f_cut_hz, Cx<T>& hp, Cx<T>& hc, T& tf,
+                  T* amp_out = nullptr, T* psi_out = nullptr) {
   T Mf = p.M_sec * f;
   if (f > f_cut_hz || Mf > MF_CUT) {
     hp = Cx<T>{T(0.0), T(0.0)};
@@ -636,6 +637,8 @@ bool phenomd_eval(const PhenomD<T>& p, double f, double f_cut_hz, Cx<T>& hp, Cx<
   T amp = p.amp_scale / (Mf * sqrt(v)) * amp_hat(p, Mf);
   T psi = phi_full(p, Mf) - p.t0 * (Mf - p.MfRef) - p.phi_shift;
   tf = p.M_sec / (2.0 * PI) * (dphi_full(p, Mf) - p.t0);
+  if (amp_out) *amp_out = amp;
+  if (psi_out) *psi_out = psi;
   T c = cos(psi), s = sin(psi);
   // h22 = amp e^{-i psi}; hp = pfac h22, hc = -i cfac h22
   hp = Cx<T>{p.pfac * amp * c, -(p.pfac * amp * s)};
@@ -794,13 +797,14 @@ double oracle_whittle(const double* d, const double* h, const double* S, int nch
 
 // PhenomD container on arbitrary frequencies; hp, hc complex interleaved.
 int oracle_phenomd(const double* th, const double* f, int64_t n, double f_ref, double f_cut_hz, double* hp, double* hc,
-                   double* tf, double* info) {
+                   double* tf, double* info, double* amp_psi) {
   PhenomD<double> p;
   phenomd_setup<double>(th, f_ref, p);
   for (int64_t i = 0; i < n; ++i) {
     Cx<double> a, b;
-    double t;
-    phenomd_eval<double>(p, f[i], f_cut_hz, a, b, t);
+    double t, am = 0.0, ps = 0.0;
+    phenomd_eval<double>(p, f[i], f_cut_hz, a, b, t, &am, &ps);
+    if (amp_psi) { amp_psi[2 * i] = am; amp_psi[2 * i + 1] = ps; }
     hp[2 * i] = a.re; hp[2 * i + 1] = a.im;
     hc[2 * i] = b.re; hc[2 * i + 1] = b.im;
     tf[i] = t;

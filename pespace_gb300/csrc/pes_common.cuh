@@ -22,63 +22,70 @@ constexpr double kEulerGamma = 0.5772156649015329;
 constexpr double kAUsec = kAU / kCSI;  // orbit.py:12
 
 // ------------------------------------------------------------------ dual numbers
-template <int N>
+// Forward-mode dual number: FP64 value and N tangents of type D (double for
+// exact derivatives; float to run the tangent arithmetic on the FP32 pipes
+// while the value stays FP64).
+template <int N, class D = double>
 struct Dual {
   double v;
-  double d[N];
+  D d[N];
 };
+template <int N> using DualF = Dual<N, float>;
 
 PES_HD double val(double x) { return x; }
-template <int N> PES_HD double val(const Dual<N>& x) { return x.v; }
+template <int N, class D> PES_HD double val(const Dual<N, D>& x) { return x.v; }
 
-template <int N>
-PES_HD Dual<N> mkdual(double x) {
-  Dual<N> r;
+template <int N, class D = double>
+PES_HD Dual<N, D> mkdual(double x) {
+  Dual<N, D> r;
   r.v = x;
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = 0.0;
+  for (int i = 0; i < N; ++i) r.d[i] = D(0);
   return r;
 }
 
-template <int N> PES_HD Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v + b.v;
+#define PES_DUAL template <int N, class D> PES_HD
+PES_DUAL Dual<N, D> operator+(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v + b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
-template <int N> PES_HD Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v - b.v;
+PES_DUAL Dual<N, D> operator-(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v - b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
-template <int N> PES_HD Dual<N> operator-(const Dual<N>& a) { Dual<N> r; r.v = -a.v;
+PES_DUAL Dual<N, D> operator-(const Dual<N, D>& a) { Dual<N, D> r; r.v = -a.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
-template <int N> PES_HD Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v * b.v;
+PES_DUAL Dual<N, D> operator*(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v * b.v;
+  const D av = D(a.v), bv = D(b.v);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i]; return r; }
-template <int N> PES_HD Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v / b.v; const double ib = 1.0 / b.v;
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bv + av * b.d[i]; return r; }
+PES_DUAL Dual<N, D> operator/(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v / b.v;
+  const D ib = D(1.0 / b.v), rv = D(r.v);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib; return r; }
-template <int N> PES_HD Dual<N> operator+(const Dual<N>& a, double b) { Dual<N> r = a; r.v = a.v + b; return r; }
-template <int N> PES_HD Dual<N> operator+(double a, const Dual<N>& b) { Dual<N> r = b; r.v = a + b.v; return r; }
-template <int N> PES_HD Dual<N> operator-(const Dual<N>& a, double b) { Dual<N> r = a; r.v = a.v - b; return r; }
-template <int N> PES_HD Dual<N> operator-(double a, const Dual<N>& b) { Dual<N> r = -b; r.v = a - b.v; return r; }
-template <int N> PES_HD Dual<N> operator*(const Dual<N>& a, double b) { Dual<N> r; r.v = a.v * b;
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - rv * b.d[i]) * ib; return r; }
+PES_DUAL Dual<N, D> operator+(const Dual<N, D>& a, double b) { Dual<N, D> r = a; r.v = a.v + b; return r; }
+PES_DUAL Dual<N, D> operator+(double a, const Dual<N, D>& b) { Dual<N, D> r = b; r.v = a + b.v; return r; }
+PES_DUAL Dual<N, D> operator-(const Dual<N, D>& a, double b) { Dual<N, D> r = a; r.v = a.v - b; return r; }
+PES_DUAL Dual<N, D> operator-(double a, const Dual<N, D>& b) { Dual<N, D> r = -b; r.v = a - b.v; return r; }
+PES_DUAL Dual<N, D> operator*(const Dual<N, D>& a, double b) { Dual<N, D> r; r.v = a.v * b; const D bb = D(b);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b; return r; }
-template <int N> PES_HD Dual<N> operator*(double a, const Dual<N>& b) { Dual<N> r; r.v = a * b.v;
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bb; return r; }
+PES_DUAL Dual<N, D> operator*(double a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a * b.v; const D aa = D(a);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a * b.d[i]; return r; }
-template <int N> PES_HD Dual<N> operator/(const Dual<N>& a, double b) { Dual<N> r; r.v = a.v / b;
+  for (int i = 0; i < N; ++i) r.d[i] = aa * b.d[i]; return r; }
+PES_DUAL Dual<N, D> operator/(const Dual<N, D>& a, double b) { Dual<N, D> r; r.v = a.v / b; const D ib = D(1.0 / b);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / b; return r; }
-template <int N> PES_HD Dual<N> operator/(double a, const Dual<N>& b) { return mkdual<N>(a) / b; }
-template <int N> PES_HD bool operator<(const Dual<N>& a, double b) { return a.v < b; }
-template <int N> PES_HD bool operator<=(const Dual<N>& a, double b) { return a.v <= b; }
-template <int N> PES_HD bool operator>(const Dual<N>& a, double b) { return a.v > b; }
-template <int N> PES_HD bool operator>=(const Dual<N>& a, double b) { return a.v >= b; }
-template <int N> PES_HD bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
-template <int N> PES_HD bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib; return r; }
+PES_DUAL Dual<N, D> operator/(double a, const Dual<N, D>& b) { return mkdual<N, D>(a) / b; }
+PES_DUAL bool operator<(const Dual<N, D>& a, double b) { return a.v < b; }
+PES_DUAL bool operator<=(const Dual<N, D>& a, double b) { return a.v <= b; }
+PES_DUAL bool operator>(const Dual<N, D>& a, double b) { return a.v > b; }
+PES_DUAL bool operator>=(const Dual<N, D>& a, double b) { return a.v >= b; }
+PES_DUAL bool operator<(const Dual<N, D>& a, const Dual<N, D>& b) { return a.v < b.v; }
+PES_DUAL bool operator>=(const Dual<N, D>& a, const Dual<N, D>& b) { return a.v >= b.v; }
 
-template <int N> PES_HD Dual<N> chain1(const Dual<N>& a, double fv, double dfv) { Dual<N> r; r.v = fv;
+PES_DUAL Dual<N, D> chain1(const Dual<N, D>& a, double fv, double dfv) { Dual<N, D> r; r.v = fv; const D df = D(dfv);
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * dfv; return r; }
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * df; return r; }
 
 // double overloads (device: CUDA libdevice; host: libm)
 PES_HD double dsin(double x) { return ::sin(x); }
@@ -98,21 +105,22 @@ PES_HD double datan(double x) { return ::atan(x); }
 PES_HD double dpow(double x, double p) { return ::pow(x, p); }
 PES_HD double dabs(double x) { return ::fabs(x); }
 
-template <int N> PES_HD Dual<N> dsin(const Dual<N>& a) { double s, c; dsincos(a.v, &s, &c); return chain1(a, s, c); }
-template <int N> PES_HD Dual<N> dcos(const Dual<N>& a) { double s, c; dsincos(a.v, &s, &c); return chain1(a, c, -s); }
-template <int N> PES_HD void dsincos(const Dual<N>& a, Dual<N>* s, Dual<N>* c) {
+PES_DUAL Dual<N, D> dsin(const Dual<N, D>& a) { double s, c; dsincos(a.v, &s, &c); return chain1(a, s, c); }
+PES_DUAL Dual<N, D> dcos(const Dual<N, D>& a) { double s, c; dsincos(a.v, &s, &c); return chain1(a, c, -s); }
+PES_DUAL void dsincos(const Dual<N, D>& a, Dual<N, D>* s, Dual<N, D>* c) {
   double sv, cv; dsincos(a.v, &sv, &cv); *s = chain1(a, sv, cv); *c = chain1(a, cv, -sv); }
-template <int N> PES_HD Dual<N> dexp(const Dual<N>& a) { double e = ::exp(a.v); return chain1(a, e, e); }
-template <int N> PES_HD Dual<N> dlog(const Dual<N>& a) { return chain1(a, ::log(a.v), 1.0 / a.v); }
-template <int N> PES_HD Dual<N> dsqrt(const Dual<N>& a) { double s = ::sqrt(a.v); return chain1(a, s, 0.5 / s); }
-template <int N> PES_HD Dual<N> dcbrt(const Dual<N>& a) { double c = ::cbrt(a.v); return chain1(a, c, 1.0 / (3.0 * c * c)); }
-template <int N> PES_HD Dual<N> datan(const Dual<N>& a) { return chain1(a, ::atan(a.v), 1.0 / (1.0 + a.v * a.v)); }
-template <int N> PES_HD Dual<N> dpow(const Dual<N>& a, double p) { double q = ::pow(a.v, p); return chain1(a, q, p * q / a.v); }
-template <int N> PES_HD Dual<N> dabs(const Dual<N>& a) { return a.v < 0.0 ? -a : a; }
+PES_DUAL Dual<N, D> dexp(const Dual<N, D>& a) { double e = ::exp(a.v); return chain1(a, e, e); }
+PES_DUAL Dual<N, D> dlog(const Dual<N, D>& a) { return chain1(a, ::log(a.v), 1.0 / a.v); }
+PES_DUAL Dual<N, D> dsqrt(const Dual<N, D>& a) { double s = ::sqrt(a.v); return chain1(a, s, 0.5 / s); }
+PES_DUAL Dual<N, D> dcbrt(const Dual<N, D>& a) { double c = ::cbrt(a.v); return chain1(a, c, 1.0 / (3.0 * c * c)); }
+PES_DUAL Dual<N, D> datan(const Dual<N, D>& a) { return chain1(a, ::atan(a.v), 1.0 / (1.0 + a.v * a.v)); }
+PES_DUAL Dual<N, D> dpow(const Dual<N, D>& a, double p) { double q = ::pow(a.v, p); return chain1(a, q, p * q / a.v); }
+PES_DUAL Dual<N, D> dabs(const Dual<N, D>& a) { return a.v < 0.0 ? -a : a; }
+#undef PES_DUAL
 
 template <class T> struct Lift { PES_HD static T from(double x); };
 template <> struct Lift<double> { PES_HD static double from(double x) { return x; } };
-template <int N> struct Lift<Dual<N>> { PES_HD static Dual<N> from(double x) { return mkdual<N>(x); } };
+template <int N, class D> struct Lift<Dual<N, D>> { PES_HD static Dual<N, D> from(double x) { return mkdual<N, D>(x); } };
 template <class T> PES_HD T lift(double x) { return Lift<T>::from(x); }
 
 // ------------------------------------------------------------------ complex

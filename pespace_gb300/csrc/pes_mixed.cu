@@ -29,6 +29,12 @@ constexpr int kMixThreads = 128;  // 4 warps; each warp owns 32 consecutive runs
 constexpr int kMoments = 4;       // t^0..t^3
 constexpr int kSparseThreads = 128;
 constexpr int kScratchRows = 5;   // doubles per node in the per-(sample, det, q) spline scratch
+// Gradient: one pass with FP64 values and FP32 tangents for the 9 parameters
+// that enter the node quantities non-trivially; ln D_L (G ~ 1/D_L) and phi_c
+// (Phi_s shifts by -2 phi_c) are applied analytically.
+constexpr int kMixNT = 9;
+__device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
+using GradScalar = DualF<kMixNT>;
 
 struct MixedDev {
   int32_t J;                // nodes
@@ -50,11 +56,13 @@ struct MixedDev {
   double* yv;               // [B][n_det][7][J] node values
   double* scr;              // [B][n_det][7][5 J] spline scratch
   double* cphi;             // [B][n_det][J][4] phase spline coefficients (FP64)
-  float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32)
+  float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32: a_hi, b, c, d)
+  float* cglo;              // [B][n_det][J][6] a - a_hi (the value at the left node in float-float)
   double* mom;              // [B][n_det][J][7][4] adjoint moments
   double* ybar;             // [B][n_det][7][J] node adjoints
   double* part;             // [B][nblk_dense] lnL partials
-  double* gpart;            // [B][n_det][nblk_sparse][kGradTangents] gradient partials
+  double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
+  void* gblocks;            // [B] SampleBlock<GradScalar>
   double* gdir;             // [B][n_det] direct t_c term of the gradient
 };
 
@@ -118,45 +126,89 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
   for (int q = 0; q < kNodeQ; ++q) out[(size_t)q * M.J + j] = y[q];
 }
 
-// Backward: recompute node values with NT tangents and contract with the node adjoints.
-template <int NT>
-__global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G,
-                                                               const SampleBlock<Dual<NT>>* __restrict__ blocks) {
-  __shared__ SampleBlock<Dual<NT>> sb;
-  __shared__ double red[kSparseThreads / 32][NT];
+// Gradient set-up: per sample, the coefficient block with exact FP64
+// tangents, stored with FP32 tangents for the node kernel.
+__global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_t B,
+                             SampleBlock<GradScalar>* __restrict__ out) {
+  using TD = Dual<kMixNT, double>;
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  double raw[11];
+  for (int j = 0; j < 11; ++j) raw[j] = theta[11 * s + j];
+  SampleBlock<GradScalar>& o = out[s];
+  if (!theta_in_domain(raw)) {
+    o.status = kSampleOutOfDomain;
+    return;
+  }
+  TD th[11];
+  for (int j = 0; j < 11; ++j) {
+    int slot = -1;
+    for (int k = 0; k < kMixNT; ++k)
+      if (kSlotParam[k] == j) slot = k;
+    th[j] = Seed<TD>::make(raw[j], slot);
+  }
+  PhenomDCoef<TD> wf;
+  phenomd_setup<TD>(th, P.f_ref, wf);
+  Polar<TD> pol;
+  TD sb = th[7];
+  TD cb = dsqrt((1.0 - sb) * (1.0 + sb));
+  make_polar<TD>(th[6], sb, cb, th[8], pol);
+  static_assert(sizeof(PhenomDCoef<TD>) / sizeof(TD) == sizeof(PhenomDCoef<GradScalar>) / sizeof(GradScalar),
+                "coefficient block must be an array of scalars");
+  static_assert(sizeof(Polar<TD>) / sizeof(TD) == sizeof(Polar<GradScalar>) / sizeof(GradScalar),
+                "polarisation block must be an array of scalars");
+  auto narrow = [](const TD* a, GradScalar* b, int n) {
+    for (int k = 0; k < n; ++k) {
+      b[k].v = a[k].v;
+      for (int i = 0; i < kMixNT; ++i) b[k].d[i] = (float)a[k].d[i];
+    }
+  };
+  narrow(reinterpret_cast<const TD*>(&wf), reinterpret_cast<GradScalar*>(&o.wf),
+         sizeof(PhenomDCoef<TD>) / sizeof(TD));
+  narrow(reinterpret_cast<const TD*>(&pol), reinterpret_cast<GradScalar*>(&o.pol), sizeof(Polar<TD>) / sizeof(TD));
+  narrow(&th[10], &o.tc, 1);
+  o.status = kSampleOk;
+}
+
+// Backward: recompute the node quantities with tangents and contract with the node adjoints.
+__global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G) {
+  __shared__ SampleBlock<GradScalar> sb;
+  __shared__ double red[kSparseThreads / 32][11];
   const int s = blockIdx.z, d = blockIdx.y;
-  load_block(blocks, s, sb);
+  load_block(reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), s, sb);
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
-  double acc[NT];
+  double acc[11];
 #pragma unroll
-  for (int k = 0; k < NT; ++k) acc[k] = 0.0;
+  for (int k = 0; k < 11; ++k) acc[k] = 0.0;
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
-    Dual<NT> y[kNodeQ];
-    node_eval<Dual<NT>>(P, M, sb, d, G.gen20[d], M.node_f[j], y);
+    GradScalar y[kNodeQ];
+    node_eval<GradScalar>(P, M, sb, d, G.gen20[d], M.node_f[j], y);
     const double* yb = M.ybar + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
 #pragma unroll
     for (int q = 0; q < kNodeQ; ++q) {
       const double w = yb[(size_t)q * M.J + j];
 #pragma unroll
-      for (int k = 0; k < NT; ++k) acc[k] += w * y[q].d[k];
+      for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += w * (double)y[q].d[k];
+      if (q > 0) acc[4] -= w * y[q].v;  // G ~ 1/D_L
+      else acc[9] -= 2.0 * w;           // Phi_s = ... - 2 phi_c
     }
   }
   const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
-  for (int k = 0; k < NT; ++k) {
+  for (int k = 0; k < 11; ++k) {
     double x = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (l == 0) red[wid][k] = x;
   }
   __syncthreads();
-  if (threadIdx.x < NT) {
+  if (threadIdx.x < 11) {
     double x = 0.0;
 #pragma unroll
     for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
-    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * kGradTangents + threadIdx.x] = x;
+    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + threadIdx.x] = x;
   }
 }
 
@@ -259,7 +311,9 @@ __global__ void k_spline_fit(MixedDev M, int64_t B) {
       o[2] = cc;
       o[3] = dc;
     } else {
-      M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4((float)a, (float)bc, (float)cc, (float)dc);
+      const float ahi = (float)a;
+      M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, (float)bc, (float)cc, (float)dc);
+      M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(a - (double)ahi);
     }
   }
 }
@@ -367,9 +421,13 @@ struct RunPhase {
   float p3h, p3l;         // cubic coefficient, head/tail
 };
 
-template <bool kGrad>
+// kMode 0: lnL partials; 1: lnL partials + adjoint moments; 2: write the model
+// h (unscaled, complex128 (n_det, 3, nbins)) to `model` (parity/debug path).
+template <int kMode>
 __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev M,
-                                                             const SampleBlock<double>* __restrict__ blocks) {
+                                                             const SampleBlock<double>* __restrict__ blocks,
+                                                             double2* __restrict__ model) {
+  constexpr bool kGrad = kMode == 1;
   __shared__ double red[kMixThreads / 32];
   const int s = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -400,10 +458,13 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         const double ph1 = wrap_2pi(D * (S1 + 2.0 * kPi * tc));
         const double ph2 = D * D * S2;
         const double ph3 = D * D * D * dd;
+        // anchor phasor: sincos of the float head, rotated by the (tiny) tail
+        const float h0 = (float)ph0;
+        const float l0 = (float)(ph0 - (double)h0);
         float s0f, c0f;
-        sincosf((float)ph0, &s0f, &c0f);
-        rp.c0 = c0f;
-        rp.s0 = s0f;
+        sincosf(h0, &s0f, &c0f);
+        rp.c0 = fmaf(-s0f, l0, c0f);
+        rp.s0 = fmaf(c0f, l0, s0f);
         rp.p1h = head_bits(ph1, 12);
         rp.p1l = (float)(ph1 - (double)rp.p1h);
         rp.p2h = head_bits(ph2, 13);
@@ -456,17 +517,25 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
                             (r.p1l * u + r.p2l * u2 + r.p3l * u3);
           float sd_, cd_;
           sincosf(del, &sd_, &cd_);
-          const float cph = r.c0 * cd_ - r.s0 * sd_;
-          const float sph = r.s0 * cd_ + r.c0 * sd_;
+          float cph = r.c0 * cd_ - r.s0 * sd_;
+          float sph = r.s0 * cd_ + r.c0 * sd_;
+          // FP32 sincos carries a small systematic magnitude excess (mean of
+          // s^2 + c^2 - 1 is about +1.8e-8): renormalise with one Newton step
+          // for 1/|e| so the model amplitude is unbiased.
+          const float m2 = fmaf(cph, cph, fmaf(sph, sph, -1.0f));  // |e|^2 - 1, one rounding
+          const float corr = -0.5f * m2;
+          cph = fmaf(corr, cph, cph);
+          sph = fmaf(corr, sph, sph);
           const float4* G = M.cg + (sd * M.J + j) * 6;
+          const float* Glo = M.cglo + (sd * M.J + j) * 6;
           float term = 0.0f;
           float aphi = 0.0f;
           float ag[6];
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
-            const float gr = cr.x + t * (cr.y + t * (cr.z + t * cr.w));
-            const float gi = ci.x + t * (ci.y + t * (ci.z + t * ci.w));
+            const float gr = cr.x + (Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w)));
+            const float gi = ci.x + (Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w)));
             const float hr = gr * cph + gi * sph;
             const float hi = gi * cph - gr * sph;
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
@@ -474,6 +543,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             const float w = M.wgt[off];
             const float er = dv.x - hr, ei = dv.y - hi;
             term = fmaf(er * er + ei * ei, w, term);
+            if (kMode == 2) model[off] = make_double2((double)hr / M.scale, (double)hi / M.scale);
             if (kGrad) {
               ag[2 * ch] = w * (er * cph - ei * sph);
               ag[2 * ch + 1] = w * (er * sph + ei * cph);
@@ -538,24 +608,19 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
 }
 
-__global__ void k_mixed_grad_finalize(MixedDev M, const SampleBlock<Dual<kGradTangents>>* __restrict__ blocks,
-                                      int64_t B, int pass, double* __restrict__ grad) {
+__global__ void k_mixed_grad_finalize(MixedDev M, int64_t B, double* __restrict__ grad) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
-  constexpr int NT = kGradTangents;
-  const bool ok = blocks[s].status == kSampleOk;
-  for (int k = 0; k < NT; ++k) {
-    const int pidx = pass * NT + k;
-    if (pidx >= 11) break;
+  const bool ok = reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks)[s].status == kSampleOk;
+  for (int p = 0; p < 11; ++p) {
     double acc = 0.0;
     if (ok) {
       for (int d = 0; d < M.n_det; ++d) {
-        for (int b = 0; b < M.nblk_sparse; ++b)
-          acc += M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + b) * NT + k];
-        if (pidx == 10) acc += M.gdir[(size_t)s * M.n_det + d];
+        for (int b = 0; b < M.nblk_sparse; ++b) acc += M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + b) * 11 + p];
+        if (p == 10) acc += M.gdir[(size_t)s * M.n_det + d];
       }
     }
-    grad[11 * s + pidx] = acc;
+    grad[11 * s + p] = acc;
   }
 }
 
@@ -592,6 +657,10 @@ int mixed_create(PesPlan* p) {
   PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
   PES_REQUIRE(d.k0 >= 1, "mixed plan: the grid must start above 0 Hz (k0 >= 1)");
   PES_REQUIRE(d.nbins >= 8, "mixed plan: needs at least 8 bins");
+  for (int k = 0; k < d.n_det; ++k)
+    PES_REQUIRE(d.det[k].orbit.kind == 0,
+                "mixed plan: detector %d has a geocentric orbit; its 3.65-day constellation rotation is not "
+                "resolved by the sparse grid, use the fp64 precision for it", k);
   MixedBuffers* mb = new MixedBuffers();
   p->mixed = mb;
   MixedDev& M = mb->dev;
@@ -633,19 +702,22 @@ int mixed_create(PesPlan* p) {
   int rc = PES_OK;
   double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
   int32_t *chb, *chl, *chi, *nsp, *nch;
+  SampleBlock<GradScalar>* gblk;
   float* bin_t;
   float2* dat;
   float* wgt;
   float4* cg;
+  float* cglo;
   const size_t sd = (size_t)B * nd;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
       (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * kScratchRows * J)) ||
-      (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) ||
+      (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
-      (rc = alloc(mb, &gpart, sd * M.nblk_sparse * kGradTangents)) || (rc = alloc(mb, &gdir, sd)))
+      (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
+      (rc = alloc(mb, &gblk, (size_t)B)))
     return rc;
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chb, cb.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
@@ -667,11 +739,13 @@ int mixed_create(PesPlan* p) {
   M.scr = scr;
   M.cphi = cphi;
   M.cg = cg;
+  M.cglo = cglo;
   M.mom = mom;
   M.ybar = ybar;
   M.part = part;
   M.gpart = gpart;
   M.gdir = gdir;
+  M.gblocks = gblk;
   // the dense-path partial buffer is not needed; gradient set-up blocks are shared
   return PES_OK;
 }
@@ -691,6 +765,26 @@ int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cud
   MixedDev& M = p->mixed->dev;
   k_mixed_ingest<<<ceil_div(p->desc.nbins, 256), 256, 0, st>>>(p->dev, M, det,
                                                                reinterpret_cast<const double2*>(data), psd);
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
+// Dense model of every detector for one parameter set: out (n_det, 3, nbins) complex.
+int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t st) {
+  MixedDev& M = p->mixed->dev;
+  const GenArg& G = p->mixed->gen;
+  SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
+  k_setup<double><<<1, 64, 0, st>>>(p->dev, theta_dev, 1, 0, blocks);
+  PES_CHECK_LAUNCH();
+  k_mixed_ranges<<<1, 64, 0, st>>>(M, blocks, 1);
+  PES_CHECK_LAUNCH();
+  k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
+  PES_CHECK_LAUNCH();
+  k_spline_fit<<<ceil_div((int64_t)M.n_det * kNodeQ, 64), 64, 0, st>>>(M, 1);
+  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
+  k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
+                                                                  reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
   return PES_OK;
 }
@@ -727,9 +821,9 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     ProfScope ps(p, kKDenseMixed, st);
     dim3 grid(M.nblk_dense, (unsigned)B);
     if (grad)
-      k_dense_mixed<true><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks);
+      k_dense_mixed<1><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
     else
-      k_dense_mixed<false><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks);
+      k_dense_mixed<0><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
   {
@@ -743,26 +837,23 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     k_spline_adjoint<<<ceil_div(nsd, 64), 64, 0, st>>>(M, B, 4.0 * p->dev.df);
   }
   PES_CHECK_LAUNCH();
-  constexpr int NT = kGradTangents;
-  SampleBlock<Dual<NT>>* dblocks = reinterpret_cast<SampleBlock<Dual<NT>>*>(p->blocks);
-  for (int pass = 0; pass * NT < 11; ++pass) {
-    {
-      ProfScope ps(p, kKSetup, st);
-      k_setup<Dual<NT>><<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B, pass, dblocks);
-    }
-    PES_CHECK_LAUNCH();
-    {
-      ProfScope ps(p, kKAdjoint, st);
-      dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
-      k_sparse_bwd<NT><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, dblocks);
-    }
-    PES_CHECK_LAUNCH();
-    {
-      ProfScope ps(p, kKFinalize, st);
-      k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, dblocks, B, pass, grad);
-    }
-    PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKSetup, st);
+    k_setup_grad<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B,
+                                                 reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks));
   }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKAdjoint, st);
+    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
+    k_sparse_bwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G);
+  }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKFinalize, st);
+    k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, B, grad);
+  }
+  PES_CHECK_LAUNCH();
   return PES_OK;
 }
 

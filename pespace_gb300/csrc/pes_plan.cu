@@ -375,10 +375,23 @@ int pes_plan_model_tdi(PesPlan* p, int32_t det, int32_t orthogonal, const double
                        void* stream) {
   PES_REQUIRE(p && theta && out, "pes_plan_model_tdi: null pointer");
   PES_REQUIRE(det >= 0 && det < p->desc.n_det, "pes_plan_model_tdi: detector out of range");
+  PES_REQUIRE(p->desc.precision == PES_PRECISION_FP64 || orthogonal,
+              "pes_plan_model_tdi: mixed plans model the A/E/T channels only");
   cudaStream_t st = as_stream(stream);
   double* d_theta = nullptr;
   PES_CHECK_CUDA(cudaMallocAsync(&d_theta, 11 * sizeof(double), st));
   PES_CHECK_CUDA(cudaMemcpyAsync(d_theta, theta, 11 * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (p->desc.precision == PES_PRECISION_MIXED) {
+    const size_t n3 = (size_t)3 * p->desc.nbins;
+    double* all = nullptr;
+    PES_CHECK_CUDA(cudaMallocAsync(&all, sizeof(double2) * p->desc.n_det * n3, st));
+    int rc = mixed_model(p, d_theta, all, st);
+    if (rc != PES_OK) return rc;
+    PES_CHECK_CUDA(cudaMemcpyAsync(out, all + 2 * n3 * det, sizeof(double2) * n3, cudaMemcpyDeviceToDevice, st));
+    PES_CHECK_CUDA(cudaFreeAsync(all, st));
+    PES_CHECK_CUDA(cudaFreeAsync(d_theta, st));
+    return PES_OK;
+  }
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
   k_setup<double><<<1, 1, 0, st>>>(p->dev, d_theta, 1, 0, blocks);
   PES_CHECK_LAUNCH();

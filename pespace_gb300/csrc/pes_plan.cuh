@@ -130,20 +130,20 @@ template <> struct Seed<double> {
   PES_HD static double make(double v, int) { return v; }
   static constexpr int N = 0;
 };
-template <int N> struct Seed<Dual<N>> {
-  PES_HD static Dual<N> make(double v, int slot) {
-    Dual<N> r = mkdual<N>(v);
-    if (slot >= 0 && slot < N) r.d[slot] = 1.0;
+template <int N, class D> struct Seed<Dual<N, D>> {
+  PES_HD static Dual<N, D> make(double v, int slot) {
+    Dual<N, D> r = mkdual<N, D>(v);
+    if (slot >= 0 && slot < N) r.d[slot] = D(1);
     return r;
   }
   static constexpr int NT = N;
 };
 template <class T> struct NumTangents { static constexpr int value = 0; };
-template <int N> struct NumTangents<Dual<N>> { static constexpr int value = N; };
+template <int N, class D> struct NumTangents<Dual<N, D>> { static constexpr int value = N; };
 
 template <class T> PES_HD void scalar_to(const T& x, double* out);
 template <> PES_HD void scalar_to<double>(const double& x, double* out) { out[0] = x; }
-template <int N> PES_HD void scalar_to(const Dual<N>& x, double* out) {
+template <int N, class D> PES_HD void scalar_to(const Dual<N, D>& x, double* out) {
   out[0] = x.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) out[1 + i] = x.d[i];
@@ -205,6 +205,7 @@ __global__ void k_setup(PlanDev P, const double* __restrict__ theta, int64_t B, 
 int mixed_create(PesPlan* p);
 void mixed_destroy(PesPlan* p);
 int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cudaStream_t st);
+int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t st);
 int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* grad, int32_t* status,
               cudaStream_t st);
 }  // namespace pes
