@@ -94,6 +94,26 @@ int64_t pes_whittle_workspace_len(int64_t n);
 int pes_whittle_lnl(const double* data, const double* response, const double* psd, int32_t n_chan, int64_t n,
                     double df, double* workspace, int64_t workspace_len, double* out, void* stream);
 
+/* Allocation-free variant of pes_whittle_lnl (no counterpart in the reference).
+ * For callers that may not allocate device memory at all: code running while a
+ * stream is being captured into a CUDA graph (cudaMalloc is not permitted
+ * there), and host runtimes that own the device memory pool and forbid
+ * libraries from allocating (an XLA/JAX FFI custom call, a taichi-managed
+ * context).  It needs no workspace argument: its scratch is a file-scope
+ * device array of PES_WHITTLE_NOALLOC_PARTIALS doubles (8 KB) that every GPU
+ * loading this library holds until the process exits.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress), so make
+ * the first call on each device before any stream capture.  All calls share
+ * the one array: calls whose kernels overlap on the GPU (different streams, or
+ * host threads) race and must be serialised by the caller.  The scratch needs
+ * no clearing (each call writes every partial it reads).
+ * Limits: 1 <= n_chan <= 3, 0 <= n <= PES_WHITTLE_NOALLOC_MAX_BINS; sizes
+ * outside them return PES_EINVAL with a message.  Calls no allocating routine. */
+#define PES_WHITTLE_NOALLOC_PARTIALS 1024
+#define PES_WHITTLE_NOALLOC_MAX_BINS 2147483647LL
+int pes_whittle_lnl_noalloc(const double* data, const double* response, const double* psd, int32_t n_chan, int64_t n,
+                            double df, double* out, void* stream);
+
 /* Waveform producer (the external tiwave `update_waveform` contract used at
  * pespace/inference/interface_bilby.py:97; container layout antenna.py:438-458):
  * IMRPhenomD (2,2) plus/cross polarisations and t(f) at `freqs`, t_c = 0,

@@ -3,6 +3,7 @@
 // IMRPhenomD waveform producer.  FP64 throughout, one thread per frequency.
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 
 #include "pes_abi_common.cuh"
 #include "pes_physics.cuh"
@@ -118,6 +119,37 @@ __global__ void k_whittle_final(const double* __restrict__ partial, int nblk, do
   for (int i = threadIdx.x; i < nblk; i += blockDim.x) acc += partial[i];
   double r = block_sum(acc, sh);
   if (threadIdx.x == 0) out[0] = scale * r;
+}
+
+// Scratch of the allocation-free Whittle entry point: one partial sum per block
+// of k_whittle_partial (at most kWhittleMaxBlocks).  8 KB that every device
+// which loads this library keeps until the process exits.
+constexpr int kNoAllocPartials = kWhittleMaxBlocks;
+static __device__ __align__(256) double g_whittle_scratch[kNoAllocPartials];
+
+// Device address of g_whittle_scratch for each device, looked up on the first
+// call made with that device current.
+constexpr int kMaxDevices = 64;
+static std::mutex g_scratch_mu;
+static double* g_scratch_ptr[kMaxDevices] = {};
+
+static int whittle_scratch(double** out) {
+  int dev = -1;
+  PES_CHECK_CUDA(cudaGetDevice(&dev));
+  PES_REQUIRE(dev >= 0 && dev < kMaxDevices, "pes_whittle_lnl_noalloc: device index %d unsupported", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (g_scratch_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_whittle_scratch);
+    if (e != cudaSuccess) {
+      set_error("pes_whittle_lnl_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
+                cudaGetErrorString(e));
+      return PES_ECUDA;
+    }
+    g_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return PES_OK;
 }
 
 struct ThetaArg {
@@ -238,6 +270,37 @@ int pes_whittle_lnl(const double* data, const double* response, const double* ps
                                                                  n_chan, n, per_block, workspace);
   PES_CHECK_LAUNCH();
   k_whittle_final<<<1, kWhittleThreads, 0, st>>>(workspace, (int)nblk, -2.0 * df, out);
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
+int pes_whittle_lnl_noalloc(const double* data, const double* response, const double* psd, int32_t n_chan,
+                            int64_t n, double df, double* out, void* stream) {
+  PES_REQUIRE(n_chan >= 1 && n_chan <= 3, "pes_whittle_lnl_noalloc: n_chan must be 1..3, got %d", n_chan);
+  PES_REQUIRE(n >= 0 && n <= PES_WHITTLE_NOALLOC_MAX_BINS,
+              "pes_whittle_lnl_noalloc: n = %lld outside [0, %lld]", (long long)n,
+              (long long)PES_WHITTLE_NOALLOC_MAX_BINS);
+  PES_REQUIRE(out, "pes_whittle_lnl_noalloc: null out");
+  const int64_t nblk = pes_whittle_workspace_len(n);
+  PES_REQUIRE(nblk <= kNoAllocPartials, "pes_whittle_lnl_noalloc: %lld partial sums exceed the %d-entry scratch",
+              (long long)nblk, kNoAllocPartials);
+  double* scratch = nullptr;
+  int rc = whittle_scratch(&scratch);
+  if (rc != PES_OK) return rc;
+  cudaStream_t st = as_stream(stream);
+  if (n == 0) {
+    PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
+    return PES_OK;
+  }
+  PES_REQUIRE(data && response && psd, "pes_whittle_lnl_noalloc: null pointer");
+  // every partial the final pass reads is written by the first pass, so the
+  // scratch needs no clearing between calls
+  const int64_t per_block = (n + nblk - 1) / nblk;
+  k_whittle_partial<<<(unsigned)nblk, kWhittleThreads, 0, st>>>(reinterpret_cast<const double2*>(data),
+                                                                 reinterpret_cast<const double2*>(response), psd,
+                                                                 n_chan, n, per_block, scratch);
+  PES_CHECK_LAUNCH();
+  k_whittle_final<<<1, kWhittleThreads, 0, st>>>(scratch, (int)nblk, -2.0 * df, out);
   PES_CHECK_LAUNCH();
   return PES_OK;
 }
