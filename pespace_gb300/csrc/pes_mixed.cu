@@ -64,6 +64,13 @@ struct MixedDev {
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
   double* gdir;             // [B][n_det] direct t_c term of the gradient
+  // Amplitude kink at f_peak: the transfer quantities carry C_q max(0, Mf - Mf_peak)^2
+  // (C_q = jump/2 * R_q, R_q = G_q(f_peak)/Ahat(f_peak)); it is removed from the
+  // node data before the spline fit and added back per bin.
+  double* kinkR;            // [B][n_det][6] R_q
+  double* kinkC;            // [B][n_det][6] C_q
+  float* kinkF;             // [B][n_det][8] Msec, Mf_peak, C_0..C_5 (FP32 copies for the dense stage)
+  double* kinkM;            // [B][n_det][18] dense adjoint moments: sum A_q x^2, sum A_q x f, sum A_q x
 };
 
 struct GenArg {
@@ -109,6 +116,36 @@ __device__ __forceinline__ void load_block(const SampleBlock<T>* blocks, int s, 
   for (int j = threadIdx.x; j < n8; j += blockDim.x) dst[j] = src[j];
 }
 
+// Kink coefficients per (sample, detector).
+__global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= B * (int64_t)M.n_det) return;
+  const int64_t s = t / M.n_det;
+  const int d = (int)(t % M.n_det);
+  const SampleBlock<double>& b = blocks[s];
+  double* R = M.kinkR + (size_t)t * 6;
+  double* C = M.kinkC + (size_t)t * 6;
+  float* F = M.kinkF + (size_t)t * 8;
+  for (int q = 0; q < 6; ++q) {
+    R[q] = 0.0;
+    C[q] = 0.0;
+    F[2 + q] = 0.0f;
+  }
+  F[0] = 0.0f;
+  F[1] = 1.0e30f;
+  if (b.status != kSampleOk) return;
+  double y[kNodeQ], ahat, jump;
+  node_eval<double>(P, M, b, d, G.gen20[d], b.wf.fpeak / b.wf.Msec, y);
+  amp_peak_jump<double>(b.wf, ahat, jump);
+  F[0] = (float)b.wf.Msec;
+  F[1] = (float)b.wf.fpeak;
+  for (int q = 0; q < 6; ++q) {
+    R[q] = y[1 + q] / ahat;
+    C[q] = 0.5 * jump * R[q];
+    F[2 + q] = (float)C[q];
+  }
+}
+
 // Forward: node values in FP64.  grid (ceil(J/128), n_det, B)
 __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedDev M, GenArg G,
                                                                const SampleBlock<double>* __restrict__ blocks) {
@@ -120,7 +157,14 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
   const int ns = M.nsp[s];
   if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J) return;
   double y[kNodeQ];
-  node_eval<double>(P, M, sb, d, G.gen20[d], M.node_f[j], y);
+  const double fj = M.node_f[j];
+  node_eval<double>(P, M, sb, d, G.gen20[d], fj, y);
+  const double xk = sb.wf.Msec * fj - sb.wf.fpeak;
+  if (xk > 0.0) {
+    const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) y[1 + q] -= C[q] * xk * xk;
+  }
   double* out = M.yv + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
 #pragma unroll
   for (int q = 0; q < kNodeQ; ++q) out[(size_t)q * M.J + j] = y[q];
@@ -171,7 +215,7 @@ __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_
 }
 
 // Backward: recompute the node quantities with tangents and contract with the node adjoints.
-__global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G) {
+__global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G, double wscale) {
   __shared__ SampleBlock<GradScalar> sb;
   __shared__ double red[kSparseThreads / 32][11];
   const int s = blockIdx.z, d = blockIdx.y;
@@ -184,7 +228,17 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
   for (int k = 0; k < 11; ++k) acc[k] = 0.0;
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
     GradScalar y[kNodeQ];
-    node_eval<GradScalar>(P, M, sb, d, G.gen20[d], M.node_f[j], y);
+    const double fj = M.node_f[j];
+    node_eval<GradScalar>(P, M, sb, d, G.gen20[d], fj, y);
+    const GradScalar xk = sb.wf.Msec * fj - sb.wf.fpeak;
+    if (xk.v > 0.0) {
+      GradScalar ahat, jump;
+      amp_peak_jump<GradScalar>(sb.wf, ahat, jump);
+      const GradScalar x2h = 0.5 * (xk * xk) * jump;
+      const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - R[q] * x2h;  // R_q held fixed
+    }
     const double* yb = M.ybar + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
 #pragma unroll
     for (int q = 0; q < kNodeQ; ++q) {
@@ -193,6 +247,21 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
       for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += w * (double)y[q].d[k];
       if (q > 0) acc[4] -= w * y[q].v;  // G ~ 1/D_L
       else acc[9] -= 2.0 * w;           // Phi_s = ... - 2 phi_c
+    }
+  }
+  // dense-side kink term C_q x^2 (x = Msec f - Mf_peak): one thread per (sample, detector)
+  if (blockIdx.x == 0 && threadIdx.x == 0 && sb.status == kSampleOk && ns >= 3) {
+    GradScalar ahat, jump;
+    amp_peak_jump<GradScalar>(sb.wf, ahat, jump);
+    const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
+    const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
+    const double* K = M.kinkM + ((size_t)s * M.n_det + d) * 18;
+    for (int q = 0; q < 6; ++q) {
+      const double K2 = wscale * K[q], K1f = wscale * K[6 + q], K1 = wscale * K[12 + q];
+      for (int k = 0; k < kMixNT; ++k)
+        acc[kSlotParam[k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
+                              2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
+      acc[4] -= C[q] * K2;  // C_q ~ 1/D_L
     }
   }
   const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -472,6 +541,18 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         rp.p3h = head_bits(ph3, 8);
         rp.p3l = (float)(ph3 - (double)rp.p3h);
       }
+      // ---- amplitude kink at f_peak (FP32 copies)
+      const float* KF = M.kinkF + sd * 8;
+      const float kMsec = KF[0], kMfpk = KF[1];
+      float kC[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) kC[q] = KF[2 + q];
+      const float fstep_f = (float)P.f_step;
+      float km[18];
+      if (kGrad) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) km[k] = 0.0f;
+      }
       // ---- runs of the group, one bin per lane
       float mq[kNodeQ * kMoments];
       int cur_iv = -1;
@@ -528,14 +609,17 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           sph = fmaf(corr, sph, sph);
           const float4* G = M.cg + (sd * M.J + j) * 6;
           const float* Glo = M.cglo + (sd * M.J + j) * 6;
+          const float fbin = (float)(P.k0 + i) * fstep_f;
+          const float xk = fmaf(kMsec, fbin, -kMfpk);
+          const float x2 = xk > 0.0f ? xk * xk : 0.0f;
           float term = 0.0f;
           float aphi = 0.0f;
           float ag[6];
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
-            const float gr = cr.x + (Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w)));
-            const float gi = ci.x + (Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w)));
+            const float gr = cr.x + fmaf(kC[2 * ch], x2, Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w)));
+            const float gi = ci.x + fmaf(kC[2 * ch + 1], x2, Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w)));
             const float hr = gr * cph + gi * sph;
             const float hi = gi * cph - gr * sph;
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
@@ -555,6 +639,15 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float tk = acc + yk;
           comp = (tk - acc) - yk;
           acc = tk;
+          if (kGrad && xk > 0.0f) {
+            const float xf = xk * fbin;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+              km[q] = fmaf(ag[q], x2, km[q]);
+              km[6 + q] = fmaf(ag[q], xf, km[6 + q]);
+              km[12 + q] = fmaf(ag[q], xk, km[12 + q]);
+            }
+          }
           if (kGrad) {
             const float tp[kMoments] = {1.0f, t, t * t, t * t * t};
 #pragma unroll
@@ -573,6 +666,15 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
           if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, (double)x);
+        }
+      }
+      if (kGrad) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+          double x = (double)km[k];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+          if (lane == 0 && x != 0.0) atomicAdd(M.kinkM + sd * 18 + k, x);
         }
       }
     }
@@ -703,6 +805,8 @@ int mixed_create(PesPlan* p) {
   double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
   int32_t *chb, *chl, *chi, *nsp, *nch;
   SampleBlock<GradScalar>* gblk;
+  double *kR, *kC, *kM;
+  float* kF;
   float* bin_t;
   float2* dat;
   float* wgt;
@@ -717,7 +821,8 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
-      (rc = alloc(mb, &gblk, (size_t)B)))
+      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
+      (rc = alloc(mb, &kF, sd * 8)) || (rc = alloc(mb, &kM, sd * 18)))
     return rc;
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chb, cb.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
@@ -746,6 +851,10 @@ int mixed_create(PesPlan* p) {
   M.gpart = gpart;
   M.gdir = gdir;
   M.gblocks = gblk;
+  M.kinkR = kR;
+  M.kinkC = kC;
+  M.kinkF = kF;
+  M.kinkM = kM;
   // the dense-path partial buffer is not needed; gradient set-up blocks are shared
   return PES_OK;
 }
@@ -778,6 +887,8 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_LAUNCH();
   k_mixed_ranges<<<1, 64, 0, st>>>(M, blocks, 1);
   PES_CHECK_LAUNCH();
+  k_kink<<<1, 64, 0, st>>>(p->dev, M, G, blocks, 1);
+  PES_CHECK_LAUNCH();
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
   k_spline_fit<<<ceil_div((int64_t)M.n_det * kNodeQ, 64), 64, 0, st>>>(M, 1);
@@ -806,6 +917,11 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKSparse, st);
+    k_kink<<<ceil_div(B * (int64_t)M.n_det, 64), 64, 0, st>>>(p->dev, M, G, blocks, B);
+  }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKSparse, st);
     dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
     k_sparse_fwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   }
@@ -816,7 +932,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     k_spline_fit<<<ceil_div(nsd, 64), 64, 0, st>>>(M, B);
   }
   PES_CHECK_LAUNCH();
-  if (grad) PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(double) * B * M.n_det * M.J * kNodeQ * kMoments, st));
+  if (grad) {
+    PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(double) * B * M.n_det * M.J * kNodeQ * kMoments, st));
+    PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(double) * B * M.n_det * 18, st));
+  }
   {
     ProfScope ps(p, kKDenseMixed, st);
     dim3 grid(M.nblk_dense, (unsigned)B);
@@ -846,7 +965,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   {
     ProfScope ps(p, kKAdjoint, st);
     dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
-    k_sparse_bwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G);
+    k_sparse_bwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
   }
   PES_CHECK_LAUNCH();
   {

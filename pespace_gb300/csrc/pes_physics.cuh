@@ -316,6 +316,22 @@ PES_HD void phenomd_eval(const PhenomDCoef<T>& c, const T& Mf, T& amp, T& psi, T
   amp = c.amp_scale / (Mf * dsqrt(u)) * phenomd_amphat(c, Mf, u);
 }
 
+// Ahat at f_peak and the jump of d^2 Ahat / dMf^2 there: the intermediate
+// polynomial and the merger-ringdown Lorentzian join with C1 continuity only.
+template <class T>
+PES_HD void amp_peak_jump(const PhenomDCoef<T>& c, T& ahat_pk, T& jump) {
+  const T fp = c.fpeak;
+  const T x = fp - c.fRD, a = c.g3fDM;
+  const T D = x * x + a * a;
+  const T A = c.g1 * a / D * dexp(-c.g2 * x / a);
+  const T L1 = -c.g2 / a - 2.0 * x / D;
+  const T L2 = -2.0 * (a * a - x * x) / (D * D);
+  const T d2m = A * (L1 * L1 + L2);
+  const T d2i = 2.0 * c.dl[2] + fp * (6.0 * c.dl[3] + 12.0 * c.dl[4] * fp);
+  ahat_pk = A;
+  jump = d2m - d2i;
+}
+
 template <class T>
 PES_HD void solve5(T A[5][5], T b[5], T x[5]) {
   for (int col = 0; col < 5; ++col) {
