@@ -28,7 +28,6 @@ constexpr int kChunkMax = 32;     // bins per phase-anchored run (one warp)
 constexpr int kMixThreads = 128;  // 4 warps; each warp owns 32 consecutive runs
 constexpr int kMoments = 4;       // t^0..t^3
 constexpr int kSparseThreads = 128;
-constexpr int kScratchRows = 5;   // doubles per node in the per-(sample, det, q) spline scratch
 // Gradient: one pass with FP64 values and FP32 tangents for the 9 parameters
 // that enter the node quantities non-trivially; ln D_L (G ~ 1/D_L) and phi_c
 // (Phi_s shifts by -2 phi_c) are applied analytically.
@@ -53,13 +52,19 @@ struct MixedDev {
   float* wgt;               // [n_det][3][nbins] inverse scaled PSD (0 off the channel mask)
   int32_t* nsp;             // [B] spline intervals of the sample (nodes 0..nsp)
   int32_t* nch;             // [B] runs with a live bin
-  double* yv;               // [B][n_det][7][J] node values
-  double* scr;              // [B][n_det][7][5 J] spline scratch
+  const double* gh;         // [J] node spacing h_i
+  const double* ginvh;      // [J] 1 / h_i
+  const double* glo;        // [J] reduced not-a-knot system, rows 1..J-2 (first-row elimination included)
+  const double* gup;        // [J]
+  const double* ginvden;    // [J] 1 / Thomas pivots
+  const double* gcp;        // [J] Thomas super-diagonal ratios
+  double* yv;               // [B][n_det][J][7] node values (quantity fastest)
+  double* scr;              // [B][n_det][J][7] spline scratch
   double* cphi;             // [B][n_det][J][4] phase spline coefficients (FP64)
   float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32: a_hi, b, c, d)
   float* cglo;              // [B][n_det][J][6] a - a_hi (the value at the left node in float-float)
   double* mom;              // [B][n_det][J][7][4] adjoint moments
-  double* ybar;             // [B][n_det][7][J] node adjoints
+  double* ybar;             // [B][n_det][J][7] node adjoints
   double* part;             // [B][nblk_dense] lnL partials
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
@@ -165,9 +170,9 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
 #pragma unroll
     for (int q = 0; q < 6; ++q) y[1 + q] -= C[q] * xk * xk;
   }
-  double* out = M.yv + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
+  double* out = M.yv + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
 #pragma unroll
-  for (int q = 0; q < kNodeQ; ++q) out[(size_t)q * M.J + j] = y[q];
+  for (int q = 0; q < kNodeQ; ++q) out[q] = y[q];
 }
 
 // Gradient set-up: per sample, the coefficient block with exact FP64
@@ -239,10 +244,10 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
 #pragma unroll
       for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - R[q] * x2h;  // R_q held fixed
     }
-    const double* yb = M.ybar + ((size_t)s * M.n_det + d) * kNodeQ * M.J;
+    const double* yb = M.ybar + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
 #pragma unroll
     for (int q = 0; q < kNodeQ; ++q) {
-      const double w = yb[(size_t)q * M.J + j];
+      const double w = yb[q];
 #pragma unroll
       for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += w * (double)y[q].d[k];
       if (q > 0) acc[4] -= w * y[q].v;  // G ~ 1/D_L
@@ -325,14 +330,17 @@ __device__ __forceinline__ void nak_row(const double* f, int n, int i, double& l
   }
 }
 
-__device__ __forceinline__ void nak_ends(const double* f, int n, const double* m, double& m0, double& mn) {
+__device__ __forceinline__ void nak_ends(const double* f, int n, double m1, double m2, double mn1, double mn2,
+                                         double& m0, double& mn) {
   const double h0 = f[1] - f[0], h1 = f[2] - f[1];
-  m0 = ((h0 + h1) * m[1] - h0 * m[2]) / h1;
+  m0 = ((h0 + h1) * m1 - h0 * m2) / h1;
   const double ha = f[n - 1] - f[n - 2], hb = f[n] - f[n - 1];
-  mn = ((ha + hb) * m[n - 1] - hb * m[n - 2]) / ha;
+  mn = ((ha + hb) * mn1 - hb * mn2) / ha;
 }
 
-// Thread per (sample, detector, quantity): fit and store interval coefficients.
+// Thread per (sample, detector, quantity), quantity fastest: fit and store the
+// interval coefficients.  Rows 1..n-2 of the reduced system are the shared
+// grid's (pivots precomputed); only the last row depends on the sample's n.
 __global__ void k_spline_fit(MixedDev M, int64_t B) {
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int q = (int)(tid % kNodeQ);
@@ -342,37 +350,42 @@ __global__ void k_spline_fit(MixedDev M, int64_t B) {
   const int n = M.nsp[s];
   if (n < 3) return;
   const double* f = M.node_f;
-  const double* y = M.yv + ((size_t)sd * kNodeQ + q) * M.J;
-  double* cpr = M.scr + ((size_t)sd * kNodeQ + q) * kScratchRows * M.J;  // c'
-  double* dpr = cpr + M.J;                                                 // d'
-  double* m = dpr + M.J;                                                   // m_0..m_n
-  double cprev = 0.0, dprev = 0.0;
-  double slope_prev = (y[1] - y[0]) / (f[1] - f[0]);
-  for (int i = 1; i <= n - 1; ++i) {
-    double lo, di, up;
-    nak_row(f, n, i, lo, di, up);
-    const double slope = (y[i + 1] - y[i]) / (f[i + 1] - f[i]);
+  const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;   // y[i * kNodeQ]
+  double* S = M.scr + (size_t)sd * M.J * kNodeQ + q;        // d' then m, S[i * kNodeQ]
+  double slope_prev = (y[kNodeQ] - y[0]) * M.ginvh[0];
+  double dprev = 0.0;
+  for (int i = 1; i <= n - 2; ++i) {
+    const double slope = (y[(i + 1) * kNodeQ] - y[i * kNodeQ]) * M.ginvh[i];
     const double r = 6.0 * (slope - slope_prev);
     slope_prev = slope;
-    const double den = di - lo * cprev;
-    cprev = up / den;
+    dprev = (r - M.glo[i] * dprev) * M.ginvden[i];
+    S[i * kNodeQ] = dprev;
+  }
+  double lo, di, up;
+  nak_row(f, n, n - 1, lo, di, up);
+  {
+    const double slope = (y[n * kNodeQ] - y[(n - 1) * kNodeQ]) * M.ginvh[n - 1];
+    const double r = 6.0 * (slope - slope_prev);
+    const double den = di - lo * M.gcp[n - 2];
     dprev = (r - lo * dprev) / den;
-    cpr[i] = cprev;
-    dpr[i] = dprev;
+    S[(n - 1) * kNodeQ] = dprev;
   }
-  double mnext = 0.0;
-  for (int i = n - 1; i >= 1; --i) {
-    const double mi = dpr[i] - cpr[i] * mnext;
-    m[i] = mi;
-    mnext = mi;
+  double mnext = dprev;
+  for (int i = n - 2; i >= 1; --i) {
+    const double m = S[i * kNodeQ] - M.gcp[i] * mnext;
+    S[i * kNodeQ] = m;
+    mnext = m;
   }
-  nak_ends(f, n, m, m[0], m[n]);
+  double m0, mn;
+  nak_ends(f, n, S[1 * kNodeQ], S[2 * kNodeQ], S[(n - 1) * kNodeQ], S[(n - 2) * kNodeQ], m0, mn);
+  double mi = m0;
   for (int i = 0; i < n; ++i) {
-    const double h = f[i + 1] - f[i];
-    const double a = y[i];
-    const double bc = (y[i + 1] - y[i]) / h - h * (2.0 * m[i] + m[i + 1]) / 6.0;
-    const double cc = 0.5 * m[i];
-    const double dc = (m[i + 1] - m[i]) / (6.0 * h);
+    const double mj = (i + 1 == n) ? mn : S[(i + 1) * kNodeQ];
+    const double h = M.gh[i];
+    const double a = y[i * kNodeQ];
+    const double bc = (y[(i + 1) * kNodeQ] - a) * M.ginvh[i] - h * (2.0 * mi + mj) * (1.0 / 6.0);
+    const double cc = 0.5 * mi;
+    const double dc = (mj - mi) * M.ginvh[i] * (1.0 / 6.0);
     if (q == 0) {
       double* o = M.cphi + ((size_t)sd * M.J + i) * 4;
       o[0] = a;
@@ -384,11 +397,12 @@ __global__ void k_spline_fit(MixedDev M, int64_t B) {
       M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, (float)bc, (float)cc, (float)dc);
       M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(a - (double)ahi);
     }
+    mi = mj;
   }
 }
 
 // Transpose of the fit: interval coefficient adjoints (the dense moments,
-// times wscale) -> node adjoints ybar.  Also the direct t_c term (q == 0).
+// times wscale) -> node adjoints ybar; also the direct t_c term (q == 0).
 __global__ void k_spline_adjoint(MixedDev M, int64_t B, double wscale) {
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int q = (int)(tid % kNodeQ);
@@ -396,65 +410,74 @@ __global__ void k_spline_adjoint(MixedDev M, int64_t B, double wscale) {
   if (sd >= B * (int64_t)M.n_det) return;
   const int64_t s = sd / M.n_det;
   const int n = M.nsp[s];
-  double* yb = M.ybar + ((size_t)sd * kNodeQ + q) * M.J;
-  for (int i = 0; i < M.J; ++i) yb[i] = 0.0;
+  double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;  // yb[i * kNodeQ]
   if (q == 0) M.gdir[sd] = 0.0;
-  if (n < 3) return;
-  const double* f = M.node_f;
-  const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments;
-  double* mb = M.scr + ((size_t)sd * kNodeQ + q) * kScratchRows * M.J;  // mbar_0..mbar_n
-  double* Db = mb + M.J;                                                 // Dbar_0..Dbar_{n-1}
-  double* cpt = Db + M.J;                                                // transposed-solve c'
-  double* dpt = cpt + M.J;                                               // transposed-solve d'
-  for (int i = 0; i <= n; ++i) mb[i] = 0.0;
-  double gd = 0.0;
-  for (int i = 0; i < n; ++i) {
-    const double h = f[i + 1] - f[i];
-    const double* mm = mom + ((size_t)i * kNodeQ + q) * kMoments;
-    const double ab = wscale * mm[0], bb = wscale * mm[1], cb = wscale * mm[2], db = wscale * mm[3];
-    if (q == 0) gd += 2.0 * kPi * (f[i] * mm[0] + mm[1]);  // sum_bins A_phi 2 pi f
-    yb[i] += ab;
-    Db[i] = bb;
-    mb[i] += -h * bb / 3.0 + 0.5 * cb - db / (6.0 * h);
-    mb[i + 1] += -h * bb / 6.0 + db / (6.0 * h);
+  if (n < 3) {
+    for (int i = 0; i < M.J; ++i) yb[i * kNodeQ] = 0.0;
+    return;
   }
+  const double* f = M.node_f;
+  const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;  // + i*7*4
+  double* X = M.scr + (size_t)sd * M.J * kNodeQ + q;  // mbar, then z, then rbar
+  // 1. coefficient adjoints -> mbar (X[0..n]); direct t_c term
+  double gd = 0.0;
+  double carry = 0.0;  // contribution to mbar_i from interval i-1
+  for (int i = 0; i < n; ++i) {
+    const double* mm = mom + (size_t)i * kNodeQ * kMoments;
+    const double h = M.gh[i], ih = M.ginvh[i];
+    const double bb = wscale * mm[1], cb = wscale * mm[2], db = wscale * mm[3];
+    if (q == 0) gd += 2.0 * kPi * (f[i] * mm[0] + mm[1]);
+    X[i * kNodeQ] = carry + (-h * bb * (1.0 / 3.0) + 0.5 * cb - db * ih * (1.0 / 6.0));
+    carry = -h * bb * (1.0 / 6.0) + db * ih * (1.0 / 6.0);
+  }
+  X[n * kNodeQ] = carry;
   if (q == 0) M.gdir[sd] = wscale * gd;
   {  // eliminated end second derivatives
-    const double h0 = f[1] - f[0], h1 = f[2] - f[1];
-    mb[1] += mb[0] * (h0 + h1) / h1;
-    mb[2] -= mb[0] * h0 / h1;
-    const double ha = f[n - 1] - f[n - 2], hb = f[n] - f[n - 1];
-    mb[n - 1] += mb[n] * (ha + hb) / ha;
-    mb[n - 2] -= mb[n] * hb / ha;
+    const double h0 = M.gh[0], h1 = M.gh[1];
+    const double mb0 = X[0], mbn = X[n * kNodeQ];
+    X[1 * kNodeQ] += mb0 * (h0 + h1) / h1;
+    X[2 * kNodeQ] -= mb0 * h0 / h1;
+    const double ha = M.gh[n - 2], hb = M.gh[n - 1];
+    X[(n - 1) * kNodeQ] += mbn * (ha + hb) / ha;
+    X[(n - 2) * kNodeQ] -= mbn * hb / ha;
   }
-  // rbar = A^{-T} mbar over rows 1..n-1; A^T row i: sub = up_{i-1}, diag = di_i, super = lo_{i+1}
-  double cprev = 0.0, dprev = 0.0;
-  for (int i = 1; i <= n - 1; ++i) {
-    double lo, di, up, lo_n = 0.0, di_n, up_n, lo_p, di_p, up_p = 0.0;
-    nak_row(f, n, i, lo, di, up);
-    if (i > 1) nak_row(f, n, i - 1, lo_p, di_p, up_p);
-    if (i < n - 1) nak_row(f, n, i + 1, lo_n, di_n, up_n);
-    const double sub = (i > 1) ? up_p : 0.0;
-    const double sup = (i < n - 1) ? lo_n : 0.0;
-    const double den = di - sub * cprev;
-    cprev = sup / den;
-    dprev = (mb[i] - sub * dprev) / den;
-    cpt[i] = cprev;
-    dpt[i] = dprev;
+  // 2. A^T rbar = mbar with A = L U (Thomas): U^T z = mbar, then L^T rbar = z
+  double lo_l, di_l, up_l;
+  nak_row(f, n, n - 1, lo_l, di_l, up_l);
+  const double den_l = di_l - lo_l * M.gcp[n - 2];
+  double zprev = 0.0;
+  for (int i = 1; i <= n - 2; ++i) {
+    const double sub = (i > 1) ? M.gup[i - 1] : 0.0;
+    zprev = (X[i * kNodeQ] - sub * zprev) * M.ginvden[i];
+    X[i * kNodeQ] = zprev;
   }
-  double rnext = 0.0;
-  for (int i = n - 1; i >= 1; --i) {
-    const double ri = dpt[i] - cpt[i] * rnext;
-    rnext = ri;
-    // r_i = 6 (D_i - D_{i-1})
-    Db[i] += 6.0 * ri;
-    Db[i - 1] -= 6.0 * ri;
+  {
+    const double sub = (n - 1 > 1) ? M.gup[n - 2] : 0.0;
+    zprev = (X[(n - 1) * kNodeQ] - sub * zprev) / den_l;
+    X[(n - 1) * kNodeQ] = zprev;
   }
-  for (int i = 0; i < n; ++i) {
-    const double h = f[i + 1] - f[i];
-    yb[i + 1] += Db[i] / h;
-    yb[i] -= Db[i] / h;
+  double xnext = zprev;  // rbar_{n-1}
+  for (int i = n - 2; i >= 1; --i) {
+    const double l_next = ((i + 1 == n - 1) ? lo_l : M.glo[i + 1]) * M.ginvden[i];
+    const double xi = X[i * kNodeQ] - l_next * xnext;
+    X[i * kNodeQ] = xi;
+    xnext = xi;
   }
+  // 3. slopes and node adjoints: Dbar_i = bbar_i + 6 (rbar_i - rbar_{i+1})
+  double dprevbar = 0.0;  // Dbar_{i-1} * (1/h_{i-1})
+  for (int i = 0; i <= n; ++i) {
+    double ybi = dprevbar;
+    if (i < n) {
+      const double* mm = mom + (size_t)i * kNodeQ * kMoments;
+      const double ri = (i >= 1 && i <= n - 1) ? X[i * kNodeQ] : 0.0;
+      const double rn = (i + 1 <= n - 1) ? X[(i + 1) * kNodeQ] : 0.0;
+      const double Db = wscale * mm[1] + 6.0 * (ri - rn);
+      ybi += wscale * mm[0] - Db * M.ginvh[i];
+      dprevbar = Db * M.ginvh[i];
+    }
+    yb[i * kNodeQ] = ybi;
+  }
+  for (int i = n + 1; i < M.J; ++i) yb[i * kNodeQ] = 0.0;
 }
 
 // ------------------------------------------------------------------ dense stage
@@ -609,7 +632,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           sph = fmaf(corr, sph, sph);
           const float4* G = M.cg + (sd * M.J + j) * 6;
           const float* Glo = M.cglo + (sd * M.J + j) * 6;
-          const float fbin = (float)(P.k0 + i) * fstep_f;
+          const float fbin = (float)(int)(P.k0 + i) * fstep_f;
           const float xk = fmaf(kMsec, fbin, -kMfpk);
           const float x2 = xk > 0.0f ? xk * xk : 0.0f;
           float term = 0.0f;
@@ -803,6 +826,7 @@ int mixed_create(PesPlan* p) {
   M.nblk_sparse = (int32_t)ceil_div(J, kSparseThreads);
   int rc = PES_OK;
   double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
+  double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
   int32_t *chb, *chl, *chi, *nsp, *nch;
   SampleBlock<GradScalar>* gblk;
   double *kR, *kC, *kM;
@@ -816,7 +840,9 @@ int mixed_create(PesPlan* p) {
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
       (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
-      (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * kScratchRows * J)) ||
+      (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
+      (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
+      (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -825,6 +851,37 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &kF, sd * 8)) || (rc = alloc(mb, &kM, sd * 18)))
     return rc;
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+  {
+    // shared not-a-knot system of the node grid: rows 1..J-2 with the first-row
+    // elimination and without the last-row one (that row depends on the sample)
+    std::vector<double> h(J, 0.0), ih(J, 0.0), lo(J, 0.0), up(J, 0.0), iden(J, 0.0), cp(J, 0.0);
+    for (int i = 0; i + 1 < J; ++i) {
+      h[i] = nf[i + 1] - nf[i];
+      ih[i] = 1.0 / h[i];
+    }
+    double cprev = 0.0;
+    for (int i = 1; i + 1 < J; ++i) {
+      const double h0 = h[i - 1], h1 = h[i];
+      double l = h0, dgl = 2.0 * (h0 + h1), u = h1;
+      if (i == 1) {
+        dgl += h0 * (h0 + h1) / h1;
+        u -= h0 * h0 / h1;
+        l = 0.0;
+      }
+      const double den = dgl - l * cprev;
+      lo[i] = l;
+      up[i] = u;
+      iden[i] = 1.0 / den;
+      cp[i] = u / den;
+      cprev = cp[i];
+    }
+    PES_CHECK_CUDA(cudaMemcpy(gh, h.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(ginvh, ih.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(glo, lo.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(gup, up.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(ginvden, iden.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(gcp, cp.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+  }
   PES_CHECK_CUDA(cudaMemcpy(chb, cb.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chl, cl.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chi, ci.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
@@ -840,6 +897,12 @@ int mixed_create(PesPlan* p) {
   M.wgt = wgt;
   M.nsp = nsp;
   M.nch = nch;
+  M.gh = gh;
+  M.ginvh = ginvh;
+  M.glo = glo;
+  M.gup = gup;
+  M.ginvden = ginvden;
+  M.gcp = gcp;
   M.yv = yv;
   M.scr = scr;
   M.cphi = cphi;
