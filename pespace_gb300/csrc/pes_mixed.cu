@@ -15,7 +15,14 @@
 //     sum_bins A_q(f) t^p of each spline interval; a transposed spline solve
 //     turns them into node adjoints, and the sparse stage is recomputed with
 //     dual numbers and contracted with those adjoints (no dense residuals are
-//     stored).
+//     stored);
+//  5. exact bins: far below merger a light system's time-to-coalescence moves
+//     so fast with f that the constellation's yearly motion advances by more
+//     than kOrbitPhaseMax radians across one node interval; the splines do
+//     not resolve that, so the bins below the first resolved interval are
+//     evaluated directly in FP64 (model, residual, FP32 tangents for the
+//     gradient) and the dense stage skips them.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -32,6 +39,9 @@ constexpr int kSparseThreads = 128;
 // that enter the node quantities non-trivially; ln D_L (G ~ 1/D_L) and phi_c
 // (Phi_s shifts by -2 phi_c) are applied analytically.
 constexpr int kMixNT = 9;
+constexpr double kOrbitPhaseMax = 0.3;  // rad of yearly orbital phase per node interval
+constexpr int kExactBlocks = 4;         // blocks per sample of the exact-bin kernel
+constexpr int kExactThreads = 128;
 __device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
 using GradScalar = DualF<kMixNT>;
 
@@ -50,8 +60,14 @@ struct MixedDev {
   const float* bin_t;       // [nbins] f_i - f_iv(i)
   float2* dat;              // [n_det][3][nbins] scaled data
   float* wgt;               // [n_det][3][nbins] inverse scaled PSD (0 off the channel mask)
+  float2* dd;               // [n_det][nbins] sum_c |d|^2 / S in FP64, as a float-float pair (hi, lo)
   int32_t* nsp;             // [B] spline intervals of the sample (nodes 0..nsp)
   int32_t* nch;             // [B] runs with a live bin
+  int32_t* xbin;            // [B] bins [0, xbin) are evaluated exactly (not splined)
+  const int32_t* iv_first;  // [J + 1] first bin of each interval (nbins past the last)
+  double omega;             // largest yearly orbital angular frequency of the detectors
+  double* xpart;            // [B][kExactBlocks] exact-bin lnL partials
+  double* xgpart;           // [B][kExactBlocks][11] exact-bin gradient partials
   const double* gh;         // [J] node spacing h_i
   const double* ginvh;      // [J] 1 / h_i
   const double* glo;        // [J] reduced not-a-knot system, rows 1..J-2 (first-row elimination included)
@@ -74,7 +90,7 @@ struct MixedDev {
   // node data before the spline fit and added back per bin.
   double* kinkR;            // [B][n_det][6] R_q
   double* kinkC;            // [B][n_det][6] C_q
-  float* kinkF;             // [B][n_det][8] Msec, Mf_peak, C_0..C_5 (FP32 copies for the dense stage)
+  float* kinkF;             // [B][n_det][16] Msec f_step, -, C_0..C_5 as float-float (hi x6, lo x6), -, -
   double* kinkM;            // [B][n_det][18] dense adjoint moments: sum A_q x^2, sum A_q x f, sum A_q x
 };
 
@@ -130,24 +146,23 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
   const SampleBlock<double>& b = blocks[s];
   double* R = M.kinkR + (size_t)t * 6;
   double* C = M.kinkC + (size_t)t * 6;
-  float* F = M.kinkF + (size_t)t * 8;
+  float* F = M.kinkF + (size_t)t * 16;
+  for (int q = 0; q < 16; ++q) F[q] = 0.0f;
   for (int q = 0; q < 6; ++q) {
     R[q] = 0.0;
     C[q] = 0.0;
-    F[2 + q] = 0.0f;
   }
-  F[0] = 0.0f;
-  F[1] = 1.0e30f;
   if (b.status != kSampleOk) return;
   double y[kNodeQ], ahat, jump;
   node_eval<double>(P, M, b, d, G.gen20[d], b.wf.fpeak / b.wf.Msec, y);
   amp_peak_jump<double>(b.wf, ahat, jump);
-  F[0] = (float)b.wf.Msec;
-  F[1] = (float)b.wf.fpeak;
+  F[0] = (float)(b.wf.Msec * P.f_step);
   for (int q = 0; q < 6; ++q) {
     R[q] = y[1 + q] / ahat;
     C[q] = 0.5 * jump * R[q];
-    F[2 + q] = (float)C[q];
+    const float hi = (float)C[q];
+    F[2 + q] = hi;
+    F[8 + q] = (float)(C[q] - (double)hi);
   }
 }
 
@@ -287,12 +302,15 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
 }
 
 // ------------------------------------------------------------------ per-sample ranges
-// nsp: intervals 0..nsp-1 cover every live bin (nodes 0..nsp); nch: runs with a live bin.
+// nsp: intervals 0..nsp-1 cover every live bin (nodes 0..nsp); nch: runs with a
+// live bin; xbin: bins below the first interval whose yearly orbital phase
+// advance omega |t(f_{j+1}) - t(f_j)| is at most kOrbitPhaseMax (that advance
+// falls monotonically with f over the inspiral, so a bisection finds it).
 __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
   const SampleBlock<double>& b = blocks[s];
-  int ns = 0, nc = 0;
+  int ns = 0, nc = 0, xb = 0;
   if (b.status == kSampleOk && b.kcut > 0) {
     const int64_t last = b.kcut - 1;
     int lo = 0, hi = M.nchunks - 1;  // last run whose first bin is <= last
@@ -304,9 +322,25 @@ __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict
     ns = M.ch_iv[lo] + 1;
     if (ns < 3) ns = 3;
     if (ns > M.J - 1) ns = M.J - 1;
+    auto unresolved = [&](int j) {
+      double a, ps, t0, t1;
+      phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j], a, ps, t0);
+      phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j + 1], a, ps, t1);
+      return M.omega * fabs(t1 - t0) > kOrbitPhaseMax;
+    };
+    if (unresolved(0)) {
+      int lo2 = 0, hi2 = ns - 1;  // last unresolved interval
+      while (lo2 < hi2) {
+        int mid = (lo2 + hi2 + 1) >> 1;
+        if (unresolved(mid)) lo2 = mid; else hi2 = mid - 1;
+      }
+      const int64_t first = M.iv_first[lo2 + 1];
+      xb = (int)(first < b.kcut ? first : b.kcut);
+    }
   }
   M.nsp[s] = ns;
   M.nch[s] = nc;
+  M.xbin[s] = xb;
 }
 
 // ------------------------------------------------------------------ splines
@@ -480,6 +514,84 @@ __global__ void k_spline_adjoint(MixedDev M, int64_t B, double wscale) {
   for (int i = n + 1; i < M.J; ++i) yb[i * kNodeQ] = 0.0;
 }
 
+// ------------------------------------------------------------------ exact bins
+// Bins [0, xbin[s]) evaluated directly (FP64 model and residual against the
+// FP64 data).  kMode 0: lnL partials (T = double); 1: gradient partials
+// (T = GradScalar, FP64 values with FP32 tangents); 2: write the model.
+// grid (kExactBlocks, B); threads stride over the sample's exact bins.
+template <int kMode, class T>
+__global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, GenArg G,
+                                                         const SampleBlock<T>* __restrict__ blocks,
+                                                         double2* __restrict__ model) {
+  constexpr int NV = kMode == 1 ? 11 : 1;
+  __shared__ SampleBlock<T> sb;
+  __shared__ double red[kExactThreads / 32][NV];
+  const int s = blockIdx.y;
+  const int xb = M.xbin[s];
+  if (xb == 0) return;  // uniform per block; the finalizers skip such samples
+  load_block(blocks, s, sb);
+  __syncthreads();
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  const double inv_scale = 1.0 / M.scale;
+  if (sb.status == kSampleOk) {
+    for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xb; i += kExactBlocks * kExactThreads) {
+      const double f = (double)(P.k0 + i) * P.f_step;
+      for (int d = 0; d < M.n_det; ++d) {
+        T y[kNodeQ];
+        node_eval<T>(P, M, sb, d, G.gen20[d], f, y);
+        const T ph = y[0] + (2.0 * kPi * f) * sb.tc;
+        T sn, cs;
+        dsincos(ph, &sn, &cs);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          // h = G exp(-i ph)
+          const T hr = (y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn) * inv_scale;
+          const T hi = (y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn) * inv_scale;
+          const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
+          if constexpr (kMode == 2) {
+            model[off] = make_double2(val(hr), val(hi));
+            continue;
+          }
+          const double w = P.w[off];
+          const double2 dv = P.data[off];
+          const double rr = dv.x - val(hr), ri = dv.y - val(hi);
+          if constexpr (kMode == 0) {
+            acc[0] += w * (rr * rr + ri * ri);
+          } else if constexpr (kMode == 1) {
+            // d/dtheta of w |d - h|^2 = -2 w Re((d - h)^* dh)
+#pragma unroll
+            for (int k = 0; k < kMixNT; ++k)
+              acc[kSlotParam[k]] -= 2.0 * w * (rr * (double)hr.d[k] + ri * (double)hi.d[k]);
+            acc[4] += 2.0 * w * (rr * hr.v + ri * hi.v);  // dh/dlnD_L = -h
+            acc[9] += 4.0 * w * (rr * hi.v - ri * hr.v);  // dh/dphi_c = 2 i h
+          }
+        }
+      }
+    }
+  }
+  if (kMode == 2) return;
+  const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (l == 0) red[wid][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double x = 0.0;
+#pragma unroll
+    for (int w = 0; w < kExactThreads / 32; ++w) x += red[w][threadIdx.x];
+    if (kMode == 0)
+      M.xpart[(size_t)s * kExactBlocks + blockIdx.x] = x;
+    else
+      M.xgpart[((size_t)s * kExactBlocks + blockIdx.x) * 11 + threadIdx.x] = x;
+  }
+}
+
 // ------------------------------------------------------------------ dense stage
 // 2 pi split into a 12-bit head and two tails for exact FP32 reduction of
 // exactly-representable arguments up to ~2^11 turns.
@@ -507,6 +619,7 @@ __device__ __forceinline__ double wrap_2pi(double x) {
 }
 
 struct RunPhase {
+  float x0;               // Msec f - Mf_peak at the run start (FP64, rounded once)
   float c0, s0;           // cos, sin of the anchored phase at the run start
   float p1h, p1l;         // per-bin increment (wrapped), head/tail
   float p2h, p2l;         // quadratic coefficient, head/tail
@@ -525,16 +638,18 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int g = blockIdx.x * (kMixThreads / 32) + wid;  // run group
   const int nc = M.nch[s];
+  const int xb = M.xbin[s];
   const int64_t kcut = blocks[s].kcut;
   const double tc = blocks[s].tc;
   const int first = g * kChunkMax;
   float acc = 0.0f, comp = 0.0f;
+  float dsh = 0.0f, dsl = 0.0f;  // float-float sum of the FP64 |d|^2/S of the weak-template bins
   if (blocks[s].status == kSampleOk && first < nc) {
     const int cl = first + lane;
     for (int d = 0; d < M.n_det; ++d) {
       const size_t sd = (size_t)s * M.n_det + d;
       // ---- per-run phase anchors, one run per lane (FP64)
-      RunPhase rp = {1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      RunPhase rp = {0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
       if (cl < nc) {
         const int j = M.ch_iv[cl];
         const int kb = M.ch_begin[cl];
@@ -550,6 +665,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         const double ph1 = wrap_2pi(D * (S1 + 2.0 * kPi * tc));
         const double ph2 = D * D * S2;
         const double ph3 = D * D * D * dd;
+        rp.x0 = (float)fma(blocks[s].wf.Msec, fb, -blocks[s].wf.fpeak);
         // anchor phasor: sincos of the float head, rotated by the (tiny) tail
         const float h0 = (float)ph0;
         const float l0 = (float)(ph0 - (double)h0);
@@ -564,12 +680,15 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         rp.p3h = head_bits(ph3, 8);
         rp.p3l = (float)(ph3 - (double)rp.p3h);
       }
-      // ---- amplitude kink at f_peak (FP32 copies)
-      const float* KF = M.kinkF + sd * 8;
-      const float kMsec = KF[0], kMfpk = KF[1];
-      float kC[6];
+      // ---- amplitude kink at f_peak (float-float coefficients)
+      const float* KF = M.kinkF + sd * 16;
+      const float kSlope = KF[0];
+      float kC[6], kCl[6];
 #pragma unroll
-      for (int q = 0; q < 6; ++q) kC[q] = KF[2 + q];
+      for (int q = 0; q < 6; ++q) {
+        kC[q] = KF[2 + q];
+        kCl[q] = KF[8 + q];
+      }
       const float fstep_f = (float)P.f_step;
       float km[18];
       if (kGrad) {
@@ -587,6 +706,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
       for (int c = first; c < last; ++c) {
         const int src = c - first;
         RunPhase r;
+        r.x0 = __shfl_sync(0xffffffffu, rp.x0, src);
         r.c0 = __shfl_sync(0xffffffffu, rp.c0, src);
         r.s0 = __shfl_sync(0xffffffffu, rp.s0, src);
         r.p1h = __shfl_sync(0xffffffffu, rp.p1h, src);
@@ -598,6 +718,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         const int j = M.ch_iv[c];
         const int kb = M.ch_begin[c];
         const int len = M.ch_len[c];
+        if (kb < xb) continue;  // exact bins (runs never straddle an interval boundary)
         if (kGrad && j != cur_iv) {
           if (cur_iv >= 0) {
             // flush the previous interval's moments
@@ -633,16 +754,18 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float4* G = M.cg + (sd * M.J + j) * 6;
           const float* Glo = M.cglo + (sd * M.J + j) * 6;
           const float fbin = (float)(int)(P.k0 + i) * fstep_f;
-          const float xk = fmaf(kMsec, fbin, -kMfpk);
+          const float xk = fmaf(kSlope, u, r.x0);
           const float x2 = xk > 0.0f ? xk * xk : 0.0f;
-          float term = 0.0f;
+          float term = 0.0f;  // |d - h|^2 w
+          float cross = 0.0f;  // (|h|^2 - 2 Re(d^* h)) w
+          float hh = 0.0f;     // |h|^2 w
           float aphi = 0.0f;
           float ag[6];
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
-            const float gr = cr.x + fmaf(kC[2 * ch], x2, Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w)));
-            const float gi = ci.x + fmaf(kC[2 * ch + 1], x2, Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w)));
+            const float gr = cr.x + fmaf(kC[2 * ch], x2, fmaf(kCl[2 * ch], x2, Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w))));
+            const float gi = ci.x + fmaf(kC[2 * ch + 1], x2, fmaf(kCl[2 * ch + 1], x2, Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w))));
             const float hr = gr * cph + gi * sph;
             const float hi = gi * cph - gr * sph;
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
@@ -650,12 +773,28 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             const float w = M.wgt[off];
             const float er = dv.x - hr, ei = dv.y - hi;
             term = fmaf(er * er + ei * ei, w, term);
+            const float h2 = fmaf(hr, hr, hi * hi);
+            hh = fmaf(h2, w, hh);
+            cross = fmaf(fmaf(-2.0f, fmaf(dv.x, hr, dv.y * hi), h2), w, cross);
             if (kMode == 2) model[off] = make_double2((double)hr / M.scale, (double)hi / M.scale);
             if (kGrad) {
               ag[2 * ch] = w * (er * cph - ei * sph);
               ag[2 * ch + 1] = w * (er * sph + ei * cph);
               aphi = fmaf(w, dv.x * hi - dv.y * hr, aphi);
             }
+          }
+          // Where the template is weaker than the residual, |d - h|^2 w =
+          // |d|^2 w + (|h|^2 - 2 Re(d^* h)) w with the first term taken from
+          // the FP64 data (float-float): the FP32 rounding then scales with
+          // |h| instead of |d|, which matters when the data hold a loud signal.
+          if (hh < term) {
+            const float2 D = M.dd[(size_t)d * P.nbins + i];
+            const float t1 = dsh + D.x;
+            const float bp = t1 - dsh;
+            const float e1 = (dsh - (t1 - bp)) + (D.x - bp);
+            dsh = t1;
+            dsl += e1 + D.y;
+            term = cross;
           }
           // compensated accumulation
           const float yk = term - comp;
@@ -703,7 +842,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
     }
   }
   // deterministic reduction: lanes (FP64) -> warps -> block partial
-  double v = (double)acc - (double)comp;
+  double v = ((double)acc - (double)comp) + ((double)dsh + (double)dsl);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if (lane == 0) red[wid] = v;
@@ -728,21 +867,29 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   }
   double acc = 0.0;
   for (int k = 0; k < M.nblk_dense; ++k) acc += M.part[(size_t)s * M.nblk_dense + k];
+  if (M.xbin[s] > 0)
+    for (int k = 0; k < kExactBlocks; ++k) acc += M.xpart[(size_t)s * kExactBlocks + k];
   const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
   lnl[s] = v;
   if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
 }
 
-__global__ void k_mixed_grad_finalize(MixedDev M, int64_t B, double* __restrict__ grad) {
+__global__ void k_mixed_grad_finalize(MixedDev M, int64_t B, double xscale, double* __restrict__ grad) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
   const bool ok = reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks)[s].status == kSampleOk;
+  const bool exact = M.xbin[s] > 0;
   for (int p = 0; p < 11; ++p) {
     double acc = 0.0;
     if (ok) {
       for (int d = 0; d < M.n_det; ++d) {
         for (int b = 0; b < M.nblk_sparse; ++b) acc += M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + b) * 11 + p];
         if (p == 10) acc += M.gdir[(size_t)s * M.n_det + d];
+      }
+      if (exact) {
+        double x = 0.0;
+        for (int b = 0; b < kExactBlocks; ++b) x += M.xgpart[((size_t)s * kExactBlocks + b) * 11 + p];
+        acc += xscale * x;
       }
     }
     grad[11 * s + p] = acc;
@@ -754,13 +901,18 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
                                const double* __restrict__ psd) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.nbins) return;
+  double dd = 0.0;
   for (int ch = 0; ch < 3; ++ch) {
     const size_t off = ((size_t)det * 3 + ch) * P.nbins + i;
     const double2 v = data[ch * P.nbins + i];
     M.dat[off] = make_float2((float)(v.x * M.scale), (float)(v.y * M.scale));
-    const double w = ((P.chan_mask >> ch) & 1) ? 1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale) : 0.0;
+    const bool on = (P.chan_mask >> ch) & 1;
+    const double w = on ? 1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale) : 0.0;
     M.wgt[off] = (float)w;
+    if (on) dd += (v.x * v.x + v.y * v.y) / psd[ch * P.nbins + i];
   }
+  const float hi = (float)dd;
+  M.dd[(size_t)det * P.nbins + i] = make_float2(hi, (float)(dd - (double)hi));
 }
 
 // ------------------------------------------------------------------ host side
@@ -805,11 +957,13 @@ int mixed_create(PesPlan* p) {
   nf[J - 1] = fhi;
   std::vector<float> bt(n);
   std::vector<int32_t> cb, cl, ci;
+  std::vector<int32_t> ivf(J + 1, (int32_t)n);
   int j = 0;
   int run_iv = -1, run_len = 0;
   for (int64_t i = 0; i < n; ++i) {
     const double f = (double)(d.k0 + i) * d.f_step;
     while (j + 1 < J - 1 && nf[j + 1] <= f) ++j;
+    for (int jj = j; jj >= 0 && ivf[jj] == (int32_t)n; --jj) ivf[jj] = (int32_t)i;
     bt[i] = (float)(f - nf[j]);
     if (j != run_iv || run_len == kChunkMax) {
       cb.push_back((int32_t)i);
@@ -821,25 +975,29 @@ int mixed_create(PesPlan* p) {
     cl.back() += 1;
     run_len += 1;
   }
+  M.omega = 0.0;
+  for (int k = 0; k < nd; ++k) M.omega = std::max(M.omega, std::fabs(d.det[k].orbit.omega_revolution));
   M.nchunks = (int32_t)cb.size();
   M.nblk_dense = (int32_t)ceil_div(M.nchunks, (long long)kChunkMax * (kMixThreads / 32));
   M.nblk_sparse = (int32_t)ceil_div(J, kSparseThreads);
   int rc = PES_OK;
   double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
-  int32_t *chb, *chl, *chi, *nsp, *nch;
+  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
+  double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
   double *kR, *kC, *kM;
   float* kF;
   float* bin_t;
   float2* dat;
   float* wgt;
+  float2* ddv;
   float4* cg;
   float* cglo;
   const size_t sd = (size_t)B * nd;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
-      (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
+      (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
@@ -848,8 +1006,12 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
-      (rc = alloc(mb, &kF, sd * 8)) || (rc = alloc(mb, &kM, sd * 18)))
+      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 18)) || (rc = alloc(mb, &xbin, B)) ||
+      (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * kExactBlocks)) ||
+      (rc = alloc(mb, &xgpart, (size_t)B * kExactBlocks * 11)))
     return rc;
+  PES_CHECK_CUDA(cudaMemcpy(ivfirst, ivf.data(), sizeof(int32_t) * (J + 1), cudaMemcpyHostToDevice));
+  PES_CHECK_CUDA(cudaMemset(xbin, 0, sizeof(int32_t) * B));
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
   {
     // shared not-a-knot system of the node grid: rows 1..J-2 with the first-row
@@ -888,6 +1050,7 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaMemcpy(bin_t, bt.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemset(dat, 0, sizeof(float2) * nd * 3 * n));
   PES_CHECK_CUDA(cudaMemset(wgt, 0, sizeof(float) * nd * 3 * n));
+  PES_CHECK_CUDA(cudaMemset(ddv, 0, sizeof(float2) * nd * n));
   M.node_f = node_f;
   M.ch_begin = chb;
   M.ch_len = chl;
@@ -895,8 +1058,13 @@ int mixed_create(PesPlan* p) {
   M.bin_t = bin_t;
   M.dat = dat;
   M.wgt = wgt;
+  M.dd = ddv;
   M.nsp = nsp;
   M.nch = nch;
+  M.xbin = xbin;
+  M.iv_first = ivfirst;
+  M.xpart = xpart;
+  M.xgpart = xgpart;
   M.gh = gh;
   M.ginvh = ginvh;
   M.glo = glo;
@@ -960,6 +1128,9 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
                                                                   reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
+  k_exact<2, double><<<dim3(kExactBlocks, 1), kExactThreads, 0, st>>>(p->dev, M, G, blocks,
+                                                                      reinterpret_cast<double2*>(out));
+  PES_CHECK_LAUNCH();
   return PES_OK;
 }
 
@@ -1009,6 +1180,11 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   {
+    ProfScope ps(p, kKDenseFp64, st);
+    k_exact<0, double><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, st>>>(p->dev, M, G, blocks, nullptr);
+  }
+  PES_CHECK_LAUNCH();
+  {
     ProfScope ps(p, kKFinalize, st);
     k_mixed_finalize<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, M, blocks, B, lnl, status);
   }
@@ -1032,8 +1208,14 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   {
+    ProfScope ps(p, kKDenseFp64, st);
+    k_exact<1, GradScalar><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, st>>>(
+        p->dev, M, G, reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), nullptr);
+  }
+  PES_CHECK_LAUNCH();
+  {
     ProfScope ps(p, kKFinalize, st);
-    k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, B, grad);
+    k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, B, -2.0 * p->dev.df, grad);
   }
   PES_CHECK_LAUNCH();
   return PES_OK;

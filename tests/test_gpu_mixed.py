@@ -1,13 +1,13 @@
 """Mixed-precision plan (FP64 sparse grid + FP32 dense bulk) against the FP64 oracle.
 
-Bar (the benchmark spec): |dlnL| <= 1e-2 against the FP64 oracle.  For very loud
-templates (|lnL| >> 1e6) the FP32 bulk leaves a random per-bin model error of
-~1e-7 that sums to ~3e-8 |lnL|, so the bar is applied to the median and each
-sample is bounded by 1e-2 + 4e-8 |lnL|; light systems whose lowest bins lie
-decades before coalescence (orbital motion of radians per node interval) are
-the other source of outliers.  The gradient is the exact gradient of the interpolated
-model, checked against the oracle's forward-mode duals to 1e-3 of the
-gradient norm.
+Bar: |dlnL| <= 1e-2 against the FP64 oracle.  For templates far louder than
+the data (|lnL| >> 1e6) the FP32 bulk leaves a random model error of ~1e-7
+per bin that sums to a few 1e-9 |lnL|, so the bar is applied to the median
+and each sample is bounded by 1e-2 + 1e-8 |lnL|.  Light
+systems whose lowest bins lie decades before coalescence go through the exact
+FP64 bins of the mixed plan.  The gradient is the exact gradient of the
+interpolated model, checked against the oracle's forward-mode duals to 1e-3
+of the gradient norm.
 """
 
 import numpy as np
@@ -46,7 +46,7 @@ def test_mixed_lnl_injection_perturbed(cuda_lib, oracle, dataset):
     assert np.all(mixed.last_status.cpu().numpy() == 0)
     assert err[0] <= 1e-2  # the injection
     assert np.median(err) <= 1e-2, err
-    assert np.all(err <= 1e-2 + 4e-8 * np.abs(want)), err
+    assert np.all(err <= 1e-2 + 1e-8 * np.abs(want)), err
     # deterministic forward
     assert np.array_equal(got, mixed.log_likelihood_batch(thetas).cpu().numpy())
 
@@ -69,7 +69,8 @@ def test_mixed_prior_batch_cutoff(cuda_lib, oracle, network):
     want = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(thetas, nthreads=8)
     err = np.abs(got - want)
     assert np.median(err) <= 1e-2, np.sort(err)[-5:]
-    assert np.all(err <= 1e-2 + 4e-8 * np.abs(want) + 0.2 * (np.abs(want) < 2e6)), np.sort(err)[-5:]
+    # FP32 floor of the dense stage: a few 1e-9 of |lnL| for templates far louder than the data
+    assert np.all(err <= 1e-2 + 1e-8 * np.abs(want)), np.sort(err)[-5:]
 
 
 def test_mixed_rejects_geocentric(cuda_lib, oracle, dataset):
