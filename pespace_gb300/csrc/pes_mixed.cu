@@ -372,52 +372,90 @@ __device__ __forceinline__ void nak_ends(const double* f, int n, double m1, doub
   mn = ((ha + hb) * mn1 - hb * mn2) / ha;
 }
 
-// Thread per (sample, detector, quantity), quantity fastest: fit and store the
-// interval coefficients.  Rows 1..n-2 of the reduced system are the shared
-// grid's (pivots precomputed); only the last row depends on the sample's n.
-__global__ void k_spline_fit(MixedDev M, int64_t B) {
-  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int q = (int)(tid % kNodeQ);
-  const int64_t sd = tid / kNodeQ;
-  if (sd >= B * (int64_t)M.n_det) return;
+// The two recurrences of a tridiagonal solve, x_i = alpha_i x_{i-1} + beta_i,
+// are split over the 32 lanes of a warp: each lane runs its segment of rows
+// from 0 to get the segment's affine map x_in -> A x_in + B, a warp scan of
+// those maps gives the exact value entering every segment, and the lane then
+// reruns its segment from that value.  `reverse` scans from lane 31 down.
+__device__ __forceinline__ double segment_carry_in(double A, double B, bool reverse) {
+  const int lane = threadIdx.x & 31;
+  const int pos = reverse ? 31 - lane : lane;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double Ap = reverse ? __shfl_down_sync(0xffffffffu, A, o) : __shfl_up_sync(0xffffffffu, A, o);
+    const double Bp = reverse ? __shfl_down_sync(0xffffffffu, B, o) : __shfl_up_sync(0xffffffffu, B, o);
+    if (pos >= o) {
+      B = fma(A, Bp, B);
+      A = A * Ap;
+    }
+  }
+  const double prev = reverse ? __shfl_down_sync(0xffffffffu, B, 1) : __shfl_up_sync(0xffffffffu, B, 1);
+  return pos == 0 ? 0.0 : prev;
+}
+
+constexpr int kSplineThreads = kNodeQ * 32;  // one warp per quantity, one block per (sample, detector)
+
+// Fit: warp per (sample, detector, quantity); lane l owns intervals and rows
+// [l*seg, (l+1)*seg) of the sample's n intervals.  Rows 1..n-2 use the shared
+// grid's precomputed Thomas factors, row n-1 the sample's not-a-knot end row.
+__global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sd = blockIdx.x;
   const int64_t s = sd / M.n_det;
   const int n = M.nsp[s];
   if (n < 3) return;
   const double* f = M.node_f;
-  const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;   // y[i * kNodeQ]
-  double* S = M.scr + (size_t)sd * M.J * kNodeQ + q;        // d' then m, S[i * kNodeQ]
-  double slope_prev = (y[kNodeQ] - y[0]) * M.ginvh[0];
-  double dprev = 0.0;
-  for (int i = 1; i <= n - 2; ++i) {
-    const double slope = (y[(i + 1) * kNodeQ] - y[i * kNodeQ]) * M.ginvh[i];
-    const double r = 6.0 * (slope - slope_prev);
-    slope_prev = slope;
-    dprev = (r - M.glo[i] * dprev) * M.ginvden[i];
-    S[i * kNodeQ] = dprev;
+  const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;  // y[i * kNodeQ]
+  double* S = M.scr + (size_t)sd * M.J * kNodeQ + q;       // d' then m
+  const int seg = (n + 31) >> 5;
+  const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);  // intervals [i0, i1)
+  const int r0 = max(1, i0), r1 = i1;                          // rows [r0, r1), all <= n - 1
+  double lo_l, di_l, up_l;
+  nak_row(f, n, n - 1, lo_l, di_l, up_l);
+  const double iden_l = 1.0 / (di_l - lo_l * M.gcp[n - 2]);
+  // forward elimination d'_i = (r_i - lo_i d'_{i-1}) / den_i
+  double A = 1.0, x = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (r0 < r1) {
+      double sp = (y[r0 * kNodeQ] - y[(r0 - 1) * kNodeQ]) * M.ginvh[r0 - 1];
+      for (int i = r0; i < r1; ++i) {
+        const double sl = (y[(i + 1) * kNodeQ] - y[i * kNodeQ]) * M.ginvh[i];
+        const double r = 6.0 * (sl - sp);
+        sp = sl;
+        const bool last = i == n - 1;
+        const double l = last ? lo_l : M.glo[i];
+        const double id = last ? iden_l : M.ginvden[i];
+        x = (r - l * x) * id;
+        if (pass == 0) A = -l * id * A;
+        else S[i * kNodeQ] = x;
+      }
+    }
+    if (pass == 0) x = segment_carry_in(A, x, false);
   }
-  double lo, di, up;
-  nak_row(f, n, n - 1, lo, di, up);
-  {
-    const double slope = (y[n * kNodeQ] - y[(n - 1) * kNodeQ]) * M.ginvh[n - 1];
-    const double r = 6.0 * (slope - slope_prev);
-    const double den = di - lo * M.gcp[n - 2];
-    dprev = (r - lo * dprev) / den;
-    S[(n - 1) * kNodeQ] = dprev;
+  // back substitution m_i = d'_i - cp_i m_{i+1}  (m_{n-1} = d'_{n-1})
+  __syncwarp();
+  A = 1.0;
+  x = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r1 - 1; i >= r0; --i) {
+      const double c = (i == n - 1) ? 0.0 : M.gcp[i];
+      x = S[i * kNodeQ] - c * x;
+      if (pass == 0) A = -c * A;
+      else S[i * kNodeQ] = x;
+    }
+    if (pass == 0) x = segment_carry_in(A, x, true);
   }
-  double mnext = dprev;
-  for (int i = n - 2; i >= 1; --i) {
-    const double m = S[i * kNodeQ] - M.gcp[i] * mnext;
-    S[i * kNodeQ] = m;
-    mnext = m;
-  }
+  __syncwarp();
   double m0, mn;
   nak_ends(f, n, S[1 * kNodeQ], S[2 * kNodeQ], S[(n - 1) * kNodeQ], S[(n - 2) * kNodeQ], m0, mn);
-  double mi = m0;
-  for (int i = 0; i < n; ++i) {
+  if (i0 >= i1) return;
+  double mi = (i0 == 0) ? m0 : S[i0 * kNodeQ];
+  double a = y[i0 * kNodeQ];
+  for (int i = i0; i < i1; ++i) {
     const double mj = (i + 1 == n) ? mn : S[(i + 1) * kNodeQ];
     const double h = M.gh[i];
-    const double a = y[i * kNodeQ];
-    const double bc = (y[(i + 1) * kNodeQ] - a) * M.ginvh[i] - h * (2.0 * mi + mj) * (1.0 / 6.0);
+    const double an = y[(i + 1) * kNodeQ];
+    const double bc = (an - a) * M.ginvh[i] - h * (2.0 * mi + mj) * (1.0 / 6.0);
     const double cc = 0.5 * mi;
     const double dc = (mj - mi) * M.ginvh[i] * (1.0 / 6.0);
     if (q == 0) {
@@ -432,86 +470,103 @@ __global__ void k_spline_fit(MixedDev M, int64_t B) {
       M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(a - (double)ahi);
     }
     mi = mj;
+    a = an;
   }
 }
 
 // Transpose of the fit: interval coefficient adjoints (the dense moments,
 // times wscale) -> node adjoints ybar; also the direct t_c term (q == 0).
-__global__ void k_spline_adjoint(MixedDev M, int64_t B, double wscale) {
-  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int q = (int)(tid % kNodeQ);
-  const int64_t sd = tid / kNodeQ;
-  if (sd >= B * (int64_t)M.n_det) return;
+// Same warp decomposition as the fit.
+__global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, double wscale) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sd = blockIdx.x;
   const int64_t s = sd / M.n_det;
   const int n = M.nsp[s];
   double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;  // yb[i * kNodeQ]
-  if (q == 0) M.gdir[sd] = 0.0;
   if (n < 3) {
-    for (int i = 0; i < M.J; ++i) yb[i * kNodeQ] = 0.0;
+    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+    if (q == 0 && lane == 0) M.gdir[sd] = 0.0;
     return;
   }
   const double* f = M.node_f;
   const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;  // + i*7*4
-  double* X = M.scr + (size_t)sd * M.J * kNodeQ + q;  // mbar, then z, then rbar
-  // 1. coefficient adjoints -> mbar (X[0..n]); direct t_c term
-  double gd = 0.0;
-  double carry = 0.0;  // contribution to mbar_i from interval i-1
-  for (int i = 0; i < n; ++i) {
-    const double* mm = mom + (size_t)i * kNodeQ * kMoments;
+  double* X = M.scr + (size_t)sd * M.J * kNodeQ + q;  // z, then rbar
+  const int seg = (n + 31) >> 5;
+  const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);
+  const int r0 = max(1, i0), r1 = i1;
+  auto mm = [&](int i, int p) { return wscale * mom[(size_t)i * kNodeQ * kMoments + p]; };
+  // mbar_i = (interval i-1 part) + (interval i part)
+  auto mbar_left = [&](int i) {  // from interval i (to node i)
     const double h = M.gh[i], ih = M.ginvh[i];
-    const double bb = wscale * mm[1], cb = wscale * mm[2], db = wscale * mm[3];
-    if (q == 0) gd += 2.0 * kPi * (f[i] * mm[0] + mm[1]);
-    X[i * kNodeQ] = carry + (-h * bb * (1.0 / 3.0) + 0.5 * cb - db * ih * (1.0 / 6.0));
-    carry = -h * bb * (1.0 / 6.0) + db * ih * (1.0 / 6.0);
-  }
-  X[n * kNodeQ] = carry;
-  if (q == 0) M.gdir[sd] = wscale * gd;
-  {  // eliminated end second derivatives
-    const double h0 = M.gh[0], h1 = M.gh[1];
-    const double mb0 = X[0], mbn = X[n * kNodeQ];
-    X[1 * kNodeQ] += mb0 * (h0 + h1) / h1;
-    X[2 * kNodeQ] -= mb0 * h0 / h1;
-    const double ha = M.gh[n - 2], hb = M.gh[n - 1];
-    X[(n - 1) * kNodeQ] += mbn * (ha + hb) / ha;
-    X[(n - 2) * kNodeQ] -= mbn * hb / ha;
-  }
-  // 2. A^T rbar = mbar with A = L U (Thomas): U^T z = mbar, then L^T rbar = z
+    return -h * mm(i, 1) * (1.0 / 3.0) + 0.5 * mm(i, 2) - mm(i, 3) * ih * (1.0 / 6.0);
+  };
+  auto mbar_right = [&](int i) {  // from interval i (to node i + 1)
+    const double h = M.gh[i], ih = M.ginvh[i];
+    return -h * mm(i, 1) * (1.0 / 6.0) + mm(i, 3) * ih * (1.0 / 6.0);
+  };
+  const double mb0 = mbar_left(0), mbn = mbar_right(n - 1);
+  const double h0 = M.gh[0], h1 = M.gh[1], ha = M.gh[n - 2], hb = M.gh[n - 1];
+  auto xrow = [&](int i) {  // right-hand side of row i (1..n-1) after the end eliminations
+    double v = mbar_right(i - 1) + mbar_left(i);
+    if (i == 1) v += mb0 * (h0 + h1) / h1;
+    if (i == 2) v -= mb0 * h0 / h1;
+    if (i == n - 1) v += mbn * (ha + hb) / ha;
+    if (i == n - 2) v -= mbn * hb / ha;
+    return v;
+  };
   double lo_l, di_l, up_l;
   nak_row(f, n, n - 1, lo_l, di_l, up_l);
-  const double den_l = di_l - lo_l * M.gcp[n - 2];
-  double zprev = 0.0;
-  for (int i = 1; i <= n - 2; ++i) {
-    const double sub = (i > 1) ? M.gup[i - 1] : 0.0;
-    zprev = (X[i * kNodeQ] - sub * zprev) * M.ginvden[i];
-    X[i * kNodeQ] = zprev;
-  }
-  {
-    const double sub = (n - 1 > 1) ? M.gup[n - 2] : 0.0;
-    zprev = (X[(n - 1) * kNodeQ] - sub * zprev) / den_l;
-    X[(n - 1) * kNodeQ] = zprev;
-  }
-  double xnext = zprev;  // rbar_{n-1}
-  for (int i = n - 2; i >= 1; --i) {
-    const double l_next = ((i + 1 == n - 1) ? lo_l : M.glo[i + 1]) * M.ginvden[i];
-    const double xi = X[i * kNodeQ] - l_next * xnext;
-    X[i * kNodeQ] = xi;
-    xnext = xi;
-  }
-  // 3. slopes and node adjoints: Dbar_i = bbar_i + 6 (rbar_i - rbar_{i+1})
-  double dprevbar = 0.0;  // Dbar_{i-1} * (1/h_{i-1})
-  for (int i = 0; i <= n; ++i) {
-    double ybi = dprevbar;
-    if (i < n) {
-      const double* mm = mom + (size_t)i * kNodeQ * kMoments;
-      const double ri = (i >= 1 && i <= n - 1) ? X[i * kNodeQ] : 0.0;
-      const double rn = (i + 1 <= n - 1) ? X[(i + 1) * kNodeQ] : 0.0;
-      const double Db = wscale * mm[1] + 6.0 * (ri - rn);
-      ybi += wscale * mm[0] - Db * M.ginvh[i];
-      dprevbar = Db * M.ginvh[i];
+  const double iden_l = 1.0 / (di_l - lo_l * M.gcp[n - 2]);
+  // U^T z = mbar: z_i = (x_i - up_{i-1} z_{i-1}) / den_i
+  double A = 1.0, x = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r0; i < r1; ++i) {
+      const double sub = (i > 1) ? M.gup[i - 1] : 0.0;
+      const double id = (i == n - 1) ? iden_l : M.ginvden[i];
+      x = (xrow(i) - sub * x) * id;
+      if (pass == 0) A = -sub * id * A;
+      else X[i * kNodeQ] = x;
     }
-    yb[i * kNodeQ] = ybi;
+    if (pass == 0) x = segment_carry_in(A, x, false);
   }
-  for (int i = n + 1; i < M.J; ++i) yb[i * kNodeQ] = 0.0;
+  __syncwarp();
+  // L^T rbar = z: rbar_i = z_i - (lo_{i+1} / den_i) rbar_{i+1}
+  A = 1.0;
+  x = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r1 - 1; i >= r0; --i) {
+      const double c = (i == n - 1) ? 0.0 : ((i + 1 == n - 1) ? lo_l : M.glo[i + 1]) * M.ginvden[i];
+      x = X[i * kNodeQ] - c * x;
+      if (pass == 0) A = -c * A;
+      else X[i * kNodeQ] = x;
+    }
+    if (pass == 0) x = segment_carry_in(A, x, true);
+  }
+  __syncwarp();
+  // node adjoints: ybar_i = Dbar_{i-1}/h_{i-1} + wscale mm0_i - Dbar_i/h_i,
+  // Dbar_i = wscale mm1_i + 6 (rbar_i - rbar_{i+1}); direct t_c term
+  auto rb = [&](int i) { return (i >= 1 && i <= n - 1) ? X[i * kNodeQ] : 0.0; };
+  double gd = 0.0;
+  if (i0 < i1) {
+    double rcur = rb(i0);
+    double dprev = 0.0;
+    if (i0 > 0) dprev = (mm(i0 - 1, 1) + 6.0 * (rb(i0 - 1) - rcur)) * M.ginvh[i0 - 1];
+    for (int i = i0; i < i1; ++i) {
+      const double rnext = rb(i + 1);
+      const double Db = mm(i, 1) + 6.0 * (rcur - rnext);
+      yb[i * kNodeQ] = dprev + mm(i, 0) - Db * M.ginvh[i];
+      dprev = Db * M.ginvh[i];
+      rcur = rnext;
+      if (q == 0) gd += 2.0 * kPi * (f[i] * mom[(size_t)i * kNodeQ * kMoments] + mom[(size_t)i * kNodeQ * kMoments + 1]);
+    }
+    if (i1 == n) yb[n * kNodeQ] = dprev;
+  }
+  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+  if (q == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gd += __shfl_xor_sync(0xffffffffu, gd, o);
+    if (lane == 0) M.gdir[sd] = wscale * gd;
+  }
 }
 
 // ------------------------------------------------------------------ exact bins
@@ -1122,7 +1177,7 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_LAUNCH();
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
-  k_spline_fit<<<ceil_div((int64_t)M.n_det * kNodeQ, 64), 64, 0, st>>>(M, 1);
+  k_spline_fit<<<M.n_det, kSplineThreads, 0, st>>>(M);
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
   k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
@@ -1163,7 +1218,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   const int64_t nsd = B * (int64_t)M.n_det * kNodeQ;
   {
     ProfScope ps(p, kKSpline, st);
-    k_spline_fit<<<ceil_div(nsd, 64), 64, 0, st>>>(M, B);
+    k_spline_fit<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
   }
   PES_CHECK_LAUNCH();
   if (grad) {
@@ -1192,7 +1247,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (!grad) return PES_OK;
   {
     ProfScope ps(p, kKAdjoint, st);
-    k_spline_adjoint<<<ceil_div(nsd, 64), 64, 0, st>>>(M, B, 4.0 * p->dev.df);
+    k_spline_adjoint<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
   }
   PES_CHECK_LAUNCH();
   {
