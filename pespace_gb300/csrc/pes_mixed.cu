@@ -91,7 +91,7 @@ struct MixedDev {
   double* kinkR;            // [B][n_det][6] R_q
   double* kinkC;            // [B][n_det][6] C_q
   float* kinkF;             // [B][n_det][16] Msec f_step, -, C_0..C_5 as float-float (hi x6, lo x6), -, -
-  double* kinkM;            // [B][n_det][18] dense adjoint moments: sum A_q x^2, sum A_q x f, sum A_q x
+  double* kinkM;            // [B][n_det][12] dense adjoint moments: sum A_q x^2, sum A_q x
 };
 
 struct GenArg {
@@ -102,6 +102,10 @@ struct MixedBuffers {
   MixedDev dev;
   GenArg gen;
   std::vector<void*> allocs;
+  // The exact-bin kernels use a few SMs for a long dependent chain each; they
+  // run on a side stream beside the sparse/spline/dense stages.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -275,9 +279,11 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
     amp_peak_jump<GradScalar>(sb.wf, ahat, jump);
     const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
     const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
-    const double* K = M.kinkM + ((size_t)s * M.n_det + d) * 18;
+    const double* K = M.kinkM + ((size_t)s * M.n_det + d) * 12;
     for (int q = 0; q < 6; ++q) {
-      const double K2 = wscale * K[q], K1f = wscale * K[6 + q], K1 = wscale * K[12 + q];
+      // sum A_q x f = (sum A_q x^2 + Mf_peak sum A_q x) / Msec  (f = (x + Mf_peak) / Msec)
+      const double K2 = wscale * K[q], K1 = wscale * K[6 + q];
+      const double K1f = (K2 + sb.wf.fpeak.v * K1) / sb.wf.Msec.v;
       for (int k = 0; k < kMixNT; ++k)
         acc[kSlotParam[k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
                               2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
@@ -655,8 +661,10 @@ constexpr float kTwoPiMid = 0.0019353071693331003f;   // float(2 pi - hi)
 constexpr float kTwoPiLo = 1.0253131677018246e-11f;   // float(2 pi - hi - mid)
 constexpr float kInvTwoPi = 0.159154943091895336f;
 
+constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23: (y + M) - M rounds |y| < 2^22 to an integer
+
 __device__ __forceinline__ float reduce_exact(float x) {
-  const float k = rintf(x * kInvTwoPi);
+  const float k = fmaf(x, kInvTwoPi, kRoundMagic) - kRoundMagic;
   float r = fmaf(-k, kTwoPiHi, x);
   r = fmaf(-k, kTwoPiMid, r);
   r = fmaf(-k, kTwoPiLo, r);
@@ -667,6 +675,13 @@ __device__ __forceinline__ float reduce_exact(float x) {
 __device__ __forceinline__ float head_bits(double x, int bits) {
   const long long m = ~((1LL << (53 - bits)) - 1);
   return (float)__longlong_as_double(__double_as_longlong(x) & m);
+}
+
+// Error-free transformation: s + e == a + b exactly (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
 }
 
 __device__ __forceinline__ double wrap_2pi(double x) {
@@ -744,11 +759,11 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         kC[q] = KF[2 + q];
         kCl[q] = KF[8 + q];
       }
-      const float fstep_f = (float)P.f_step;
-      float km[18];
+      float km[12];
+      bool kinked = false;
       if (kGrad) {
 #pragma unroll
-        for (int k = 0; k < 18; ++k) km[k] = 0.0f;
+        for (int k = 0; k < 12; ++k) km[k] = 0.0f;
       }
       // ---- runs of the group, one bin per lane
       float mq[kNodeQ * kMoments];
@@ -808,7 +823,6 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           sph = fmaf(corr, sph, sph);
           const float4* G = M.cg + (sd * M.J + j) * 6;
           const float* Glo = M.cglo + (sd * M.J + j) * 6;
-          const float fbin = (float)(int)(P.k0 + i) * fstep_f;
           const float xk = fmaf(kSlope, u, r.x0);
           const float x2 = xk > 0.0f ? xk * xk : 0.0f;
           float term = 0.0f;  // |d - h|^2 w
@@ -844,9 +858,8 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           // |h| instead of |d|, which matters when the data hold a loud signal.
           if (hh < term) {
             const float2 D = M.dd[(size_t)d * P.nbins + i];
-            const float t1 = dsh + D.x;
-            const float bp = t1 - dsh;
-            const float e1 = (dsh - (t1 - bp)) + (D.x - bp);
+            float t1, e1;
+            two_sum(dsh, D.x, t1, e1);
             dsh = t1;
             dsl += e1 + D.y;
             term = cross;
@@ -857,12 +870,11 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           comp = (tk - acc) - yk;
           acc = tk;
           if (kGrad && xk > 0.0f) {
-            const float xf = xk * fbin;
+            kinked = true;
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
               km[q] = fmaf(ag[q], x2, km[q]);
-              km[6 + q] = fmaf(ag[q], xf, km[6 + q]);
-              km[12 + q] = fmaf(ag[q], xk, km[12 + q]);
+              km[6 + q] = fmaf(ag[q], xk, km[6 + q]);
             }
           }
           if (kGrad) {
@@ -885,22 +897,36 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, (double)x);
         }
       }
-      if (kGrad) {
+      if (kGrad && __any_sync(0xffffffffu, kinked)) {
 #pragma unroll
-        for (int k = 0; k < 18; ++k) {
-          double x = (double)km[k];
+        for (int k = 0; k < 12; ++k) {
+          float x = km[k];
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if (lane == 0 && x != 0.0) atomicAdd(M.kinkM + sd * 18 + k, x);
+          if (lane == 0) atomicAdd(M.kinkM + sd * 12 + k, (double)x);
         }
       }
     }
   }
-  // deterministic reduction: lanes (FP64) -> warps -> block partial
-  double v = ((double)acc - (double)comp) + ((double)dsh + (double)dsl);
+  // deterministic reduction: lanes (float-float) -> warps (FP64) -> block partial
+  float vh, vl;
+  two_sum(acc, -comp, vh, vl);
+  {
+    float th, tl;
+    two_sum(vh, dsh, th, tl);
+    vh = th;
+    vl += tl + dsl;
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if (lane == 0) red[wid] = v;
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, vh, o);
+    const float ol = __shfl_down_sync(0xffffffffu, vl, o);
+    float th, tl;
+    two_sum(vh, oh, th, tl);
+    vh = th;
+    vl += tl + ol;
+  }
+  if (lane == 0) red[wid] = (double)vh + (double)vl;
   __syncthreads();
   if (threadIdx.x == 0) {
     double x = 0.0;
@@ -995,6 +1021,9 @@ int mixed_create(PesPlan* p) {
                 "resolved by the sparse grid, use the fp64 precision for it", k);
   MixedBuffers* mb = new MixedBuffers();
   p->mixed = mb;
+  PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->side, cudaStreamNonBlocking));
+  PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->fork, cudaEventDisableTiming));
+  PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->join, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
   const int J = d.n_sparse;
@@ -1061,7 +1090,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
-      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 18)) || (rc = alloc(mb, &xbin, B)) ||
+      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) ||
       (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * kExactBlocks)) ||
       (rc = alloc(mb, &xgpart, (size_t)B * kExactBlocks * 11)))
     return rc;
@@ -1147,7 +1176,11 @@ int mixed_create(PesPlan* p) {
 
 void mixed_destroy(PesPlan* p) {
   if (!p->mixed) return;
+  if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
   for (void* a : p->mixed->allocs) cudaFree(a);
+  if (p->mixed->fork) cudaEventDestroy(p->mixed->fork);
+  if (p->mixed->join) cudaEventDestroy(p->mixed->join);
+  if (p->mixed->side) cudaStreamDestroy(p->mixed->side);
   delete p->mixed;
   p->mixed = nullptr;
 }
@@ -1204,6 +1237,30 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     k_mixed_ranges<<<ceil_div(B, 64), 64, 0, st>>>(M, blocks, B);
   }
   PES_CHECK_LAUNCH();
+  // side stream: exact bins (and the gradient set-up they need)
+  cudaStream_t side = p->mixed->side;
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->fork, st));
+  PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->fork, 0));
+  {
+    ProfScope ps(p, kKDenseFp64, side);
+    k_exact<0, double><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+  }
+  PES_CHECK_LAUNCH();
+  if (grad) {
+    {
+      ProfScope ps(p, kKSetup, side);
+      k_setup_grad<<<ceil_div(B, 64), 64, 0, side>>>(p->dev, theta, B,
+                                                     reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks));
+    }
+    PES_CHECK_LAUNCH();
+    {
+      ProfScope ps(p, kKDenseFp64, side);
+      k_exact<1, GradScalar><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, side>>>(
+          p->dev, M, G, reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), nullptr);
+    }
+    PES_CHECK_LAUNCH();
+  }
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
   {
     ProfScope ps(p, kKSparse, st);
     k_kink<<<ceil_div(B * (int64_t)M.n_det, 64), 64, 0, st>>>(p->dev, M, G, blocks, B);
@@ -1215,7 +1272,6 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     k_sparse_fwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   }
   PES_CHECK_LAUNCH();
-  const int64_t nsd = B * (int64_t)M.n_det * kNodeQ;
   {
     ProfScope ps(p, kKSpline, st);
     k_spline_fit<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
@@ -1223,7 +1279,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   if (grad) {
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(double) * B * M.n_det * M.J * kNodeQ * kMoments, st));
-    PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(double) * B * M.n_det * 18, st));
+    PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(double) * B * M.n_det * 12, st));
   }
   {
     ProfScope ps(p, kKDenseMixed, st);
@@ -1234,11 +1290,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
       k_dense_mixed<0><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
-  {
-    ProfScope ps(p, kKDenseFp64, st);
-    k_exact<0, double><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, st>>>(p->dev, M, G, blocks, nullptr);
-  }
-  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->join, 0));
   {
     ProfScope ps(p, kKFinalize, st);
     k_mixed_finalize<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, M, blocks, B, lnl, status);
@@ -1251,21 +1303,9 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   {
-    ProfScope ps(p, kKSetup, st);
-    k_setup_grad<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B,
-                                                 reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks));
-  }
-  PES_CHECK_LAUNCH();
-  {
     ProfScope ps(p, kKAdjoint, st);
     dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
     k_sparse_bwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
-  }
-  PES_CHECK_LAUNCH();
-  {
-    ProfScope ps(p, kKDenseFp64, st);
-    k_exact<1, GradScalar><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, st>>>(
-        p->dev, M, G, reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), nullptr);
   }
   PES_CHECK_LAUNCH();
   {
