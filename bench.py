@@ -116,10 +116,12 @@ def measured_peaks():
     return None
 
 
-def fp64_peak_tflops(torch):
-    """FP64 throughput denominator: cuBLAS DGEMM 8192^3 (best of 5)."""
-    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
-    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+def gemm_peak_tflops(torch, dtype):
+    """Pipe throughput denominator: cuBLAS GEMM 8192^3 in `dtype` (best of 5; TF32 off for FP32)."""
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(8192, 8192, dtype=dtype, device="cuda")
+    b = torch.randn(8192, 8192, dtype=dtype, device="cuda")
     for _ in range(2):
         torch.matmul(a, b)
     torch.cuda.synchronize()
@@ -132,6 +134,7 @@ def fp64_peak_tflops(torch):
         e.synchronize()
         best = min(best, s.elapsed_time(e) / 1e3)
     del a, b
+    torch.backends.cuda.matmul.allow_tf32 = tf32
     return 2 * 8192 ** 3 / best / 1e12
 
 
@@ -237,6 +240,7 @@ def run_native(args):
             step_ms.append((s, e))
         barrier()
     times = [s.elapsed_time(e) for s, e in step_ms]
+    work = eng.last_work(B)
     lib.pes_plan_stats(eng._plan, launches, dev_ms)
     lib.pes_plan_profile(eng._plan, 0)
     kern = {lib.pes_kernel_class_name(k).decode(): (int(launches[k]), float(dev_ms[k])) for k in range(n_cls)
@@ -279,15 +283,14 @@ def run_native(args):
         err = float((a - b).abs().max().item())
         del ref
 
-    # ---------------- roofline of the dominant kernel
-    dom = max(kern.items(), key=lambda kv: kv[1][1])
-    peaks = measured_peaks()
-    fp64_peak = fp64_peak_tflops(torch) if rank == 0 else None
+    # ---------------- roofline of the dominant kernel (the dense stage)
     roofline = None
     if rank == 0:
         from pespace_gb300 import census
 
-        roofline = census.roofline(dom[0], dom[1], eng, theta, fp64_peak, peaks)
+        dom = "dense_mixed" if args.precision == "mixed" else "dense_fp64"
+        roofline = census.roofline(dom, kern[dom], work, True, gemm_peak_tflops(torch, torch.float32))
+        roofline["fp64_peak_tflops"] = gemm_peak_tflops(torch, torch.float64)
 
     if rank == 0:
         line = {
@@ -303,6 +306,7 @@ def run_native(args):
                     "d2h_bytes_per_step": int(B * 12 * 8)},
             "gpu_launches": int(gpu_launches),
             "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in kern.items()},
+            "work_per_step": work,
             "roofline": roofline,
             "clocks": clocks.summary(),
         }
@@ -310,7 +314,7 @@ def run_native(args):
             line["max_abs_dlnl_vs_fp64"] = err
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            n = max(threads, 16)
+            n = 20 * threads  # about 10 s of the 16-core host
             v, dt = cpu_baseline_run(n, threads, "")
             line["cpu_baseline"] = {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
                                     "sample": f"{n} prior samples, full grid, FP64 dense + forward-mode gradient "

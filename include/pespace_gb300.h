@@ -180,6 +180,15 @@ int pes_plan_profile(PesPlan* plan, int32_t enable);
 int pes_plan_stats(PesPlan* plan, int64_t* launches /* host [8] */, double* device_ms /* host [8] */);
 const char* pes_kernel_class_name(int32_t k);
 
+/* Work units of the last pes_lnl_batch / pes_lnl_grad_batch call of B samples
+ * (host; synchronises `stream`), for roofline bookkeeping.  No reference
+ * counterpart.  out[0]: bins through the mixed plan's FP32 dense stage,
+ * summed over samples and detectors; out[1]: bins evaluated directly in FP64
+ * (all live bins of an fp64 plan, the exact low-frequency bins of a mixed
+ * plan); out[2]: sparse-node evaluations (mixed plans); out[3]: samples in
+ * the parameter domain. */
+int pes_plan_work(PesPlan* plan, int64_t B, int64_t* out /* host [4] */, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

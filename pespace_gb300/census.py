@@ -1,24 +1,57 @@
 """Roofline bookkeeping for bench.py: algorithmic work per kernel launch.
 
-The FP64 operation counts per unit of work are produced by counting the
-operations of the templated physics code (see ``csrc/pes_census.cu``); until
-that census exists for a kernel class, the roofline entry reports the
-measured time and leaves the fraction empty.
+Mixed plan, kernel class ``dense_mixed`` (one ``k_dense_mixed`` launch per
+call).  Its bins are compute work on data that stays in L2 (125410 bins x
+48 B per detector), so the bound is the FP32 pipe.  FP32 arithmetic per bin
+and detector, counted from the kernel source (FMA = 2 flops, add/mul = 1):
+
+  phase advance: three exact 2 pi reductions and the FP32 tails      38
+  FMA-only sincos of the advance                                      29
+  rotation by the run's anchor phasor and renormalisation            15
+  per channel (x3): spline value with the peak-kink term 24, model
+    rotation 6, residual 2, |d - h|^2 w 5, |h|^2 w and the cross
+    term of the weak-template form 12                       49 x 3 = 147
+  kink coordinate 3, compensated sum 4, weak-template branch 8       15
+                                                       lnL pass:    244
+  gradient pass: per-channel adjoints 13 x 3 = 39, interval moments
+    (7 quantities x t^0..t^3) 58                              +97 = 341
+
+The per-bin kink moments of post-peak bins are not counted (a lower bound).
+The FP64 run anchors (about 30 FP64 operations per run of <= 32 bins) are
+not in the FP32 count either.
+
+Peak: cuBLAS SGEMM 8192^3 with TF32 off, measured in bench.py (FP32 pipe).
+Traffic: DRAM bytes per dense bin measured by ncu on a 256-sample batch of
+the same workload (dram__bytes_read.sum + dram__bytes_write.sum of one
+k_dense_mixed<1> launch divided by its 19 595 338 dense bins); scaled here by
+the launch's dense bins.
 """
 
-CENSUS = {}
+FP32_FLOPS_PER_DENSE_BIN = {"lnl": 244, "grad": 341}
+DRAM_BYTES_PER_DENSE_BIN = 4.744  # (89.56 MB + 3.40 MB) / 19 595 338 bins, ncu --set full, 256 samples
 
 
-def roofline(kernel_class, launches_ms, engine, theta, fp64_peak_tflops, peaks):
+def roofline(kernel_class, launches_ms, work, grad, fp32_peak_tflops):
+    """Roofline entry for the dominant kernel.
+
+    kernel_class: profiler class name; launches_ms: (launches, summed device ms)
+    over the timed steps; work: WhittleLikelihood.last_work() of one step;
+    grad: whether the step ran the gradient pass.
+    """
     launches, ms = launches_ms
     per_launch_ms = ms / max(1, launches)
     entry = {"kernel": kernel_class, "launches": launches, "avg_launch_ms": per_launch_ms,
-             "bound": "fp64", "unit": "TFLOP/s", "peak": fp64_peak_tflops,
-             "peak_source": "measured cuBLAS DGEMM 8192^3 in bench.py", "achieved": None, "frac": None,
-             "traffic": None}
-    c = CENSUS.get(kernel_class)
-    if c is not None:
-        flops = c(engine, theta)
+             "bound": None, "unit": "TFLOP/s", "peak": None, "peak_source": None, "achieved": None,
+             "frac": None, "traffic": None, "units_per_launch": None}
+    if kernel_class == "dense_mixed":
+        bins = work["dense_bins"]
+        flops = bins * FP32_FLOPS_PER_DENSE_BIN["grad" if grad else "lnl"]
+        entry.update(bound="fp32", peak=fp32_peak_tflops,
+                     peak_source="measured cuBLAS SGEMM 8192^3 (TF32 off) in bench.py",
+                     units_per_launch={"dense_bins": bins, "fp32_flops": flops})
         entry["achieved"] = flops / (per_launch_ms / 1e3) / 1e12
-        entry["frac"] = entry["achieved"] / fp64_peak_tflops if fp64_peak_tflops else None
+        if fp32_peak_tflops:
+            entry["frac"] = entry["achieved"] / fp32_peak_tflops
+        if DRAM_BYTES_PER_DENSE_BIN is not None:
+            entry["traffic"] = DRAM_BYTES_PER_DENSE_BIN * bins
     return entry

@@ -671,6 +671,40 @@ __device__ __forceinline__ float reduce_exact(float x) {
   return r;
 }
 
+// sin and cos of |x| < 2^21 in FP32 FMA arithmetic only: x = k pi/2 + r with
+// k the nearest integer (magic-number rounding, k read from the float's bits)
+// and pi/2 in three parts (k * hi exact for |k| < 2^15), then Taylor
+// polynomials on |r| <= pi/4 (truncation below 2e-9) and the quadrant swap.
+constexpr float kTwoOverPi = 0.6366197466850281f;
+constexpr float kPiO2Hi = 1.5703125f;
+constexpr float kPiO2Mid = 0.0004838267923332751f;
+constexpr float kPiO2Lo = 2.5632829192545614e-12f;
+
+__device__ __forceinline__ void sincos_poly(float x, float* sp, float* cp) {
+  const float kf = fmaf(x, kTwoOverPi, kRoundMagic);
+  const int k = __float_as_int(kf) - __float_as_int(kRoundMagic);
+  const float kr = kf - kRoundMagic;
+  float r = fmaf(-kr, kPiO2Hi, x);
+  r = fmaf(-kr, kPiO2Mid, r);
+  r = fmaf(-kr, kPiO2Lo, r);
+  const float r2 = r * r;
+  float ps = fmaf(r2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+  ps = fmaf(ps, r2, 1.0f / 120.0f);
+  ps = fmaf(ps, r2, -1.0f / 6.0f);
+  const float sr = fmaf(ps * r2, r, r);
+  float pc = fmaf(r2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+  pc = fmaf(pc, r2, -1.0f / 720.0f);
+  pc = fmaf(pc, r2, 1.0f / 24.0f);
+  pc = fmaf(pc, r2, -0.5f);
+  const float cr = fmaf(pc, r2, 1.0f);
+  float sv = (k & 1) ? cr : sr;
+  float cv = (k & 1) ? sr : cr;
+  if (k & 2) sv = -sv;
+  if ((k + 1) & 2) cv = -cv;
+  *sp = sv;
+  *cp = cv;
+}
+
 // head of x truncated to `bits` significant bits (so that head * small integer is exact in FP32)
 __device__ __forceinline__ float head_bits(double x, int bits) {
   const long long m = ~((1LL << (53 - bits)) - 1);
@@ -740,7 +774,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         const float h0 = (float)ph0;
         const float l0 = (float)(ph0 - (double)h0);
         float s0f, c0f;
-        sincosf(h0, &s0f, &c0f);
+        sincos_poly(h0, &s0f, &c0f);
         rp.c0 = fmaf(-s0f, l0, c0f);
         rp.s0 = fmaf(c0f, l0, s0f);
         rp.p1h = head_bits(ph1, 12);
@@ -811,12 +845,11 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float del = reduce_exact(r.p1h * u) + reduce_exact(r.p2h * u2) + reduce_exact(r.p3h * u3) +
                             (r.p1l * u + r.p2l * u2 + r.p3l * u3);
           float sd_, cd_;
-          sincosf(del, &sd_, &cd_);
+          sincos_poly(del, &sd_, &cd_);
           float cph = r.c0 * cd_ - r.s0 * sd_;
           float sph = r.s0 * cd_ + r.c0 * sd_;
-          // FP32 sincos carries a small systematic magnitude excess (mean of
-          // s^2 + c^2 - 1 is about +1.8e-8): renormalise with one Newton step
-          // for 1/|e| so the model amplitude is unbiased.
+          // Renormalise the rotated phasor with one Newton step for 1/|e|
+          // so that FP32 rounding leaves the model amplitude unbiased.
           const float m2 = fmaf(cph, cph, fmaf(sph, sph, -1.0f));  // |e|^2 - 1, one rounding
           const float corr = -0.5f * m2;
           cph = fmaf(corr, cph, cph);
@@ -1219,6 +1252,24 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   k_exact<2, double><<<dim3(kExactBlocks, 1), kExactThreads, 0, st>>>(p->dev, M, G, blocks,
                                                                       reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
+int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const std::vector<int32_t>& ok,
+               int64_t* out, cudaStream_t st) {
+  const MixedDev& M = p->mixed->dev;
+  std::vector<int32_t> xb(B), ns(B);
+  if (B > 0) {
+    PES_CHECK_CUDA(cudaMemcpy(xb.data(), M.xbin, sizeof(int32_t) * B, cudaMemcpyDeviceToHost));
+    PES_CHECK_CUDA(cudaMemcpy(ns.data(), M.nsp, sizeof(int32_t) * B, cudaMemcpyDeviceToHost));
+  }
+  for (int64_t s = 0; s < B; ++s) {
+    if (!ok[s]) continue;
+    out[0] += (kcut[s] - xb[s]) * (int64_t)M.n_det;
+    out[1] += (int64_t)xb[s] * M.n_det;
+    if (ns[s] >= 3) out[2] += (int64_t)(ns[s] + 1) * M.n_det;
+  }
+  (void)st;
   return PES_OK;
 }
 

@@ -1,6 +1,7 @@
 // Batched lnL / lnL+gradient plans: set-up, data ingestion and the dense FP64
 // path (every bin evaluated in FP64: waveform -> links -> TDI -> residual,
 // fused, with a deterministic two-pass reduction per sample).
+#include <cstring>
 #include <cmath>
 #include <cstdlib>
 #include <new>
@@ -424,6 +425,29 @@ int pes_plan_stats(PesPlan* p, int64_t* launches, double* device_ms) {
     p->prof.pool.push_back(e.second.second);
   }
   p->prof.pending.clear();
+  return PES_OK;
+}
+
+int pes_plan_work(PesPlan* p, int64_t B, int64_t* out, void* stream) {
+  PES_REQUIRE(p && out, "pes_plan_work: null pointer");
+  PES_REQUIRE(B >= 0 && B <= p->desc.max_batch, "pes_plan_work: B must be 0..max_batch");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  PES_CHECK_CUDA(cudaStreamSynchronize(st));
+  // the forward set-up blocks hold kcut and status at the same offsets for every scalar type
+  std::vector<unsigned char> raw((size_t)B * sizeof(SampleBlock<double>));
+  if (B > 0) PES_CHECK_CUDA(cudaMemcpy(raw.data(), p->blocks, raw.size(), cudaMemcpyDeviceToHost));
+  std::vector<int64_t> kcut(B);
+  std::vector<int32_t> ok(B);
+  for (int64_t s = 0; s < B; ++s) {
+    SampleBlock<double> b;
+    std::memcpy(&b, raw.data() + (size_t)s * sizeof(SampleBlock<double>), sizeof(b));
+    ok[s] = b.status == kSampleOk;
+    kcut[s] = ok[s] ? b.kcut : 0;
+  }
+  for (int k = 0; k < 4; ++k) out[k] = 0;
+  for (int64_t s = 0; s < B; ++s) out[3] += ok[s];
+  if (p->desc.precision == PES_PRECISION_MIXED) return mixed_work(p, B, kcut, ok, out, st);
+  for (int64_t s = 0; s < B; ++s) out[1] += kcut[s] * p->desc.n_det;
   return PES_OK;
 }
 

@@ -206,6 +206,8 @@ int mixed_create(PesPlan* p);
 void mixed_destroy(PesPlan* p);
 int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cudaStream_t st);
 int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t st);
+int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const std::vector<int32_t>& ok,
+               int64_t* out, cudaStream_t st);
 int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* grad, int32_t* status,
               cudaStream_t st);
 }  // namespace pes

@@ -189,6 +189,16 @@ class WhittleLikelihood:
         self.last_status = status
         return out, grad
 
+    def last_work(self, batch):
+        """Work units of the last call on ``batch`` samples (the last chunk when the
+        call was split at max_batch): dict with the bins through the FP32 dense
+        stage, the bins evaluated directly in FP64, the sparse-node evaluations
+        and the samples in the parameter domain."""
+        out = (ctypes.c_int64 * 4)()
+        _lib.check(_lib.load().pes_plan_work(self._plan, min(int(batch), self.max_batch), out,
+                                             _lib.stream_handle()))
+        return {"dense_bins": out[0], "fp64_bins": out[1], "sparse_nodes": out[2], "samples": out[3]}
+
     def log_likelihood(self, params):
         """Single parameter set (dict / namedtuple with reference names); returns a float."""
         return float(self.log_likelihood_batch(theta_from_parameters(params)).item())
