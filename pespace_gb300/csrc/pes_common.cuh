@@ -22,81 +22,108 @@ constexpr double kEulerGamma = 0.5772156649015329;
 constexpr double kAUsec = kAU / kCSI;  // orbit.py:12
 
 // ------------------------------------------------------------------ dual numbers
-// Forward-mode dual number: FP64 value and N tangents of type D (double for
-// exact derivatives; float to run the tangent arithmetic on the FP32 pipes
-// while the value stays FP64).
-template <int N, class D = double>
+// Forward-mode dual number: a value of type V and N tangents of type D.
+//   Dual<N>                FP64 value and tangents (exact derivatives);
+//   DualF<N> (D = float)   FP64 value, tangent arithmetic on the FP32 pipes;
+//   DualS<N> (V = float)   FP32 value and tangents, for derivative passes whose
+//                          values are needed only through the chain rule.
+template <int N, class D = double, class V = double>
 struct Dual {
-  double v;
+  V v;
   D d[N];
 };
 template <int N> using DualF = Dual<N, float>;
+template <int N> using DualS = Dual<N, float, float>;
 
-PES_HD double val(double x) { return x; }
-template <int N, class D> PES_HD double val(const Dual<N, D>& x) { return x.v; }
-
-template <int N, class D = double>
-PES_HD Dual<N, D> mkdual(double x) {
-  Dual<N, D> r;
-  r.v = x;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = D(0);
-  return r;
-}
-
-#define PES_DUAL template <int N, class D> PES_HD
-PES_DUAL Dual<N, D> operator+(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v + b.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
-PES_DUAL Dual<N, D> operator-(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v - b.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
-PES_DUAL Dual<N, D> operator-(const Dual<N, D>& a) { Dual<N, D> r; r.v = -a.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
-PES_DUAL Dual<N, D> operator*(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v * b.v;
-  const D av = D(a.v), bv = D(b.v);
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bv + av * b.d[i]; return r; }
-PES_DUAL Dual<N, D> operator/(const Dual<N, D>& a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a.v / b.v;
-  const D ib = D(1.0 / b.v), rv = D(r.v);
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - rv * b.d[i]) * ib; return r; }
-PES_DUAL Dual<N, D> operator+(const Dual<N, D>& a, double b) { Dual<N, D> r = a; r.v = a.v + b; return r; }
-PES_DUAL Dual<N, D> operator+(double a, const Dual<N, D>& b) { Dual<N, D> r = b; r.v = a + b.v; return r; }
-PES_DUAL Dual<N, D> operator-(const Dual<N, D>& a, double b) { Dual<N, D> r = a; r.v = a.v - b; return r; }
-PES_DUAL Dual<N, D> operator-(double a, const Dual<N, D>& b) { Dual<N, D> r = -b; r.v = a - b.v; return r; }
-PES_DUAL Dual<N, D> operator*(const Dual<N, D>& a, double b) { Dual<N, D> r; r.v = a.v * b; const D bb = D(b);
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bb; return r; }
-PES_DUAL Dual<N, D> operator*(double a, const Dual<N, D>& b) { Dual<N, D> r; r.v = a * b.v; const D aa = D(a);
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = aa * b.d[i]; return r; }
-PES_DUAL Dual<N, D> operator/(const Dual<N, D>& a, double b) { Dual<N, D> r; r.v = a.v / b; const D ib = D(1.0 / b);
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib; return r; }
-PES_DUAL Dual<N, D> operator/(double a, const Dual<N, D>& b) { return mkdual<N, D>(a) / b; }
-PES_DUAL bool operator<(const Dual<N, D>& a, double b) { return a.v < b; }
-PES_DUAL bool operator<=(const Dual<N, D>& a, double b) { return a.v <= b; }
-PES_DUAL bool operator>(const Dual<N, D>& a, double b) { return a.v > b; }
-PES_DUAL bool operator>=(const Dual<N, D>& a, double b) { return a.v >= b; }
-PES_DUAL bool operator<(const Dual<N, D>& a, const Dual<N, D>& b) { return a.v < b.v; }
-PES_DUAL bool operator>=(const Dual<N, D>& a, const Dual<N, D>& b) { return a.v >= b.v; }
-
-PES_DUAL Dual<N, D> chain1(const Dual<N, D>& a, double fv, double dfv) { Dual<N, D> r; r.v = fv; const D df = D(dfv);
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * df; return r; }
-
-// double overloads (device: CUDA libdevice; host: libm)
-PES_HD double dsin(double x) { return ::sin(x); }
-PES_HD double dcos(double x) { return ::cos(x); }
-PES_HD void dsincos(double x, double* s, double* c) {
+// value functions in the value's own precision
+PES_HD double vsqrt(double x) { return ::sqrt(x); }
+PES_HD float vsqrt(float x) { return ::sqrtf(x); }
+PES_HD double vexp(double x) { return ::exp(x); }
+PES_HD float vexp(float x) { return ::expf(x); }
+PES_HD double vlog(double x) { return ::log(x); }
+PES_HD float vlog(float x) { return ::logf(x); }
+PES_HD double vcbrt(double x) { return ::cbrt(x); }
+PES_HD float vcbrt(float x) { return ::cbrtf(x); }
+PES_HD double vatan(double x) { return ::atan(x); }
+PES_HD float vatan(float x) { return ::atanf(x); }
+PES_HD double vpow(double x, double p) { return ::pow(x, p); }
+PES_HD float vpow(float x, float p) { return ::powf(x, p); }
+PES_HD void vsincos(double x, double* s, double* c) {
 #ifdef __CUDA_ARCH__
   ::sincos(x, s, c);
 #else
   *s = ::sin(x); *c = ::cos(x);
 #endif
 }
+PES_HD void vsincos(float x, float* s, float* c) {
+#ifdef __CUDA_ARCH__
+  ::sincosf(x, s, c);
+#else
+  *s = ::sinf(x); *c = ::cosf(x);
+#endif
+}
+
+PES_HD double val(double x) { return x; }
+template <int N, class D, class V> PES_HD double val(const Dual<N, D, V>& x) { return (double)x.v; }
+
+template <int N, class D = double, class V = double>
+PES_HD Dual<N, D, V> mkdual(double x) {
+  Dual<N, D, V> r;
+  r.v = V(x);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = D(0);
+  return r;
+}
+
+#define PES_DUAL template <int N, class D, class V> PES_HD
+#define PES_DT Dual<N, D, V>
+PES_DUAL PES_DT operator+(const PES_DT& a, const PES_DT& b) { PES_DT r; r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
+PES_DUAL PES_DT operator-(const PES_DT& a, const PES_DT& b) { PES_DT r; r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
+PES_DUAL PES_DT operator-(const PES_DT& a) { PES_DT r; r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
+PES_DUAL PES_DT operator*(const PES_DT& a, const PES_DT& b) { PES_DT r; r.v = a.v * b.v;
+  const D av = D(a.v), bv = D(b.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bv + av * b.d[i]; return r; }
+PES_DUAL PES_DT operator/(const PES_DT& a, const PES_DT& b) { PES_DT r; r.v = a.v / b.v;
+  const D ib = D(V(1) / b.v), rv = D(r.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - rv * b.d[i]) * ib; return r; }
+PES_DUAL PES_DT operator+(const PES_DT& a, double b) { PES_DT r = a; r.v = a.v + V(b); return r; }
+PES_DUAL PES_DT operator+(double a, const PES_DT& b) { PES_DT r = b; r.v = V(a) + b.v; return r; }
+PES_DUAL PES_DT operator-(const PES_DT& a, double b) { PES_DT r = a; r.v = a.v - V(b); return r; }
+PES_DUAL PES_DT operator-(double a, const PES_DT& b) { PES_DT r = -b; r.v = V(a) - b.v; return r; }
+PES_DUAL PES_DT operator*(const PES_DT& a, double b) { PES_DT r; r.v = a.v * V(b); const D bb = D(b);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bb; return r; }
+PES_DUAL PES_DT operator*(double a, const PES_DT& b) { PES_DT r; r.v = V(a) * b.v; const D aa = D(a);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = aa * b.d[i]; return r; }
+PES_DUAL PES_DT operator/(const PES_DT& a, double b) { PES_DT r; const V bv = V(b); r.v = a.v / bv;
+  const D ib = D(V(1) / bv);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib; return r; }
+PES_DUAL PES_DT operator/(double a, const PES_DT& b) { return mkdual<N, D, V>(a) / b; }
+PES_DUAL bool operator<(const PES_DT& a, double b) { return a.v < V(b); }
+PES_DUAL bool operator<=(const PES_DT& a, double b) { return a.v <= V(b); }
+PES_DUAL bool operator>(const PES_DT& a, double b) { return a.v > V(b); }
+PES_DUAL bool operator>=(const PES_DT& a, double b) { return a.v >= V(b); }
+PES_DUAL bool operator<(const PES_DT& a, const PES_DT& b) { return a.v < b.v; }
+PES_DUAL bool operator>=(const PES_DT& a, const PES_DT& b) { return a.v >= b.v; }
+
+PES_DUAL PES_DT chain1(const PES_DT& a, V fv, V dfv) { PES_DT r; r.v = fv; const D df = D(dfv);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * df; return r; }
+
+// double overloads (device: CUDA libdevice; host: libm)
+PES_HD double dsin(double x) { return ::sin(x); }
+PES_HD double dcos(double x) { return ::cos(x); }
+PES_HD void dsincos(double x, double* s, double* c) { vsincos(x, s, c); }
 PES_HD double dexp(double x) { return ::exp(x); }
 PES_HD double dlog(double x) { return ::log(x); }
 PES_HD double dsqrt(double x) { return ::sqrt(x); }
@@ -105,22 +132,25 @@ PES_HD double datan(double x) { return ::atan(x); }
 PES_HD double dpow(double x, double p) { return ::pow(x, p); }
 PES_HD double dabs(double x) { return ::fabs(x); }
 
-PES_DUAL Dual<N, D> dsin(const Dual<N, D>& a) { double s, c; dsincos(a.v, &s, &c); return chain1(a, s, c); }
-PES_DUAL Dual<N, D> dcos(const Dual<N, D>& a) { double s, c; dsincos(a.v, &s, &c); return chain1(a, c, -s); }
-PES_DUAL void dsincos(const Dual<N, D>& a, Dual<N, D>* s, Dual<N, D>* c) {
-  double sv, cv; dsincos(a.v, &sv, &cv); *s = chain1(a, sv, cv); *c = chain1(a, cv, -sv); }
-PES_DUAL Dual<N, D> dexp(const Dual<N, D>& a) { double e = ::exp(a.v); return chain1(a, e, e); }
-PES_DUAL Dual<N, D> dlog(const Dual<N, D>& a) { return chain1(a, ::log(a.v), 1.0 / a.v); }
-PES_DUAL Dual<N, D> dsqrt(const Dual<N, D>& a) { double s = ::sqrt(a.v); return chain1(a, s, 0.5 / s); }
-PES_DUAL Dual<N, D> dcbrt(const Dual<N, D>& a) { double c = ::cbrt(a.v); return chain1(a, c, 1.0 / (3.0 * c * c)); }
-PES_DUAL Dual<N, D> datan(const Dual<N, D>& a) { return chain1(a, ::atan(a.v), 1.0 / (1.0 + a.v * a.v)); }
-PES_DUAL Dual<N, D> dpow(const Dual<N, D>& a, double p) { double q = ::pow(a.v, p); return chain1(a, q, p * q / a.v); }
-PES_DUAL Dual<N, D> dabs(const Dual<N, D>& a) { return a.v < 0.0 ? -a : a; }
+PES_DUAL PES_DT dsin(const PES_DT& a) { V s, c; vsincos(a.v, &s, &c); return chain1(a, s, c); }
+PES_DUAL PES_DT dcos(const PES_DT& a) { V s, c; vsincos(a.v, &s, &c); return chain1(a, c, -s); }
+PES_DUAL void dsincos(const PES_DT& a, PES_DT* s, PES_DT* c) {
+  V sv, cv; vsincos(a.v, &sv, &cv); *s = chain1(a, sv, cv); *c = chain1(a, cv, -sv); }
+PES_DUAL PES_DT dexp(const PES_DT& a) { const V e = vexp(a.v); return chain1(a, e, e); }
+PES_DUAL PES_DT dlog(const PES_DT& a) { return chain1(a, vlog(a.v), V(1) / a.v); }
+PES_DUAL PES_DT dsqrt(const PES_DT& a) { const V s = vsqrt(a.v); return chain1(a, s, V(0.5) / s); }
+PES_DUAL PES_DT dcbrt(const PES_DT& a) { const V c = vcbrt(a.v); return chain1(a, c, V(1) / (V(3) * c * c)); }
+PES_DUAL PES_DT datan(const PES_DT& a) { return chain1(a, vatan(a.v), V(1) / (V(1) + a.v * a.v)); }
+PES_DUAL PES_DT dpow(const PES_DT& a, double p) { const V pv = V(p), q = vpow(a.v, pv); return chain1(a, q, pv * q / a.v); }
+PES_DUAL PES_DT dabs(const PES_DT& a) { return a.v < V(0) ? -a : a; }
+#undef PES_DT
 #undef PES_DUAL
 
 template <class T> struct Lift { PES_HD static T from(double x); };
 template <> struct Lift<double> { PES_HD static double from(double x) { return x; } };
-template <int N, class D> struct Lift<Dual<N, D>> { PES_HD static Dual<N, D> from(double x) { return mkdual<N, D>(x); } };
+template <int N, class D, class V> struct Lift<Dual<N, D, V>> {
+  PES_HD static Dual<N, D, V> from(double x) { return mkdual<N, D, V>(x); }
+};
 template <class T> PES_HD T lift(double x) { return Lift<T>::from(x); }
 
 // ------------------------------------------------------------------ complex

@@ -43,7 +43,8 @@ constexpr double kOrbitPhaseMax = 0.3;  // rad of yearly orbital phase per node 
 constexpr int kExactBlocks = 4;         // blocks per sample of the exact-bin kernel
 constexpr int kExactThreads = 128;
 __device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
-using GradScalar = DualF<kMixNT>;
+using GradScalar = DualF<kMixNT>;    // exact bins: FP64 values (phases of 1e6 rad), FP32 tangents
+using NodeGradScalar = DualS<kMixNT>;  // sparse nodes: the values enter only through the chain rule
 
 struct MixedDev {
   int32_t J;                // nodes
@@ -84,6 +85,7 @@ struct MixedDev {
   double* part;             // [B][nblk_dense] lnL partials
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
+  void* gblocks32;          // [B] SampleBlock<NodeGradScalar>
   double* gdir;             // [B][n_det] direct t_c term of the gradient
   // Amplitude kink at f_peak: the transfer quantities carry C_q max(0, Mf - Mf_peak)^2
   // (C_q = jump/2 * R_q, R_q = G_q(f_peak)/Ahat(f_peak)); it is removed from the
@@ -197,15 +199,18 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
 // Gradient set-up: per sample, the coefficient block with exact FP64
 // tangents, stored with FP32 tangents for the node kernel.
 __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_t B,
-                             SampleBlock<GradScalar>* __restrict__ out) {
+                             SampleBlock<GradScalar>* __restrict__ out,
+                             SampleBlock<NodeGradScalar>* __restrict__ out32) {
   using TD = Dual<kMixNT, double>;
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
   double raw[11];
   for (int j = 0; j < 11; ++j) raw[j] = theta[11 * s + j];
   SampleBlock<GradScalar>& o = out[s];
+  SampleBlock<NodeGradScalar>& o32 = out32[s];
   if (!theta_in_domain(raw)) {
     o.status = kSampleOutOfDomain;
+    o32.status = kSampleOutOfDomain;
     return;
   }
   TD th[11];
@@ -236,14 +241,32 @@ __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_
   narrow(reinterpret_cast<const TD*>(&pol), reinterpret_cast<GradScalar*>(&o.pol), sizeof(Polar<TD>) / sizeof(TD));
   narrow(&th[10], &o.tc, 1);
   o.status = kSampleOk;
+  static_assert(sizeof(PhenomDCoef<TD>) / sizeof(TD) ==
+                    sizeof(PhenomDCoef<NodeGradScalar>) / sizeof(NodeGradScalar),
+                "coefficient block must be an array of scalars");
+  static_assert(sizeof(Polar<TD>) / sizeof(TD) == sizeof(Polar<NodeGradScalar>) / sizeof(NodeGradScalar),
+                "polarisation block must be an array of scalars");
+  auto narrow32 = [](const TD* a, NodeGradScalar* b, int n) {
+    for (int k = 0; k < n; ++k) {
+      b[k].v = (float)a[k].v;
+      for (int i = 0; i < kMixNT; ++i) b[k].d[i] = (float)a[k].d[i];
+    }
+  };
+  narrow32(reinterpret_cast<const TD*>(&wf), reinterpret_cast<NodeGradScalar*>(&o32.wf),
+           sizeof(PhenomDCoef<TD>) / sizeof(TD));
+  narrow32(reinterpret_cast<const TD*>(&pol), reinterpret_cast<NodeGradScalar*>(&o32.pol),
+           sizeof(Polar<TD>) / sizeof(TD));
+  narrow32(&th[10], &o32.tc, 1);
+  o32.status = kSampleOk;
 }
 
 // Backward: recompute the node quantities with tangents and contract with the node adjoints.
 __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G, double wscale) {
-  __shared__ SampleBlock<GradScalar> sb;
+  using GS = NodeGradScalar;
+  __shared__ SampleBlock<GS> sb;
   __shared__ double red[kSparseThreads / 32][11];
   const int s = blockIdx.z, d = blockIdx.y;
-  load_block(reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), s, sb);
+  load_block(reinterpret_cast<const SampleBlock<GS>*>(M.gblocks32), s, sb);
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
@@ -251,14 +274,14 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
 #pragma unroll
   for (int k = 0; k < 11; ++k) acc[k] = 0.0;
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
-    GradScalar y[kNodeQ];
+    GS y[kNodeQ];
     const double fj = M.node_f[j];
-    node_eval<GradScalar>(P, M, sb, d, G.gen20[d], fj, y);
-    const GradScalar xk = sb.wf.Msec * fj - sb.wf.fpeak;
+    node_eval<GS>(P, M, sb, d, G.gen20[d], fj, y);
+    const GS xk = sb.wf.Msec * fj - sb.wf.fpeak;
     if (xk.v > 0.0) {
-      GradScalar ahat, jump;
-      amp_peak_jump<GradScalar>(sb.wf, ahat, jump);
-      const GradScalar x2h = 0.5 * (xk * xk) * jump;
+      GS ahat, jump;
+      amp_peak_jump<GS>(sb.wf, ahat, jump);
+      const GS x2h = 0.5 * (xk * xk) * jump;
       const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
 #pragma unroll
       for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - R[q] * x2h;  // R_q held fixed
@@ -275,8 +298,8 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
   }
   // dense-side kink term C_q x^2 (x = Msec f - Mf_peak): one thread per (sample, detector)
   if (blockIdx.x == 0 && threadIdx.x == 0 && sb.status == kSampleOk && ns >= 3) {
-    GradScalar ahat, jump;
-    amp_peak_jump<GradScalar>(sb.wf, ahat, jump);
+    GS ahat, jump;
+    amp_peak_jump<GS>(sb.wf, ahat, jump);
     const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
     const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
     const double* K = M.kinkM + ((size_t)s * M.n_det + d) * 12;
@@ -1103,6 +1126,7 @@ int mixed_create(PesPlan* p) {
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
+  SampleBlock<NodeGradScalar>* gblk32;
   double *kR, *kC, *kM;
   float* kF;
   float* bin_t;
@@ -1122,7 +1146,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
-      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
+      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &gblk32, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
       (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) ||
       (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * kExactBlocks)) ||
       (rc = alloc(mb, &xgpart, (size_t)B * kExactBlocks * 11)))
@@ -1199,6 +1223,7 @@ int mixed_create(PesPlan* p) {
   M.gpart = gpart;
   M.gdir = gdir;
   M.gblocks = gblk;
+  M.gblocks32 = gblk32;
   M.kinkR = kR;
   M.kinkC = kC;
   M.kinkF = kF;
@@ -1301,7 +1326,8 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     {
       ProfScope ps(p, kKSetup, side);
       k_setup_grad<<<ceil_div(B, 64), 64, 0, side>>>(p->dev, theta, B,
-                                                     reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks));
+                                                     reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks),
+                                                     reinterpret_cast<SampleBlock<NodeGradScalar>*>(M.gblocks32));
     }
     PES_CHECK_LAUNCH();
     {

@@ -130,20 +130,20 @@ template <> struct Seed<double> {
   PES_HD static double make(double v, int) { return v; }
   static constexpr int N = 0;
 };
-template <int N, class D> struct Seed<Dual<N, D>> {
-  PES_HD static Dual<N, D> make(double v, int slot) {
-    Dual<N, D> r = mkdual<N, D>(v);
+template <int N, class D, class V> struct Seed<Dual<N, D, V>> {
+  PES_HD static Dual<N, D, V> make(double v, int slot) {
+    Dual<N, D, V> r = mkdual<N, D, V>(v);
     if (slot >= 0 && slot < N) r.d[slot] = D(1);
     return r;
   }
   static constexpr int NT = N;
 };
 template <class T> struct NumTangents { static constexpr int value = 0; };
-template <int N, class D> struct NumTangents<Dual<N, D>> { static constexpr int value = N; };
+template <int N, class D, class V> struct NumTangents<Dual<N, D, V>> { static constexpr int value = N; };
 
 template <class T> PES_HD void scalar_to(const T& x, double* out);
 template <> PES_HD void scalar_to<double>(const double& x, double* out) { out[0] = x; }
-template <int N, class D> PES_HD void scalar_to(const Dual<N, D>& x, double* out) {
+template <int N, class D, class V> PES_HD void scalar_to(const Dual<N, D, V>& x, double* out) {
   out[0] = x.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) out[1 + i] = x.d[i];
