@@ -35,6 +35,8 @@ constexpr int kChunkMax = 32;     // bins per phase-anchored run (one warp)
 constexpr int kMixThreads = 128;  // 4 warps; each warp owns 32 consecutive runs
 constexpr int kMoments = 4;       // t^0..t^3
 constexpr int kSparseThreads = 128;
+// FP32 copies of the shared grid's spline factors, [kGfCount][J]: h, 1/h, lo, up, 1/den, cp.
+enum { kGfH = 0, kGfInvH, kGfLo, kGfUp, kGfInvDen, kGfCp, kGfCount };
 // Gradient: one pass with FP64 values and FP32 tangents for the 9 parameters
 // that enter the node quantities non-trivially; ln D_L (G ~ 1/D_L) and phi_c
 // (Phi_s shifts by -2 phi_c) are applied analytically.
@@ -75,6 +77,7 @@ struct MixedDev {
   const double* gup;        // [J]
   const double* ginvden;    // [J] 1 / Thomas pivots
   const double* gcp;        // [J] Thomas super-diagonal ratios
+  const float* gf;          // [kGfCount][J] FP32 copies of gh, ginvh, glo, gup, ginvden, gcp
   double* yv;               // [B][n_det][J][7] node values (quantity fastest)
   double* scr;              // [B][n_det][J][7] spline scratch
   double* cphi;             // [B][n_det][J][4] phase spline coefficients (FP64)
@@ -406,33 +409,210 @@ __device__ __forceinline__ void nak_ends(const double* f, int n, double m1, doub
 // from 0 to get the segment's affine map x_in -> A x_in + B, a warp scan of
 // those maps gives the exact value entering every segment, and the lane then
 // reruns its segment from that value.  `reverse` scans from lane 31 down.
-__device__ __forceinline__ double segment_carry_in(double A, double B, bool reverse) {
+template <class R>
+__device__ __forceinline__ R segment_carry_in(R A, R B, bool reverse) {
   const int lane = threadIdx.x & 31;
   const int pos = reverse ? 31 - lane : lane;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const double Ap = reverse ? __shfl_down_sync(0xffffffffu, A, o) : __shfl_up_sync(0xffffffffu, A, o);
-    const double Bp = reverse ? __shfl_down_sync(0xffffffffu, B, o) : __shfl_up_sync(0xffffffffu, B, o);
+    const R Ap = reverse ? __shfl_down_sync(0xffffffffu, A, o) : __shfl_up_sync(0xffffffffu, A, o);
+    const R Bp = reverse ? __shfl_down_sync(0xffffffffu, B, o) : __shfl_up_sync(0xffffffffu, B, o);
     if (pos >= o) {
-      B = fma(A, Bp, B);
+      B = A * Bp + B;
       A = A * Ap;
     }
   }
-  const double prev = reverse ? __shfl_down_sync(0xffffffffu, B, 1) : __shfl_up_sync(0xffffffffu, B, 1);
-  return pos == 0 ? 0.0 : prev;
+  const R prev = reverse ? __shfl_down_sync(0xffffffffu, B, 1) : __shfl_up_sync(0xffffffffu, B, 1);
+  return pos == 0 ? R(0) : prev;
 }
+
 
 constexpr int kSplineThreads = kNodeQ * 32;  // one warp per quantity, one block per (sample, detector)
 
-// Fit: warp per (sample, detector, quantity); lane l owns intervals and rows
+// Transfer quantities (q >= 1) of the fit: slopes and right-hand sides in FP64
+// from the FP64 node values (their differences cancel), the tridiagonal solve
+// in FP32 (these coefficients are stored in FP32), the left value as a
+// float-float pair.  Scratch per (node, quantity): (rhs | d' | m, slope).
+__device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t sd, int q, int n) {
+  const int lane = threadIdx.x & 31;
+  const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;
+  float2* S = reinterpret_cast<float2*>(M.scr + (size_t)sd * M.J * kNodeQ + q);
+  const float* fh = M.gf + (size_t)kGfH * M.J;
+  const float* fih = M.gf + (size_t)kGfInvH * M.J;
+  const float* flo = M.gf + (size_t)kGfLo * M.J;
+  const float* fid = M.gf + (size_t)kGfInvDen * M.J;
+  const float* fcp = M.gf + (size_t)kGfCp * M.J;
+  const int seg = (n + 31) >> 5;
+  const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);
+  const int r0 = max(1, i0), r1 = i1;
+  if (i0 < i1) {
+    double sp = (i0 >= 1) ? (y[i0 * kNodeQ] - y[(i0 - 1) * kNodeQ]) * M.ginvh[i0 - 1] : 0.0;
+    for (int i = i0; i < i1; ++i) {
+      const double sl = (y[(i + 1) * kNodeQ] - y[i * kNodeQ]) * M.ginvh[i];
+      S[i * kNodeQ] = make_float2(i >= 1 ? (float)(6.0 * (sl - sp)) : 0.0f, (float)sl);
+      sp = sl;
+    }
+  }
+  double lo_d, di_d, up_d;
+  nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
+  const float lo_l = (float)lo_d;
+  const float iden_l = (float)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
+  float A = 1.0f, x = 0.0f;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r0; i < r1; ++i) {
+      const bool last = i == n - 1;
+      const float l = last ? lo_l : flo[i];
+      const float id = last ? iden_l : fid[i];
+      float2 v = S[i * kNodeQ];
+      x = (v.x - l * x) * id;
+      if (pass == 0) {
+        A = -l * id * A;
+      } else {
+        v.x = x;
+        S[i * kNodeQ] = v;
+      }
+    }
+    if (pass == 0) x = segment_carry_in<float>(A, x, false);
+  }
+  A = 1.0f;
+  x = 0.0f;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r1 - 1; i >= r0; --i) {
+      const float c = (i == n - 1) ? 0.0f : fcp[i];
+      float2 v = S[i * kNodeQ];
+      x = v.x - c * x;
+      if (pass == 0) {
+        A = -c * A;
+      } else {
+        v.x = x;
+        S[i * kNodeQ] = v;
+      }
+    }
+    if (pass == 0) x = segment_carry_in<float>(A, x, true);
+  }
+  __syncwarp();
+  const float h0 = fh[0], h1 = fh[1], ha = fh[n - 2], hb = fh[n - 1];
+  const float m0 = ((h0 + h1) * S[1 * kNodeQ].x - h0 * S[2 * kNodeQ].x) / h1;
+  const float mn = ((ha + hb) * S[(n - 1) * kNodeQ].x - hb * S[(n - 2) * kNodeQ].x) / ha;
+  if (i0 >= i1) return;
+  float mi = (i0 == 0) ? m0 : S[i0 * kNodeQ].x;
+  for (int i = i0; i < i1; ++i) {
+    const float mj = (i + 1 == n) ? mn : S[(i + 1) * kNodeQ].x;
+    const float sl = S[i * kNodeQ].y;
+    const float bc = sl - fh[i] * (2.0f * mi + mj) * (1.0f / 6.0f);
+    const float cc = 0.5f * mi;
+    const float dc = (mj - mi) * fih[i] * (1.0f / 6.0f);
+    const double a = y[i * kNodeQ];
+    const float ahi = (float)a;
+    M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, bc, cc, dc);
+    M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(a - (double)ahi);
+    mi = mj;
+  }
+}
+
+// Transfer quantities (q >= 1) of the adjoint: right-hand sides from the FP64
+// moments in FP64, the transposed solve and the node adjoints in FP32.
+__device__ __forceinline__ void spline_adjoint_transfer(const MixedDev& M, int64_t sd, int q, int n, double wscale) {
+  const int lane = threadIdx.x & 31;
+  const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
+  float2* X = reinterpret_cast<float2*>(M.scr + (size_t)sd * M.J * kNodeQ + q);
+  double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
+  const float* fih = M.gf + (size_t)kGfInvH * M.J;
+  const float* flo = M.gf + (size_t)kGfLo * M.J;
+  const float* fup = M.gf + (size_t)kGfUp * M.J;
+  const float* fid = M.gf + (size_t)kGfInvDen * M.J;
+  const int seg = (n + 31) >> 5;
+  const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);
+  const int r0 = max(1, i0), r1 = i1;
+  auto mm = [&](int i, int p) { return wscale * mom[(size_t)i * kNodeQ * kMoments + p]; };
+  auto mbar_left = [&](int i) {
+    const double h = M.gh[i], ih = M.ginvh[i];
+    return -h * mm(i, 1) * (1.0 / 3.0) + 0.5 * mm(i, 2) - mm(i, 3) * ih * (1.0 / 6.0);
+  };
+  auto mbar_right = [&](int i) {
+    const double h = M.gh[i], ih = M.ginvh[i];
+    return -h * mm(i, 1) * (1.0 / 6.0) + mm(i, 3) * ih * (1.0 / 6.0);
+  };
+  {
+    const double mb0 = mbar_left(0), mbn = mbar_right(n - 1);
+    const double h0 = M.gh[0], h1 = M.gh[1], ha = M.gh[n - 2], hb = M.gh[n - 1];
+    for (int i = r0; i < r1; ++i) {
+      double v = mbar_right(i - 1) + mbar_left(i);
+      if (i == 1) v += mb0 * (h0 + h1) / h1;
+      if (i == 2) v -= mb0 * h0 / h1;
+      if (i == n - 1) v += mbn * (ha + hb) / ha;
+      if (i == n - 2) v -= mbn * hb / ha;
+      X[i * kNodeQ] = make_float2((float)v, 0.0f);
+    }
+  }
+  double lo_d, di_d, up_d;
+  nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
+  const float lo_l = (float)lo_d;
+  const float iden_l = (float)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
+  float A = 1.0f, x = 0.0f;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r0; i < r1; ++i) {
+      const float sub = (i > 1) ? fup[i - 1] : 0.0f;
+      const float id = (i == n - 1) ? iden_l : fid[i];
+      float2 v = X[i * kNodeQ];
+      x = (v.x - sub * x) * id;
+      if (pass == 0) {
+        A = -sub * id * A;
+      } else {
+        v.x = x;
+        X[i * kNodeQ] = v;
+      }
+    }
+    if (pass == 0) x = segment_carry_in<float>(A, x, false);
+  }
+  A = 1.0f;
+  x = 0.0f;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = r1 - 1; i >= r0; --i) {
+      const float c = (i == n - 1) ? 0.0f : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
+      float2 v = X[i * kNodeQ];
+      x = v.x - c * x;
+      if (pass == 0) {
+        A = -c * A;
+      } else {
+        v.x = x;
+        X[i * kNodeQ] = v;
+      }
+    }
+    if (pass == 0) x = segment_carry_in<float>(A, x, true);
+  }
+  __syncwarp();
+  auto rb = [&](int i) { return (i >= 1 && i <= n - 1) ? X[i * kNodeQ].x : 0.0f; };
+  if (i0 < i1) {
+    float rcur = rb(i0);
+    float dprev = 0.0f;
+    if (i0 > 0) dprev = ((float)mm(i0 - 1, 1) + 6.0f * (rb(i0 - 1) - rcur)) * fih[i0 - 1];
+    for (int i = i0; i < i1; ++i) {
+      const float rnext = rb(i + 1);
+      const float Db = (float)mm(i, 1) + 6.0f * (rcur - rnext);
+      yb[i * kNodeQ] = (double)(dprev + (float)mm(i, 0) - Db * fih[i]);
+      dprev = Db * fih[i];
+      rcur = rnext;
+    }
+    if (i1 == n) yb[n * kNodeQ] = (double)dprev;
+  }
+  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+}
+
+// Fit for grids of more than 32 x 32 intervals (segments in global scratch):
+// warp per (sample, detector, quantity); lane l owns intervals and rows
 // [l*seg, (l+1)*seg) of the sample's n intervals.  Rows 1..n-2 use the shared
 // grid's precomputed Thomas factors, row n-1 the sample's not-a-knot end row.
-__global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
+__global__ void __launch_bounds__(kSplineThreads) k_spline_fit_wide(MixedDev M) {
   const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t sd = blockIdx.x;
   const int64_t s = sd / M.n_det;
   const int n = M.nsp[s];
   if (n < 3) return;
+  if (q > 0) {
+    spline_fit_transfer(M, sd, q, n);
+    return;
+  }
   const double* f = M.node_f;
   const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;  // y[i * kNodeQ]
   double* S = M.scr + (size_t)sd * M.J * kNodeQ + q;       // d' then m
@@ -459,7 +639,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
         else S[i * kNodeQ] = x;
       }
     }
-    if (pass == 0) x = segment_carry_in(A, x, false);
+    if (pass == 0) x = segment_carry_in<double>(A, x, false);
   }
   // back substitution m_i = d'_i - cp_i m_{i+1}  (m_{n-1} = d'_{n-1})
   __syncwarp();
@@ -472,7 +652,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
       if (pass == 0) A = -c * A;
       else S[i * kNodeQ] = x;
     }
-    if (pass == 0) x = segment_carry_in(A, x, true);
+    if (pass == 0) x = segment_carry_in<double>(A, x, true);
   }
   __syncwarp();
   double m0, mn;
@@ -506,7 +686,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
 // Transpose of the fit: interval coefficient adjoints (the dense moments,
 // times wscale) -> node adjoints ybar; also the direct t_c term (q == 0).
 // Same warp decomposition as the fit.
-__global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, double wscale) {
+__global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint_wide(MixedDev M, double wscale) {
   const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t sd = blockIdx.x;
   const int64_t s = sd / M.n_det;
@@ -515,6 +695,10 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, d
   if (n < 3) {
     for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
     if (q == 0 && lane == 0) M.gdir[sd] = 0.0;
+    return;
+  }
+  if (q > 0) {
+    spline_adjoint_transfer(M, sd, q, n, wscale);
     return;
   }
   const double* f = M.node_f;
@@ -556,7 +740,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, d
       if (pass == 0) A = -sub * id * A;
       else X[i * kNodeQ] = x;
     }
-    if (pass == 0) x = segment_carry_in(A, x, false);
+    if (pass == 0) x = segment_carry_in<double>(A, x, false);
   }
   __syncwarp();
   // L^T rbar = z: rbar_i = z_i - (lo_{i+1} / den_i) rbar_{i+1}
@@ -569,7 +753,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, d
       if (pass == 0) A = -c * A;
       else X[i * kNodeQ] = x;
     }
-    if (pass == 0) x = segment_carry_in(A, x, true);
+    if (pass == 0) x = segment_carry_in<double>(A, x, true);
   }
   __syncwarp();
   // node adjoints: ybar_i = Dbar_{i-1}/h_{i-1} + wscale mm0_i - Dbar_i/h_i,
@@ -596,6 +780,306 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, d
     for (int o = 16; o > 0; o >>= 1) gd += __shfl_xor_sync(0xffffffffu, gd, o);
     if (lane == 0) M.gdir[sd] = wscale * gd;
   }
+}
+
+// Register-segment versions (n <= 32 x 32 intervals, the default grid): each
+// lane keeps its segment's rows in registers (fully unrolled, predicated
+// loops), so the recurrences wait on arithmetic only.  Phase (q == 0) in FP64,
+// transfer quantities in FP32 with FP64 slopes and right-hand sides.
+constexpr int kSegMax = 32;
+
+template <class R>
+__device__ __forceinline__ const R* spline_factor(const MixedDev& M, int which) {
+  if constexpr (sizeof(R) == 8) {
+    switch (which) {
+      case kGfH: return reinterpret_cast<const R*>(M.gh);
+      case kGfInvH: return reinterpret_cast<const R*>(M.ginvh);
+      case kGfLo: return reinterpret_cast<const R*>(M.glo);
+      case kGfUp: return reinterpret_cast<const R*>(M.gup);
+      case kGfInvDen: return reinterpret_cast<const R*>(M.ginvden);
+      default: return reinterpret_cast<const R*>(M.gcp);
+    }
+  } else {
+    return reinterpret_cast<const R*>(M.gf + (size_t)which * M.J);
+  }
+}
+
+template <class R>
+__device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, int q, int n, R* smem4) {
+  const int lane = threadIdx.x & 31;
+  const double* __restrict__ y = M.yv + (size_t)sd * M.J * kNodeQ + q;
+  const R* __restrict__ fh = spline_factor<R>(M, kGfH);
+  const R* __restrict__ fih = spline_factor<R>(M, kGfInvH);
+  const R* __restrict__ flo = spline_factor<R>(M, kGfLo);
+  const R* __restrict__ fid = spline_factor<R>(M, kGfInvDen);
+  const R* __restrict__ fcp = spline_factor<R>(M, kGfCp);
+  const int seg = (n + 31) >> 5;
+  const int i0 = min(n, lane * seg), cnt = min(n, i0 + seg) - i0;
+  double lo_d, di_d, up_d;
+  nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
+  const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
+  // right-hand sides 6 (slope_i - slope_{i-1}) of rows i0 + k, in FP64
+  R x[kSegMax];
+  {
+    double yp = (i0 >= 1) ? y[(i0 - 1) * kNodeQ] : 0.0;
+    double yc = y[i0 * kNodeQ];
+    double sp = (i0 >= 1) ? (yc - yp) * M.ginvh[i0 - 1] : 0.0;
+#pragma unroll
+    for (int k = 0; k < kSegMax; ++k) {
+      x[k] = R(0);
+      if (k < cnt) {
+        const int i = i0 + k;
+        const double yn = y[(i + 1) * kNodeQ];
+        const double sl = (yn - yc) * M.ginvh[i];
+        if (i >= 1) x[k] = (R)(6.0 * (sl - sp));
+        sp = sl;
+        yc = yn;
+      }
+    }
+  }
+  // forward elimination (rows 1..n-1)
+  R A = R(1), v = R(0);
+#pragma unroll
+  for (int k = 0; k < kSegMax; ++k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const bool last = i == n - 1;
+      const R l = last ? lo_l : flo[i], id = last ? iden_l : fid[i];
+      v = (x[k] - l * v) * id;
+      A = -l * id * A;
+    }
+  }
+  v = segment_carry_in<R>(A, v, false);
+#pragma unroll
+  for (int k = 0; k < kSegMax; ++k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const bool last = i == n - 1;
+      const R l = last ? lo_l : flo[i], id = last ? iden_l : fid[i];
+      v = (x[k] - l * v) * id;
+      x[k] = v;
+    }
+  }
+  // back substitution m_i = d'_i - cp_i m_{i+1}
+  A = R(1);
+  v = R(0);
+#pragma unroll
+  for (int k = kSegMax - 1; k >= 0; --k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const R c = (i == n - 1) ? R(0) : fcp[i];
+      v = x[k] - c * v;
+      A = -c * A;
+    }
+  }
+  v = segment_carry_in<R>(A, v, true);
+#pragma unroll
+  for (int k = kSegMax - 1; k >= 0; --k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const R c = (i == n - 1) ? R(0) : fcp[i];
+      v = x[k] - c * v;
+      x[k] = v;
+    }
+  }
+  // m_1, m_2, m_{n-2}, m_{n-1} for the eliminated end values
+#pragma unroll
+  for (int k = 0; k < kSegMax; ++k) {
+    const int i = i0 + k;
+    if (k < cnt) {
+      if (i == 1) smem4[0] = x[k];
+      if (i == 2) smem4[1] = x[k];
+      if (i == n - 2) smem4[2] = x[k];
+      if (i == n - 1) smem4[3] = x[k];
+    }
+  }
+  __syncwarp();
+  const R h0 = fh[0], h1 = fh[1], ha = fh[n - 2], hb = fh[n - 1];
+  const R m0 = ((h0 + h1) * smem4[0] - h0 * smem4[1]) / h1;
+  const R mn = ((ha + hb) * smem4[3] - hb * smem4[2]) / ha;
+  const R next_first = __shfl_down_sync(0xffffffffu, x[0], 1);  // m at row i0 + cnt (when it is a row)
+  double yc = y[i0 * kNodeQ];
+#pragma unroll
+  for (int k = 0; k < kSegMax; ++k) {
+    const int i = i0 + k;
+    if (k < cnt) {
+      const R mi = (i == 0) ? m0 : x[k];
+      R mj;
+      if (i + 1 == n) mj = mn;
+      else if (k + 1 < cnt) mj = x[(k + 1) < kSegMax ? k + 1 : k];
+      else mj = next_first;
+      const double yn = y[(i + 1) * kNodeQ];
+      const R sl = (R)((yn - yc) * M.ginvh[i]);
+      const R bc = sl - fh[i] * (R(2) * mi + mj) * R(1.0 / 6.0);
+      const R cc = R(0.5) * mi;
+      const R dc = (mj - mi) * fih[i] * R(1.0 / 6.0);
+      if constexpr (sizeof(R) == 8) {
+        double* o = M.cphi + ((size_t)sd * M.J + i) * 4;
+        o[0] = yc;
+        o[1] = bc;
+        o[2] = cc;
+        o[3] = dc;
+      } else {
+        const float ahi = (float)yc;
+        M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, bc, cc, dc);
+        M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(yc - (double)ahi);
+      }
+      yc = yn;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
+  __shared__ double sm4[kNodeQ][4];
+  const int q = threadIdx.x >> 5;
+  const int64_t sd = blockIdx.x;
+  const int n = M.nsp[sd / M.n_det];
+  if (n < 3) return;
+  if (q == 0)
+    spline_fit_regs<double>(M, sd, q, n, sm4[q]);
+  else
+    spline_fit_regs<float>(M, sd, q, n, reinterpret_cast<float*>(sm4[q]));
+}
+
+template <class R>
+__device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t sd, int q, int n, double wscale) {
+  const int lane = threadIdx.x & 31;
+  const double* __restrict__ mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
+  double* __restrict__ yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
+  const R* __restrict__ fih = spline_factor<R>(M, kGfInvH);
+  const R* __restrict__ flo = spline_factor<R>(M, kGfLo);
+  const R* __restrict__ fup = spline_factor<R>(M, kGfUp);
+  const R* __restrict__ fid = spline_factor<R>(M, kGfInvDen);
+  const int seg = (n + 31) >> 5;
+  const int i0 = min(n, lane * seg), cnt = min(n, i0 + seg) - i0;
+  auto mm = [&](int i, int p) { return wscale * mom[(size_t)i * kNodeQ * kMoments + p]; };
+  auto mbar_left = [&](int i) {
+    return -M.gh[i] * mm(i, 1) * (1.0 / 3.0) + 0.5 * mm(i, 2) - mm(i, 3) * M.ginvh[i] * (1.0 / 6.0);
+  };
+  auto mbar_right = [&](int i) { return -M.gh[i] * mm(i, 1) * (1.0 / 6.0) + mm(i, 3) * M.ginvh[i] * (1.0 / 6.0); };
+  const double mb0 = mbar_left(0), mbn = mbar_right(n - 1);
+  const double h0 = M.gh[0], h1 = M.gh[1], ha = M.gh[n - 2], hb = M.gh[n - 1];
+  double lo_d, di_d, up_d;
+  nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
+  const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
+  // right-hand sides (coefficient adjoints -> mbar, end eliminations), in FP64
+  R x[kSegMax];
+  {
+    double right_prev = (i0 >= 1) ? mbar_right(i0 - 1) : 0.0;
+#pragma unroll
+    for (int k = 0; k < kSegMax; ++k) {
+      x[k] = R(0);
+      const int i = i0 + k;
+      if (k < cnt) {
+        const double left = mbar_left(i);
+        if (i >= 1) {
+          double w = right_prev + left;
+          if (i == 1) w += mb0 * (h0 + h1) / h1;
+          if (i == 2) w -= mb0 * h0 / h1;
+          if (i == n - 1) w += mbn * (ha + hb) / ha;
+          if (i == n - 2) w -= mbn * hb / ha;
+          x[k] = (R)w;
+        }
+        right_prev = mbar_right(i);
+      }
+    }
+  }
+  // U^T z = mbar
+  R A = R(1), v = R(0);
+#pragma unroll
+  for (int k = 0; k < kSegMax; ++k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const R sub = (i > 1) ? fup[i - 1] : R(0), id = (i == n - 1) ? iden_l : fid[i];
+      v = (x[k] - sub * v) * id;
+      A = -sub * id * A;
+    }
+  }
+  v = segment_carry_in<R>(A, v, false);
+#pragma unroll
+  for (int k = 0; k < kSegMax; ++k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const R sub = (i > 1) ? fup[i - 1] : R(0), id = (i == n - 1) ? iden_l : fid[i];
+      v = (x[k] - sub * v) * id;
+      x[k] = v;
+    }
+  }
+  // L^T rbar = z
+  A = R(1);
+  v = R(0);
+#pragma unroll
+  for (int k = kSegMax - 1; k >= 0; --k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
+      v = x[k] - c * v;
+      A = -c * A;
+    }
+  }
+  v = segment_carry_in<R>(A, v, true);
+  R last = R(0);  // rbar of the segment's last row
+#pragma unroll
+  for (int k = kSegMax - 1; k >= 0; --k) {
+    const int i = i0 + k;
+    if (k < cnt && i >= 1) {
+      const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
+      v = x[k] - c * v;
+      x[k] = v;
+      if (k == cnt - 1) last = v;
+    }
+  }
+  // node adjoints ybar_i = Dbar_{i-1}/h_{i-1} + wscale mm0_i - Dbar_i/h_i,
+  // Dbar_i = wscale mm1_i + 6 (rbar_i - rbar_{i+1}); rbar_0 = rbar_n = 0
+  const R prev_last = __shfl_up_sync(0xffffffffu, last, 1);
+  const R next_first = __shfl_down_sync(0xffffffffu, x[0], 1);
+  double gd = 0.0;
+  if (cnt > 0) {
+    R dprev = R(0);
+    if (i0 > 0) {
+      const R r_prev = (i0 - 1 >= 1) ? prev_last : R(0);
+      dprev = ((R)mm(i0 - 1, 1) + R(6) * (r_prev - x[0])) * fih[i0 - 1];
+    }
+#pragma unroll
+    for (int k = 0; k < kSegMax; ++k) {
+      const int i = i0 + k;
+      if (k < cnt) {
+        const R rc = (i >= 1) ? x[k] : R(0);
+        R rn;
+        if (i + 1 >= n) rn = R(0);
+        else if (k + 1 < cnt) rn = x[(k + 1) < kSegMax ? k + 1 : k];
+        else rn = next_first;
+        const R Db = (R)mm(i, 1) + R(6) * (rc - rn);
+        yb[i * kNodeQ] = (double)(dprev + (R)mm(i, 0) - Db * fih[i]);
+        dprev = Db * fih[i];
+        if (q == 0) gd += 2.0 * kPi * (M.node_f[i] * mom[(size_t)i * kNodeQ * kMoments] +
+                                       mom[(size_t)i * kNodeQ * kMoments + 1]);
+      }
+    }
+    if (i0 + cnt == n) yb[n * kNodeQ] = (double)dprev;
+  }
+  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+  if (q == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gd += __shfl_xor_sync(0xffffffffu, gd, o);
+    if (lane == 0) M.gdir[sd] = wscale * gd;
+  }
+}
+
+__global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, double wscale) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sd = blockIdx.x;
+  const int n = M.nsp[sd / M.n_det];
+  if (n < 3) {
+    double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
+    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+    if (q == 0 && lane == 0) M.gdir[sd] = 0.0;
+    return;
+  }
+  if (q == 0)
+    spline_adjoint_regs<double>(M, sd, q, n, wscale);
+  else
+    spline_adjoint_regs<float>(M, sd, q, n, wscale);
 }
 
 // ------------------------------------------------------------------ exact bins
@@ -1123,6 +1607,7 @@ int mixed_create(PesPlan* p) {
   int rc = PES_OK;
   double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
+  float* gf;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
@@ -1142,6 +1627,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -1184,6 +1670,11 @@ int mixed_create(PesPlan* p) {
     PES_CHECK_CUDA(cudaMemcpy(gup, up.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
     PES_CHECK_CUDA(cudaMemcpy(ginvden, iden.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
     PES_CHECK_CUDA(cudaMemcpy(gcp, cp.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+    std::vector<float> f32((size_t)kGfCount * J);
+    const std::vector<double>* src[kGfCount] = {&h, &ih, &lo, &up, &iden, &cp};
+    for (int k = 0; k < kGfCount; ++k)
+      for (int i = 0; i < J; ++i) f32[(size_t)k * J + i] = (float)(*src[k])[i];
+    PES_CHECK_CUDA(cudaMemcpy(gf, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
   }
   PES_CHECK_CUDA(cudaMemcpy(chb, cb.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chl, cl.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
@@ -1212,6 +1703,7 @@ int mixed_create(PesPlan* p) {
   M.gup = gup;
   M.ginvden = ginvden;
   M.gcp = gcp;
+  M.gf = gf;
   M.yv = yv;
   M.scr = scr;
   M.cphi = cphi;
@@ -1268,7 +1760,10 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_LAUNCH();
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
-  k_spline_fit<<<M.n_det, kSplineThreads, 0, st>>>(M);
+  if (M.J <= kSegMax * 32 + 1)
+    k_spline_fit<<<M.n_det, kSplineThreads, 0, st>>>(M);
+  else
+    k_spline_fit_wide<<<M.n_det, kSplineThreads, 0, st>>>(M);
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
   k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
@@ -1351,7 +1846,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKSpline, st);
-    k_spline_fit<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
+    if (M.J <= kSegMax * 32 + 1)
+      k_spline_fit<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
+    else
+      k_spline_fit_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
   }
   PES_CHECK_LAUNCH();
   if (grad) {
@@ -1376,7 +1874,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (!grad) return PES_OK;
   {
     ProfScope ps(p, kKAdjoint, st);
-    k_spline_adjoint<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
+    if (M.J <= kSegMax * 32 + 1)
+      k_spline_adjoint<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
+    else
+      k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
   }
   PES_CHECK_LAUNCH();
   {

@@ -28,10 +28,11 @@ def dataset(oracle):
     return g, dets, th0
 
 
-def engines(g, dets, **kw):
+def engines(g, dets, n_sparse=1024, **kw):
     from pespace_gb300.inference import WhittleLikelihood
 
-    return (WhittleLikelihood(cuda_detectors(g, dets), precision="mixed", reference_frequency=1e-4, **kw),
+    return (WhittleLikelihood(cuda_detectors(g, dets), precision="mixed", reference_frequency=1e-4, n_sparse=n_sparse,
+                              **kw),
             WhittleLikelihood(cuda_detectors(g, dets), precision="fp64", reference_frequency=1e-4, **kw))
 
 
@@ -94,3 +95,21 @@ def test_mixed_gradient(cuda_lib, oracle, dataset):
     gg = grad.cpu().numpy()
     norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
     assert np.max(np.abs(gg - w_grad) / norm) < 1e-3, (gg, w_grad)
+
+
+@pytest.mark.parametrize("n_sparse", [600, 2048])
+def test_mixed_other_grids(cuda_lib, oracle, dataset, n_sparse):
+    """Non-default sparse grids: 600 nodes (register segments of 19 rows) and
+    2048 nodes (the global-scratch spline kernels)."""
+    g, dets, th0 = dataset
+    rng = np.random.default_rng(3)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(3)])
+    mixed, _ = engines(g, dets[:1], n_sparse=n_sparse, max_batch=4)
+    lnl, grad = mixed.log_likelihood_and_grad(thetas)
+    w_lnl, w_grad = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets[:1]], 1e-4).lnl(
+        thetas, grad=True, nthreads=8)
+    err = np.abs(lnl.cpu().numpy() - w_lnl)
+    tol = 1e-2 if n_sparse >= 1024 else 5e-2  # spline error grows as (node spacing)^4
+    assert np.all(err <= tol + 1e-8 * np.abs(w_lnl)), err
+    norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
+    assert np.max(np.abs(grad.cpu().numpy() - w_grad) / norm) < 1e-3
