@@ -83,7 +83,7 @@ struct MixedDev {
   double* cphi;             // [B][n_det][J][4] phase spline coefficients (FP64)
   float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32: a_hi, b, c, d)
   float* cglo;              // [B][n_det][J][6] a - a_hi (the value at the left node in float-float)
-  double* mom;              // [B][n_det][J][7][4] adjoint moments
+  float* mom;               // [B][n_det][J][7][4] adjoint moments (FP32 warp sums, FP32 atomics)
   double* ybar;             // [B][n_det][J][7] node adjoints
   double* part;             // [B][nblk_dense] lnL partials
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
@@ -96,7 +96,7 @@ struct MixedDev {
   double* kinkR;            // [B][n_det][6] R_q
   double* kinkC;            // [B][n_det][6] C_q
   float* kinkF;             // [B][n_det][16] Msec f_step, -, C_0..C_5 as float-float (hi x6, lo x6), -, -
-  double* kinkM;            // [B][n_det][12] dense adjoint moments: sum A_q x^2, sum A_q x
+  float* kinkM;             // [B][n_det][12] dense adjoint moments: sum A_q x^2, sum A_q x
 };
 
 struct GenArg {
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
     amp_peak_jump<GS>(sb.wf, ahat, jump);
     const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
     const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
-    const double* K = M.kinkM + ((size_t)s * M.n_det + d) * 12;
+    const float* K = M.kinkM + ((size_t)s * M.n_det + d) * 12;
     for (int q = 0; q < 6; ++q) {
       // sum A_q x f = (sum A_q x^2 + Mf_peak sum A_q x) / Msec  (f = (x + Mf_peak) / Msec)
       const double K2 = wscale * K[q], K1 = wscale * K[6 + q];
@@ -514,7 +514,7 @@ __device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t s
 // moments in FP64, the transposed solve and the node adjoints in FP32.
 __device__ __forceinline__ void spline_adjoint_transfer(const MixedDev& M, int64_t sd, int q, int n, double wscale) {
   const int lane = threadIdx.x & 31;
-  const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
+  const float* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
   float2* X = reinterpret_cast<float2*>(M.scr + (size_t)sd * M.J * kNodeQ + q);
   double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
   const float* fih = M.gf + (size_t)kGfInvH * M.J;
@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint_wide(MixedDev
     return;
   }
   const double* f = M.node_f;
-  const double* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;  // + i*7*4
+  const float* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;  // + i*7*4
   double* X = M.scr + (size_t)sd * M.J * kNodeQ + q;  // z, then rbar
   const int seg = (n + 31) >> 5;
   const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);
@@ -944,7 +944,7 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
 template <class R>
 __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t sd, int q, int n, double wscale) {
   const int lane = threadIdx.x & 31;
-  const double* __restrict__ mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
+  const float* __restrict__ mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
   double* __restrict__ yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
   const R* __restrict__ fih = spline_factor<R>(M, kGfInvH);
   const R* __restrict__ flo = spline_factor<R>(M, kGfLo);
@@ -952,33 +952,35 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   const R* __restrict__ fid = spline_factor<R>(M, kGfInvDen);
   const int seg = (n + 31) >> 5;
   const int i0 = min(n, lane * seg), cnt = min(n, i0 + seg) - i0;
-  auto mm = [&](int i, int p) { return wscale * mom[(size_t)i * kNodeQ * kMoments + p]; };
+  const R* __restrict__ fh = spline_factor<R>(M, kGfH);
+  const R ws = (R)wscale;
+  auto mm = [&](int i, int p) { return ws * (R)mom[(size_t)i * kNodeQ * kMoments + p]; };
   auto mbar_left = [&](int i) {
-    return -M.gh[i] * mm(i, 1) * (1.0 / 3.0) + 0.5 * mm(i, 2) - mm(i, 3) * M.ginvh[i] * (1.0 / 6.0);
+    return -fh[i] * mm(i, 1) * R(1.0 / 3.0) + R(0.5) * mm(i, 2) - mm(i, 3) * fih[i] * R(1.0 / 6.0);
   };
-  auto mbar_right = [&](int i) { return -M.gh[i] * mm(i, 1) * (1.0 / 6.0) + mm(i, 3) * M.ginvh[i] * (1.0 / 6.0); };
-  const double mb0 = mbar_left(0), mbn = mbar_right(n - 1);
-  const double h0 = M.gh[0], h1 = M.gh[1], ha = M.gh[n - 2], hb = M.gh[n - 1];
+  auto mbar_right = [&](int i) { return -fh[i] * mm(i, 1) * R(1.0 / 6.0) + mm(i, 3) * fih[i] * R(1.0 / 6.0); };
+  const R mb0 = mbar_left(0), mbn = mbar_right(n - 1);
+  const R h0 = fh[0], h1 = fh[1], ha = fh[n - 2], hb = fh[n - 1];
   double lo_d, di_d, up_d;
   nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
   const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
   // right-hand sides (coefficient adjoints -> mbar, end eliminations), in FP64
   R x[kSegMax];
   {
-    double right_prev = (i0 >= 1) ? mbar_right(i0 - 1) : 0.0;
+    R right_prev = (i0 >= 1) ? mbar_right(i0 - 1) : R(0);
 #pragma unroll
     for (int k = 0; k < kSegMax; ++k) {
       x[k] = R(0);
       const int i = i0 + k;
       if (k < cnt) {
-        const double left = mbar_left(i);
+        const R left = mbar_left(i);
         if (i >= 1) {
-          double w = right_prev + left;
+          R w = right_prev + left;
           if (i == 1) w += mb0 * (h0 + h1) / h1;
           if (i == 2) w -= mb0 * h0 / h1;
           if (i == n - 1) w += mbn * (ha + hb) / ha;
           if (i == n - 2) w -= mbn * hb / ha;
-          x[k] = (R)w;
+          x[k] = w;
         }
         right_prev = mbar_right(i);
       }
@@ -1038,7 +1040,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
     R dprev = R(0);
     if (i0 > 0) {
       const R r_prev = (i0 - 1 >= 1) ? prev_last : R(0);
-      dprev = ((R)mm(i0 - 1, 1) + R(6) * (r_prev - x[0])) * fih[i0 - 1];
+      dprev = (mm(i0 - 1, 1) + R(6) * (r_prev - x[0])) * fih[i0 - 1];
     }
 #pragma unroll
     for (int k = 0; k < kSegMax; ++k) {
@@ -1049,11 +1051,11 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
         if (i + 1 >= n) rn = R(0);
         else if (k + 1 < cnt) rn = x[(k + 1) < kSegMax ? k + 1 : k];
         else rn = next_first;
-        const R Db = (R)mm(i, 1) + R(6) * (rc - rn);
-        yb[i * kNodeQ] = (double)(dprev + (R)mm(i, 0) - Db * fih[i]);
+        const R Db = mm(i, 1) + R(6) * (rc - rn);
+        yb[i * kNodeQ] = (double)(dprev + mm(i, 0) - Db * fih[i]);
         dprev = Db * fih[i];
-        if (q == 0) gd += 2.0 * kPi * (M.node_f[i] * mom[(size_t)i * kNodeQ * kMoments] +
-                                       mom[(size_t)i * kNodeQ * kMoments + 1]);
+        if (q == 0) gd += 2.0 * kPi * (M.node_f[i] * (double)mom[(size_t)i * kNodeQ * kMoments] +
+                                       (double)mom[(size_t)i * kNodeQ * kMoments + 1]);
       }
     }
     if (i0 + cnt == n) yb[n * kNodeQ] = (double)dprev;
@@ -1338,7 +1340,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
               float x = mq[k];
 #pragma unroll
               for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-              if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, (double)x);
+              if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, x);
               mq[k] = 0.0f;
             }
           }
@@ -1434,7 +1436,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           float x = mq[k];
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, (double)x);
+          if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, x);
         }
       }
       if (kGrad && __any_sync(0xffffffffu, kinked)) {
@@ -1443,7 +1445,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           float x = km[k];
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if (lane == 0) atomicAdd(M.kinkM + sd * 12 + k, (double)x);
+          if (lane == 0) atomicAdd(M.kinkM + sd * 12 + k, x);
         }
       }
     }
@@ -1605,14 +1607,15 @@ int mixed_create(PesPlan* p) {
   M.nblk_dense = (int32_t)ceil_div(M.nchunks, (long long)kChunkMax * (kMixThreads / 32));
   M.nblk_sparse = (int32_t)ceil_div(J, kSparseThreads);
   int rc = PES_OK;
-  double *node_f = nullptr, *yv, *scr, *cphi, *mom, *ybar, *part, *gpart, *gdir;
+  double *node_f = nullptr, *yv, *scr, *cphi, *ybar, *part, *gpart, *gdir;
+  float *mom, *kM;
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
   float* gf;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
   SampleBlock<NodeGradScalar>* gblk32;
-  double *kR, *kC, *kM;
+  double *kR, *kC;
   float* kF;
   float* bin_t;
   float2* dat;
@@ -1853,8 +1856,8 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   if (grad) {
-    PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(double) * B * M.n_det * M.J * kNodeQ * kMoments, st));
-    PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(double) * B * M.n_det * 12, st));
+    PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
+    PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
   }
   {
     ProfScope ps(p, kKDenseMixed, st);
