@@ -61,6 +61,7 @@ struct MixedDev {
   const int32_t* ch_len;    // [nchunks]
   const int32_t* ch_iv;     // [nchunks] spline interval of the run
   const float* bin_t;       // [nbins] f_i - f_iv(i)
+  float4* runs;             // [B][n_det][nchunks][3] per-run phase anchors (RunPhase, 12 floats)
   float2* dat;              // [n_det][3][nbins] scaled data
   float* wgt;               // [n_det][3][nbins] inverse scaled PSD (0 off the channel mask)
   float2* dd;               // [n_det][nbins] sum_c |d|^2 / S in FP64, as a float-float pair (hi, lo)
@@ -1239,6 +1240,46 @@ struct RunPhase {
   float p3h, p3l;         // cubic coefficient, head/tail
 };
 
+// Per-run phase anchors in FP64, one thread per (sample, detector, run) with a
+// live, non-exact bin: the phase spline and the 2 pi f t_c term at the run's
+// first bin, wrapped, split into an FP32 head/tail phasor and exact-product
+// FP32 heads (with tails) of the per-bin increment polynomial; and the
+// peak-kink coordinate Msec f - Mf_peak at the run start.
+__global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
+                                                      const SampleBlock<double>* __restrict__ blocks) {
+  const int s = blockIdx.z, d = blockIdx.y;
+  const int c = blockIdx.x * 128 + threadIdx.x;
+  if (blocks[s].status != kSampleOk || c >= M.nch[s]) return;
+  const int kb = M.ch_begin[c];
+  if (kb < M.xbin[s]) return;
+  const size_t sd = (size_t)s * M.n_det + d;
+  const double tc = blocks[s].tc;
+  const int j = M.ch_iv[c];
+  const double fb = (double)(P.k0 + kb) * P.f_step;
+  const double t = fb - M.node_f[j];
+  const double* co = M.cphi + (sd * M.J + j) * 4;
+  const double a = co[0], b = co[1], cc = co[2], dd = co[3];
+  const double S0 = a + t * (b + t * (cc + t * dd));
+  const double S1 = b + t * (2.0 * cc + 3.0 * dd * t);
+  const double S2 = cc + 3.0 * dd * t;
+  const double D = P.f_step;
+  const double ph0 = wrap_2pi(S0 + (2.0 * kPi * fb) * tc);
+  const double ph1 = wrap_2pi(D * (S1 + 2.0 * kPi * tc));
+  const double ph2 = D * D * S2;
+  const double ph3 = D * D * D * dd;
+  const float x0 = (float)fma(blocks[s].wf.Msec, fb, -blocks[s].wf.fpeak);
+  // anchor phasor: sincos of the float head, rotated by the (tiny) tail
+  const float h0 = (float)ph0;
+  const float l0 = (float)(ph0 - (double)h0);
+  float s0f, c0f;
+  sincos_poly(h0, &s0f, &c0f);
+  const float p1h = head_bits(ph1, 12), p2h = head_bits(ph2, 13), p3h = head_bits(ph3, 8);
+  float4* o = M.runs + (sd * M.nchunks + c) * 3;
+  o[0] = make_float4(x0, fmaf(-s0f, l0, c0f), fmaf(c0f, l0, s0f), p1h);
+  o[1] = make_float4((float)(ph1 - (double)p1h), p2h, (float)(ph2 - (double)p2h), p3h);
+  o[2] = make_float4((float)(ph3 - (double)p3h), 0.0f, 0.0f, 0.0f);
+}
+
 // kMode 0: lnL partials; 1: lnL partials + adjoint moments; 2: write the model
 // h (unscaled, complex128 (n_det, 3, nbins)) to `model` (parity/debug path).
 template <int kMode>
@@ -1258,50 +1299,11 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   float acc = 0.0f, comp = 0.0f;
   float dsh = 0.0f, dsl = 0.0f;  // float-float sum of the FP64 |d|^2/S of the weak-template bins
   if (blocks[s].status == kSampleOk && first < nc) {
-    const int cl = first + lane;
     for (int d = 0; d < M.n_det; ++d) {
       const size_t sd = (size_t)s * M.n_det + d;
-      // ---- per-run phase anchors, one run per lane (FP64)
-      RunPhase rp = {0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-      if (cl < nc) {
-        const int j = M.ch_iv[cl];
-        const int kb = M.ch_begin[cl];
-        const double fb = (double)(P.k0 + kb) * P.f_step;
-        const double t = fb - M.node_f[j];
-        const double* co = M.cphi + (sd * M.J + j) * 4;
-        const double a = co[0], b = co[1], c = co[2], dd = co[3];
-        const double S0 = a + t * (b + t * (c + t * dd));
-        const double S1 = b + t * (2.0 * c + 3.0 * dd * t);
-        const double S2 = c + 3.0 * dd * t;
-        const double D = P.f_step;
-        const double ph0 = wrap_2pi(S0 + (2.0 * kPi * fb) * tc);
-        const double ph1 = wrap_2pi(D * (S1 + 2.0 * kPi * tc));
-        const double ph2 = D * D * S2;
-        const double ph3 = D * D * D * dd;
-        rp.x0 = (float)fma(blocks[s].wf.Msec, fb, -blocks[s].wf.fpeak);
-        // anchor phasor: sincos of the float head, rotated by the (tiny) tail
-        const float h0 = (float)ph0;
-        const float l0 = (float)(ph0 - (double)h0);
-        float s0f, c0f;
-        sincos_poly(h0, &s0f, &c0f);
-        rp.c0 = fmaf(-s0f, l0, c0f);
-        rp.s0 = fmaf(c0f, l0, s0f);
-        rp.p1h = head_bits(ph1, 12);
-        rp.p1l = (float)(ph1 - (double)rp.p1h);
-        rp.p2h = head_bits(ph2, 13);
-        rp.p2l = (float)(ph2 - (double)rp.p2h);
-        rp.p3h = head_bits(ph3, 8);
-        rp.p3l = (float)(ph3 - (double)rp.p3h);
-      }
-      // ---- amplitude kink at f_peak (float-float coefficients)
+      // ---- amplitude kink at f_peak (float-float coefficients, read past the peak only)
       const float* KF = M.kinkF + sd * 16;
       const float kSlope = KF[0];
-      float kC[6], kCl[6];
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        kC[q] = KF[2 + q];
-        kCl[q] = KF[8 + q];
-      }
       float km[12];
       bool kinked = false;
       if (kGrad) {
@@ -1317,21 +1319,22 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
       }
       const int last = min(nc, first + kChunkMax);
       for (int c = first; c < last; ++c) {
-        const int src = c - first;
-        RunPhase r;
-        r.x0 = __shfl_sync(0xffffffffu, rp.x0, src);
-        r.c0 = __shfl_sync(0xffffffffu, rp.c0, src);
-        r.s0 = __shfl_sync(0xffffffffu, rp.s0, src);
-        r.p1h = __shfl_sync(0xffffffffu, rp.p1h, src);
-        r.p1l = __shfl_sync(0xffffffffu, rp.p1l, src);
-        r.p2h = __shfl_sync(0xffffffffu, rp.p2h, src);
-        r.p2l = __shfl_sync(0xffffffffu, rp.p2l, src);
-        r.p3h = __shfl_sync(0xffffffffu, rp.p3h, src);
-        r.p3l = __shfl_sync(0xffffffffu, rp.p3l, src);
         const int j = M.ch_iv[c];
         const int kb = M.ch_begin[c];
         const int len = M.ch_len[c];
         if (kb < xb) continue;  // exact bins (runs never straddle an interval boundary)
+        const float4* ra = M.runs + (sd * M.nchunks + c) * 3;
+        const float4 ra0 = ra[0], ra1 = ra[1];
+        RunPhase r;
+        r.x0 = ra0.x;
+        r.c0 = ra0.y;
+        r.s0 = ra0.z;
+        r.p1h = ra0.w;
+        r.p1l = ra1.x;
+        r.p2h = ra1.y;
+        r.p2l = ra1.z;
+        r.p3h = ra1.w;
+        r.p3l = ra[2].x;
         if (kGrad && j != cur_iv) {
           if (cur_iv >= 0) {
             // flush the previous interval's moments
@@ -1367,6 +1370,13 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float* Glo = M.cglo + (sd * M.J + j) * 6;
           const float xk = fmaf(kSlope, u, r.x0);
           const float x2 = xk > 0.0f ? xk * xk : 0.0f;
+          float kink[6];
+#pragma unroll
+          for (int q = 0; q < 6; ++q) kink[q] = 0.0f;
+          if (xk > 0.0f) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) kink[q] = fmaf(KF[2 + q], x2, KF[8 + q] * x2);
+          }
           float term = 0.0f;  // |d - h|^2 w
           float cross = 0.0f;  // (|h|^2 - 2 Re(d^* h)) w
           float hh = 0.0f;     // |h|^2 w
@@ -1375,8 +1385,8 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
-            const float gr = cr.x + fmaf(kC[2 * ch], x2, fmaf(kCl[2 * ch], x2, Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w))));
-            const float gi = ci.x + fmaf(kC[2 * ch + 1], x2, fmaf(kCl[2 * ch + 1], x2, Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w))));
+            const float gr = cr.x + (kink[2 * ch] + (Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w))));
+            const float gi = ci.x + (kink[2 * ch + 1] + (Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w))));
             const float hr = gr * cph + gi * sph;
             const float hi = gi * cph - gr * sph;
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
@@ -1618,6 +1628,7 @@ int mixed_create(PesPlan* p) {
   double *kR, *kC;
   float* kF;
   float* bin_t;
+  float4* runs;
   float2* dat;
   float* wgt;
   float2* ddv;
@@ -1625,7 +1636,8 @@ int mixed_create(PesPlan* p) {
   float* cglo;
   const size_t sd = (size_t)B * nd;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
-      (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
+      (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) ||
+      (rc = alloc(mb, &runs, (size_t)B * nd * M.nchunks * 3)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
       (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
@@ -1691,6 +1703,7 @@ int mixed_create(PesPlan* p) {
   M.ch_len = chl;
   M.ch_iv = chi;
   M.bin_t = bin_t;
+  M.runs = runs;
   M.dat = dat;
   M.wgt = wgt;
   M.dd = ddv;
@@ -1769,6 +1782,8 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
     k_spline_fit_wide<<<M.n_det, kSplineThreads, 0, st>>>(M);
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
+  k_run_anchors<<<dim3((unsigned)ceil_div(M.nchunks, 128), M.n_det, 1), 128, 0, st>>>(p->dev, M, blocks);
+  PES_CHECK_LAUNCH();
   k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
                                                                   reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
@@ -1859,6 +1874,12 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
     PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
   }
+  {
+    ProfScope ps(p, kKSpline, st);
+    dim3 grid((unsigned)ceil_div(M.nchunks, 128), M.n_det, (unsigned)B);
+    k_run_anchors<<<grid, 128, 0, st>>>(p->dev, M, blocks);
+  }
+  PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKDenseMixed, st);
     dim3 grid(M.nblk_dense, (unsigned)B);
