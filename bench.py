@@ -199,13 +199,14 @@ def run_native(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pespace_gb300 import _lib
     from pespace_gb300.inference import WhittleLikelihood
-    from pespace_gb300.workloads import config0_theta, lisa_dataset, prior_samples
+    from pespace_gb300 import replicas
+    from pespace_gb300.workloads import config0_theta, lisa_dataset
 
     B = args.batch
     th0 = config0_theta(DUR - 86400.0)
     det = lisa_dataset(DUR, DT, FMIN, FMAX, th0, "1.5", seed=2026)
     eng = WhittleLikelihood(det, precision=args.precision, reference_frequency=1e-4, cut_factor=1.2, max_batch=B)
-    theta_host = torch.as_tensor(prior_samples(np.random.default_rng(2026 + rank), B, th0[10])).pin_memory()
+    theta_host = torch.as_tensor(replicas.rank_theta(rank, B, th0[10])).pin_memory()
     theta = theta_host.to("cuda")
     lib = _lib.load()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -246,12 +247,8 @@ def run_native(args):
     kern = {lib.pes_kernel_class_name(k).decode(): (int(launches[k]), float(dev_ms[k])) for k in range(n_cls)
             if launches[k]}
     gpu_launches = sum(v[0] for v in kern.values())
-    mean_ms = float(np.mean(times))
-    t_local = torch.tensor([mean_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
-    mean_ms = float(t_local.item())
-    value = world * B / (mean_ms / 1e3)
+    mean_ms = replicas.reduce_max(float(np.mean(times)), "cuda")
+    value = replicas.job_rate(world, B, mean_ms)
 
     # ---------------- e2e through host buffers
     lnl_host = torch.empty(B, dtype=torch.float64).pin_memory()
@@ -269,10 +266,7 @@ def run_native(args):
         e.record()
         e.synchronize()
         e2e_ms.append(s.elapsed_time(e))
-    t_e2e = torch.tensor([float(np.mean(e2e_ms))], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_e2e, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = world * B / (float(t_e2e.item()) / 1e3)
+    e2e_value = replicas.job_rate(world, B, replicas.reduce_max(float(np.mean(e2e_ms)), "cuda"))
 
     # ---------------- accuracy against the FP64 path on this workload
     err = None
