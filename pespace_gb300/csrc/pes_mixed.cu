@@ -57,6 +57,7 @@ struct MixedDev {
   int32_t pad;
   double scale;             // FP32 storage scale of data and model
   const double* node_f;     // [J]
+  const TdiFactor* tdn;     // [n_det][J] TDI delay factor and generation prefactor at the nodes
   const int32_t* ch_begin;  // [nchunks] first bin of the run
   const int32_t* ch_len;    // [nchunks]
   const int32_t* ch_iv;     // [nchunks] spline interval of the run
@@ -117,7 +118,7 @@ struct MixedBuffers {
 // ------------------------------------------------------------------ sparse stage
 template <class T>
 __device__ __forceinline__ void node_eval(const PlanDev& P, const MixedDev& M, const SampleBlock<T>& b, int d,
-                                          int gen20, double f, T y[kNodeQ]) {
+                                          const TdiFactor& td, double f, T y[kNodeQ]) {
   T Mf = b.wf.Msec * f;
   T amp, psi, tf;
   phenomd_eval<T>(b.wf, Mf, amp, psi, tf);
@@ -128,9 +129,7 @@ __device__ __forceinline__ void node_eval(const PlanDev& P, const MixedDev& M, c
   Cx<T> L[6], C[3];
   T kx0;
   single_links_impl<true, T>(P.orbit[d], f, hp, hc, tf + b.tc, b.pol, L, &kx0);
-  Cx<double> D, Pf;
-  tdi_factors(f, P.orbit[d].arm_sec, gen20, D, Pf);
-  tdi_channels<T>(D, Pf, 1, L, C);
+  tdi_channels<T>(cx(td.dre, td.dim), cx(td.pre, td.pim), 1, L, C);
   y[0] = psi + (2.0 * kPi * f) * kx0;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -164,7 +163,16 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
   }
   if (b.status != kSampleOk) return;
   double y[kNodeQ], ahat, jump;
-  node_eval<double>(P, M, b, d, G.gen20[d], b.wf.fpeak / b.wf.Msec, y);
+  TdiFactor td;
+  {
+    Cx<double> D, Pf;
+    tdi_factors(b.wf.fpeak / b.wf.Msec, P.orbit[d].arm_sec, G.gen20[d], D, Pf);
+    td.dre = D.re;
+    td.dim = D.im;
+    td.pre = Pf.re;
+    td.pim = Pf.im;
+  }
+  node_eval<double>(P, M, b, d, td, b.wf.fpeak / b.wf.Msec, y);
   amp_peak_jump<double>(b.wf, ahat, jump);
   F[0] = (float)(b.wf.Msec * P.f_step);
   for (int q = 0; q < 6; ++q) {
@@ -188,7 +196,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
   if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J) return;
   double y[kNodeQ];
   const double fj = M.node_f[j];
-  node_eval<double>(P, M, sb, d, G.gen20[d], fj, y);
+  node_eval<double>(P, M, sb, d, M.tdn[(size_t)d * M.J + j], fj, y);
   const double xk = sb.wf.Msec * fj - sb.wf.fpeak;
   if (xk > 0.0) {
     const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
     GS y[kNodeQ];
     const double fj = M.node_f[j];
-    node_eval<GS>(P, M, sb, d, G.gen20[d], fj, y);
+    node_eval<GS>(P, M, sb, d, M.tdn[(size_t)d * M.J + j], fj, y);
     const GS xk = sb.wf.Msec * fj - sb.wf.fpeak;
     if (xk.v > 0.0) {
       GS ahat, jump;
@@ -1111,7 +1119,7 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
       const double f = (double)(P.k0 + i) * P.f_step;
       for (int d = 0; d < M.n_det; ++d) {
         T y[kNodeQ];
-        node_eval<T>(P, M, sb, d, G.gen20[d], f, y);
+        node_eval<T>(P, M, sb, d, P.tdi[(size_t)d * P.nbins + i], f, y);
         const T ph = y[0] + (2.0 * kPi * f) * sb.tc;
         T sn, cs;
         dsincos(ph, &sn, &cs);
@@ -1621,6 +1629,7 @@ int mixed_create(PesPlan* p) {
   float *mom, *kM;
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
   float* gf;
+  TdiFactor* tdn;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
@@ -1642,7 +1651,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -1655,6 +1664,16 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaMemcpy(ivfirst, ivf.data(), sizeof(int32_t) * (J + 1), cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemset(xbin, 0, sizeof(int32_t) * B));
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
+  {
+    std::vector<TdiFactor> tf((size_t)nd * J);
+    for (int k = 0; k < nd; ++k)
+      for (int jj = 0; jj < J; ++jj) {
+        Cx<double> D, Pf;
+        tdi_factors(nf[jj], d.det[k].orbit.arm_sec, d.det[k].generation == 20, D, Pf);
+        tf[(size_t)k * J + jj] = TdiFactor{D.re, D.im, Pf.re, Pf.im};
+      }
+    PES_CHECK_CUDA(cudaMemcpy(tdn, tf.data(), sizeof(TdiFactor) * tf.size(), cudaMemcpyHostToDevice));
+  }
   {
     // shared not-a-knot system of the node grid: rows 1..J-2 with the first-row
     // elimination and without the last-row one (that row depends on the sample)
@@ -1720,6 +1739,7 @@ int mixed_create(PesPlan* p) {
   M.ginvden = ginvden;
   M.gcp = gcp;
   M.gf = gf;
+  M.tdn = tdn;
   M.yv = yv;
   M.scr = scr;
   M.cphi = cphi;

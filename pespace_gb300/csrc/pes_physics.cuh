@@ -112,6 +112,23 @@ PES_HD T sinc_ref(const T& x) {
   // utils.py:60-79: sin(x)/x with the x == 0 guard
   return (val(x) == 0.0) ? lift<T>(1.0) : dsin(x) / x;
 }
+PES_HD double sinc_ref(const double& x) {
+  if (::fabs(x) <= 2.0) {
+    double s, ds;
+    sinc_taylor(x, &s, &ds);
+    return s;
+  }
+  return ::sin(x) / x;
+}
+template <int N, class D>
+PES_HD Dual<N, D, double> sinc_ref(const Dual<N, D, double>& x) {
+  if (::fabs(x.v) <= 2.0) {
+    double s, ds;
+    sinc_taylor(x.v, &s, &ds);
+    return chain1(x, s, ds);
+  }
+  return dsin(x) / x;
+}
 
 // Six single-link responses of one time-shifted mode (hp, hc at f; tf already
 // includes t_c).  Order: 12, 21, 23, 32, 31, 13.  With kFactorDoppler the
