@@ -1288,6 +1288,27 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   o[2] = make_float4((float)(ph3 - (double)p3h), 0.0f, 0.0f, 0.0f);
 }
 
+// Warp-sum of the 28 per-lane interval moments through shared memory (rows
+// padded to 33 floats: conflict-free), added to the interval's moments with
+// one 28-lane atomic instruction.
+constexpr int kMomPad = 33;
+__device__ __forceinline__ void flush_moments(float mq[kNodeQ * kMoments], float (*sm)[kMomPad], float* dst,
+                                              int lane) {
+#pragma unroll
+  for (int k = 0; k < kNodeQ * kMoments; ++k) {
+    sm[k][lane] = mq[k];
+    mq[k] = 0.0f;
+  }
+  __syncwarp();
+  if (lane < kNodeQ * kMoments) {
+    float x = 0.0f;
+#pragma unroll 8
+    for (int l = 0; l < 32; ++l) x += sm[lane][l];
+    atomicAdd(dst + lane, x);
+  }
+  __syncwarp();
+}
+
 // kMode 0: lnL partials; 1: lnL partials + adjoint moments; 2: write the model
 // h (unscaled, complex128 (n_det, 3, nbins)) to `model` (parity/debug path).
 template <int kMode>
@@ -1296,13 +1317,13 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
   __shared__ double red[kMixThreads / 32];
+  __shared__ float msm[kGrad ? kMixThreads / 32 : 1][kGrad ? kNodeQ * kMoments : 1][kGrad ? kMomPad : 1];
   const int s = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int g = blockIdx.x * (kMixThreads / 32) + wid;  // run group
   const int nc = M.nch[s];
   const int xb = M.xbin[s];
   const int64_t kcut = blocks[s].kcut;
-  const double tc = blocks[s].tc;
   const int first = g * kChunkMax;
   float acc = 0.0f, comp = 0.0f;
   float dsh = 0.0f, dsl = 0.0f;  // float-float sum of the FP64 |d|^2/S of the weak-template bins
@@ -1344,17 +1365,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         r.p3h = ra1.w;
         r.p3l = ra[2].x;
         if (kGrad && j != cur_iv) {
-          if (cur_iv >= 0) {
-            // flush the previous interval's moments
-#pragma unroll
-            for (int k = 0; k < kNodeQ * kMoments; ++k) {
-              float x = mq[k];
-#pragma unroll
-              for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-              if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, x);
-              mq[k] = 0.0f;
-            }
-          }
+          if (cur_iv >= 0) flush_moments(mq, reinterpret_cast<float (*)[kMomPad]>(&msm[wid][0][0]), M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments, lane);
           cur_iv = j;
         }
         const int64_t i = (int64_t)kb + lane;
@@ -1448,15 +1459,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           }
         }
       }
-      if (kGrad && cur_iv >= 0) {
-#pragma unroll
-        for (int k = 0; k < kNodeQ * kMoments; ++k) {
-          float x = mq[k];
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if (lane == 0) atomicAdd(M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments + k, x);
-        }
-      }
+      if (kGrad && cur_iv >= 0) flush_moments(mq, reinterpret_cast<float (*)[kMomPad]>(&msm[wid][0][0]), M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments, lane);
       if (kGrad && __any_sync(0xffffffffu, kinked)) {
 #pragma unroll
         for (int k = 0; k < 12; ++k) {
