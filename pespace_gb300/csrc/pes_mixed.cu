@@ -101,6 +101,13 @@ struct MixedDev {
   float* kinkM;             // [B][n_det][12] dense adjoint moments: sum A_q x^2, sum A_q x
 };
 
+// Error-free transformation: s + e == a + b exactly (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
 struct GenArg {
   int32_t gen20[PES_MAX_DETECTORS];
 };
@@ -282,9 +289,9 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
-  double acc[11];
+  float acc[11];  // this node's contribution (FP32: one node per thread)
 #pragma unroll
-  for (int k = 0; k < 11; ++k) acc[k] = 0.0;
+  for (int k = 0; k < 11; ++k) acc[k] = 0.0f;
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
     GS y[kNodeQ];
     const double fj = M.node_f[j];
@@ -301,11 +308,30 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
     const double* yb = M.ybar + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
 #pragma unroll
     for (int q = 0; q < kNodeQ; ++q) {
-      const double w = yb[q];
+      const float w = (float)yb[q];
 #pragma unroll
-      for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += w * (double)y[q].d[k];
-      if (q > 0) acc[4] -= w * y[q].v;  // G ~ 1/D_L
-      else acc[9] -= 2.0 * w;           // Phi_s = ... - 2 phi_c
+      for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] = fmaf(w, y[q].d[k], acc[kSlotParam[k]]);
+      if (q > 0) acc[4] = fmaf(-w, y[q].v, acc[4]);  // G ~ 1/D_L
+      else acc[9] = fmaf(-2.0f, w, acc[9]);          // Phi_s = ... - 2 phi_c
+    }
+  }
+  // block sum: float-float across the warp, FP64 across warps
+  double accd[11];
+  {
+    const int l = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 11; ++k) {
+      float hi = acc[k], lo = 0.0f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+        const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+        float th, tl;
+        two_sum(hi, oh, th, tl);
+        hi = th;
+        lo += tl + ol;
+      }
+      accd[k] = (l == 0) ? (double)hi + (double)lo : 0.0;
     }
   }
   // dense-side kink term C_q x^2 (x = Msec f - Mf_peak): one thread per (sample, detector)
@@ -320,18 +346,15 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
       const double K2 = wscale * K[q], K1 = wscale * K[6 + q];
       const double K1f = (K2 + sb.wf.fpeak.v * K1) / sb.wf.Msec.v;
       for (int k = 0; k < kMixNT; ++k)
-        acc[kSlotParam[k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
-                              2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
-      acc[4] -= C[q] * K2;  // C_q ~ 1/D_L
+        accd[kSlotParam[k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
+                               2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
+      accd[4] -= C[q] * K2;  // C_q ~ 1/D_L
     }
   }
   const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
 #pragma unroll
-  for (int k = 0; k < 11; ++k) {
-    double x = acc[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (l == 0) red[wid][k] = x;
+    for (int k = 0; k < 11; ++k) red[wid][k] = accd[k];
   }
   __syncthreads();
   if (threadIdx.x < 11) {
@@ -1227,13 +1250,6 @@ __device__ __forceinline__ void sincos_poly(float x, float* sp, float* cp) {
 __device__ __forceinline__ float head_bits(double x, int bits) {
   const long long m = ~((1LL << (53 - bits)) - 1);
   return (float)__longlong_as_double(__double_as_longlong(x) & m);
-}
-
-// Error-free transformation: s + e == a + b exactly (Knuth's two-sum).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bp = s - a;
-  e = (a - (s - bp)) + (b - bp);
 }
 
 __device__ __forceinline__ double wrap_2pi(double x) {
