@@ -46,7 +46,12 @@ constexpr int kExactBlocks = 4;         // blocks per sample of the exact-bin ke
 constexpr int kExactThreads = 128;
 __device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
 using GradScalar = DualF<kMixNT>;    // exact bins: FP64 values (phases of 1e6 rad), FP32 tangents
-using NodeGradScalar = DualS<kMixNT>;  // sparse nodes: the values enter only through the chain rule
+// Sparse nodes: FP32 values (they enter only through the chain rule) and the 9
+// tangents split over two passes (slots 0-4, then 5-8), which halves the live
+// registers of the node evaluation.
+constexpr int kPassA = 5, kPassB = kMixNT - kPassA;
+using NodeGradA = DualS<kPassA>;
+using NodeGradB = DualS<kPassB>;
 
 struct MixedDev {
   int32_t J;                // nodes
@@ -90,7 +95,8 @@ struct MixedDev {
   double* part;             // [B][nblk_dense] lnL partials
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
-  void* gblocks32;          // [B] SampleBlock<NodeGradScalar>
+  void* gblocksA;           // [B] SampleBlock<NodeGradA> (tangent slots 0-4)
+  void* gblocksB;           // [B] SampleBlock<NodeGradB> (tangent slots 5-8)
   double* gdir;             // [B][n_det] direct t_c term of the gradient
   // Amplitude kink at f_peak: the transfer quantities carry C_q max(0, Mf - Mf_peak)^2
   // (C_q = jump/2 * R_q, R_q = G_q(f_peak)/Ahat(f_peak)); it is removed from the
@@ -217,19 +223,39 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
 
 // Gradient set-up: per sample, the coefficient block with exact FP64
 // tangents, stored with FP32 tangents for the node kernel.
+// FP32 value and tangents [Off, Off + N) of a coefficient block with FP64 tangents.
+template <int N, int Off, class TD>
+__device__ void narrow_block(const PhenomDCoef<TD>& wf, const Polar<TD>& pol, const TD& tc,
+                             SampleBlock<DualS<N>>& o) {
+  static_assert(sizeof(PhenomDCoef<TD>) / sizeof(TD) == sizeof(PhenomDCoef<DualS<N>>) / sizeof(DualS<N>),
+                "coefficient block must be an array of scalars");
+  static_assert(sizeof(Polar<TD>) / sizeof(TD) == sizeof(Polar<DualS<N>>) / sizeof(DualS<N>),
+                "polarisation block must be an array of scalars");
+  auto narrow = [](const TD* a, DualS<N>* b, int n) {
+    for (int k = 0; k < n; ++k) {
+      b[k].v = (float)a[k].v;
+      for (int i = 0; i < N; ++i) b[k].d[i] = (float)a[k].d[Off + i];
+    }
+  };
+  narrow(reinterpret_cast<const TD*>(&wf), reinterpret_cast<DualS<N>*>(&o.wf), sizeof(PhenomDCoef<TD>) / sizeof(TD));
+  narrow(reinterpret_cast<const TD*>(&pol), reinterpret_cast<DualS<N>*>(&o.pol), sizeof(Polar<TD>) / sizeof(TD));
+  narrow(&tc, &o.tc, 1);
+  o.status = kSampleOk;
+}
+
 __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_t B,
-                             SampleBlock<GradScalar>* __restrict__ out,
-                             SampleBlock<NodeGradScalar>* __restrict__ out32) {
+                             SampleBlock<GradScalar>* __restrict__ out, SampleBlock<NodeGradA>* __restrict__ outA,
+                             SampleBlock<NodeGradB>* __restrict__ outB) {
   using TD = Dual<kMixNT, double>;
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
   double raw[11];
   for (int j = 0; j < 11; ++j) raw[j] = theta[11 * s + j];
   SampleBlock<GradScalar>& o = out[s];
-  SampleBlock<NodeGradScalar>& o32 = out32[s];
   if (!theta_in_domain(raw)) {
     o.status = kSampleOutOfDomain;
-    o32.status = kSampleOutOfDomain;
+    outA[s].status = kSampleOutOfDomain;
+    outB[s].status = kSampleOutOfDomain;
     return;
   }
   TD th[11];
@@ -260,32 +286,21 @@ __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_
   narrow(reinterpret_cast<const TD*>(&pol), reinterpret_cast<GradScalar*>(&o.pol), sizeof(Polar<TD>) / sizeof(TD));
   narrow(&th[10], &o.tc, 1);
   o.status = kSampleOk;
-  static_assert(sizeof(PhenomDCoef<TD>) / sizeof(TD) ==
-                    sizeof(PhenomDCoef<NodeGradScalar>) / sizeof(NodeGradScalar),
-                "coefficient block must be an array of scalars");
-  static_assert(sizeof(Polar<TD>) / sizeof(TD) == sizeof(Polar<NodeGradScalar>) / sizeof(NodeGradScalar),
-                "polarisation block must be an array of scalars");
-  auto narrow32 = [](const TD* a, NodeGradScalar* b, int n) {
-    for (int k = 0; k < n; ++k) {
-      b[k].v = (float)a[k].v;
-      for (int i = 0; i < kMixNT; ++i) b[k].d[i] = (float)a[k].d[i];
-    }
-  };
-  narrow32(reinterpret_cast<const TD*>(&wf), reinterpret_cast<NodeGradScalar*>(&o32.wf),
-           sizeof(PhenomDCoef<TD>) / sizeof(TD));
-  narrow32(reinterpret_cast<const TD*>(&pol), reinterpret_cast<NodeGradScalar*>(&o32.pol),
-           sizeof(Polar<TD>) / sizeof(TD));
-  narrow32(&th[10], &o32.tc, 1);
-  o32.status = kSampleOk;
+  narrow_block<kPassA, 0>(wf, pol, th[10], outA[s]);
+  narrow_block<kPassB, kPassA>(wf, pol, th[10], outB[s]);
 }
 
 // Backward: recompute the node quantities with tangents and contract with the node adjoints.
-__global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G, double wscale) {
-  using GS = NodeGradScalar;
+// Pass (N, Off) handles tangent slots [Off, Off + N); the first pass also the
+// analytic ln D_L and phi_c terms.  Each pass writes only its parameters.
+template <int N, int Off>
+__global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G, double wscale) {
+  using GS = DualS<N>;
+  constexpr bool kFirst = Off == 0;
   __shared__ SampleBlock<GS> sb;
   __shared__ double red[kSparseThreads / 32][11];
   const int s = blockIdx.z, d = blockIdx.y;
-  load_block(reinterpret_cast<const SampleBlock<GS>*>(M.gblocks32), s, sb);
+  load_block(reinterpret_cast<const SampleBlock<GS>*>(kFirst ? M.gblocksA : M.gblocksB), s, sb);
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
@@ -310,9 +325,11 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
     for (int q = 0; q < kNodeQ; ++q) {
       const float w = (float)yb[q];
 #pragma unroll
-      for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] = fmaf(w, y[q].d[k], acc[kSlotParam[k]]);
-      if (q > 0) acc[4] = fmaf(-w, y[q].v, acc[4]);  // G ~ 1/D_L
-      else acc[9] = fmaf(-2.0f, w, acc[9]);          // Phi_s = ... - 2 phi_c
+      for (int k = 0; k < N; ++k) acc[kSlotParam[Off + k]] = fmaf(w, y[q].d[k], acc[kSlotParam[Off + k]]);
+      if (kFirst) {
+        if (q > 0) acc[4] = fmaf(-w, y[q].v, acc[4]);  // G ~ 1/D_L
+        else acc[9] = fmaf(-2.0f, w, acc[9]);          // Phi_s = ... - 2 phi_c
+      }
     }
   }
   // block sum: float-float across the warp, FP64 across warps
@@ -345,10 +362,10 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
       // sum A_q x f = (sum A_q x^2 + Mf_peak sum A_q x) / Msec  (f = (x + Mf_peak) / Msec)
       const double K2 = wscale * K[q], K1 = wscale * K[6 + q];
       const double K1f = (K2 + sb.wf.fpeak.v * K1) / sb.wf.Msec.v;
-      for (int k = 0; k < kMixNT; ++k)
-        accd[kSlotParam[k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
-                               2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
-      accd[4] -= C[q] * K2;  // C_q ~ 1/D_L
+      for (int k = 0; k < N; ++k)
+        accd[kSlotParam[Off + k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
+                                     2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
+      if (kFirst) accd[4] -= C[q] * K2;  // C_q ~ 1/D_L
     }
   }
   const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -358,10 +375,15 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_bwd(PlanDev P, MixedD
   }
   __syncthreads();
   if (threadIdx.x < 11) {
-    double x = 0.0;
+    bool mine = kFirst && (threadIdx.x == 4 || threadIdx.x == 9);
 #pragma unroll
-    for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
-    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + threadIdx.x] = x;
+    for (int k = 0; k < N; ++k) mine = mine || kSlotParam[Off + k] == (int)threadIdx.x;
+    if (mine) {
+      double x = 0.0;
+#pragma unroll
+      for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
+      M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + threadIdx.x] = x;
+    }
   }
 }
 
@@ -961,16 +983,17 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   }
 }
 
-__global__ void __launch_bounds__(kSplineThreads) k_spline_fit(MixedDev M) {
-  __shared__ double sm4[kNodeQ][4];
-  const int q = threadIdx.x >> 5;
-  const int64_t sd = blockIdx.x;
+// One warp per block: blockIdx.x = (sample * n_det + detector) * 7 + quantity.
+__global__ void __launch_bounds__(32) k_spline_fit(MixedDev M) {
+  __shared__ double sm4[4];
+  const int q = (int)(blockIdx.x % kNodeQ);
+  const int64_t sd = blockIdx.x / kNodeQ;
   const int n = M.nsp[sd / M.n_det];
   if (n < 3) return;
   if (q == 0)
-    spline_fit_regs<double>(M, sd, q, n, sm4[q]);
+    spline_fit_regs<double>(M, sd, q, n, sm4);
   else
-    spline_fit_regs<float>(M, sd, q, n, reinterpret_cast<float*>(sm4[q]));
+    spline_fit_regs<float>(M, sd, q, n, reinterpret_cast<float*>(sm4));
 }
 
 template <class R>
@@ -1100,9 +1123,9 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   }
 }
 
-__global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint(MixedDev M, double wscale) {
-  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t sd = blockIdx.x;
+__global__ void __launch_bounds__(32) k_spline_adjoint(MixedDev M, double wscale) {
+  const int q = (int)(blockIdx.x % kNodeQ), lane = threadIdx.x & 31;
+  const int64_t sd = blockIdx.x / kNodeQ;
   const int n = M.nsp[sd / M.n_det];
   if (n < 3) {
     double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
@@ -1652,7 +1675,8 @@ int mixed_create(PesPlan* p) {
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
-  SampleBlock<NodeGradScalar>* gblk32;
+  SampleBlock<NodeGradA>* gblkA;
+  SampleBlock<NodeGradB>* gblkB;
   double *kR, *kC;
   float* kF;
   float* bin_t;
@@ -1675,7 +1699,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
-      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &gblk32, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
+      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &gblkA, (size_t)B)) || (rc = alloc(mb, &gblkB, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
       (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) ||
       (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * kExactBlocks)) ||
       (rc = alloc(mb, &xgpart, (size_t)B * kExactBlocks * 11)))
@@ -1770,7 +1794,8 @@ int mixed_create(PesPlan* p) {
   M.gpart = gpart;
   M.gdir = gdir;
   M.gblocks = gblk;
-  M.gblocks32 = gblk32;
+  M.gblocksA = gblkA;
+  M.gblocksB = gblkB;
   M.kinkR = kR;
   M.kinkC = kC;
   M.kinkF = kF;
@@ -1816,7 +1841,7 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
   if (M.J <= kSegMax * 32 + 1)
-    k_spline_fit<<<M.n_det, kSplineThreads, 0, st>>>(M);
+    k_spline_fit<<<M.n_det * kNodeQ, 32, 0, st>>>(M);
   else
     k_spline_fit_wide<<<M.n_det, kSplineThreads, 0, st>>>(M);
   PES_CHECK_LAUNCH();
@@ -1879,7 +1904,8 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
       ProfScope ps(p, kKSetup, side);
       k_setup_grad<<<ceil_div(B, 64), 64, 0, side>>>(p->dev, theta, B,
                                                      reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks),
-                                                     reinterpret_cast<SampleBlock<NodeGradScalar>*>(M.gblocks32));
+                                                     reinterpret_cast<SampleBlock<NodeGradA>*>(M.gblocksA),
+                                                     reinterpret_cast<SampleBlock<NodeGradB>*>(M.gblocksB));
     }
     PES_CHECK_LAUNCH();
     {
@@ -1904,7 +1930,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   {
     ProfScope ps(p, kKSpline, st);
     if (M.J <= kSegMax * 32 + 1)
-      k_spline_fit<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
+      k_spline_fit<<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M);
     else
       k_spline_fit_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
   }
@@ -1938,7 +1964,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   {
     ProfScope ps(p, kKAdjoint, st);
     if (M.J <= kSegMax * 32 + 1)
-      k_spline_adjoint<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
+      k_spline_adjoint<<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
     else
       k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
   }
@@ -1946,7 +1972,13 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   {
     ProfScope ps(p, kKAdjoint, st);
     dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
-    k_sparse_bwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
+    k_sparse_bwd<kPassA, 0><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
+  }
+  PES_CHECK_LAUNCH();
+  {
+    ProfScope ps(p, kKAdjoint, st);
+    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
+    k_sparse_bwd<kPassB, kPassA><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
   }
   PES_CHECK_LAUNCH();
   {
