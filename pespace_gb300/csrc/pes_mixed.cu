@@ -125,7 +125,7 @@ struct MixedBuffers {
   // The exact-bin kernels use a few SMs for a long dependent chain each; they
   // run on a side stream beside the sparse/spline/dense stages.
   cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, xready = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -392,6 +392,10 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, Mix
 // live bin; xbin: bins below the first interval whose yearly orbital phase
 // advance omega |t(f_{j+1}) - t(f_j)| is at most kOrbitPhaseMax (that advance
 // falls monotonically with f over the inspiral, so a bisection finds it).
+// kPart 0 writes nsp and nch (needed by the sparse stage), kPart 1 xbin (needed
+// from the exact bins and the run anchors on), so the bisection can run on the
+// side stream.
+template <int kPart>
 __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
@@ -408,6 +412,11 @@ __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict
     ns = M.ch_iv[lo] + 1;
     if (ns < 3) ns = 3;
     if (ns > M.J - 1) ns = M.J - 1;
+    if (kPart == 0) {
+      M.nsp[s] = ns;
+      M.nch[s] = nc;
+      return;
+    }
     auto unresolved = [&](int j) {
       double a, ps, t0, t1;
       phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j], a, ps, t0);
@@ -424,9 +433,12 @@ __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict
       xb = (int)(first < b.kcut ? first : b.kcut);
     }
   }
-  M.nsp[s] = ns;
-  M.nch[s] = nc;
-  M.xbin[s] = xb;
+  if (kPart == 0) {
+    M.nsp[s] = ns;
+    M.nch[s] = nc;
+  } else {
+    M.xbin[s] = xb;
+  }
 }
 
 // ------------------------------------------------------------------ splines
@@ -1623,9 +1635,16 @@ int mixed_create(PesPlan* p) {
                 "resolved by the sparse grid, use the fp64 precision for it", k);
   MixedBuffers* mb = new MixedBuffers();
   p->mixed = mb;
-  PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->side, cudaStreamNonBlocking));
+  {
+    // highest priority: the side kernels are few, long-latency blocks that should
+    // get SM slots as soon as the main stream's blocks retire
+    int least = 0, greatest = 0;
+    PES_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    PES_CHECK_CUDA(cudaStreamCreateWithPriority(&mb->side, cudaStreamNonBlocking, greatest));
+  }
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->fork, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->join, cudaEventDisableTiming));
+  PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->xready, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
   const int J = d.n_sparse;
@@ -1810,6 +1829,7 @@ void mixed_destroy(PesPlan* p) {
   for (void* a : p->mixed->allocs) cudaFree(a);
   if (p->mixed->fork) cudaEventDestroy(p->mixed->fork);
   if (p->mixed->join) cudaEventDestroy(p->mixed->join);
+  if (p->mixed->xready) cudaEventDestroy(p->mixed->xready);
   if (p->mixed->side) cudaStreamDestroy(p->mixed->side);
   delete p->mixed;
   p->mixed = nullptr;
@@ -1834,7 +1854,8 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
   k_setup<double><<<1, 64, 0, st>>>(p->dev, theta_dev, 1, 0, blocks);
   PES_CHECK_LAUNCH();
-  k_mixed_ranges<<<1, 64, 0, st>>>(M, blocks, 1);
+  k_mixed_ranges<0><<<1, 64, 0, st>>>(M, blocks, 1);
+  k_mixed_ranges<1><<<1, 64, 0, st>>>(M, blocks, 1);
   PES_CHECK_LAUNCH();
   k_kink<<<1, 64, 0, st>>>(p->dev, M, G, blocks, 1);
   PES_CHECK_LAUNCH();
@@ -1887,13 +1908,19 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKOther, st);
-    k_mixed_ranges<<<ceil_div(B, 64), 64, 0, st>>>(M, blocks, B);
+    k_mixed_ranges<0><<<ceil_div(B, 64), 64, 0, st>>>(M, blocks, B);
   }
   PES_CHECK_LAUNCH();
-  // side stream: exact bins (and the gradient set-up they need)
+  // side stream: the exact-bin range, the exact bins and the gradient set-up they need
   cudaStream_t side = p->mixed->side;
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->fork, st));
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->fork, 0));
+  {
+    ProfScope ps(p, kKOther, side);
+    k_mixed_ranges<1><<<ceil_div(B, 64), 64, 0, side>>>(M, blocks, B);
+  }
+  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->xready, side));
   {
     ProfScope ps(p, kKDenseFp64, side);
     k_exact<0, double><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
@@ -1939,6 +1966,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
     PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
   }
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->xready, 0));
   {
     ProfScope ps(p, kKSpline, st);
     dim3 grid((unsigned)ceil_div(M.nchunks, 128), M.n_det, (unsigned)B);

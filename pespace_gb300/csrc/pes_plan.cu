@@ -184,14 +184,34 @@ __global__ void k_row_norm(PlanDev P, const double2* __restrict__ data, const do
   row[i] = acc;
 }
 
-// suffix[k] = sum_{i >= k} row[i]; one block, sequential chunks (set-up only)
-__global__ void k_suffix(int64_t n, const double* __restrict__ row, double* __restrict__ suffix) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// suffix[k] = sum_{i >= k} row[i] (set-up only): one block; every thread sums
+// its contiguous chunk, thread 0 turns the chunk totals into the carries from
+// the chunks above (fixed order), and every thread writes its chunk.
+constexpr int kSuffixThreads = 1024;
+__global__ void __launch_bounds__(kSuffixThreads) k_suffix(int64_t n, const double* __restrict__ row,
+                                                           double* __restrict__ suffix) {
+  __shared__ double part[kSuffixThreads];
+  const int t = threadIdx.x;
+  const int64_t chunk = (n + kSuffixThreads - 1) / kSuffixThreads;
+  const int64_t lo = min(n, (int64_t)t * chunk), hi = min(n, lo + chunk);
   double acc = 0.0;
-  suffix[n] = 0.0;
-  for (int64_t i = n - 1; i >= 0; --i) {
-    acc += row[i];
-    suffix[i] = acc;
+  for (int64_t i = hi - 1; i >= lo; --i) acc += row[i];
+  part[t] = acc;
+  __syncthreads();
+  if (t == 0) {
+    double c = 0.0;
+    for (int u = kSuffixThreads - 1; u >= 0; --u) {
+      const double v = part[u];
+      part[u] = c;
+      c += v;
+    }
+    suffix[n] = 0.0;
+  }
+  __syncthreads();
+  double c = part[t];
+  for (int64_t i = hi - 1; i >= lo; --i) {
+    c += row[i];
+    suffix[i] = c;
   }
 }
 
@@ -326,7 +346,7 @@ int pes_plan_set_data(PesPlan* p, int32_t det, const double* data, const double*
   PES_CHECK_LAUNCH();
   k_row_norm<<<ceil_div(n, 256), 256, 0, st>>>(p->dev, p->data, p->w, p->d_row);
   PES_CHECK_LAUNCH();
-  k_suffix<<<1, 32, 0, st>>>(n, p->d_row, p->suffix);
+  k_suffix<<<1, kSuffixThreads, 0, st>>>(n, p->d_row, p->suffix);
   PES_CHECK_LAUNCH();
   p->data_set_mask |= 1u << det;
   if (p->mixed) {
