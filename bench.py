@@ -268,6 +268,30 @@ def run_native(args):
         e2e_ms.append(s.elapsed_time(e))
     e2e_value = replicas.job_rate(world, B, replicas.reduce_max(float(np.mean(e2e_ms)), "cuda"))
 
+    # ---------------- lnL-only calls and CUDA-graph replays of the lnL+gradient call
+    from pespace_gb300.inference import CapturedStep
+
+    def timed(fn, n):
+        ms = []
+        for _ in range(n):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            ms.append(s.elapsed_time(e))
+        return float(np.mean(ms))
+
+    for _ in range(max(3, args.warmup)):
+        eng.log_likelihood_batch(theta)
+    lnl_ms = replicas.reduce_max(timed(lambda: eng.log_likelihood_batch(theta), args.steps), "cuda")
+    graph_step = CapturedStep(eng, B)
+    for _ in range(max(3, args.warmup)):
+        graph_step(theta)
+    graph_ms = replicas.reduce_max(timed(lambda: graph_step(theta), args.steps), "cuda")
+    del graph_step
+
     # ---------------- accuracy against the FP64 path on this workload
     err = None
     if args.precision == "mixed":
@@ -301,6 +325,10 @@ def run_native(args):
             "gpu_launches": int(gpu_launches),
             "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in kern.items()},
             "work_per_step": work,
+            "dense_bins_per_s": world * (work["dense_bins"] + work["fp64_bins"]) / (mean_ms / 1e3),
+            "lnl_only": {"value": replicas.job_rate(world, B, lnl_ms), "unit": "lnL evals/s", "ms_per_step": lnl_ms},
+            "cuda_graph": {"value": replicas.job_rate(world, B, graph_ms), "unit": "lnL+grad evals/s",
+                           "ms_per_step": graph_ms},
             "roofline": roofline,
             "clocks": clocks.summary(),
         }

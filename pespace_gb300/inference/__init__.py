@@ -1,6 +1,7 @@
 """Likelihoods (single-sample plugin path and the batched plan engine)."""
 
 from .likelihood import (  # noqa: F401
+    CapturedStep,
     LikelihoodBilbyInterface,
     WhittleLikelihood,
     compute_whittle_likelihood,

@@ -212,6 +212,52 @@ class WhittleLikelihood:
         return out
 
 
+class CapturedStep:
+    """One batched lnL (+ gradient) call of an engine captured in a CUDA graph.
+
+    The graph is recorded once on fixed device buffers (``theta``, ``lnl``,
+    ``grad``, ``status``); ``__call__`` copies new parameters into ``theta``
+    and replays it, which removes the per-launch host cost of the kernels and
+    event waits of a call.  The engine's measurement hooks must be off while
+    capturing.
+    """
+
+    def __init__(self, engine, batch, grad=True):
+        if batch < 1 or batch > engine.max_batch:
+            raise ValueError(f"batch must be 1..{engine.max_batch}, got {batch}")
+        self.engine, self.batch, self.with_grad = engine, int(batch), bool(grad)
+        dev = torch.device("cuda")
+        self.theta = torch.zeros((batch, 11), dtype=torch.float64, device=dev)
+        self.lnl = torch.empty(batch, dtype=torch.float64, device=dev)
+        self.grad = torch.empty((batch, 11), dtype=torch.float64, device=dev) if grad else None
+        self.status = torch.empty(batch, dtype=torch.int32, device=dev)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self._launch()  # warm-up outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._launch()
+
+    def _launch(self):
+        lib = _lib.load()
+        if self.with_grad:
+            rc = lib.pes_lnl_grad_batch(self.engine._plan, _lib.ptr(self.theta), self.batch, _lib.ptr(self.lnl),
+                                        _lib.ptr(self.grad), _lib.ptr(self.status), _lib.stream_handle())
+        else:
+            rc = lib.pes_lnl_batch(self.engine._plan, _lib.ptr(self.theta), self.batch, _lib.ptr(self.lnl),
+                                   _lib.ptr(self.status), _lib.stream_handle())
+        _lib.check(rc)
+
+    def __call__(self, theta):
+        """Replay on new parameters (B, 11); returns lnL (and the gradient) views of the graph's buffers."""
+        self.theta.copy_(torch.as_tensor(theta, dtype=torch.float64, device="cuda").reshape(self.batch, 11))
+        self.graph.replay()
+        return (self.lnl, self.grad) if self.with_grad else self.lnl
+
+
 class _LogLikelihoodFn(torch.autograd.Function):
     """lnL(theta) with the gradient from the plan's derivative kernels."""
 

@@ -113,3 +113,26 @@ def test_mixed_other_grids(cuda_lib, oracle, dataset, n_sparse):
     assert np.all(err <= tol + 1e-8 * np.abs(w_lnl)), err
     norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
     assert np.max(np.abs(grad.cpu().numpy() - w_grad) / norm) < 1e-3
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_cuda_graph_replay(cuda_lib, oracle, dataset, precision):
+    """A captured lnL+gradient call replays identically to the direct call,
+    on new parameters too (mixed gradients within FP32 atomic-order noise)."""
+    from pespace_gb300.inference import CapturedStep, WhittleLikelihood
+
+    g, dets, th0 = dataset
+    eng = WhittleLikelihood(cuda_detectors(g, dets[:1]), precision=precision, reference_frequency=1e-4,
+                            max_batch=8)
+    rng = np.random.default_rng(23)
+    step = CapturedStep(eng, 8)
+    for _ in range(2):
+        thetas = np.stack([perturbed(th0, rng) for _ in range(8)])
+        lnl, grad = step(thetas)
+        lnl, grad = lnl.clone(), grad.clone()
+        want_lnl, want_grad = eng.log_likelihood_and_grad(thetas)
+        assert torch.equal(lnl, want_lnl)
+        if precision == "fp64":
+            assert torch.equal(grad, want_grad)
+        else:
+            assert torch.allclose(grad, want_grad, rtol=1e-5, atol=1e-6 * float(want_grad.abs().max()))

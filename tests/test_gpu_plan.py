@@ -156,3 +156,31 @@ def test_edge_cases_and_status(cuda_lib, oracle, dataset):
     th = torch.as_tensor(np.stack([th0] * 5), device="cuda")
     out = torch.empty(5, dtype=torch.float64, device="cuda")
     assert lib.pes_lnl_batch(eng._plan, _lib.ptr(th), 5, _lib.ptr(out), None, None) == _lib.PES_EINVAL
+
+
+def test_gradient_central_differences(cuda_lib, oracle, dataset):
+    """FP64 plan gradient against central finite differences of its own lnL
+    (step 1e-6 relative: 1e-6 in ln Mc and ln D_L, 1e-6 max(|x|, 1) for the
+    others).  The mixed
+    plan's lnL carries FP32 rounding of ~1e-9 |lnL|, which such a step turns
+    into differences far above its gradient error; its gradient is checked
+    against the oracle's dual numbers instead."""
+    from pespace_gb300.inference import WhittleLikelihood
+
+    g, dets, th0 = dataset
+    eng = WhittleLikelihood(cuda_detectors(g, dets[:1]), precision="fp64", reference_frequency=1e-4, max_batch=32)
+    rng = np.random.default_rng(17)
+    base = np.stack([th0, perturbed(th0, rng)])
+    _, grad = eng.log_likelihood_and_grad(base)
+    grad = grad.cpu().numpy()
+    for b in range(base.shape[0]):
+        steps = 1e-6 * np.maximum(np.abs(base[b]), 1.0)
+        steps[[0, 4]] = 1e-6  # ln Mc, ln D_L: a relative step of 1e-6 in Mc and D_L
+        pts = np.repeat(base[b][None], 22, axis=0)
+        for k in range(11):
+            pts[2 * k, k] += steps[k]
+            pts[2 * k + 1, k] -= steps[k]
+        v = eng.log_likelihood_batch(pts).cpu().numpy()
+        fd = (v[0::2] - v[1::2]) / (2 * steps)
+        norm = np.linalg.norm(grad[b])
+        assert np.max(np.abs(fd - grad[b])) / norm < 1e-4, (b, fd, grad[b])
