@@ -180,6 +180,17 @@ int pes_plan_profile(PesPlan* plan, int32_t enable);
 int pes_plan_stats(PesPlan* plan, int64_t* launches /* host [8] */, double* device_ms /* host [8] */);
 const char* pes_kernel_class_name(int32_t k);
 
+/* Fisher matrices at B parameter sets (row-major (B, 11, 11), parameter order
+ * of theta): F_ij = 4 df Re sum_{det, c, f} conj(dh_i) dh_j / S_c(f) over the
+ * plan's channels and each sample's live bins, derivatives of the A/E/T model
+ * by FP64 forward-mode dual numbers (both precisions of plan).  The data are
+ * not used, only the PSDs.  Replaces pespace/inference/fisher.py:27-162
+ * (fisher_matrix).  Out-of-domain samples get NaN and their status.  The first
+ * call allocates the plan's Fisher workspace (about 6 KB + 25 KB per sample of
+ * max_batch). */
+int pes_fisher_batch(PesPlan* plan, const double* theta, int64_t B, double* fisher /* (B,11,11) */,
+                     int32_t* status /* nullable */, void* stream);
+
 /* Work units of the last pes_lnl_batch / pes_lnl_grad_batch call of B samples
  * (host; synchronises `stream`), for roofline bookkeeping.  No reference
  * counterpart.  out[0]: bins through the mixed plan's FP32 dense stage,

@@ -104,6 +104,7 @@ def lib():
         L.oracle_phenomd.argtypes = [vp, vp, i64, d, d, vp, vp, vp, vp, vp]
         L.oracle_model_tdi.argtypes = [P(OraclePlan), ctypes.c_int, ctypes.c_int, vp, vp]
         L.oracle_lnl_batch.argtypes = [P(OraclePlan), vp, i64, vp, vp, ctypes.c_int]
+        L.oracle_fisher_batch.argtypes = [P(OraclePlan), vp, i64, vp, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -343,6 +344,14 @@ class Plan:
         lib().oracle_lnl_batch(ctypes.byref(self.plan), _p(theta), B, _p(out),
                                _p(g) if grad else None, int(nthreads))
         return (out, g) if grad else out
+
+    def fisher(self, theta, nthreads=0):
+        """(B, 11, 11) Fisher matrices (fisher.py:27-162) at the rows of theta."""
+        theta = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        B = theta.shape[0]
+        out = np.zeros((B, 11, 11))
+        lib().oracle_fisher_batch(ctypes.byref(self.plan), _p(theta), B, _p(out), int(nthreads))
+        return out
 
     def model_tdi(self, det, theta, orthogonal=True):
         theta = np.ascontiguousarray(theta, dtype=np.float64)

@@ -718,6 +718,48 @@ T lnl_one(const OraclePlan& pl, const T* th) {
   return -2.0 * pl.df * acc;
 }
 
+// Fisher matrix at one parameter set, fisher.py:27-162:
+// F_ij = 4 df Re sum_{det, c, f} conj(dh_i) dh_j / S_c(f) over the channels of
+// the mask and the live bins (the model is zero above the sample's cut, so
+// its derivatives are too); derivatives by forward-mode dual numbers.
+void fisher_one(const OraclePlan& pl, const double* t, double* F) {
+  using D11 = Dual<11>;
+  D11 th[11];
+  for (int j = 0; j < 11; ++j) {
+    th[j] = D11(t[j]);
+    th[j].d[j] = 1.0;
+  }
+  PhenomD<D11> wf;
+  phenomd_setup(th, pl.f_ref, wf);
+  D11 sb = th[7];
+  D11 cb = sqrt((1.0 - sb) * (1.0 + sb));
+  D11 P[3][3], X[3][3], k[3];
+  polarization(th[6], sb, cb, th[8], P, X, k);
+  double fmax = double(pl.k0 + pl.nbins - 1) * pl.f_step + 1.0;
+  double fcut = sample_cut_hz(wf, pl.cut_factor, fmax);
+  double acc[11][11] = {};
+  for (int64_t i = 0; i < pl.nbins; ++i) {
+    double f = double(pl.k0 + i) * pl.f_step;
+    Cx<D11> hp, hc;
+    D11 tf;
+    if (!phenomd_eval(wf, f, fcut, hp, hc, tf)) continue;
+    for (int d = 0; d < pl.n_det; ++d) {
+      const OracleDet& det = pl.dets[d];
+      Cx<D11> L[6], h[3];
+      response_at_f(det.orbit, f, 1, &hp, &hc, &tf, th[10], P, X, k, L);
+      tdi_at_f(f, det.orbit.arm_sec, det.gen20, 1, L, h);
+      for (int c = 0; c < 3; ++c) {
+        if (!((pl.chan_mask >> c) & 1)) continue;
+        const double w = 1.0 / det.psd[c * pl.nbins + i];
+        for (int a = 0; a < 11; ++a)
+          for (int b = a; b < 11; ++b) acc[a][b] += w * (h[c].re.d[a] * h[c].re.d[b] + h[c].im.d[a] * h[c].im.d[b]);
+      }
+    }
+  }
+  for (int a = 0; a < 11; ++a)
+    for (int b = a; b < 11; ++b) F[11 * a + b] = F[11 * b + a] = 4.0 * pl.df * acc[a][b];
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -860,6 +902,15 @@ int oracle_lnl_batch(const OraclePlan* pl, const double* th, int64_t B, double* 
       lnl[b] = lnl_one<double>(*pl, t);
     }
   }
+  return 0;
+}
+
+int oracle_fisher_batch(const OraclePlan* pl, const double* th, int64_t B, double* F, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int64_t b = 0; b < B; ++b) fisher_one(*pl, th + 11 * b, F + 121 * b);
   return 0;
 }
 

@@ -95,6 +95,7 @@ SIGNATURES = {
     "pes_plan_stats": (ctypes.c_int, [_vp, _vp, _vp]),
     "pes_kernel_class_name": (ctypes.c_char_p, [_i32]),
     "pes_plan_work": (ctypes.c_int, [_vp, _i64, _vp, _vp]),
+    "pes_fisher_batch": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
 }
 KERNEL_CLASSES = 8
 

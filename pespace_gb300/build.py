@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpespace_gb300.so")
-SOURCES = ["pes_plugins.cu", "pes_plan.cu", "pes_mixed.cu"]
+SOURCES = ["pes_plugins.cu", "pes_plan.cu", "pes_mixed.cu", "pes_fisher.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -323,6 +323,8 @@ int pes_plan_destroy(PesPlan* p) {
   }
   for (auto e : p->prof.pool) cudaEventDestroy(e);
   if (p->mixed) mixed_destroy(p);
+  cudaFree(p->fisher_blocks);
+  cudaFree(p->fisher_partial);
   cudaFree(p->data);
   cudaFree(p->w);
   cudaFree(p->tdi);

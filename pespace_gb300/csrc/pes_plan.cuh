@@ -93,6 +93,8 @@ struct PesPlan {
   int32_t* status = nullptr;   // [max_batch] internal status when the caller passes NULL
   unsigned data_set_mask = 0;
   pes::MixedBuffers* mixed = nullptr;
+  void* fisher_blocks = nullptr;     // [max_batch] SampleBlock<Dual<11>> (first Fisher call)
+  double* fisher_partial = nullptr;  // [max_batch][blocks][66]
   pes::Profiler prof;
 };
 

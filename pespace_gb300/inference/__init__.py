@@ -8,3 +8,4 @@ from .likelihood import (  # noqa: F401
     log_likelihood,
     noise_weighted_inner_product,
 )
+from .fisher import fisher_matrix, sample_from_fisher, wrap_angle_params  # noqa: F401,E402

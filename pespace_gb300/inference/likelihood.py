@@ -189,6 +189,21 @@ class WhittleLikelihood:
         self.last_status = status
         return out, grad
 
+    def fisher_matrix(self, theta):
+        """(B, 11, 11) Fisher matrices at the rows of a (B, 11) parameter tensor
+        (fisher.py:27-162 over this engine's detectors, channels and per-sample
+        cut; FP64 derivatives for either precision)."""
+        theta = self._prep(theta)
+        B = theta.shape[0]
+        out = torch.empty((B, 11, 11), dtype=torch.float64, device="cuda")
+        status = torch.empty(B, dtype=torch.int32, device="cuda")
+        for lo in range(0, B, self.max_batch):
+            hi = min(B, lo + self.max_batch)
+            _lib.check(_lib.load().pes_fisher_batch(self._plan, _lib.ptr(theta[lo:hi]), hi - lo, _lib.ptr(out[lo:hi]),
+                                                    _lib.ptr(status[lo:hi]), _lib.stream_handle()))
+        self.last_status = status
+        return out
+
     def last_work(self, batch):
         """Work units of the last call on ``batch`` samples (the last chunk when the
         call was split at max_batch): dict with the bins through the FP32 dense
