@@ -42,7 +42,8 @@ enum { kGfH = 0, kGfInvH, kGfLo, kGfUp, kGfInvDen, kGfCp, kGfCount };
 // (Phi_s shifts by -2 phi_c) are applied analytically.
 constexpr int kMixNT = 9;
 constexpr double kOrbitPhaseMax = 0.3;  // rad of yearly orbital phase per node interval
-constexpr int kExactBlocks = 4;         // blocks per sample of the exact-bin kernel
+constexpr int kExactBlocks = 4;         // blocks per sample of the exact-bin kernel (heliocentric plans)
+constexpr int kExactBlocksGeo = 64;     // with a geocentric detector most inspiral bins are exact
 constexpr int kExactThreads = 128;
 __device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
 using GradScalar = DualF<kMixNT>;    // exact bins: FP64 values (phases of 1e6 rad), FP32 tangents
@@ -76,8 +77,9 @@ struct MixedDev {
   int32_t* xbin;            // [B] bins [0, xbin) are evaluated exactly (not splined)
   const int32_t* iv_first;  // [J + 1] first bin of each interval (nbins past the last)
   double omega;             // largest yearly orbital angular frequency of the detectors
-  double* xpart;            // [B][kExactBlocks] exact-bin lnL partials
-  double* xgpart;           // [B][kExactBlocks][11] exact-bin gradient partials
+  int32_t xblocks;          // blocks per sample of the exact-bin kernel
+  double* xpart;            // [B][xblocks] exact-bin lnL partials
+  double* xgpart;           // [B][xblocks][11] exact-bin gradient partials
   const double* gh;         // [J] node spacing h_i
   const double* ginvh;      // [J] 1 / h_i
   const double* glo;        // [J] reduced not-a-knot system, rows 1..J-2 (first-row elimination included)
@@ -1155,7 +1157,7 @@ __global__ void __launch_bounds__(32) k_spline_adjoint(MixedDev M, double wscale
 // Bins [0, xbin[s]) evaluated directly (FP64 model and residual against the
 // FP64 data).  kMode 0: lnL partials (T = double); 1: gradient partials
 // (T = GradScalar, FP64 values with FP32 tangents); 2: write the model.
-// grid (kExactBlocks, B); threads stride over the sample's exact bins.
+// grid (xblocks, B); threads stride over the sample's exact bins.
 template <int kMode, class T>
 __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, GenArg G,
                                                          const SampleBlock<T>* __restrict__ blocks,
@@ -1173,7 +1175,7 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   for (int k = 0; k < NV; ++k) acc[k] = 0.0;
   const double inv_scale = 1.0 / M.scale;
   if (sb.status == kSampleOk) {
-    for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xb; i += kExactBlocks * kExactThreads) {
+    for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xb; i += gridDim.x * kExactThreads) {
       const double f = (double)(P.k0 + i) * P.f_step;
       for (int d = 0; d < M.n_det; ++d) {
         T y[kNodeQ];
@@ -1223,9 +1225,9 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
 #pragma unroll
     for (int w = 0; w < kExactThreads / 32; ++w) x += red[w][threadIdx.x];
     if (kMode == 0)
-      M.xpart[(size_t)s * kExactBlocks + blockIdx.x] = x;
+      M.xpart[(size_t)s * gridDim.x + blockIdx.x] = x;
     else
-      M.xgpart[((size_t)s * kExactBlocks + blockIdx.x) * 11 + threadIdx.x] = x;
+      M.xgpart[((size_t)s * gridDim.x + blockIdx.x) * 11 + threadIdx.x] = x;
   }
 }
 
@@ -1563,7 +1565,7 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   double acc = 0.0;
   for (int k = 0; k < M.nblk_dense; ++k) acc += M.part[(size_t)s * M.nblk_dense + k];
   if (M.xbin[s] > 0)
-    for (int k = 0; k < kExactBlocks; ++k) acc += M.xpart[(size_t)s * kExactBlocks + k];
+    for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
   const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
   lnl[s] = v;
   if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
@@ -1583,7 +1585,7 @@ __global__ void k_mixed_grad_finalize(MixedDev M, int64_t B, double xscale, doub
       }
       if (exact) {
         double x = 0.0;
-        for (int b = 0; b < kExactBlocks; ++b) x += M.xgpart[((size_t)s * kExactBlocks + b) * 11 + p];
+        for (int b = 0; b < M.xblocks; ++b) x += M.xgpart[((size_t)s * M.xblocks + b) * 11 + p];
         acc += xscale * x;
       }
     }
@@ -1629,10 +1631,6 @@ int mixed_create(PesPlan* p) {
   PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
   PES_REQUIRE(d.k0 >= 1, "mixed plan: the grid must start above 0 Hz (k0 >= 1)");
   PES_REQUIRE(d.nbins >= 8, "mixed plan: needs at least 8 bins");
-  for (int k = 0; k < d.n_det; ++k)
-    PES_REQUIRE(d.det[k].orbit.kind == 0,
-                "mixed plan: detector %d has a geocentric orbit; its 3.65-day constellation rotation is not "
-                "resolved by the sparse grid, use the fp64 precision for it", k);
   MixedBuffers* mb = new MixedBuffers();
   p->mixed = mb;
   {
@@ -1680,8 +1678,17 @@ int mixed_create(PesPlan* p) {
     cl.back() += 1;
     run_len += 1;
   }
+  // fastest orbital angular frequency: the yearly revolution, or a geocentric
+  // constellation's rotation about the Earth (TianQin: 3.65 days)
   M.omega = 0.0;
-  for (int k = 0; k < nd; ++k) M.omega = std::max(M.omega, std::fabs(d.det[k].orbit.omega_revolution));
+  M.xblocks = kExactBlocks;
+  for (int k = 0; k < nd; ++k) {
+    M.omega = std::max(M.omega, std::fabs(d.det[k].orbit.omega_revolution));
+    if (d.det[k].orbit.kind == 1) {
+      M.omega = std::max(M.omega, std::fabs(d.det[k].orbit.omega_rotation));
+      M.xblocks = kExactBlocksGeo;
+    }
+  }
   M.nchunks = (int32_t)cb.size();
   M.nblk_dense = (int32_t)ceil_div(M.nchunks, (long long)kChunkMax * (kMixThreads / 32));
   M.nblk_sparse = (int32_t)ceil_div(J, kSparseThreads);
@@ -1720,8 +1727,8 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &gblkA, (size_t)B)) || (rc = alloc(mb, &gblkB, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
       (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) ||
-      (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * kExactBlocks)) ||
-      (rc = alloc(mb, &xgpart, (size_t)B * kExactBlocks * 11)))
+      (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * M.xblocks)) ||
+      (rc = alloc(mb, &xgpart, (size_t)B * M.xblocks * 11)))
     return rc;
   PES_CHECK_CUDA(cudaMemcpy(ivfirst, ivf.data(), sizeof(int32_t) * (J + 1), cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemset(xbin, 0, sizeof(int32_t) * B));
@@ -1872,7 +1879,7 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
                                                                   reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
-  k_exact<2, double><<<dim3(kExactBlocks, 1), kExactThreads, 0, st>>>(p->dev, M, G, blocks,
+  k_exact<2, double><<<dim3(M.xblocks, 1), kExactThreads, 0, st>>>(p->dev, M, G, blocks,
                                                                       reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
   return PES_OK;
@@ -1923,7 +1930,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->xready, side));
   {
     ProfScope ps(p, kKDenseFp64, side);
-    k_exact<0, double><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+    k_exact<0, double><<<dim3(M.xblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
   if (grad) {
@@ -1937,7 +1944,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     PES_CHECK_LAUNCH();
     {
       ProfScope ps(p, kKDenseFp64, side);
-      k_exact<1, GradScalar><<<dim3(kExactBlocks, (unsigned)B), kExactThreads, 0, side>>>(
+      k_exact<1, GradScalar><<<dim3(M.xblocks, (unsigned)B), kExactThreads, 0, side>>>(
           p->dev, M, G, reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), nullptr);
     }
     PES_CHECK_LAUNCH();

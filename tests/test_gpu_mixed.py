@@ -74,12 +74,20 @@ def test_mixed_prior_batch_cutoff(cuda_lib, oracle, network):
     assert np.all(err <= 1e-2 + 1e-8 * np.abs(want)), np.sort(err)[-5:]
 
 
-def test_mixed_rejects_geocentric(cuda_lib, oracle, dataset):
-    from pespace_gb300 import PesError
-
+def test_mixed_geocentric_network(cuda_lib, oracle, dataset):
+    """LISA + TianQin: the geocentric constellation's 3.65-day rotation makes
+    most inspiral bins exact (FP64); lnL and gradient against the oracle."""
     g, dets, th0 = dataset
-    with pytest.raises(PesError, match="geocentric"):
-        engines(g, dets, max_batch=4)
+    rng = np.random.default_rng(31)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(3)] + list(random_prior_theta(rng, 4, th0[10])))
+    mixed, _ = engines(g, dets, max_batch=8, cut_factor=1.2)
+    lnl, grad = mixed.log_likelihood_and_grad(thetas)
+    w_lnl, w_grad = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(
+        thetas, grad=True, nthreads=8)
+    err = np.abs(lnl.cpu().numpy() - w_lnl)
+    assert np.all(err <= 1e-2 + 1e-8 * np.abs(w_lnl)), err
+    norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
+    assert np.max(np.abs(grad.cpu().numpy() - w_grad) / norm) < 1e-3
 
 
 def test_mixed_gradient(cuda_lib, oracle, dataset):
