@@ -28,7 +28,7 @@ the launch's dense bins.
 """
 
 FP32_FLOPS_PER_DENSE_BIN = {"lnl": 244, "grad": 341}
-DRAM_BYTES_PER_DENSE_BIN = 4.744  # (89.56 MB + 3.40 MB) / 19 595 338 bins, ncu --set full, 256 samples
+DRAM_BYTES_PER_DENSE_BIN = 4.97  # (93.04 MB + 4.34 MB) / 19 595 338 bins, ncu --set full, 256 samples
 
 
 def roofline(kernel_class, launches_ms, work, grad, fp32_peak_tflops):
