@@ -16,6 +16,7 @@ parameters copied from pinned host memory and lnL/gradient copied back.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
     python bench.py --impl reference   # the reference's CPU path (oracle port)
+    python bench.py --workload ref-shape   # the reference's published benchmark shape
 
 Multi-GPU (torchrun): replicas; every rank evaluates its own 1024 samples
 (weak scaling); rank 0 prints the line with the max-over-ranks step time.
@@ -35,7 +36,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-DUR, DT, FMIN, FMAX = 2.0 ** 22, 8.0, 1e-4, 0.03
+# (T, dt, f_min, f_max, TDI generation, description)
+WORKLOADS = {
+    "adjoint": (2.0 ** 22, 8.0, 1e-4, 0.03, "1.5",
+                "adjoint: 1024-sample prior batch, LISA TDI1.5 AET, T=2^22 s, dt=8 s, 125410 bins, cutoff 1.2 f_RD"),
+    # the shape of the reference's own published timings (65 471 bins x 3, TDI 2.0),
+    # with IMRPhenomD in place of the reference's IMRPhenomXAS
+    "ref-shape": (655360.0, 5.0, 1e-4, 0.1, "2.0",
+                  "ref-shape: 1024-sample prior batch, LISA TDI2.0 AET, T=655360 s, dt=5 s, 65471 bins, "
+                  "cutoff 1.2 f_RD, IMRPhenomD"),
+}
+DUR, DT, FMIN, FMAX, GEN, WORKLOAD = WORKLOADS["adjoint"]
 BATCH = 1024
 METRIC = "lnL+grad evals/s, 1024 MBHB samples, 1 GB300: mixed vs FP64, |dlnL|<=1e-2"
 
@@ -50,7 +61,11 @@ def parse():
                     choices=["mixed", "fp64"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--workload", default="adjoint", choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    global DUR, DT, FMIN, FMAX, GEN, WORKLOAD
+    DUR, DT, FMIN, FMAX, GEN, WORKLOAD = WORKLOADS[args.workload]
+    return args
 
 
 def dist_env():
@@ -138,7 +153,7 @@ def gemm_peak_tflops(torch, dtype):
     return 2 * 8192 ** 3 / best / 1e12
 
 
-def cpu_baseline_run(n_samples, threads, precision_note):
+def cpu_baseline_run(n_samples, threads, precision_note, grad=True):
     """The reference's CPU path (oracle port, FP64 dense, OpenMP over samples)."""
     from oracle import fdpath as oracle
     from pespace_gb300.workloads import config0_theta, prior_samples
@@ -147,16 +162,16 @@ def cpu_baseline_run(n_samples, threads, precision_note):
     g = oracle.grid(DUR, DT, FMIN, FMAX)
     th0 = config0_theta(DUR - 86400.0)
     orb = oracle.heliocentric(2.5e9, 0.0, -math.pi / 9)
-    psd = oracle.psd(g["freqs"], "AET", False, "1.5", **oracle.PSD_PRESETS["LISA_SciRDv1"])
+    psd = oracle.psd(g["freqs"], "AET", False, GEN, **oracle.PSD_PRESETS["LISA_SciRDv1"])
     noise = oracle.noise_realization(g, psd, "AET", 2026)
     data = np.stack([noise[c] for c in "AET"])
     psd_arr = np.stack([psd[c] for c in "AET"])
-    plan = oracle.Plan(g, [(orb, "1.5", data, psd_arr)], 1e-4, cut_factor=1.2)
+    plan = oracle.Plan(g, [(orb, GEN, data, psd_arr)], 1e-4, cut_factor=1.2)
     data = data + plan.model_tdi(0, th0)
-    plan = oracle.Plan(g, [(orb, "1.5", data, psd_arr)], 1e-4, cut_factor=1.2)
+    plan = oracle.Plan(g, [(orb, GEN, data, psd_arr)], 1e-4, cut_factor=1.2)
     thetas = prior_samples(np.random.default_rng(2026), n_samples, th0[10])
     t0 = time.perf_counter()
-    plan.lnl(thetas, grad=True, nthreads=threads)
+    plan.lnl(thetas, grad=grad, nthreads=threads)
     dt = time.perf_counter() - t0
     return n_samples / dt, dt
 
@@ -178,10 +193,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "lnL+grad evals/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "adjoint: 1024-sample prior batch, LISA TDI1.5 AET, T=2^22 s, dt=8 s, 125410 bins",
-                   "global_batch": BATCH, "sample_per_step": n},
+        "config": {"workload": WORKLOAD, "global_batch": BATCH, "sample_per_step": n},
         "cpu_baseline": {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} prior samples per step, full 125410-bin grid, FP64 dense with "
+                         "sample": f"{n} prior samples per step, full grid, FP64 dense with "
                                    "forward-mode gradient; taichi/jax absent on this host"},
         "e2e": {"value": v, "unit": "lnL+grad evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -204,7 +218,7 @@ def run_native(args):
 
     B = args.batch
     th0 = config0_theta(DUR - 86400.0)
-    det = lisa_dataset(DUR, DT, FMIN, FMAX, th0, "1.5", seed=2026)
+    det = lisa_dataset(DUR, DT, FMIN, FMAX, th0, GEN, seed=2026)
     eng = WhittleLikelihood(det, precision=args.precision, reference_frequency=1e-4, cut_factor=1.2, max_batch=B)
     theta_host = torch.as_tensor(replicas.rank_theta(rank, B, th0[10])).pin_memory()
     theta = theta_host.to("cuda")
@@ -315,8 +329,7 @@ def run_native(args):
             "metric": METRIC, "value": value, "unit": "lnL+grad evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-            "config": {"workload": "adjoint: 1024-sample prior batch, LISA TDI1.5 AET, T=2^22 s, dt=8 s, "
-                                   "125410 bins, cutoff 1.2 f_RD", "precision": args.precision,
+            "config": {"workload": WORKLOAD, "precision": args.precision,
                        "global_batch": B * world, "per_gpu_batch": B, "nbins": int(eng.desc.nbins),
                        "l2": "flushed between steps (512 MB write outside the timed events)",
                        "parallelism": f"replicas x{world}"},
@@ -341,6 +354,11 @@ def run_native(args):
             line["cpu_baseline"] = {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
                                     "sample": f"{n} prior samples, full grid, FP64 dense + forward-mode gradient "
                                               f"({dt:.1f} s)"}
+            # lnL only on one core: the setting of the reference's published single-core figure
+            n1 = 32
+            v1, dt1 = cpu_baseline_run(n1, 1, "", grad=False)
+            line["cpu_baseline_1core_lnl"] = {"value": v1, "unit": "lnL evals/s", "cores": 1, "kind": "port",
+                                              "sample": f"{n1} prior samples, full grid, FP64 dense ({dt1:.1f} s)"}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

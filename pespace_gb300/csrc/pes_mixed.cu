@@ -63,7 +63,8 @@ struct MixedDev {
   int32_t pad;
   double scale;             // FP32 storage scale of data and model
   const double* node_f;     // [J]
-  const TdiFactor* tdn;     // [n_det][J] TDI delay factor and generation prefactor at the nodes
+  const TdiFactor* tdn;     // [n_det][J] TDI delay factor at the nodes (prefactor set to 1)
+  float2* pbin;             // [n_det][nbins] TDI generation prefactor P(f) per bin (FP32 of the FP64 value)
   const int32_t* ch_begin;  // [nchunks] first bin of the run
   const int32_t* ch_len;    // [nchunks]
   const int32_t* ch_iv;     // [nchunks] spline interval of the run
@@ -184,8 +185,8 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
     tdi_factors(b.wf.fpeak / b.wf.Msec, P.orbit[d].arm_sec, G.gen20[d], D, Pf);
     td.dre = D.re;
     td.dim = D.im;
-    td.pre = Pf.re;
-    td.pim = Pf.im;
+    td.pre = 1.0;  // the generation prefactor is applied per bin, outside the splines
+    td.pim = 0.0;
   }
   node_eval<double>(P, M, b, d, td, b.wf.fpeak / b.wf.Msec, y);
   amp_peak_jump<double>(b.wf, ahat, jump);
@@ -1426,18 +1427,29 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float t = M.bin_t[i];
           const float u = (float)lane;
           const float u2 = u * u, u3 = u2 * u;
+          // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike
           const float del = reduce_exact(r.p1h * u) + reduce_exact(r.p2h * u2) + reduce_exact(r.p3h * u3) +
-                            (r.p1l * u + r.p2l * u2 + r.p3l * u3);
+                            fmaf(r.p1l, u, fmaf(r.p2l, u2, r.p3l * u3));
           float sd_, cd_;
           sincos_poly(del, &sd_, &cd_);
-          float cph = r.c0 * cd_ - r.s0 * sd_;
-          float sph = r.s0 * cd_ + r.c0 * sd_;
+          float cph = fmaf(r.c0, cd_, -(r.s0 * sd_));
+          float sph = fmaf(r.s0, cd_, r.c0 * sd_);
           // Renormalise the rotated phasor with one Newton step for 1/|e|
           // so that FP32 rounding leaves the model amplitude unbiased.
           const float m2 = fmaf(cph, cph, fmaf(sph, sph, -1.0f));  // |e|^2 - 1, one rounding
           const float corr = -0.5f * m2;
           cph = fmaf(corr, cph, cph);
           sph = fmaf(corr, sph, sph);
+          {
+            // TDI generation prefactor P(f): its zeros (f L = k/2) stay out of the
+            // splines; with h = G (c - i s) the factor multiplies c - i s
+            const float2 pf = M.pbin[(size_t)d * P.nbins + i];
+            // explicit FMAs: the lnL and lnL+gradient kernels must round alike
+            const float c2 = fmaf(pf.x, cph, pf.y * sph);
+            const float s2 = fmaf(pf.x, sph, -(pf.y * cph));
+            cph = c2;
+            sph = s2;
+          }
           const float4* G = M.cg + (sd * M.J + j) * 6;
           const float* Glo = M.cglo + (sd * M.J + j) * 6;
           const float xk = fmaf(kSlope, u, r.x0);
@@ -1457,15 +1469,15 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
-            const float gr = cr.x + (kink[2 * ch] + (Glo[2 * ch] + t * (cr.y + t * (cr.z + t * cr.w))));
-            const float gi = ci.x + (kink[2 * ch + 1] + (Glo[2 * ch + 1] + t * (ci.y + t * (ci.z + t * ci.w))));
-            const float hr = gr * cph + gi * sph;
-            const float hi = gi * cph - gr * sph;
+            const float gr = cr.x + (kink[2 * ch] + fmaf(t, fmaf(t, fmaf(t, cr.w, cr.z), cr.y), Glo[2 * ch]));
+            const float gi = ci.x + (kink[2 * ch + 1] + fmaf(t, fmaf(t, fmaf(t, ci.w, ci.z), ci.y), Glo[2 * ch + 1]));
+            const float hr = fmaf(gr, cph, gi * sph);
+            const float hi = fmaf(gi, cph, -(gr * sph));
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
             const float2 dv = M.dat[off];
             const float w = M.wgt[off];
             const float er = dv.x - hr, ei = dv.y - hi;
-            term = fmaf(er * er + ei * ei, w, term);
+            term = fmaf(fmaf(er, er, ei * ei), w, term);
             const float h2 = fmaf(hr, hr, hi * hi);
             hh = fmaf(h2, w, hh);
             cross = fmaf(fmaf(-2.0f, fmaf(dv.x, hr, dv.y * hi), h2), w, cross);
@@ -1610,6 +1622,8 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
   }
   const float hi = (float)dd;
   M.dd[(size_t)det * P.nbins + i] = make_float2(hi, (float)(dd - (double)hi));
+  const TdiFactor tf = P.tdi[(size_t)det * P.nbins + i];
+  M.pbin[(size_t)det * P.nbins + i] = make_float2((float)tf.pre, (float)tf.pim);
 }
 
 // ------------------------------------------------------------------ host side
@@ -1698,6 +1712,7 @@ int mixed_create(PesPlan* p) {
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
   float* gf;
   TdiFactor* tdn;
+  float2* pbin;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
@@ -1720,7 +1735,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &pbin, (size_t)nd * n)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -1739,7 +1754,8 @@ int mixed_create(PesPlan* p) {
       for (int jj = 0; jj < J; ++jj) {
         Cx<double> D, Pf;
         tdi_factors(nf[jj], d.det[k].orbit.arm_sec, d.det[k].generation == 20, D, Pf);
-        tf[(size_t)k * J + jj] = TdiFactor{D.re, D.im, Pf.re, Pf.im};
+        (void)Pf;  // the generation prefactor P(f) is applied per bin, outside the splines
+        tf[(size_t)k * J + jj] = TdiFactor{D.re, D.im, 1.0, 0.0};
       }
     PES_CHECK_CUDA(cudaMemcpy(tdn, tf.data(), sizeof(TdiFactor) * tf.size(), cudaMemcpyHostToDevice));
   }
@@ -1809,6 +1825,7 @@ int mixed_create(PesPlan* p) {
   M.gcp = gcp;
   M.gf = gf;
   M.tdn = tdn;
+  M.pbin = pbin;
   M.yv = yv;
   M.scr = scr;
   M.cphi = cphi;

@@ -33,7 +33,7 @@ def _as_theta(fiducial_params):
         return (th[None], True) if th.dim() == 1 else (th, False)
     get = fiducial_params.get if isinstance(fiducial_params, dict) else (lambda k, d=None: getattr(fiducial_params, k, d))
     keys = fiducial_params.keys() if isinstance(fiducial_params, dict) else fiducial_params._fields
-    values = {k: np.asarray(get(k)) for k in keys}
+    values = {k: np.asarray(get(k).detach().cpu() if isinstance(get(k), torch.Tensor) else get(k)) for k in keys}
     shape = np.broadcast_shapes(*(v.shape for v in values.values()))
     if shape == ():
         return torch.as_tensor(theta_from_parameters({k: float(v) for k, v in values.items()}))[None], True

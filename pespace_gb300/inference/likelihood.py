@@ -11,12 +11,13 @@
 """
 
 import ctypes
+from collections import namedtuple
 
 import numpy as np
 import torch
 
 from .. import _lib
-from ..waveform.phenomd import theta_from_parameters
+from ..waveform.phenomd import IMRPhenomD, theta_from_parameters
 
 
 def _rows(data, labels, channels):
@@ -117,6 +118,10 @@ class WhittleLikelihood:
         self.detector = detector
         self.channels = tuple(channels)
         self.precision = precision
+        # likelihood_jax.py:119-127: waveform parameters, then the response's
+        self.likelihood_param_type = namedtuple(
+            "LikelihoodParams", (*IMRPhenomD.required_params, "ecliptic_longitude", "ecliptic_latitude",
+                                 "polarization", "coalescence_time"))
         self.max_batch = int(max_batch)
         desc = _lib.PesPlanDesc()
         desc.nbins = info0.frequency_series_length
@@ -215,8 +220,15 @@ class WhittleLikelihood:
         return {"dense_bins": out[0], "fp64_bins": out[1], "sparse_nodes": out[2], "samples": out[3]}
 
     def log_likelihood(self, params):
-        """Single parameter set (dict / namedtuple with reference names); returns a float."""
-        return float(self.log_likelihood_batch(theta_from_parameters(params)).item())
+        """likelihood_jax.py:207-260 call: a ``likelihood_param_type`` namedtuple
+        (or a dict with the same names).  Scalar fields give a float; 1-D array
+        fields of a common length (what a vectorised sampler passes) give a
+        (B,) CUDA tensor evaluated in one batched call."""
+        from .fisher import _as_theta
+
+        theta, single = _as_theta(params)
+        out = self.log_likelihood_batch(theta)
+        return float(out[0].item()) if single else out
 
     def model_tdi(self, theta, det=0, orthogonal=True):
         """Dense A/E/T model of one detector (parity / debugging)."""

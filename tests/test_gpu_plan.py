@@ -25,7 +25,7 @@ def tianqin(oracle, gen="1.5"):
             dict(oms_level=1e-24, acc_level=1e-30, arm_length_sec=np.sqrt(3) * 1e8 / oracle.C_SI, tianqin=True))
 
 
-def cuda_detectors(g, dets):
+def cuda_detectors(g, dets, grid=None):
     from pespace_gb300.detector.antenna import FDResponseModelMarset2018, InterferometerAntenna
     from pespace_gb300.detector.orbit import KaplerianHeliocentric, KeplerianGeocentric
     from pespace_gb300.detector.tdi import FDMichelsonConstantEqualArm, TDIChannelData
@@ -33,7 +33,8 @@ def cuda_detectors(g, dets):
     out = []
     for name, orb_desc, gen, data, psd in dets:
         td = TDIChannelData()
-        td.set_fd_data_from_zero(("A", "E", "T"), DUR, DT, 0.0, FMIN, FMAX)
+        dur, dt, fmin, fmax = grid if grid is not None else (DUR, DT, FMIN, FMAX)
+        td.set_fd_data_from_zero(("A", "E", "T"), dur, dt, 0.0, fmin, fmax)
         td.fd_data.copy_(torch.as_tensor(data, device="cuda"))
         td.fd_noise_power_density = torch.as_tensor(psd, device="cuda")
         if orb_desc.kind == 0:
@@ -184,3 +185,26 @@ def test_gradient_central_differences(cuda_lib, oracle, dataset):
         fd = (v[0::2] - v[1::2]) / (2 * steps)
         norm = np.linalg.norm(grad[b])
         assert np.max(np.abs(fd - grad[b])) / norm < 1e-4, (b, fd, grad[b])
+
+
+def test_reference_parameter_tuple_calls(cuda_lib, oracle, dataset):
+    """likelihood_param_type / log_likelihood(namedtuple) as a JAX-style sampler
+    calls them: scalar fields give a float, array fields a batched tensor."""
+    from pespace_gb300.inference import WhittleLikelihood
+
+    g, dets, th0 = dataset
+    eng = WhittleLikelihood(cuda_detectors(g, dets[:1]), precision="fp64", reference_frequency=1e-4, max_batch=8)
+    rng = np.random.default_rng(29)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(3)])
+    eta = thetas[:, 1] / (1 + thetas[:, 1]) ** 2
+    P = eng.likelihood_param_type
+    assert P._fields[-4:] == ("ecliptic_longitude", "ecliptic_latitude", "polarization", "coalescence_time")
+    batch = P(chirp_mass=np.exp(thetas[:, 0]), symmetric_mass_ratio=eta, chi_1=thetas[:, 2], chi_2=thetas[:, 3],
+              luminosity_distance=np.exp(thetas[:, 4]), reference_phase=thetas[:, 9],
+              inclination=np.arccos(thetas[:, 5]), ecliptic_longitude=thetas[:, 6],
+              ecliptic_latitude=np.arcsin(thetas[:, 7]), polarization=thetas[:, 8], coalescence_time=thetas[:, 10])
+    want = eng.log_likelihood_batch(thetas).cpu().numpy()
+    got = eng.log_likelihood(batch).cpu().numpy()
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-9)
+    one = eng.log_likelihood(P(*[np.asarray(f)[0] for f in batch]))
+    assert isinstance(one, float) and abs(one - want[0]) <= 1e-9 + 1e-12 * abs(want[0])
