@@ -321,7 +321,7 @@ def run_native(args):
         from pespace_gb300 import census
 
         dom = "dense_mixed" if args.precision == "mixed" else "dense_fp64"
-        roofline = census.roofline(dom, kern[dom], work, True, gemm_peak_tflops(torch, torch.float32))
+        roofline = census.roofline(dom, kern[dom], args.steps, work, True, gemm_peak_tflops(torch, torch.float32))
         roofline["fp64_peak_tflops"] = gemm_peak_tflops(torch, torch.float64)
 
     if rank == 0:

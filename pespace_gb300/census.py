@@ -31,25 +31,30 @@ FP32_FLOPS_PER_DENSE_BIN = {"lnl": 244, "grad": 341}
 DRAM_BYTES_PER_DENSE_BIN = 4.97  # (93.04 MB + 4.34 MB) / 19 595 338 bins, ncu --set full, 256 samples
 
 
-def roofline(kernel_class, launches_ms, work, grad, fp32_peak_tflops):
+def roofline(kernel_class, launches_ms, steps, work, grad, fp32_peak_tflops):
     """Roofline entry for the dominant kernel.
 
     kernel_class: profiler class name; launches_ms: (launches, summed device ms)
-    over the timed steps; work: WhittleLikelihood.last_work() of one step;
-    grad: whether the step ran the gradient pass.
+    over the timed steps; steps: timed steps; work: WhittleLikelihood.last_work()
+    of one step; grad: whether the step ran the gradient pass.  A step may run
+    the kernel more than once (a large batch runs as two halves), so the
+    achieved rate is the step's work over the step's summed kernel time, and
+    the work and traffic are given per launch.
     """
     launches, ms = launches_ms
     per_launch_ms = ms / max(1, launches)
+    per_step_ms = ms / max(1, steps)
+    per_step_launches = launches / max(1, steps)
     entry = {"kernel": kernel_class, "launches": launches, "avg_launch_ms": per_launch_ms,
              "bound": None, "unit": "TFLOP/s", "peak": None, "peak_source": None, "achieved": None,
              "frac": None, "traffic": None, "units_per_launch": None}
     if kernel_class == "dense_mixed":
-        bins = work["dense_bins"]
+        bins = work["dense_bins"] / per_step_launches
         flops = bins * FP32_FLOPS_PER_DENSE_BIN["grad" if grad else "lnl"]
         entry.update(bound="fp32", peak=fp32_peak_tflops,
                      peak_source="measured cuBLAS SGEMM 8192^3 (TF32 off) in bench.py",
                      units_per_launch={"dense_bins": bins, "fp32_flops": flops})
-        entry["achieved"] = flops / (per_launch_ms / 1e3) / 1e12
+        entry["achieved"] = flops * per_step_launches / (per_step_ms / 1e3) / 1e12
         if fp32_peak_tflops:
             entry["frac"] = entry["achieved"] / fp32_peak_tflops
         if DRAM_BYTES_PER_DENSE_BIN is not None:
