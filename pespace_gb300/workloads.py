@@ -62,3 +62,32 @@ def lisa_dataset(duration, delta_time, fmin, fmax, theta_inj, generation="1.5", 
     th = np.asarray(theta_inj, dtype=np.float64)
     det.inject_signal(wf.from_theta(th), th[6], math.asin(th[7]), th[8], th[10])
     return det
+
+
+def network_dataset(duration, delta_time, fmin, fmax, theta_inj, generation="1.5", seed=2026, f_ref=1e-4):
+    """Three-detector network of the higher-mode benchmark configuration, with
+    the (2,2)-mode IMRPhenomD injection: LISA-like (2.5e9 m, trailing 20 deg),
+    Taiji-like (3e9 m, leading 20 deg; OMS 8e-12, acceleration 3e-15) and
+    TianQin-like geocentric (sqrt(3) 1e8 m; OMS 1e-12, acceleration 1e-15);
+    seeded noise per detector (seed, seed + 1, seed + 2)."""
+    from .detector.antenna import FDResponseModelMarset2018, InterferometerAntenna
+    from .detector.orbit import KaplerianHeliocentric, KeplerianGeocentric
+    from .detector.tdi import FDMichelsonConstantEqualArm, TDIChannelData
+    from .waveform import IMRPhenomD
+
+    specs = [("LISA", KaplerianHeliocentric(2.5e9, 0.0, -PI / 9), "LISA_SciRDv1"),
+             ("Taiji", KaplerianHeliocentric(3.0e9, 0.0, PI / 9), "Taiji_TDC"),
+             ("TianQin", KeplerianGeocentric(math.sqrt(3.0) * 1e8), "Tianqin_GWSpace")]
+    th = np.asarray(theta_inj, dtype=np.float64)
+    dets = []
+    for k, (name, orbit, noise) in enumerate(specs):
+        td = TDIChannelData()
+        td.set_fd_data_from_zero(("A", "E", "T"), duration, delta_time, 0.0, fmin, fmax)
+        td.set_fd_noise_power_density_from_model(noise, tdi_generation=generation)
+        det = InterferometerAntenna(name, td, orbit, FDResponseModelMarset2018(),
+                                    FDMichelsonConstantEqualArm(generation, True))
+        td.add_into_fd_data(td.get_fd_noise_realization(seed=seed + k))
+        wf = IMRPhenomD(td.data_info.frequency_samples_array, f_ref)
+        det.inject_signal(wf.from_theta(th), th[6], math.asin(th[7]), th[8], th[10])
+        dets.append(det)
+    return tuple(dets)
