@@ -167,3 +167,39 @@ def test_mixed_tdi2_prefactor_zero(cuda_lib, oracle):
     err = np.abs(got - want)
     assert np.median(err) <= 1e-2, np.sort(err)[-5:]
     assert np.all(err <= 1e-2 + 2e-8 * np.abs(want)), np.sort(err)[-5:]
+
+
+def test_mixed_edge_cases_and_status(cuda_lib, oracle, dataset):
+    """Out-of-domain and NaN samples in a mixed batch: status 2 and lnL = -inf,
+    zero gradient rows, the valid neighbours unaffected; an empty batch; a batch
+    beyond max_batch through the C ABI is rejected; channel subsets."""
+    from pespace_gb300 import _lib
+    from pespace_gb300.inference import WhittleLikelihood
+
+    g, dets, th0 = dataset
+    eng = WhittleLikelihood(cuda_detectors(g, dets[:1]), precision="mixed", reference_frequency=1e-4, max_batch=4)
+    bad = np.stack([th0, th0, th0, th0])
+    bad[1, 1] = 0.5      # q < 1
+    bad[2, 3] = -1.0     # |chi2| = 1
+    bad[3, 10] = np.nan  # NaN t_c
+    lnl, grad = eng.log_likelihood_and_grad(bad)
+    lnl, grad, st = lnl.cpu().numpy(), grad.cpu().numpy(), eng.last_status.cpu().numpy()
+    assert st[0] == 0 and np.isfinite(lnl[0]) and np.all(np.isfinite(grad[0]))
+    assert list(st[1:]) == [2, 2, 2] and np.all(np.isneginf(lnl[1:])) and np.all(grad[1:] == 0)
+    alone = eng.log_likelihood_batch(th0[None]).cpu().numpy()
+    assert lnl[0] == alone[0]
+    assert eng.log_likelihood_batch(np.zeros((0, 11))).numel() == 0
+    lib = _lib.load()
+    th = torch.as_tensor(np.stack([th0] * 5), device="cuda")
+    out = torch.empty(5, dtype=torch.float64, device="cuda")
+    assert lib.pes_lnl_batch(eng._plan, _lib.ptr(th), 5, _lib.ptr(out), None, None) == _lib.PES_EINVAL
+    # channel subsets against the oracle
+    rng = np.random.default_rng(41)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(3)])
+    for chans in (("A", "E"), ("T",)):
+        sub = WhittleLikelihood(cuda_detectors(g, dets[:1]), channels=chans, precision="mixed",
+                                reference_frequency=1e-4, max_batch=4)
+        got = sub.log_likelihood_batch(thetas).cpu().numpy()
+        plan = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets[:1]], 1e-4, channels=chans)
+        want = plan.lnl(thetas)
+        assert np.all(np.abs(got - want) <= 1e-2 + 1e-8 * np.abs(want)), (chans, got - want)
