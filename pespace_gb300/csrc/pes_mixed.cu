@@ -75,9 +75,10 @@ struct MixedDev {
   float2* dd;               // [n_det][nbins] sum_c |d|^2 / S in FP64, as a float-float pair (hi, lo)
   int32_t* nsp;             // [B] spline intervals of the sample (nodes 0..nsp)
   int32_t* nch;             // [B] runs with a live bin
-  int32_t* xbin;            // [B] bins [0, xbin) are evaluated exactly (not splined)
+  int32_t* xbin;            // [B] max over detectors of xbind
+  int32_t* xbind;           // [B][n_det] bins [0, xbind) of a detector are evaluated exactly (not splined)
   const int32_t* iv_first;  // [J + 1] first bin of each interval (nbins past the last)
-  double omega;             // largest yearly orbital angular frequency of the detectors
+  double omega[PES_MAX_DETECTORS];  // fastest orbital angular frequency of each detector
   int32_t xblocks;          // blocks per sample of the exact-bin kernel
   double* xpart;            // [B][xblocks] exact-bin lnL partials
   double* xgpart;           // [B][xblocks][11] exact-bin gradient partials
@@ -420,21 +421,28 @@ __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict
       M.nch[s] = nc;
       return;
     }
-    auto unresolved = [&](int j) {
-      double a, ps, t0, t1;
-      phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j], a, ps, t0);
-      phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j + 1], a, ps, t1);
-      return M.omega * fabs(t1 - t0) > kOrbitPhaseMax;
-    };
-    if (unresolved(0)) {
-      int lo2 = 0, hi2 = ns - 1;  // last unresolved interval
-      while (lo2 < hi2) {
-        int mid = (lo2 + hi2 + 1) >> 1;
-        if (unresolved(mid)) lo2 = mid; else hi2 = mid - 1;
+    for (int d = 0; d < M.n_det; ++d) {
+      auto unresolved = [&](int j) {
+        double a, ps, t0, t1;
+        phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j], a, ps, t0);
+        phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j + 1], a, ps, t1);
+        return M.omega[d] * fabs(t1 - t0) > kOrbitPhaseMax;
+      };
+      int xbd = 0;
+      if (unresolved(0)) {
+        int lo2 = 0, hi2 = ns - 1;  // last unresolved interval
+        while (lo2 < hi2) {
+          int mid = (lo2 + hi2 + 1) >> 1;
+          if (unresolved(mid)) lo2 = mid; else hi2 = mid - 1;
+        }
+        const int64_t first = M.iv_first[lo2 + 1];
+        xbd = (int)(first < b.kcut ? first : b.kcut);
       }
-      const int64_t first = M.iv_first[lo2 + 1];
-      xb = (int)(first < b.kcut ? first : b.kcut);
+      M.xbind[s * M.n_det + d] = xbd;
+      xb = xbd > xb ? xbd : xb;
     }
+  } else if (kPart == 1) {
+    for (int d = 0; d < M.n_det; ++d) M.xbind[s * M.n_det + d] = 0;
   }
   if (kPart == 0) {
     M.nsp[s] = ns;
@@ -668,7 +676,7 @@ __device__ __forceinline__ void spline_adjoint_transfer(const MixedDev& M, int64
   for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
 }
 
-// Fit for grids of more than 32 x 32 intervals (segments in global scratch):
+// Fit for grids of more than 64 x 32 intervals (segments in global scratch):
 // warp per (sample, detector, quantity); lane l owns intervals and rows
 // [l*seg, (l+1)*seg) of the sample's n intervals.  Rows 1..n-2 use the shared
 // grid's precomputed Thomas factors, row n-1 the sample's not-a-knot end row.
@@ -851,11 +859,15 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint_wide(MixedDev
   }
 }
 
-// Register-segment versions (n <= 32 x 32 intervals, the default grid): each
+// Register-segment versions (n <= 64 x 32 intervals; segments of 32 rows for
+// the default grid of 1024 nodes, of 64 rows up to 2049 nodes): each
 // lane keeps its segment's rows in registers (fully unrolled, predicated
 // loops), so the recurrences wait on arithmetic only.  Phase (q == 0) in FP64,
 // transfer quantities in FP32 with FP64 slopes and right-hand sides.
-constexpr int kSegMax = 32;
+constexpr int kSegMax = 64;  // longest register segment (grids of up to 64 x 32 intervals)
+
+// Register segment length for a grid of J nodes (0: use the global-scratch kernels).
+inline int spline_seg(int J) { return J <= 32 * 32 + 1 ? 32 : (J <= kSegMax * 32 + 1 ? kSegMax : 0); }
 
 template <class R>
 __device__ __forceinline__ const R* spline_factor(const MixedDev& M, int which) {
@@ -873,7 +885,7 @@ __device__ __forceinline__ const R* spline_factor(const MixedDev& M, int which) 
   }
 }
 
-template <class R>
+template <int kSeg, class R>
 __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, int q, int n, R* smem4) {
   const int lane = threadIdx.x & 31;
   const double* __restrict__ y = M.yv + (size_t)sd * M.J * kNodeQ + q;
@@ -888,13 +900,13 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
   const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
   // right-hand sides 6 (slope_i - slope_{i-1}) of rows i0 + k, in FP64
-  R x[kSegMax];
+  R x[kSeg];
   {
     double yp = (i0 >= 1) ? y[(i0 - 1) * kNodeQ] : 0.0;
     double yc = y[i0 * kNodeQ];
     double sp = (i0 >= 1) ? (yc - yp) * M.ginvh[i0 - 1] : 0.0;
 #pragma unroll
-    for (int k = 0; k < kSegMax; ++k) {
+    for (int k = 0; k < kSeg; ++k) {
       x[k] = R(0);
       if (k < cnt) {
         const int i = i0 + k;
@@ -909,7 +921,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   // forward elimination (rows 1..n-1)
   R A = R(1), v = R(0);
 #pragma unroll
-  for (int k = 0; k < kSegMax; ++k) {
+  for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const bool last = i == n - 1;
@@ -920,7 +932,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   }
   v = segment_carry_in<R>(A, v, false);
 #pragma unroll
-  for (int k = 0; k < kSegMax; ++k) {
+  for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const bool last = i == n - 1;
@@ -933,7 +945,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   A = R(1);
   v = R(0);
 #pragma unroll
-  for (int k = kSegMax - 1; k >= 0; --k) {
+  for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const R c = (i == n - 1) ? R(0) : fcp[i];
@@ -943,7 +955,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   }
   v = segment_carry_in<R>(A, v, true);
 #pragma unroll
-  for (int k = kSegMax - 1; k >= 0; --k) {
+  for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const R c = (i == n - 1) ? R(0) : fcp[i];
@@ -953,7 +965,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   }
   // m_1, m_2, m_{n-2}, m_{n-1} for the eliminated end values
 #pragma unroll
-  for (int k = 0; k < kSegMax; ++k) {
+  for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt) {
       if (i == 1) smem4[0] = x[k];
@@ -969,13 +981,13 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   const R next_first = __shfl_down_sync(0xffffffffu, x[0], 1);  // m at row i0 + cnt (when it is a row)
   double yc = y[i0 * kNodeQ];
 #pragma unroll
-  for (int k = 0; k < kSegMax; ++k) {
+  for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt) {
       const R mi = (i == 0) ? m0 : x[k];
       R mj;
       if (i + 1 == n) mj = mn;
-      else if (k + 1 < cnt) mj = x[(k + 1) < kSegMax ? k + 1 : k];
+      else if (k + 1 < cnt) mj = x[(k + 1) < kSeg ? k + 1 : k];
       else mj = next_first;
       const double yn = y[(i + 1) * kNodeQ];
       const R sl = (R)((yn - yc) * M.ginvh[i]);
@@ -999,6 +1011,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
 }
 
 // One warp per block: blockIdx.x = (sample * n_det + detector) * 7 + quantity.
+template <int kSeg>
 __global__ void __launch_bounds__(32) k_spline_fit(MixedDev M) {
   __shared__ double sm4[4];
   const int q = (int)(blockIdx.x % kNodeQ);
@@ -1006,12 +1019,12 @@ __global__ void __launch_bounds__(32) k_spline_fit(MixedDev M) {
   const int n = M.nsp[sd / M.n_det];
   if (n < 3) return;
   if (q == 0)
-    spline_fit_regs<double>(M, sd, q, n, sm4);
+    spline_fit_regs<kSeg, double>(M, sd, q, n, sm4);
   else
-    spline_fit_regs<float>(M, sd, q, n, reinterpret_cast<float*>(sm4));
+    spline_fit_regs<kSeg, float>(M, sd, q, n, reinterpret_cast<float*>(sm4));
 }
 
-template <class R>
+template <int kSeg, class R>
 __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t sd, int q, int n, double wscale) {
   const int lane = threadIdx.x & 31;
   const float* __restrict__ mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
@@ -1035,11 +1048,11 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
   const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
   // right-hand sides (coefficient adjoints -> mbar, end eliminations), in FP64
-  R x[kSegMax];
+  R x[kSeg];
   {
     R right_prev = (i0 >= 1) ? mbar_right(i0 - 1) : R(0);
 #pragma unroll
-    for (int k = 0; k < kSegMax; ++k) {
+    for (int k = 0; k < kSeg; ++k) {
       x[k] = R(0);
       const int i = i0 + k;
       if (k < cnt) {
@@ -1059,7 +1072,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   // U^T z = mbar
   R A = R(1), v = R(0);
 #pragma unroll
-  for (int k = 0; k < kSegMax; ++k) {
+  for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const R sub = (i > 1) ? fup[i - 1] : R(0), id = (i == n - 1) ? iden_l : fid[i];
@@ -1069,7 +1082,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   }
   v = segment_carry_in<R>(A, v, false);
 #pragma unroll
-  for (int k = 0; k < kSegMax; ++k) {
+  for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const R sub = (i > 1) ? fup[i - 1] : R(0), id = (i == n - 1) ? iden_l : fid[i];
@@ -1081,7 +1094,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   A = R(1);
   v = R(0);
 #pragma unroll
-  for (int k = kSegMax - 1; k >= 0; --k) {
+  for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
@@ -1092,7 +1105,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   v = segment_carry_in<R>(A, v, true);
   R last = R(0);  // rbar of the segment's last row
 #pragma unroll
-  for (int k = kSegMax - 1; k >= 0; --k) {
+  for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
@@ -1113,13 +1126,13 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
       dprev = (mm(i0 - 1, 1) + R(6) * (r_prev - x[0])) * fih[i0 - 1];
     }
 #pragma unroll
-    for (int k = 0; k < kSegMax; ++k) {
+    for (int k = 0; k < kSeg; ++k) {
       const int i = i0 + k;
       if (k < cnt) {
         const R rc = (i >= 1) ? x[k] : R(0);
         R rn;
         if (i + 1 >= n) rn = R(0);
-        else if (k + 1 < cnt) rn = x[(k + 1) < kSegMax ? k + 1 : k];
+        else if (k + 1 < cnt) rn = x[(k + 1) < kSeg ? k + 1 : k];
         else rn = next_first;
         const R Db = mm(i, 1) + R(6) * (rc - rn);
         yb[i * kNodeQ] = (double)(dprev + mm(i, 0) - Db * fih[i]);
@@ -1138,6 +1151,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   }
 }
 
+template <int kSeg>
 __global__ void __launch_bounds__(32) k_spline_adjoint(MixedDev M, double wscale) {
   const int q = (int)(blockIdx.x % kNodeQ), lane = threadIdx.x & 31;
   const int64_t sd = blockIdx.x / kNodeQ;
@@ -1149,13 +1163,13 @@ __global__ void __launch_bounds__(32) k_spline_adjoint(MixedDev M, double wscale
     return;
   }
   if (q == 0)
-    spline_adjoint_regs<double>(M, sd, q, n, wscale);
+    spline_adjoint_regs<kSeg, double>(M, sd, q, n, wscale);
   else
-    spline_adjoint_regs<float>(M, sd, q, n, wscale);
+    spline_adjoint_regs<kSeg, float>(M, sd, q, n, wscale);
 }
 
 // ------------------------------------------------------------------ exact bins
-// Bins [0, xbin[s]) evaluated directly (FP64 model and residual against the
+// Bins [0, xbind[s][d]) of each detector evaluated directly (FP64 model and residual against the
 // FP64 data).  kMode 0: lnL partials (T = double); 1: gradient partials
 // (T = GradScalar, FP64 values with FP32 tangents); 2: write the model.
 // grid (xblocks, B); threads stride over the sample's exact bins.
@@ -1176,9 +1190,10 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   for (int k = 0; k < NV; ++k) acc[k] = 0.0;
   const double inv_scale = 1.0 / M.scale;
   if (sb.status == kSampleOk) {
-    for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xb; i += gridDim.x * kExactThreads) {
-      const double f = (double)(P.k0 + i) * P.f_step;
-      for (int d = 0; d < M.n_det; ++d) {
+    for (int d = 0; d < M.n_det; ++d) {
+      const int xbd = M.xbind[(size_t)s * M.n_det + d];
+      for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xbd; i += gridDim.x * kExactThreads) {
+        const double f = (double)(P.k0 + i) * P.f_step;
         T y[kNodeQ];
         node_eval<T>(P, M, sb, d, P.tdi[(size_t)d * P.nbins + i], f, y);
         const T ph = y[0] + (2.0 * kPi * f) * sb.tc;
@@ -1313,7 +1328,7 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   const int c = blockIdx.x * 128 + threadIdx.x;
   if (blocks[s].status != kSampleOk || c >= M.nch[s]) return;
   const int kb = M.ch_begin[c];
-  if (kb < M.xbin[s]) return;
+  if (kb < M.xbind[(size_t)s * M.n_det + d]) return;
   const size_t sd = (size_t)s * M.n_det + d;
   const double tc = blocks[s].tc;
   const int j = M.ch_iv[c];
@@ -1376,7 +1391,6 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int g = blockIdx.x * (kMixThreads / 32) + wid;  // run group
   const int nc = M.nch[s];
-  const int xb = M.xbin[s];
   const int64_t kcut = blocks[s].kcut;
   const int first = g * kChunkMax;
   float acc = 0.0f, comp = 0.0f;
@@ -1384,6 +1398,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   if (blocks[s].status == kSampleOk && first < nc) {
     for (int d = 0; d < M.n_det; ++d) {
       const size_t sd = (size_t)s * M.n_det + d;
+      const int xb = M.xbind[sd];
       // ---- amplitude kink at f_peak (float-float coefficients, read past the peak only)
       const float* KF = M.kinkF + sd * 16;
       const float kSlope = KF[0];
@@ -1694,12 +1709,12 @@ int mixed_create(PesPlan* p) {
   }
   // fastest orbital angular frequency: the yearly revolution, or a geocentric
   // constellation's rotation about the Earth (TianQin: 3.65 days)
-  M.omega = 0.0;
   M.xblocks = kExactBlocks;
+  for (int k = 0; k < PES_MAX_DETECTORS; ++k) M.omega[k] = 0.0;
   for (int k = 0; k < nd; ++k) {
-    M.omega = std::max(M.omega, std::fabs(d.det[k].orbit.omega_revolution));
+    M.omega[k] = std::fabs(d.det[k].orbit.omega_revolution);
     if (d.det[k].orbit.kind == 1) {
-      M.omega = std::max(M.omega, std::fabs(d.det[k].orbit.omega_rotation));
+      M.omega[k] = std::max(M.omega[k], std::fabs(d.det[k].orbit.omega_rotation));
       M.xblocks = kExactBlocksGeo;
     }
   }
@@ -1713,7 +1728,7 @@ int mixed_create(PesPlan* p) {
   float* gf;
   TdiFactor* tdn;
   float2* pbin;
-  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *ivfirst;
+  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
   SampleBlock<NodeGradA>* gblkA;
@@ -1741,12 +1756,13 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &gblkA, (size_t)B)) || (rc = alloc(mb, &gblkB, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
-      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) ||
+      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) || (rc = alloc(mb, &xbind, (size_t)B * nd)) ||
       (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * M.xblocks)) ||
       (rc = alloc(mb, &xgpart, (size_t)B * M.xblocks * 11)))
     return rc;
   PES_CHECK_CUDA(cudaMemcpy(ivfirst, ivf.data(), sizeof(int32_t) * (J + 1), cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemset(xbin, 0, sizeof(int32_t) * B));
+  PES_CHECK_CUDA(cudaMemset(xbind, 0, sizeof(int32_t) * B * nd));
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
   {
     std::vector<TdiFactor> tf((size_t)nd * J);
@@ -1814,6 +1830,7 @@ int mixed_create(PesPlan* p) {
   M.nsp = nsp;
   M.nch = nch;
   M.xbin = xbin;
+  M.xbind = xbind;
   M.iv_first = ivfirst;
   M.xpart = xpart;
   M.xgpart = xgpart;
@@ -1885,8 +1902,10 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_LAUNCH();
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
-  if (M.J <= kSegMax * 32 + 1)
-    k_spline_fit<<<M.n_det * kNodeQ, 32, 0, st>>>(M);
+  if (spline_seg(M.J) == 32)
+    k_spline_fit<32><<<M.n_det * kNodeQ, 32, 0, st>>>(M);
+  else if (spline_seg(M.J) == kSegMax)
+    k_spline_fit<kSegMax><<<M.n_det * kNodeQ, 32, 0, st>>>(M);
   else
     k_spline_fit_wide<<<M.n_det, kSplineThreads, 0, st>>>(M);
   PES_CHECK_LAUNCH();
@@ -1905,15 +1924,17 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
 int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const std::vector<int32_t>& ok,
                int64_t* out, cudaStream_t st) {
   const MixedDev& M = p->mixed->dev;
-  std::vector<int32_t> xb(B), ns(B);
+  std::vector<int32_t> xb((size_t)B * M.n_det), ns(B);
   if (B > 0) {
-    PES_CHECK_CUDA(cudaMemcpy(xb.data(), M.xbin, sizeof(int32_t) * B, cudaMemcpyDeviceToHost));
+    PES_CHECK_CUDA(cudaMemcpy(xb.data(), M.xbind, sizeof(int32_t) * B * M.n_det, cudaMemcpyDeviceToHost));
     PES_CHECK_CUDA(cudaMemcpy(ns.data(), M.nsp, sizeof(int32_t) * B, cudaMemcpyDeviceToHost));
   }
   for (int64_t s = 0; s < B; ++s) {
     if (!ok[s]) continue;
-    out[0] += (kcut[s] - xb[s]) * (int64_t)M.n_det;
-    out[1] += (int64_t)xb[s] * M.n_det;
+    for (int d = 0; d < M.n_det; ++d) {
+      out[0] += kcut[s] - xb[(size_t)s * M.n_det + d];
+      out[1] += xb[(size_t)s * M.n_det + d];
+    }
     if (ns[s] >= 3) out[2] += (int64_t)(ns[s] + 1) * M.n_det;
   }
   (void)st;
@@ -1980,8 +2001,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKSpline, st);
-    if (M.J <= kSegMax * 32 + 1)
-      k_spline_fit<<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M);
+    if (spline_seg(M.J) == 32)
+      k_spline_fit<32><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M);
+    else if (spline_seg(M.J) == kSegMax)
+      k_spline_fit<kSegMax><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M);
     else
       k_spline_fit_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
   }
@@ -2015,8 +2038,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (!grad) return PES_OK;
   {
     ProfScope ps(p, kKAdjoint, st);
-    if (M.J <= kSegMax * 32 + 1)
-      k_spline_adjoint<<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
+    if (spline_seg(M.J) == 32)
+      k_spline_adjoint<32><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
+    else if (spline_seg(M.J) == kSegMax)
+      k_spline_adjoint<kSegMax><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
     else
       k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
   }

@@ -105,10 +105,11 @@ def test_mixed_gradient(cuda_lib, oracle, dataset):
     assert np.max(np.abs(gg - w_grad) / norm) < 1e-3, (gg, w_grad)
 
 
-@pytest.mark.parametrize("n_sparse", [600, 2048])
+@pytest.mark.parametrize("n_sparse", [600, 2048, 3000])
 def test_mixed_other_grids(cuda_lib, oracle, dataset, n_sparse):
-    """Non-default sparse grids: 600 nodes (register segments of 19 rows) and
-    2048 nodes (the global-scratch spline kernels)."""
+    """Non-default sparse grids: 600 nodes (register segments of 19 rows),
+    2048 nodes (register segments of 64 rows) and 3000 nodes (the
+    global-scratch spline kernels)."""
     g, dets, th0 = dataset
     rng = np.random.default_rng(3)
     thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(3)])
