@@ -24,6 +24,7 @@
 //     gradient) and the dense stage skips them.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <vector>
 
 #include "pes_plan.cuh"
@@ -64,6 +65,12 @@ struct MixedDev {
   double scale;             // FP32 storage scale of data and model
   const double* node_f;     // [J]
   const TdiFactor* tdn;     // [n_det][J] TDI delay factor at the nodes (prefactor set to 1)
+  // float-float copies for the node evaluations on the FP32 pipes
+  OrbitFF orbit_ff[PES_MAX_DETECTORS];
+  FF scale_ff;
+  FF fstep_ff;              // bin spacing
+  const float2* node_ff;    // [J] node frequencies (hi, lo)
+  const float4* tdn_ff;     // [n_det][J] node delay factor D (re hi, re lo, im hi, im lo)
   float2* pbin;             // [n_det][nbins] TDI generation prefactor P(f) per bin (FP32 of the FP64 value)
   const int32_t* ch_begin;  // [nchunks] first bin of the run
   const int32_t* ch_len;    // [nchunks]
@@ -155,6 +162,49 @@ __device__ __forceinline__ void node_eval(const PlanDev& P, const MixedDev& M, c
   }
 }
 
+// node_eval in float-float arithmetic: the same node quantities from the FF
+// copies of the sample block, orbit and TDI factors.  kPre applies the TDI
+// generation prefactor Pf (exact bins); nodes take it as 1.
+template <bool kPre>
+__device__ __forceinline__ void node_eval_ff(const MixedDev& M, const SampleBlock<FF>& b, int d, const Cx<FF>& D,
+                                             const Cx<FF>& Pf, const FF& f, FF y[kNodeQ]) {
+  const FF Mf = b.wf.Msec * f;
+  FF amp, psi, tf;
+  phenomd_eval<FF>(b.wf, Mf, amp, psi, tf);
+  amp = amp * M.scale_ff;
+  const FF zero = ff_make(0.0f, 0.0f);
+  Cx<FF> hp = cx(b.wf.pfac * amp, zero);
+  Cx<FF> hc = cx(zero, -(b.wf.cfac * amp));
+  Cx<FF> L[6], C[3];
+  FF kx0;
+  single_links_impl<true, FF>(M.orbit_ff[d], f, hp, hc, tf + b.tc, b.pol, L, &kx0);
+  tdi_channels_t<kPre, FF>(D, Pf, 1, L, C);
+  y[0] = psi + (2.0 * kPi * f) * kx0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    y[1 + 2 * c] = C[c].re;
+    y[2 + 2 * c] = C[c].im;
+  }
+}
+
+// FF copy of a sample block (wf, pol, tc converted; cut and status copied),
+// written cooperatively by the block's threads.  The two layouts coincide:
+// sizeof(FF) == sizeof(double).
+__device__ __forceinline__ void narrow_block_ff(const SampleBlock<double>& a, SampleBlock<FF>& b) {
+  static_assert(sizeof(SampleBlock<FF>) == sizeof(SampleBlock<double>), "FF block layout");
+  static_assert(offsetof(SampleBlock<FF>, fcut) == offsetof(SampleBlock<double>, fcut), "FF block layout");
+  constexpr int nv = (int)(offsetof(SampleBlock<double>, fcut) / sizeof(double));  // wf, pol, tc
+  const double* src = reinterpret_cast<const double*>(&a);
+  FF* dst = reinterpret_cast<FF*>(&b);
+  for (int j = threadIdx.x; j < nv; j += blockDim.x) dst[j] = ff_from(src[j]);
+  if (threadIdx.x == 0) {
+    b.fcut = a.fcut;
+    b.kcut = a.kcut;
+    b.status = a.status;
+    b.pad = 0;
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void load_block(const SampleBlock<T>* blocks, int s, SampleBlock<T>& sb) {
   const int n8 = sizeof(SampleBlock<T>) / 8;
@@ -201,19 +251,30 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
   }
 }
 
-// Forward: node values in FP64.  grid (ceil(J/128), n_det, B)
+// Forward: node values in float-float arithmetic, stored as FP64.  grid (ceil(J/128), n_det, B)
 __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedDev M, GenArg G,
                                                                const SampleBlock<double>* __restrict__ blocks) {
   __shared__ SampleBlock<double> sb;
+  __shared__ SampleBlock<FF> sbf;
   const int s = blockIdx.z, d = blockIdx.y;
   load_block(blocks, s, sb);
+  __syncthreads();
+  narrow_block_ff(sb, sbf);
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
   if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J) return;
   double y[kNodeQ];
+  {
+    const float2 fn = M.node_ff[j];
+    const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
+    const Cx<FF> D = cx(ff_make(t4.x, t4.y), ff_make(t4.z, t4.w));
+    FF yf[kNodeQ];
+    node_eval_ff<false>(M, sbf, d, D, D, ff_make(fn.x, fn.y), yf);
+#pragma unroll
+    for (int q = 0; q < kNodeQ; ++q) y[q] = ff_to(yf[q]);
+  }
   const double fj = M.node_f[j];
-  node_eval<double>(P, M, sb, d, M.tdn[(size_t)d * M.J + j], fj, y);
   const double xk = sb.wf.Msec * fj - sb.wf.fpeak;
   if (xk > 0.0) {
     const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
@@ -1178,13 +1239,19 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
                                                          const SampleBlock<T>* __restrict__ blocks,
                                                          double2* __restrict__ model) {
   constexpr int NV = kMode == 1 ? 11 : 1;
+  constexpr bool kFF = kMode != 1;  // value passes evaluate the bins in float-float arithmetic
   __shared__ SampleBlock<T> sb;
+  __shared__ SampleBlock<FF> sbf;
   __shared__ double red[kExactThreads / 32][NV];
   const int s = blockIdx.y;
   const int xb = M.xbin[s];
   if (xb == 0) return;  // uniform per block; the finalizers skip such samples
   load_block(blocks, s, sb);
   __syncthreads();
+  if constexpr (kFF) {
+    narrow_block_ff(sb, sbf);
+    __syncthreads();
+  }
   double acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) acc[k] = 0.0;
@@ -1193,6 +1260,32 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
     for (int d = 0; d < M.n_det; ++d) {
       const int xbd = M.xbind[(size_t)s * M.n_det + d];
       for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xbd; i += gridDim.x * kExactThreads) {
+        if constexpr (kFF) {
+          const FF f = ff_mulf(M.fstep_ff, (float)(P.k0 + i));  // k0 + i < 2^24: exact in FP32
+          const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
+          FF y[kNodeQ];
+          node_eval_ff<true>(M, sbf, d, cx(ff_from(tdb.dre), ff_from(tdb.dim)), cx(ff_from(tdb.pre), ff_from(tdb.pim)),
+                             f, y);
+          // phase reduced modulo 2 pi in FP64, then its sine and cosine in FF
+          const double phd = ff_to(y[0] + (2.0 * kPi * f) * sbf.tc);
+          FF sn, cs;
+          dsincos(ff_from(phd - (2.0 * kPi) * rint(phd * (1.0 / (2.0 * kPi)))), &sn, &cs);
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            const double hr = ff_to(y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn) * inv_scale;
+            const double hi = ff_to(y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn) * inv_scale;
+            const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
+            if constexpr (kMode == 2) {
+              model[off] = make_double2(hr, hi);
+            } else {
+              const double w = P.w[off];
+              const double2 dv = P.data[off];
+              const double rr = dv.x - hr, ri = dv.y - hi;
+              acc[0] += w * (rr * rr + ri * ri);
+            }
+          }
+          continue;
+        }
         const double f = (double)(P.k0 + i) * P.f_step;
         T y[kNodeQ];
         node_eval<T>(P, M, sb, d, P.tdi[(size_t)d * P.nbins + i], f, y);
@@ -1659,6 +1752,7 @@ int mixed_create(PesPlan* p) {
   const PesPlanDesc& d = p->desc;
   PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
   PES_REQUIRE(d.k0 >= 1, "mixed plan: the grid must start above 0 Hz (k0 >= 1)");
+  PES_REQUIRE(d.k0 + d.nbins < (int64_t)1 << 24, "mixed plan: bin indices k0 + i must stay below 2^24");
   PES_REQUIRE(d.nbins >= 8, "mixed plan: needs at least 8 bins");
   MixedBuffers* mb = new MixedBuffers();
   p->mixed = mb;
@@ -1680,6 +1774,8 @@ int mixed_create(PesPlan* p) {
   M.J = J;
   M.n_det = nd;
   M.scale = 3.085677581491367e16 / (1.476625038050124729627979840144936351e3 * 4.925490947641266978197229498498379006e-6);
+  M.scale_ff = ff_from(M.scale);
+  M.fstep_ff = ff_from(d.f_step);
   for (int k = 0; k < nd; ++k) mb->gen.gen20[k] = d.det[k].generation == 20;
   // shared sparse grid, bin -> interval map, runs
   const double flo = (double)d.k0 * d.f_step, fhi = (double)(d.k0 + n - 1) * d.f_step;
@@ -1727,6 +1823,8 @@ int mixed_create(PesPlan* p) {
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
   float* gf;
   TdiFactor* tdn;
+  float4* tdn_ff;
+  float2* node_ff;
   float2* pbin;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
   double *xpart, *xgpart;
@@ -1750,7 +1848,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &pbin, (size_t)nd * n)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) || (rc = alloc(mb, &pbin, (size_t)nd * n)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -1765,16 +1863,29 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaMemset(xbind, 0, sizeof(int32_t) * B * nd));
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
   {
+    std::vector<float2> nff(J);
+    for (int jj = 0; jj < J; ++jj) {
+      const FF v = ff_from(nf[jj]);
+      nff[jj] = make_float2(v.hi, v.lo);
+    }
+    PES_CHECK_CUDA(cudaMemcpy(node_ff, nff.data(), sizeof(float2) * J, cudaMemcpyHostToDevice));
+  }
+  {
     std::vector<TdiFactor> tf((size_t)nd * J);
+    std::vector<float4> tff((size_t)nd * J);
     for (int k = 0; k < nd; ++k)
       for (int jj = 0; jj < J; ++jj) {
         Cx<double> D, Pf;
         tdi_factors(nf[jj], d.det[k].orbit.arm_sec, d.det[k].generation == 20, D, Pf);
         (void)Pf;  // the generation prefactor P(f) is applied per bin, outside the splines
         tf[(size_t)k * J + jj] = TdiFactor{D.re, D.im, 1.0, 0.0};
+        const FF re = ff_from(D.re), im = ff_from(D.im);
+        tff[(size_t)k * J + jj] = make_float4(re.hi, re.lo, im.hi, im.lo);
       }
     PES_CHECK_CUDA(cudaMemcpy(tdn, tf.data(), sizeof(TdiFactor) * tf.size(), cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(tdn_ff, tff.data(), sizeof(float4) * tff.size(), cudaMemcpyHostToDevice));
   }
+  for (int k = 0; k < PES_MAX_DETECTORS; ++k) M.orbit_ff[k] = orbit_ff(k < nd ? d.det[k].orbit : d.det[0].orbit);
   {
     // shared not-a-knot system of the node grid: rows 1..J-2 with the first-row
     // elimination and without the last-row one (that row depends on the sample)
@@ -1842,6 +1953,8 @@ int mixed_create(PesPlan* p) {
   M.gcp = gcp;
   M.gf = gf;
   M.tdn = tdn;
+  M.tdn_ff = tdn_ff;
+  M.node_ff = node_ff;
   M.pbin = pbin;
   M.yv = yv;
   M.scr = scr;

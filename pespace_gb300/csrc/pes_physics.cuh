@@ -10,15 +10,47 @@
 #pragma once
 
 #include "pes_common.cuh"
+#include "pes_ff.cuh"
 #include "../../include/pespace_gb300.h"
 
 namespace pes {
 
 // ------------------------------------------------------------------ orbits
+// An orbit's parameters as float-float values (same field names as PesOrbit),
+// for node evaluations in FF arithmetic.
+struct OrbitFF {
+  int32_t kind;
+  int32_t pad;
+  FF arm_sec, rotation_initial, revolution_initial, omega_revolution, r_sec, omega_rotation;
+  FF slam_ref, clam_ref, sbeta_ref, cbeta_ref;
+  FF ck[3], sk[3];
+};
+
+inline OrbitFF orbit_ff(const PesOrbit& o) {
+  OrbitFF r;
+  r.kind = o.kind;
+  r.pad = 0;
+  r.arm_sec = ff_from(o.arm_sec);
+  r.rotation_initial = ff_from(o.rotation_initial);
+  r.revolution_initial = ff_from(o.revolution_initial);
+  r.omega_revolution = ff_from(o.omega_revolution);
+  r.r_sec = ff_from(o.r_sec);
+  r.omega_rotation = ff_from(o.omega_rotation);
+  r.slam_ref = ff_from(o.slam_ref);
+  r.clam_ref = ff_from(o.clam_ref);
+  r.sbeta_ref = ff_from(o.sbeta_ref);
+  r.cbeta_ref = ff_from(o.cbeta_ref);
+  for (int k = 0; k < 3; ++k) {
+    r.ck[k] = ff_from(o.ck[k]);
+    r.sk[k] = ff_from(o.sk[k]);
+  }
+  return r;
+}
+
 // n[i] = unit vector of link i+1 (n1: 2->3, n2: 3->1, n3: 1->2); xd[i] = node
 // i+1 relative to the constellation centre x0 (light-seconds, SSB axes).
-template <class T>
-PES_HD void constellation_parts(const PesOrbit& o, const T& t, T n[3][3], T xd[3][3], T x0[3]) {
+template <class T, class O>
+PES_HD void constellation_parts(const O& o, const T& t, T n[3][3], T xd[3][3], T x0[3]) {
   T c0, s0;
   T alpha = o.omega_revolution * t + o.revolution_initial;
   dsincos(alpha, &s0, &c0);
@@ -52,7 +84,7 @@ PES_HD void constellation_parts(const PesOrbit& o, const T& t, T n[3][3], T xd[3
       xd[k][2] = o.r_sec * (-o.cbeta_ref * sks[k]);
     }
   }
-  const double inv_arm = 1.0 / o.arm_sec;
+  const auto inv_arm = 1.0 / o.arm_sec;
   x0[0] = c0 * kAUsec;
   x0[1] = s0 * kAUsec;
   x0[2] = lift<T>(0.0);
@@ -112,6 +144,7 @@ PES_HD T sinc_ref(const T& x) {
   // utils.py:60-79: sin(x)/x with the x == 0 guard
   return (val(x) == 0.0) ? lift<T>(1.0) : dsin(x) / x;
 }
+PES_HD FF sinc_ref(const FF& x) { return ff_sinc(x); }
 PES_HD double sinc_ref(const double& x) {
   if (::fabs(x) <= 2.0) {
     double s, ds;
@@ -135,8 +168,8 @@ PES_HD Dual<N, D, double> sinc_ref(const Dual<N, D, double>& x) {
 // propagation delays use node positions relative to the constellation centre
 // and the centre's delay k.x0 is returned instead (the links then miss the
 // factor exp(-2 pi i f k.x0)); otherwise the links are those of antenna.py.
-template <bool kFactorDoppler, class T>
-PES_HD void single_links_impl(const PesOrbit& o, double f, const Cx<T>& hp, const Cx<T>& hc, const T& tf,
+template <bool kFactorDoppler, class T, class O, class Fq>
+PES_HD void single_links_impl(const O& o, Fq f, const Cx<T>& hp, const Cx<T>& hc, const T& tf,
                               const Polar<T>& pol, Cx<T> out[6], T* kx0_out) {
   T n[3][3], xd[3][3], x0[3];
   constellation_parts(o, tf, n, xd, x0);
@@ -162,9 +195,9 @@ PES_HD void single_links_impl(const PesOrbit& o, double f, const Cx<T>& hp, cons
     }
   }
   if (kFactorDoppler) *kx0_out = pol.k[0] * x0[0] + pol.k[1] * x0[1];
-  const double arm = o.arm_sec;
-  const double pifL = kPi * f * arm;
-  const double ce = -kPi * f;
+  const auto arm = o.arm_sec;
+  const auto pifL = kPi * f * arm;
+  const auto ce = -kPi * f;
   Cx<T> e[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -206,13 +239,19 @@ PES_HD void tdi_factors(double f, double arm, int gen20, Cx<double>& D, Cx<doubl
   }
 }
 
-template <class T>
-PES_HD void tdi_channels(const Cx<double>& D, const Cx<double>& P, int orth, const Cx<T> L[6], Cx<T> out[3]) {
-  Cx<T> Dt = cx(lift<T>(D.re), lift<T>(D.im)), Pt = cx(lift<T>(P.re), lift<T>(P.im));
+// X/Y/Z (or A/E/T) from the six links with delay factor Dt; kPre applies the
+// generation prefactor Pt, else it is taken as 1.
+template <bool kPre, class T>
+PES_HD void tdi_channels_t(const Cx<T>& Dt, const Cx<T>& Pt, int orth, const Cx<T> L[6], Cx<T> out[3]) {
   // L: 0=12 1=21 2=23 3=32 4=31 5=13
-  Cx<T> X = cmul(Pt, (L[5] - L[0]) + cmul(Dt, L[4] - L[1]));
-  Cx<T> Y = cmul(Pt, (L[1] - L[2]) + cmul(Dt, L[0] - L[3]));
-  Cx<T> Z = cmul(Pt, (L[3] - L[4]) + cmul(Dt, L[2] - L[5]));
+  Cx<T> X = (L[5] - L[0]) + cmul(Dt, L[4] - L[1]);
+  Cx<T> Y = (L[1] - L[2]) + cmul(Dt, L[0] - L[3]);
+  Cx<T> Z = (L[3] - L[4]) + cmul(Dt, L[2] - L[5]);
+  if (kPre) {
+    X = cmul(Pt, X);
+    Y = cmul(Pt, Y);
+    Z = cmul(Pt, Z);
+  }
   if (orth) {
     const double r2 = 0.70710678118654752, r6 = 0.40824829046386302, r3 = 0.57735026918962576;
     out[0] = cscale(r2, Z - X);
@@ -223,6 +262,11 @@ PES_HD void tdi_channels(const Cx<double>& D, const Cx<double>& P, int orth, con
     out[1] = Y;
     out[2] = Z;
   }
+}
+
+template <class T>
+PES_HD void tdi_channels(const Cx<double>& D, const Cx<double>& P, int orth, const Cx<T> L[6], Cx<T> out[3]) {
+  tdi_channels_t<true, T>(cx(lift<T>(D.re), lift<T>(D.im)), cx(lift<T>(P.re), lift<T>(P.im)), orth, L, out);
 }
 
 // ------------------------------------------------------------------ IMRPhenomD
