@@ -220,6 +220,7 @@ PES_DUAL PES_DT dabs(const PES_DT& a) { return a.v < V(0) ? -a : a; }
 
 template <class T> struct Lift { PES_HD static T from(double x); };
 template <> struct Lift<double> { PES_HD static double from(double x) { return x; } };
+template <> struct Lift<float> { PES_HD static float from(double x) { return (float)x; } };
 template <int N, class D, class V> struct Lift<Dual<N, D, V>> {
   PES_HD static Dual<N, D, V> from(double x) { return mkdual<N, D, V>(x); }
 };

@@ -67,7 +67,9 @@ struct MixedDev {
   const TdiFactor* tdn;     // [n_det][J] TDI delay factor at the nodes (prefactor set to 1)
   // float-float copies for the node evaluations on the FP32 pipes
   OrbitFF orbit_ff[PES_MAX_DETECTORS];
+  OrbitF orbit_f[PES_MAX_DETECTORS];  // FP32 copies for the derivative passes
   FF scale_ff;
+  float scale_f;
   FF fstep_ff;              // bin spacing
   const float2* node_ff;    // [J] node frequencies (hi, lo)
   const float4* tdn_ff;     // [n_det][J] node delay factor D (re hi, re lo, im hi, im lo)
@@ -162,24 +164,25 @@ __device__ __forceinline__ void node_eval(const PlanDev& P, const MixedDev& M, c
   }
 }
 
-// node_eval in float-float arithmetic: the same node quantities from the FF
-// copies of the sample block, orbit and TDI factors.  kPre applies the TDI
-// generation prefactor Pf (exact bins); nodes take it as 1.
-template <bool kPre>
-__device__ __forceinline__ void node_eval_ff(const MixedDev& M, const SampleBlock<FF>& b, int d, const Cx<FF>& D,
-                                             const Cx<FF>& Pf, const FF& f, FF y[kNodeQ]) {
-  const FF Mf = b.wf.Msec * f;
-  FF amp, psi, tf;
-  phenomd_eval<FF>(b.wf, Mf, amp, psi, tf);
-  amp = amp * M.scale_ff;
-  const FF zero = ff_make(0.0f, 0.0f);
-  Cx<FF> hp = cx(b.wf.pfac * amp, zero);
-  Cx<FF> hc = cx(zero, -(b.wf.cfac * amp));
-  Cx<FF> L[6], C[3];
-  FF kx0;
-  single_links_impl<true, FF>(M.orbit_ff[d], f, hp, hc, tf + b.tc, b.pol, L, &kx0);
-  tdi_channels_t<kPre, FF>(D, Pf, 1, L, C);
-  y[0] = psi + (2.0 * kPi * f) * kx0;
+// node_eval with the orbit, frequency and TDI factors in the scalar types of
+// the caller's pass: FF orbit and frequency for the float-float value passes,
+// FP32 ones for the FP32 derivative passes (no FP64 on the way).  kPre
+// applies the TDI generation prefactor Pf (exact bins); nodes take it as 1.
+template <bool kPre, class T, class O, class Fq>
+__device__ __forceinline__ void node_eval_g(const O& orbit, const Fq& scale, const SampleBlock<T>& b,
+                                            const Cx<T>& D, const Cx<T>& Pf, const Fq& f, T y[kNodeQ]) {
+  const T Mf = b.wf.Msec * f;
+  T amp, psi, tf;
+  phenomd_eval<T>(b.wf, Mf, amp, psi, tf);
+  amp = amp * scale;
+  const T zero = lift<T>(0.0);
+  Cx<T> hp = cx(b.wf.pfac * amp, zero);
+  Cx<T> hc = cx(zero, -(b.wf.cfac * amp));
+  Cx<T> L[6], C[3];
+  T kx0;
+  single_links_impl<true, T>(orbit, f, hp, hc, tf + b.tc, b.pol, L, &kx0);
+  tdi_channels_t<kPre, T>(D, Pf, 1, L, C);
+  y[0] = psi + (lift<Fq>(2.0 * kPi) * f) * kx0;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     y[1 + 2 * c] = C[c].re;
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
     const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
     const Cx<FF> D = cx(ff_make(t4.x, t4.y), ff_make(t4.z, t4.w));
     FF yf[kNodeQ];
-    node_eval_ff<false>(M, sbf, d, D, D, ff_make(fn.x, fn.y), yf);
+    node_eval_g<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, D, D, ff_make(fn.x, fn.y), yf);
 #pragma unroll
     for (int q = 0; q < kNodeQ; ++q) y[q] = ff_to(yf[q]);
   }
@@ -374,8 +377,12 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, Mix
   for (int k = 0; k < 11; ++k) acc[k] = 0.0f;
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
     GS y[kNodeQ];
-    const double fj = M.node_f[j];
-    node_eval<GS>(P, M, sb, d, M.tdn[(size_t)d * M.J + j], fj, y);
+    const float fj = M.node_ff[j].x;
+    {
+      const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
+      const Cx<GS> D = cx(lift<GS>(t4.x), lift<GS>(t4.z));
+      node_eval_g<false, GS>(M.orbit_f[d], M.scale_f, sb, D, D, fj, y);
+    }
     const GS xk = sb.wf.Msec * fj - sb.wf.fpeak;
     if (xk.v > 0.0) {
       GS ahat, jump;
@@ -1264,8 +1271,8 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
           const FF f = ff_mulf(M.fstep_ff, (float)(P.k0 + i));  // k0 + i < 2^24: exact in FP32
           const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
           FF y[kNodeQ];
-          node_eval_ff<true>(M, sbf, d, cx(ff_from(tdb.dre), ff_from(tdb.dim)), cx(ff_from(tdb.pre), ff_from(tdb.pim)),
-                             f, y);
+          node_eval_g<true, FF>(M.orbit_ff[d], M.scale_ff, sbf, cx(ff_from(tdb.dre), ff_from(tdb.dim)),
+                                cx(ff_from(tdb.pre), ff_from(tdb.pim)), f, y);
           // phase reduced modulo 2 pi in FP64, then its sine and cosine in FF
           const double phd = ff_to(y[0] + (2.0 * kPi * f) * sbf.tc);
           FF sn, cs;
@@ -1775,6 +1782,7 @@ int mixed_create(PesPlan* p) {
   M.n_det = nd;
   M.scale = 3.085677581491367e16 / (1.476625038050124729627979840144936351e3 * 4.925490947641266978197229498498379006e-6);
   M.scale_ff = ff_from(M.scale);
+  M.scale_f = (float)M.scale;
   M.fstep_ff = ff_from(d.f_step);
   for (int k = 0; k < nd; ++k) mb->gen.gen20[k] = d.det[k].generation == 20;
   // shared sparse grid, bin -> interval map, runs
@@ -1885,7 +1893,10 @@ int mixed_create(PesPlan* p) {
     PES_CHECK_CUDA(cudaMemcpy(tdn, tf.data(), sizeof(TdiFactor) * tf.size(), cudaMemcpyHostToDevice));
     PES_CHECK_CUDA(cudaMemcpy(tdn_ff, tff.data(), sizeof(float4) * tff.size(), cudaMemcpyHostToDevice));
   }
-  for (int k = 0; k < PES_MAX_DETECTORS; ++k) M.orbit_ff[k] = orbit_ff(k < nd ? d.det[k].orbit : d.det[0].orbit);
+  for (int k = 0; k < PES_MAX_DETECTORS; ++k) {
+    M.orbit_ff[k] = orbit_ff(k < nd ? d.det[k].orbit : d.det[0].orbit);
+    M.orbit_f[k] = orbit_f(k < nd ? d.det[k].orbit : d.det[0].orbit);
+  }
   {
     // shared not-a-knot system of the node grid: rows 1..J-2 with the first-row
     // elimination and without the last-row one (that row depends on the sample)

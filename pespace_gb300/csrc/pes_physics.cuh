@@ -26,6 +26,36 @@ struct OrbitFF {
   FF ck[3], sk[3];
 };
 
+// The same in FP32, for derivative passes that run entirely on the FP32 pipes.
+struct OrbitF {
+  int32_t kind;
+  int32_t pad;
+  float arm_sec, rotation_initial, revolution_initial, omega_revolution, r_sec, omega_rotation;
+  float slam_ref, clam_ref, sbeta_ref, cbeta_ref;
+  float ck[3], sk[3];
+};
+
+inline OrbitF orbit_f(const PesOrbit& o) {
+  OrbitF r;
+  r.kind = o.kind;
+  r.pad = 0;
+  r.arm_sec = (float)o.arm_sec;
+  r.rotation_initial = (float)o.rotation_initial;
+  r.revolution_initial = (float)o.revolution_initial;
+  r.omega_revolution = (float)o.omega_revolution;
+  r.r_sec = (float)o.r_sec;
+  r.omega_rotation = (float)o.omega_rotation;
+  r.slam_ref = (float)o.slam_ref;
+  r.clam_ref = (float)o.clam_ref;
+  r.sbeta_ref = (float)o.sbeta_ref;
+  r.cbeta_ref = (float)o.cbeta_ref;
+  for (int k = 0; k < 3; ++k) {
+    r.ck[k] = (float)o.ck[k];
+    r.sk[k] = (float)o.sk[k];
+  }
+  return r;
+}
+
 inline OrbitFF orbit_ff(const PesOrbit& o) {
   OrbitFF r;
   r.kind = o.kind;
@@ -84,7 +114,7 @@ PES_HD void constellation_parts(const O& o, const T& t, T n[3][3], T xd[3][3], T
       xd[k][2] = o.r_sec * (-o.cbeta_ref * sks[k]);
     }
   }
-  const auto inv_arm = 1.0 / o.arm_sec;
+  const auto inv_arm = lift<decltype(o.arm_sec)>(1.0) / o.arm_sec;
   x0[0] = c0 * kAUsec;
   x0[1] = s0 * kAUsec;
   x0[2] = lift<T>(0.0);
@@ -196,8 +226,8 @@ PES_HD void single_links_impl(const O& o, Fq f, const Cx<T>& hp, const Cx<T>& hc
   }
   if (kFactorDoppler) *kx0_out = pol.k[0] * x0[0] + pol.k[1] * x0[1];
   const auto arm = o.arm_sec;
-  const auto pifL = kPi * f * arm;
-  const auto ce = -kPi * f;
+  const auto pifL = lift<Fq>(kPi) * f * arm;
+  const auto ce = -(lift<Fq>(kPi) * f);
   Cx<T> e[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
