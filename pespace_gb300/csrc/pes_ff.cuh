@@ -27,6 +27,7 @@
 
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 #include "pes_common.cuh"
 
@@ -215,6 +216,37 @@ PES_HD void dsincos(const FF& x, FF* s, FF* c) {
   if ((k + 1) & 2) cv = -cv;
   *s = sv;
   *c = cv;
+}
+
+// 2 pi = kTwoPiA + kTwoPiB + kTwoPiC (A has 8 significant bits: k * A exact for |k| < 2^16)
+constexpr float kTwoPiA = 6.28125f;
+constexpr float kTwoPiB = 1.9353071693331003e-3f;
+constexpr float kTwoPiC = 1.0253376273028358e-11f;
+
+// x - 2 pi rint(x / 2 pi) for |x| < 2^18 (x.hi - k A is exact: k A is within
+// a factor two of x.hi for k != 0)
+PES_HD FF ff_wrap_2pi(const FF& x) {
+  const float kf = rintf(x.hi * 0.15915494309189535f);
+  FF r = ff_addf(x, -kf * kTwoPiA);
+  r = r - ff_two_prod(kf, kTwoPiB);
+  return ff_addf(r, -kf * kTwoPiC);
+}
+
+// x.hi truncated to its leading `bits` significant bits (so that the head
+// times a small integer is exact in FP32), and the FF remainder as a float.
+PES_HD float ff_head(const FF& x, int bits, float* tail) {
+  const unsigned m = ~((1u << (24 - bits)) - 1u);
+#ifdef __CUDA_ARCH__
+  const float h = __uint_as_float(__float_as_uint(x.hi) & m);
+#else
+  unsigned u;
+  memcpy(&u, &x.hi, 4);
+  u &= m;
+  float h;
+  memcpy(&h, &u, 4);
+#endif
+  *tail = (x.hi - h) + x.lo;
+  return h;
 }
 
 // sin(x)/x: Taylor series in z = x^2 for |x| <= 2 (FF for the terms down to

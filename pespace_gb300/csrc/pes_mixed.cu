@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <type_traits>
 #include <vector>
 
 #include "pes_plan.cuh"
@@ -98,13 +99,14 @@ struct MixedDev {
   const double* ginvden;    // [J] 1 / Thomas pivots
   const double* gcp;        // [J] Thomas super-diagonal ratios
   const float* gf;          // [kGfCount][J] FP32 copies of gh, ginvh, glo, gup, ginvden, gcp
-  double* yv;               // [B][n_det][J][7] node values (quantity fastest)
+  const FF* gff;            // [kGfCount][J] float-float copies of the same
+  FF* yv;                   // [B][n_det][7][J] node values (float-float, node fastest)
   double* scr;              // [B][n_det][J][7] spline scratch
-  double* cphi;             // [B][n_det][J][4] phase spline coefficients (FP64)
+  FF* cphi;                 // [B][n_det][J][4] phase spline coefficients (float-float)
   float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32: a_hi, b, c, d)
   float* cglo;              // [B][n_det][J][6] a - a_hi (the value at the left node in float-float)
   float* mom;               // [B][n_det][J][7][4] adjoint moments (FP32 warp sums, FP32 atomics)
-  double* ybar;             // [B][n_det][J][7] node adjoints
+  float* ybar;              // [B][n_det][J][7] node adjoints (FP32: the derivative passes run in FP32)
   double* part;             // [B][nblk_dense] lnL partials
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
@@ -254,7 +256,7 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
   }
 }
 
-// Forward: node values in float-float arithmetic, stored as FP64.  grid (ceil(J/128), n_det, B)
+// Forward: node values in float-float arithmetic.  grid (ceil(J/128), n_det, B)
 __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedDev M, GenArg G,
                                                                const SampleBlock<double>* __restrict__ blocks) {
   __shared__ SampleBlock<double> sb;
@@ -267,26 +269,23 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
   if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J) return;
-  double y[kNodeQ];
+  FF y[kNodeQ];
   {
     const float2 fn = M.node_ff[j];
     const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
     const Cx<FF> D = cx(ff_make(t4.x, t4.y), ff_make(t4.z, t4.w));
-    FF yf[kNodeQ];
-    node_eval_g<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, D, D, ff_make(fn.x, fn.y), yf);
+    node_eval_g<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, D, D, ff_make(fn.x, fn.y), y);
+    const FF xk = sbf.wf.Msec * ff_make(fn.x, fn.y) - sbf.wf.fpeak;
+    if (xk.hi > 0.0f) {
+      const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
+      const FF x2 = xk * xk;
 #pragma unroll
-    for (int q = 0; q < kNodeQ; ++q) y[q] = ff_to(yf[q]);
+      for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - ff_from(C[q]) * x2;
+    }
   }
-  const double fj = M.node_f[j];
-  const double xk = sb.wf.Msec * fj - sb.wf.fpeak;
-  if (xk > 0.0) {
-    const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
+  FF* out = M.yv + ((size_t)s * M.n_det + d) * kNodeQ * M.J + j;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) y[1 + q] -= C[q] * xk * xk;
-  }
-  double* out = M.yv + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
-#pragma unroll
-  for (int q = 0; q < kNodeQ; ++q) out[q] = y[q];
+  for (int q = 0; q < kNodeQ; ++q) out[(size_t)q * M.J] = y[q];
 }
 
 // Gradient set-up: per sample, the coefficient block with exact FP64
@@ -392,10 +391,10 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, Mix
 #pragma unroll
       for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - R[q] * x2h;  // R_q held fixed
     }
-    const double* yb = M.ybar + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
+    const float* yb = M.ybar + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
 #pragma unroll
     for (int q = 0; q < kNodeQ; ++q) {
-      const float w = (float)yb[q];
+      const float w = yb[q];
 #pragma unroll
       for (int k = 0; k < N; ++k) acc[kSlotParam[Off + k]] = fmaf(w, y[q].d[k], acc[kSlotParam[Off + k]]);
       if (kFirst) {
@@ -554,21 +553,33 @@ __device__ __forceinline__ void nak_ends(const double* f, int n, double m1, doub
 // from 0 to get the segment's affine map x_in -> A x_in + B, a warp scan of
 // those maps gives the exact value entering every segment, and the lane then
 // reruns its segment from that value.  `reverse` scans from lane 31 down.
+// Warp shuffles for the spline scalars (float, double, float-float).
+__device__ __forceinline__ float warp_shfl_up(float x, int o) { return __shfl_up_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ float warp_shfl_down(float x, int o) { return __shfl_down_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ double warp_shfl_up(double x, int o) { return __shfl_up_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ double warp_shfl_down(double x, int o) { return __shfl_down_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ FF warp_shfl_up(const FF& x, int o) {
+  return ff_make(__shfl_up_sync(0xffffffffu, x.hi, o), __shfl_up_sync(0xffffffffu, x.lo, o));
+}
+__device__ __forceinline__ FF warp_shfl_down(const FF& x, int o) {
+  return ff_make(__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o));
+}
+
 template <class R>
 __device__ __forceinline__ R segment_carry_in(R A, R B, bool reverse) {
   const int lane = threadIdx.x & 31;
   const int pos = reverse ? 31 - lane : lane;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const R Ap = reverse ? __shfl_down_sync(0xffffffffu, A, o) : __shfl_up_sync(0xffffffffu, A, o);
-    const R Bp = reverse ? __shfl_down_sync(0xffffffffu, B, o) : __shfl_up_sync(0xffffffffu, B, o);
+    const R Ap = reverse ? warp_shfl_down(A, o) : warp_shfl_up(A, o);
+    const R Bp = reverse ? warp_shfl_down(B, o) : warp_shfl_up(B, o);
     if (pos >= o) {
       B = A * Bp + B;
       A = A * Ap;
     }
   }
-  const R prev = reverse ? __shfl_down_sync(0xffffffffu, B, 1) : __shfl_up_sync(0xffffffffu, B, 1);
-  return pos == 0 ? R(0) : prev;
+  const R prev = reverse ? warp_shfl_down(B, 1) : warp_shfl_up(B, 1);
+  return pos == 0 ? lift<R>(0.0) : prev;
 }
 
 
@@ -580,7 +591,8 @@ constexpr int kSplineThreads = kNodeQ * 32;  // one warp per quantity, one block
 // float-float pair.  Scratch per (node, quantity): (rhs | d' | m, slope).
 __device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t sd, int q, int n) {
   const int lane = threadIdx.x & 31;
-  const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;
+  const FF* yq = M.yv + ((size_t)sd * kNodeQ + q) * M.J;
+  auto y = [&](int i) { return ff_to(yq[i]); };
   float2* S = reinterpret_cast<float2*>(M.scr + (size_t)sd * M.J * kNodeQ + q);
   const float* fh = M.gf + (size_t)kGfH * M.J;
   const float* fih = M.gf + (size_t)kGfInvH * M.J;
@@ -591,9 +603,9 @@ __device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t s
   const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);
   const int r0 = max(1, i0), r1 = i1;
   if (i0 < i1) {
-    double sp = (i0 >= 1) ? (y[i0 * kNodeQ] - y[(i0 - 1) * kNodeQ]) * M.ginvh[i0 - 1] : 0.0;
+    double sp = (i0 >= 1) ? (y(i0) - y(i0 - 1)) * M.ginvh[i0 - 1] : 0.0;
     for (int i = i0; i < i1; ++i) {
-      const double sl = (y[(i + 1) * kNodeQ] - y[i * kNodeQ]) * M.ginvh[i];
+      const double sl = (y(i + 1) - y(i)) * M.ginvh[i];
       S[i * kNodeQ] = make_float2(i >= 1 ? (float)(6.0 * (sl - sp)) : 0.0f, (float)sl);
       sp = sl;
     }
@@ -647,10 +659,9 @@ __device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t s
     const float bc = sl - fh[i] * (2.0f * mi + mj) * (1.0f / 6.0f);
     const float cc = 0.5f * mi;
     const float dc = (mj - mi) * fih[i] * (1.0f / 6.0f);
-    const double a = y[i * kNodeQ];
-    const float ahi = (float)a;
-    M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, bc, cc, dc);
-    M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(a - (double)ahi);
+    const FF a = yq[i];
+    M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(a.hi, bc, cc, dc);
+    M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = a.lo;
     mi = mj;
   }
 }
@@ -661,7 +672,7 @@ __device__ __forceinline__ void spline_adjoint_transfer(const MixedDev& M, int64
   const int lane = threadIdx.x & 31;
   const float* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
   float2* X = reinterpret_cast<float2*>(M.scr + (size_t)sd * M.J * kNodeQ + q);
-  double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
+  float* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
   const float* fih = M.gf + (size_t)kGfInvH * M.J;
   const float* flo = M.gf + (size_t)kGfLo * M.J;
   const float* fup = M.gf + (size_t)kGfUp * M.J;
@@ -735,13 +746,13 @@ __device__ __forceinline__ void spline_adjoint_transfer(const MixedDev& M, int64
     for (int i = i0; i < i1; ++i) {
       const float rnext = rb(i + 1);
       const float Db = (float)mm(i, 1) + 6.0f * (rcur - rnext);
-      yb[i * kNodeQ] = (double)(dprev + (float)mm(i, 0) - Db * fih[i]);
+      yb[i * kNodeQ] = dprev + (float)mm(i, 0) - Db * fih[i];
       dprev = Db * fih[i];
       rcur = rnext;
     }
-    if (i1 == n) yb[n * kNodeQ] = (double)dprev;
+    if (i1 == n) yb[n * kNodeQ] = dprev;
   }
-  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0f;
 }
 
 // Fit for grids of more than 64 x 32 intervals (segments in global scratch):
@@ -759,7 +770,8 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit_wide(MixedDev M) 
     return;
   }
   const double* f = M.node_f;
-  const double* y = M.yv + (size_t)sd * M.J * kNodeQ + q;  // y[i * kNodeQ]
+  const FF* yq = M.yv + ((size_t)sd * kNodeQ + q) * M.J;
+  auto y = [&](int i) { return ff_to(yq[i]); };
   double* S = M.scr + (size_t)sd * M.J * kNodeQ + q;       // d' then m
   const int seg = (n + 31) >> 5;
   const int i0 = min(n, lane * seg), i1 = min(n, i0 + seg);  // intervals [i0, i1)
@@ -771,9 +783,9 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit_wide(MixedDev M) 
   double A = 1.0, x = 0.0;
   for (int pass = 0; pass < 2; ++pass) {
     if (r0 < r1) {
-      double sp = (y[r0 * kNodeQ] - y[(r0 - 1) * kNodeQ]) * M.ginvh[r0 - 1];
+      double sp = (y(r0) - y(r0 - 1)) * M.ginvh[r0 - 1];
       for (int i = r0; i < r1; ++i) {
-        const double sl = (y[(i + 1) * kNodeQ] - y[i * kNodeQ]) * M.ginvh[i];
+        const double sl = (y(i + 1) - y(i)) * M.ginvh[i];
         const double r = 6.0 * (sl - sp);
         sp = sl;
         const bool last = i == n - 1;
@@ -804,20 +816,20 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit_wide(MixedDev M) 
   nak_ends(f, n, S[1 * kNodeQ], S[2 * kNodeQ], S[(n - 1) * kNodeQ], S[(n - 2) * kNodeQ], m0, mn);
   if (i0 >= i1) return;
   double mi = (i0 == 0) ? m0 : S[i0 * kNodeQ];
-  double a = y[i0 * kNodeQ];
+  double a = y(i0);
   for (int i = i0; i < i1; ++i) {
     const double mj = (i + 1 == n) ? mn : S[(i + 1) * kNodeQ];
     const double h = M.gh[i];
-    const double an = y[(i + 1) * kNodeQ];
+    const double an = y(i + 1);
     const double bc = (an - a) * M.ginvh[i] - h * (2.0 * mi + mj) * (1.0 / 6.0);
     const double cc = 0.5 * mi;
     const double dc = (mj - mi) * M.ginvh[i] * (1.0 / 6.0);
     if (q == 0) {
-      double* o = M.cphi + ((size_t)sd * M.J + i) * 4;
-      o[0] = a;
-      o[1] = bc;
-      o[2] = cc;
-      o[3] = dc;
+      FF* o = M.cphi + ((size_t)sd * M.J + i) * 4;
+      o[0] = yq[i];
+      o[1] = ff_from(bc);
+      o[2] = ff_from(cc);
+      o[3] = ff_from(dc);
     } else {
       const float ahi = (float)a;
       M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, (float)bc, (float)cc, (float)dc);
@@ -836,9 +848,9 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint_wide(MixedDev
   const int64_t sd = blockIdx.x;
   const int64_t s = sd / M.n_det;
   const int n = M.nsp[s];
-  double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;  // yb[i * kNodeQ]
+  float* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;  // yb[i * kNodeQ]
   if (n < 3) {
-    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0f;
     if (q == 0 && lane == 0) M.gdir[sd] = 0.0;
     return;
   }
@@ -912,14 +924,14 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_adjoint_wide(MixedDev
     for (int i = i0; i < i1; ++i) {
       const double rnext = rb(i + 1);
       const double Db = mm(i, 1) + 6.0 * (rcur - rnext);
-      yb[i * kNodeQ] = dprev + mm(i, 0) - Db * M.ginvh[i];
+      yb[i * kNodeQ] = (float)(dprev + mm(i, 0) - Db * M.ginvh[i]);
       dprev = Db * M.ginvh[i];
       rcur = rnext;
       if (q == 0) gd += 2.0 * kPi * (f[i] * mom[(size_t)i * kNodeQ * kMoments] + mom[(size_t)i * kNodeQ * kMoments + 1]);
     }
-    if (i1 == n) yb[n * kNodeQ] = dprev;
+    if (i1 == n) yb[n * kNodeQ] = (float)dprev;
   }
-  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0f;
   if (q == 0) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gd += __shfl_xor_sync(0xffffffffu, gd, o);
@@ -939,7 +951,9 @@ inline int spline_seg(int J) { return J <= 32 * 32 + 1 ? 32 : (J <= kSegMax * 32
 
 template <class R>
 __device__ __forceinline__ const R* spline_factor(const MixedDev& M, int which) {
-  if constexpr (sizeof(R) == 8) {
+  if constexpr (std::is_same<R, FF>::value) {
+    return M.gff + (size_t)which * M.J;
+  } else if constexpr (sizeof(R) == 8) {
     switch (which) {
       case kGfH: return reinterpret_cast<const R*>(M.gh);
       case kGfInvH: return reinterpret_cast<const R*>(M.ginvh);
@@ -953,49 +967,77 @@ __device__ __forceinline__ const R* spline_factor(const MixedDev& M, int which) 
   }
 }
 
-template <int kSeg, class R>
-__device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, int q, int n, R* smem4) {
+// Register-segment fit, staged through shared memory.  Each warp solves one
+// (sample, detector, quantity) system; lane l owns rows [l seg, (l+1) seg).
+// Those lane-strided accesses go to shared memory only: the block first
+// copies the shared grid's factor tables and each warp its system's node
+// values with coalesced loads (rows padded by one slot per 32, so that the
+// lane-strided reads are free of bank conflicts for seg = 32).
+// R = FF for the phase (q == 0), float for the transfer quantities; slopes
+// and right-hand sides from the float-float node values in FF.
+template <class R> __device__ __forceinline__ R ff_to_r(const FF& x);
+template <> __device__ __forceinline__ float ff_to_r<float>(const FF& x) { return x.hi; }
+template <> __device__ __forceinline__ FF ff_to_r<FF>(const FF& x) { return x; }
+
+constexpr int kFitWarps = 4;  // systems per block of the staged fit
+__host__ __device__ __forceinline__ int fit_pad(int i) { return i + (i >> 5); }
+__host__ __device__ __forceinline__ int fit_rows(int J) { return fit_pad(J) + 1; }
+
+// dynamic shared memory of one staged-fit block: five R tables (h, 1/h, lo,
+// 1/den, cp), the FF 1/h table for the slopes (the R table itself for R = FF),
+// then per warp the node values and the four end-row values.
+// Grids of more than 32 x 32 intervals leave the tables in global memory
+// (staging them would leave room for one block per SM).
+template <class R, bool kStageTables>
+__host__ __device__ __forceinline__ size_t fit_smem_bytes(int J) {
+  const size_t rows = (size_t)fit_rows(J);
+  const size_t tables =
+      kStageTables ? 5 * rows * sizeof(R) + (std::is_same<R, FF>::value ? 0 : rows * sizeof(FF)) : 0;
+  return ((tables + 15) & ~(size_t)15) + (size_t)kFitWarps * (rows * sizeof(FF) + 4 * sizeof(FF));
+}
+
+template <int kSeg, class R, bool kStageTables>
+__device__ __forceinline__ void spline_fit_staged(const MixedDev& M, int64_t sd, int q, int n, const R* t_h,
+                                                  const R* t_ih, const R* t_lo, const R* t_id, const R* t_cp,
+                                                  const FF* t_gih, const FF* y, R* smem4) {
   const int lane = threadIdx.x & 31;
-  const double* __restrict__ y = M.yv + (size_t)sd * M.J * kNodeQ + q;
-  const R* __restrict__ fh = spline_factor<R>(M, kGfH);
-  const R* __restrict__ fih = spline_factor<R>(M, kGfInvH);
-  const R* __restrict__ flo = spline_factor<R>(M, kGfLo);
-  const R* __restrict__ fid = spline_factor<R>(M, kGfInvDen);
-  const R* __restrict__ fcp = spline_factor<R>(M, kGfCp);
-  const int seg = (n + 31) >> 5;
+  auto tp = [](int i) { return kStageTables ? fit_pad(i) : i; };
+  // staged: segments of 32 rows whatever n (lanes past n idle), which keeps
+  // the lane-strided shared-memory reads free of bank conflicts
+  const int seg = kStageTables ? 32 : (n + 31) >> 5;
   const int i0 = min(n, lane * seg), cnt = min(n, i0 + seg) - i0;
   double lo_d, di_d, up_d;
   nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
-  const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
-  // right-hand sides 6 (slope_i - slope_{i-1}) of rows i0 + k, in FP64
+  const R lo_l = lift<R>(lo_d), iden_l = lift<R>(1.0 / (di_d - lo_d * M.gcp[n - 2]));
+  const R zero = lift<R>(0.0);
+  // right-hand sides 6 (slope_i - slope_{i-1}) of rows i0 + k
   R x[kSeg];
   {
-    double yp = (i0 >= 1) ? y[(i0 - 1) * kNodeQ] : 0.0;
-    double yc = y[i0 * kNodeQ];
-    double sp = (i0 >= 1) ? (yc - yp) * M.ginvh[i0 - 1] : 0.0;
+    FF yc = y[fit_pad(i0)];
+    FF sp = (i0 >= 1) ? (yc - y[fit_pad(i0 - 1)]) * t_gih[tp(i0 - 1)] : ff_make(0.0f, 0.0f);
 #pragma unroll
     for (int k = 0; k < kSeg; ++k) {
-      x[k] = R(0);
+      x[k] = zero;
       if (k < cnt) {
         const int i = i0 + k;
-        const double yn = y[(i + 1) * kNodeQ];
-        const double sl = (yn - yc) * M.ginvh[i];
-        if (i >= 1) x[k] = (R)(6.0 * (sl - sp));
+        const FF yn = y[fit_pad(i + 1)];
+        const FF sl = (yn - yc) * t_gih[tp(i)];
+        if (i >= 1) x[k] = ff_to_r<R>(ff_mulf(sl - sp, 6.0f));
         sp = sl;
         yc = yn;
       }
     }
   }
   // forward elimination (rows 1..n-1)
-  R A = R(1), v = R(0);
+  R A = lift<R>(1.0), v = zero;
 #pragma unroll
   for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const bool last = i == n - 1;
-      const R l = last ? lo_l : flo[i], id = last ? iden_l : fid[i];
+      const R l = last ? lo_l : t_lo[tp(i)], id = last ? iden_l : t_id[tp(i)];
       v = (x[k] - l * v) * id;
-      A = -l * id * A;
+      A = -(l * id) * A;
     }
   }
   v = segment_carry_in<R>(A, v, false);
@@ -1004,19 +1046,19 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
       const bool last = i == n - 1;
-      const R l = last ? lo_l : flo[i], id = last ? iden_l : fid[i];
+      const R l = last ? lo_l : t_lo[tp(i)], id = last ? iden_l : t_id[tp(i)];
       v = (x[k] - l * v) * id;
       x[k] = v;
     }
   }
   // back substitution m_i = d'_i - cp_i m_{i+1}
-  A = R(1);
-  v = R(0);
+  A = lift<R>(1.0);
+  v = zero;
 #pragma unroll
   for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
-      const R c = (i == n - 1) ? R(0) : fcp[i];
+      const R c = (i == n - 1) ? zero : t_cp[tp(i)];
       v = x[k] - c * v;
       A = -c * A;
     }
@@ -1026,7 +1068,7 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
   for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
-      const R c = (i == n - 1) ? R(0) : fcp[i];
+      const R c = (i == n - 1) ? zero : t_cp[tp(i)];
       v = x[k] - c * v;
       x[k] = v;
     }
@@ -1043,11 +1085,12 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
     }
   }
   __syncwarp();
-  const R h0 = fh[0], h1 = fh[1], ha = fh[n - 2], hb = fh[n - 1];
+  const R h0 = t_h[tp(0)], h1 = t_h[tp(1)], ha = t_h[tp(n - 2)], hb = t_h[tp(n - 1)];
   const R m0 = ((h0 + h1) * smem4[0] - h0 * smem4[1]) / h1;
   const R mn = ((ha + hb) * smem4[3] - hb * smem4[2]) / ha;
-  const R next_first = __shfl_down_sync(0xffffffffu, x[0], 1);  // m at row i0 + cnt (when it is a row)
-  double yc = y[i0 * kNodeQ];
+  const R next_first = warp_shfl_down(x[0], 1);  // m at row i0 + cnt (when it is a row)
+  const R sixth = lift<R>(1.0 / 6.0), half = lift<R>(0.5), two = lift<R>(2.0);
+  FF yc = y[fit_pad(i0)];
 #pragma unroll
   for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
@@ -1057,61 +1100,100 @@ __device__ __forceinline__ void spline_fit_regs(const MixedDev& M, int64_t sd, i
       if (i + 1 == n) mj = mn;
       else if (k + 1 < cnt) mj = x[(k + 1) < kSeg ? k + 1 : k];
       else mj = next_first;
-      const double yn = y[(i + 1) * kNodeQ];
-      const R sl = (R)((yn - yc) * M.ginvh[i]);
-      const R bc = sl - fh[i] * (R(2) * mi + mj) * R(1.0 / 6.0);
-      const R cc = R(0.5) * mi;
-      const R dc = (mj - mi) * fih[i] * R(1.0 / 6.0);
-      if constexpr (sizeof(R) == 8) {
-        double* o = M.cphi + ((size_t)sd * M.J + i) * 4;
+      const FF yn = y[fit_pad(i + 1)];
+      const R sl = ff_to_r<R>((yn - yc) * t_gih[tp(i)]);
+      const R bc = sl - t_h[tp(i)] * (two * mi + mj) * sixth;
+      const R cc = half * mi;
+      const R dc = (mj - mi) * t_ih[tp(i)] * sixth;
+      if constexpr (std::is_same<R, FF>::value) {
+        FF* o = M.cphi + ((size_t)sd * M.J + i) * 4;
         o[0] = yc;
         o[1] = bc;
         o[2] = cc;
         o[3] = dc;
       } else {
-        const float ahi = (float)yc;
-        M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, bc, cc, dc);
-        M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(yc - (double)ahi);
+        M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(yc.hi, bc, cc, dc);
+        M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = yc.lo;
       }
       yc = yn;
     }
   }
 }
 
-// One warp per block: blockIdx.x = (sample * n_det + detector) * 7 + quantity.
-template <int kSeg>
-__global__ void __launch_bounds__(32) k_spline_fit(MixedDev M) {
-  __shared__ double sm4[4];
-  const int q = (int)(blockIdx.x % kNodeQ);
-  const int64_t sd = blockIdx.x / kNodeQ;
+// kFitWarps systems per block.  R = FF: the phase systems (one per sample and
+// detector, q = 0); R = float: the six transfer systems (q = 1..6).
+template <int kSeg, class R>
+__global__ void __launch_bounds__(kFitWarps * 32) k_spline_fit(MixedDev M, int64_t n_sys) {
+  extern __shared__ __align__(16) unsigned char fit_smem[];
+  constexpr bool kPhase = std::is_same<R, FF>::value;
+  constexpr bool kStage = kSeg == 32;
+  const int rows = fit_rows(M.J);
+  const R* src = kPhase ? reinterpret_cast<const R*>(M.gff) : reinterpret_cast<const R*>(M.gf);
+  R* t_h = reinterpret_cast<R*>(fit_smem);
+  R* t_ih = t_h + rows;
+  R* t_lo = t_ih + rows;
+  R* t_id = t_lo + rows;
+  R* t_cp = t_id + rows;
+  FF* t_gih = kPhase ? reinterpret_cast<FF*>(t_ih) : reinterpret_cast<FF*>(t_cp + rows);
+  const size_t tables = kStage ? 5 * (size_t)rows * sizeof(R) + (kPhase ? 0 : (size_t)rows * sizeof(FF)) : 0;
+  unsigned char* wbase = fit_smem + ((tables + 15) & ~(size_t)15);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  FF* ys = reinterpret_cast<FF*>(wbase + (size_t)warp * (rows * sizeof(FF) + 4 * sizeof(FF)));
+  R* sm4 = reinterpret_cast<R*>(ys + rows);
+  if (!kStage) {
+    t_h = const_cast<R*>(src + (size_t)kGfH * M.J);
+    t_ih = const_cast<R*>(src + (size_t)kGfInvH * M.J);
+    t_lo = const_cast<R*>(src + (size_t)kGfLo * M.J);
+    t_id = const_cast<R*>(src + (size_t)kGfInvDen * M.J);
+    t_cp = const_cast<R*>(src + (size_t)kGfCp * M.J);
+    t_gih = const_cast<FF*>(M.gff + (size_t)kGfInvH * M.J);
+  }
+  // shared grid tables (coalesced)
+  if (kStage) {
+    const int which[5] = {kGfH, kGfInvH, kGfLo, kGfInvDen, kGfCp};
+#pragma unroll
+    for (int t = 0; t < 5; ++t) {
+      R* dst = t_h + (size_t)t * rows;
+      const R* sp = src + (size_t)which[t] * M.J;
+      for (int i = threadIdx.x; i < M.J; i += blockDim.x) dst[fit_pad(i)] = sp[i];
+    }
+    if (!kPhase) {
+      const FF* sp = M.gff + (size_t)kGfInvH * M.J;
+      for (int i = threadIdx.x; i < M.J; i += blockDim.x) t_gih[fit_pad(i)] = sp[i];
+    }
+  }
+  __syncthreads();
+  const int64_t sys = (int64_t)blockIdx.x * kFitWarps + warp;
+  if (sys >= n_sys) return;
+  const int64_t sd = kPhase ? sys : sys / 6;
+  const int q = kPhase ? 0 : 1 + (int)(sys % 6);
   const int n = M.nsp[sd / M.n_det];
   if (n < 3) return;
-  if (q == 0)
-    spline_fit_regs<kSeg, double>(M, sd, q, n, sm4);
-  else
-    spline_fit_regs<kSeg, float>(M, sd, q, n, reinterpret_cast<float*>(sm4));
+  const FF* yq = M.yv + ((size_t)sd * kNodeQ + q) * M.J;
+  for (int i = lane; i <= n; i += 32) ys[fit_pad(i)] = yq[i];
+  __syncwarp();
+  spline_fit_staged<kSeg, R, kStage>(M, sd, q, n, t_h, t_ih, t_lo, t_id, t_cp, t_gih, ys, sm4);
 }
 
-template <int kSeg, class R>
-__device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t sd, int q, int n, double wscale) {
+// Transpose of the fit with the same lane segments.  mom(i, p) gives the
+// interval moments, the tables are indexed through tp (padded rows when they
+// were staged in shared memory).
+template <int kSeg, class R, class MomAt, class TabIdx>
+__device__ __forceinline__ void spline_adjoint_seg(const MixedDev& M, int64_t sd, int q, int n, int seg, double wscale,
+                                                   const R* __restrict__ fh, const R* __restrict__ fih,
+                                                   const R* __restrict__ flo, const R* __restrict__ fup,
+                                                   const R* __restrict__ fid, MomAt mom, TabIdx tp) {
   const int lane = threadIdx.x & 31;
-  const float* __restrict__ mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
-  double* __restrict__ yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
-  const R* __restrict__ fih = spline_factor<R>(M, kGfInvH);
-  const R* __restrict__ flo = spline_factor<R>(M, kGfLo);
-  const R* __restrict__ fup = spline_factor<R>(M, kGfUp);
-  const R* __restrict__ fid = spline_factor<R>(M, kGfInvDen);
-  const int seg = (n + 31) >> 5;
+  float* __restrict__ yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
   const int i0 = min(n, lane * seg), cnt = min(n, i0 + seg) - i0;
-  const R* __restrict__ fh = spline_factor<R>(M, kGfH);
   const R ws = (R)wscale;
-  auto mm = [&](int i, int p) { return ws * (R)mom[(size_t)i * kNodeQ * kMoments + p]; };
+  auto mm = [&](int i, int p) { return ws * (R)mom(i, p); };
   auto mbar_left = [&](int i) {
-    return -fh[i] * mm(i, 1) * R(1.0 / 3.0) + R(0.5) * mm(i, 2) - mm(i, 3) * fih[i] * R(1.0 / 6.0);
+    return -fh[tp(i)] * mm(i, 1) * R(1.0 / 3.0) + R(0.5) * mm(i, 2) - mm(i, 3) * fih[tp(i)] * R(1.0 / 6.0);
   };
-  auto mbar_right = [&](int i) { return -fh[i] * mm(i, 1) * R(1.0 / 6.0) + mm(i, 3) * fih[i] * R(1.0 / 6.0); };
+  auto mbar_right = [&](int i) { return -fh[tp(i)] * mm(i, 1) * R(1.0 / 6.0) + mm(i, 3) * fih[tp(i)] * R(1.0 / 6.0); };
   const R mb0 = mbar_left(0), mbn = mbar_right(n - 1);
-  const R h0 = fh[0], h1 = fh[1], ha = fh[n - 2], hb = fh[n - 1];
+  const R h0 = fh[tp(0)], h1 = fh[tp(1)], ha = fh[tp(n - 2)], hb = fh[tp(n - 1)];
   double lo_d, di_d, up_d;
   nak_row(M.node_f, n, n - 1, lo_d, di_d, up_d);
   const R lo_l = (R)lo_d, iden_l = (R)(1.0 / (di_d - lo_d * M.gcp[n - 2]));
@@ -1143,7 +1225,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
-      const R sub = (i > 1) ? fup[i - 1] : R(0), id = (i == n - 1) ? iden_l : fid[i];
+      const R sub = (i > 1) ? fup[tp(i - 1)] : R(0), id = (i == n - 1) ? iden_l : fid[tp(i)];
       v = (x[k] - sub * v) * id;
       A = -sub * id * A;
     }
@@ -1153,7 +1235,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   for (int k = 0; k < kSeg; ++k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
-      const R sub = (i > 1) ? fup[i - 1] : R(0), id = (i == n - 1) ? iden_l : fid[i];
+      const R sub = (i > 1) ? fup[tp(i - 1)] : R(0), id = (i == n - 1) ? iden_l : fid[tp(i)];
       v = (x[k] - sub * v) * id;
       x[k] = v;
     }
@@ -1165,7 +1247,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
-      const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
+      const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[tp(i + 1)]) * fid[tp(i)];
       v = x[k] - c * v;
       A = -c * A;
     }
@@ -1176,7 +1258,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   for (int k = kSeg - 1; k >= 0; --k) {
     const int i = i0 + k;
     if (k < cnt && i >= 1) {
-      const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[i + 1]) * fid[i];
+      const R c = (i == n - 1) ? R(0) : ((i + 1 == n - 1) ? lo_l : flo[tp(i + 1)]) * fid[tp(i)];
       v = x[k] - c * v;
       x[k] = v;
       if (k == cnt - 1) last = v;
@@ -1191,7 +1273,7 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
     R dprev = R(0);
     if (i0 > 0) {
       const R r_prev = (i0 - 1 >= 1) ? prev_last : R(0);
-      dprev = (mm(i0 - 1, 1) + R(6) * (r_prev - x[0])) * fih[i0 - 1];
+      dprev = (mm(i0 - 1, 1) + R(6) * (r_prev - x[0])) * fih[tp(i0 - 1)];
     }
 #pragma unroll
     for (int k = 0; k < kSeg; ++k) {
@@ -1203,15 +1285,15 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
         else if (k + 1 < cnt) rn = x[(k + 1) < kSeg ? k + 1 : k];
         else rn = next_first;
         const R Db = mm(i, 1) + R(6) * (rc - rn);
-        yb[i * kNodeQ] = (double)(dprev + mm(i, 0) - Db * fih[i]);
-        dprev = Db * fih[i];
-        if (q == 0) gd += 2.0 * kPi * (M.node_f[i] * (double)mom[(size_t)i * kNodeQ * kMoments] +
-                                       (double)mom[(size_t)i * kNodeQ * kMoments + 1]);
+        yb[i * kNodeQ] = (float)(dprev + mm(i, 0) - Db * fih[tp(i)]);
+        dprev = Db * fih[tp(i)];
+        if (q == 0) gd += 2.0 * kPi * (M.node_f[i] * (double)mom(i, 0) +
+                                       (double)mom(i, 1));
       }
     }
-    if (i0 + cnt == n) yb[n * kNodeQ] = (double)dprev;
+    if (i0 + cnt == n) yb[n * kNodeQ] = (float)dprev;
   }
-  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+  for (int i = n + 1 + lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0f;
   if (q == 0) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gd += __shfl_xor_sync(0xffffffffu, gd, o);
@@ -1219,21 +1301,79 @@ __device__ __forceinline__ void spline_adjoint_regs(const MixedDev& M, int64_t s
   }
 }
 
+// Register-segment adjoint, one system per warp, moments and tables read
+// lane-strided from global memory (grids of more than 32 x 32 intervals).
 template <int kSeg>
 __global__ void __launch_bounds__(32) k_spline_adjoint(MixedDev M, double wscale) {
   const int q = (int)(blockIdx.x % kNodeQ), lane = threadIdx.x & 31;
   const int64_t sd = blockIdx.x / kNodeQ;
   const int n = M.nsp[sd / M.n_det];
   if (n < 3) {
-    double* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
-    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0;
+    float* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
+    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0f;
     if (q == 0 && lane == 0) M.gdir[sd] = 0.0;
     return;
   }
+  const float* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
+  auto mat = [mom](int i, int p) { return mom[(size_t)i * kNodeQ * kMoments + p]; };
+  auto tp = [](int i) { return i; };
   if (q == 0)
-    spline_adjoint_regs<kSeg, double>(M, sd, q, n, wscale);
+    spline_adjoint_seg<kSeg, double>(M, sd, q, n, (n + 31) >> 5, wscale, spline_factor<double>(M, kGfH),
+                                     spline_factor<double>(M, kGfInvH), spline_factor<double>(M, kGfLo),
+                                     spline_factor<double>(M, kGfUp), spline_factor<double>(M, kGfInvDen), mat, tp);
   else
-    spline_adjoint_regs<kSeg, float>(M, sd, q, n, wscale);
+    spline_adjoint_seg<kSeg, float>(M, sd, q, n, (n + 31) >> 5, wscale, spline_factor<float>(M, kGfH),
+                                    spline_factor<float>(M, kGfInvH), spline_factor<float>(M, kGfLo),
+                                    spline_factor<float>(M, kGfUp), spline_factor<float>(M, kGfInvDen), mat, tp);
+}
+
+// Staged adjoint (32-row segments): kFitWarps systems per block; the block
+// copies the grid tables (h, 1/h, lo, up, 1/den; FP64 for the phase systems,
+// FP32 for the transfer ones) and each warp its system's four moments per
+// interval to shared memory with coalesced loads.
+template <class R>
+__host__ __device__ __forceinline__ size_t adj_smem_bytes(int J) {
+  const size_t rows = (size_t)fit_rows(J);
+  return ((5 * rows * sizeof(R) + 15) & ~(size_t)15) + (size_t)kFitWarps * rows * sizeof(float4);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kFitWarps * 32) k_spline_adjoint_staged(MixedDev M, int64_t n_sys, double wscale) {
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  constexpr bool kPhase = std::is_same<R, double>::value;
+  const int rows = fit_rows(M.J);
+  R* tab = reinterpret_cast<R*>(adj_smem);
+  const int which[5] = {kGfH, kGfInvH, kGfLo, kGfUp, kGfInvDen};
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    const R* src = spline_factor<R>(M, which[t]);
+    for (int i = threadIdx.x; i < M.J; i += blockDim.x) tab[(size_t)t * rows + fit_pad(i)] = src[i];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sys = (int64_t)blockIdx.x * kFitWarps + warp;
+  if (sys >= n_sys) return;
+  const int64_t sd = kPhase ? sys : sys / 6;
+  const int q = kPhase ? 0 : 1 + (int)(sys % 6);
+  const int n = M.nsp[sd / M.n_det];
+  if (n < 3) {
+    float* yb = M.ybar + (size_t)sd * M.J * kNodeQ + q;
+    for (int i = lane; i < M.J; i += 32) yb[i * kNodeQ] = 0.0f;
+    if (q == 0 && lane == 0) M.gdir[sd] = 0.0;
+    return;
+  }
+  float4* ms = reinterpret_cast<float4*>(adj_smem + ((5 * (size_t)rows * sizeof(R) + 15) & ~(size_t)15)) +
+               (size_t)warp * rows;
+  const float* mom = M.mom + (size_t)sd * M.J * kNodeQ * kMoments + (size_t)q * kMoments;
+  for (int i = lane; i < n; i += 32)
+    ms[fit_pad(i)] = *reinterpret_cast<const float4*>(mom + (size_t)i * kNodeQ * kMoments);
+  __syncwarp();
+  auto mat = [ms](int i, int p) {
+    const float4 v = ms[fit_pad(i)];
+    return p == 0 ? v.x : (p == 1 ? v.y : (p == 2 ? v.z : v.w));
+  };
+  spline_adjoint_seg<32, R>(M, sd, q, n, 32, wscale, tab, tab + rows, tab + 2 * rows, tab + 3 * rows, tab + 4 * rows,
+                            mat, [](int i) { return fit_pad(i); });
 }
 
 // ------------------------------------------------------------------ exact bins
@@ -1432,29 +1572,35 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   const size_t sd = (size_t)s * M.n_det + d;
   const double tc = blocks[s].tc;
   const int j = M.ch_iv[c];
+  const FF* co = M.cphi + (sd * M.J + j) * 4;
+  const FF a = co[0], b = co[1], cc = co[2], dd = co[3];
+  const float2 nfj = M.node_ff[j];
+  const FF t = ff_mulf(M.fstep_ff, (float)(P.k0 + kb)) - ff_make(nfj.x, nfj.y);  // k0 + kb < 2^24
+  const FF ddt = dd * t;
+  const FF S0 = a + t * (b + t * (cc + ddt));
+  const FF S1 = b + t * (ff_mulf(cc, 2.0f) + ff_mulf(ddt, 3.0f));
+  const FF S2 = cc + ff_mulf(ddt, 3.0f);
+  const FF D = M.fstep_ff;
+  // anchored phase S0 + 2 pi f t_c: the product's whole cycles removed in FP64
+  // (f t_c reaches 1e6 cycles), the sum wrapped in FP64, the rest in FF
   const double fb = (double)(P.k0 + kb) * P.f_step;
-  const double t = fb - M.node_f[j];
-  const double* co = M.cphi + (sd * M.J + j) * 4;
-  const double a = co[0], b = co[1], cc = co[2], dd = co[3];
-  const double S0 = a + t * (b + t * (cc + t * dd));
-  const double S1 = b + t * (2.0 * cc + 3.0 * dd * t);
-  const double S2 = cc + 3.0 * dd * t;
-  const double D = P.f_step;
-  const double ph0 = wrap_2pi(S0 + (2.0 * kPi * fb) * tc);
-  const double ph1 = wrap_2pi(D * (S1 + 2.0 * kPi * tc));
-  const double ph2 = D * D * S2;
-  const double ph3 = D * D * D * dd;
+  const double cyc = fb * tc;
+  const double ph0d = ff_to(S0) + (2.0 * kPi) * (cyc - rint(cyc));
+  const FF ph0 = ff_from(ph0d - (2.0 * kPi) * rint(ph0d * (1.0 / (2.0 * kPi))));
+  const FF ph1 = ff_wrap_2pi(D * (S1 + ff_from(tc) * (2.0 * kPi)));
+  const FF ph2 = (D * D) * S2;
+  const FF ph3 = (D * D) * (D * dd);
   const float x0 = (float)fma(blocks[s].wf.Msec, fb, -blocks[s].wf.fpeak);
   // anchor phasor: sincos of the float head, rotated by the (tiny) tail
-  const float h0 = (float)ph0;
-  const float l0 = (float)(ph0 - (double)h0);
   float s0f, c0f;
-  sincos_poly(h0, &s0f, &c0f);
-  const float p1h = head_bits(ph1, 12), p2h = head_bits(ph2, 13), p3h = head_bits(ph3, 8);
+  sincos_poly(ph0.hi, &s0f, &c0f);
+  const float l0 = ph0.lo;
+  float p1l, p2l, p3l;
+  const float p1h = ff_head(ph1, 12, &p1l), p2h = ff_head(ph2, 13, &p2l), p3h = ff_head(ph3, 8, &p3l);
   float4* o = M.runs + (sd * M.nchunks + c) * 3;
   o[0] = make_float4(x0, fmaf(-s0f, l0, c0f), fmaf(c0f, l0, s0f), p1h);
-  o[1] = make_float4((float)(ph1 - (double)p1h), p2h, (float)(ph2 - (double)p2h), p3h);
-  o[2] = make_float4((float)(ph3 - (double)p3h), 0.0f, 0.0f, 0.0f);
+  o[1] = make_float4(p1l, p2h, p2l, p3h);
+  o[2] = make_float4(p3l, 0.0f, 0.0f, 0.0f);
 }
 
 // Warp-sum of the 28 per-lane interval moments through shared memory (rows
@@ -1755,6 +1901,28 @@ static int alloc(MixedBuffers* mb, X** ptr, size_t count) {
   return PES_OK;
 }
 
+// Spline fit of the first B samples: staged register-segment kernels (phase
+// systems in FF, transfer systems in FP32), or the global-scratch kernel for
+// grids beyond 64 x 32 intervals.
+static void launch_spline_fit(const MixedDev& M, int64_t B, cudaStream_t st) {
+  const int64_t nsd = B * M.n_det;
+  const int seg = spline_seg(M.J);
+  if (seg == 0) {
+    k_spline_fit_wide<<<(unsigned)nsd, kSplineThreads, 0, st>>>(M);
+    return;
+  }
+  const unsigned bp = (unsigned)ceil_div(nsd, (int64_t)kFitWarps);
+  const unsigned bt = (unsigned)ceil_div(nsd * 6, (int64_t)kFitWarps);
+  const size_t sp = fit_smem_bytes<FF, true>(M.J), sf = fit_smem_bytes<float, true>(M.J);
+  if (seg == 32) {
+    k_spline_fit<32, FF><<<bp, kFitWarps * 32, sp, st>>>(M, nsd);
+    k_spline_fit<32, float><<<bt, kFitWarps * 32, sf, st>>>(M, nsd * 6);
+  } else {
+    k_spline_fit<kSegMax, FF><<<bp, kFitWarps * 32, fit_smem_bytes<FF, false>(M.J), st>>>(M, nsd);
+    k_spline_fit<kSegMax, float><<<bt, kFitWarps * 32, fit_smem_bytes<float, false>(M.J), st>>>(M, nsd * 6);
+  }
+}
+
 int mixed_create(PesPlan* p) {
   const PesPlanDesc& d = p->desc;
   PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
@@ -1780,6 +1948,21 @@ int mixed_create(PesPlan* p) {
   const int64_t B = d.max_batch;
   M.J = J;
   M.n_det = nd;
+  if (spline_seg(J) == 32) {
+    PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_fit<32, FF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)fit_smem_bytes<FF, true>(J)));
+    PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_fit<32, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)fit_smem_bytes<float, true>(J)));
+    PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_adjoint_staged<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)adj_smem_bytes<double>(J)));
+    PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_adjoint_staged<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)adj_smem_bytes<float>(J)));
+  } else if (spline_seg(J) == kSegMax) {
+    PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_fit<kSegMax, FF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)fit_smem_bytes<FF, false>(J)));
+    PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_fit<kSegMax, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)fit_smem_bytes<float, false>(J)));
+  }
   M.scale = 3.085677581491367e16 / (1.476625038050124729627979840144936351e3 * 4.925490947641266978197229498498379006e-6);
   M.scale_ff = ff_from(M.scale);
   M.scale_f = (float)M.scale;
@@ -1826,7 +2009,9 @@ int mixed_create(PesPlan* p) {
   M.nblk_dense = (int32_t)ceil_div(M.nchunks, (long long)kChunkMax * (kMixThreads / 32));
   M.nblk_sparse = (int32_t)ceil_div(J, kSparseThreads);
   int rc = PES_OK;
-  double *node_f = nullptr, *yv, *scr, *cphi, *ybar, *part, *gpart, *gdir;
+  double *node_f = nullptr, *scr, *part, *gpart, *gdir;
+  float* ybar;
+  FF *yv, *cphi, *gff;
   float *mom, *kM;
   double *gh, *ginvh, *glo, *gup, *ginvden, *gcp;
   float* gf;
@@ -1856,7 +2041,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) || (rc = alloc(mb, &pbin, (size_t)nd * n)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) || (rc = alloc(mb, &pbin, (size_t)nd * n)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -1932,6 +2117,10 @@ int mixed_create(PesPlan* p) {
     for (int k = 0; k < kGfCount; ++k)
       for (int i = 0; i < J; ++i) f32[(size_t)k * J + i] = (float)(*src[k])[i];
     PES_CHECK_CUDA(cudaMemcpy(gf, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+    std::vector<FF> fff((size_t)kGfCount * J);
+    for (int k = 0; k < kGfCount; ++k)
+      for (int i = 0; i < J; ++i) fff[(size_t)k * J + i] = ff_from((*src[k])[i]);
+    PES_CHECK_CUDA(cudaMemcpy(gff, fff.data(), sizeof(FF) * fff.size(), cudaMemcpyHostToDevice));
   }
   PES_CHECK_CUDA(cudaMemcpy(chb, cb.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chl, cl.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
@@ -1963,6 +2152,7 @@ int mixed_create(PesPlan* p) {
   M.ginvden = ginvden;
   M.gcp = gcp;
   M.gf = gf;
+  M.gff = gff;
   M.tdn = tdn;
   M.tdn_ff = tdn_ff;
   M.node_ff = node_ff;
@@ -2026,12 +2216,7 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_LAUNCH();
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
-  if (spline_seg(M.J) == 32)
-    k_spline_fit<32><<<M.n_det * kNodeQ, 32, 0, st>>>(M);
-  else if (spline_seg(M.J) == kSegMax)
-    k_spline_fit<kSegMax><<<M.n_det * kNodeQ, 32, 0, st>>>(M);
-  else
-    k_spline_fit_wide<<<M.n_det, kSplineThreads, 0, st>>>(M);
+  launch_spline_fit(M, 1, st);
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
   k_run_anchors<<<dim3((unsigned)ceil_div(M.nchunks, 128), M.n_det, 1), 128, 0, st>>>(p->dev, M, blocks);
@@ -2125,12 +2310,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKSpline, st);
-    if (spline_seg(M.J) == 32)
-      k_spline_fit<32><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M);
-    else if (spline_seg(M.J) == kSegMax)
-      k_spline_fit<kSegMax><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M);
-    else
-      k_spline_fit_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M);
+    launch_spline_fit(M, B, st);
   }
   PES_CHECK_LAUNCH();
   if (grad) {
@@ -2162,12 +2342,17 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (!grad) return PES_OK;
   {
     ProfScope ps(p, kKAdjoint, st);
-    if (spline_seg(M.J) == 32)
-      k_spline_adjoint<32><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
-    else if (spline_seg(M.J) == kSegMax)
+    if (spline_seg(M.J) == 32) {
+      const int64_t nsd = B * M.n_det;
+      k_spline_adjoint_staged<double><<<(unsigned)ceil_div(nsd, (int64_t)kFitWarps), kFitWarps * 32,
+                                        adj_smem_bytes<double>(M.J), st>>>(M, nsd, 4.0 * p->dev.df);
+      k_spline_adjoint_staged<float><<<(unsigned)ceil_div(nsd * 6, (int64_t)kFitWarps), kFitWarps * 32,
+                                       adj_smem_bytes<float>(M.J), st>>>(M, nsd * 6, 4.0 * p->dev.df);
+    } else if (spline_seg(M.J) == kSegMax) {
       k_spline_adjoint<kSegMax><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
-    else
+    } else {
       k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
+    }
   }
   PES_CHECK_LAUNCH();
   {

@@ -172,7 +172,7 @@ PES_HD T quad6(const T n[3], const T M[6]) {
 template <class T>
 PES_HD T sinc_ref(const T& x) {
   // utils.py:60-79: sin(x)/x with the x == 0 guard
-  return (val(x) == 0.0) ? lift<T>(1.0) : dsin(x) / x;
+  return (x.v == 0) ? lift<T>(1.0) : dsin(x) / x;
 }
 PES_HD FF sinc_ref(const FF& x) { return ff_sinc(x); }
 PES_HD double sinc_ref(const double& x) {
