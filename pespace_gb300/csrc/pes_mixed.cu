@@ -74,14 +74,17 @@ struct MixedDev {
   FF fstep_ff;              // bin spacing
   const float2* node_ff;    // [J] node frequencies (hi, lo)
   const float4* tdn_ff;     // [n_det][J] node delay factor D (re hi, re lo, im hi, im lo)
-  float2* pbin;             // [n_det][nbins] TDI generation prefactor P(f) per bin (FP32 of the FP64 value)
   const int32_t* ch_begin;  // [nchunks] first bin of the run
   const int32_t* ch_len;    // [nchunks]
   const int32_t* ch_iv;     // [nchunks] spline interval of the run
   const float* bin_t;       // [nbins] f_i - f_iv(i)
   float4* runs;             // [B][n_det][nchunks][3] per-run phase anchors (RunPhase, 12 floats)
-  float2* dat;              // [n_det][3][nbins] scaled data
-  float* wgt;               // [n_det][3][nbins] inverse scaled PSD (0 off the channel mask)
+  // Per (detector, bin) inputs of the dense stage, packed for three 16-byte loads:
+  //   part 0: d_A (re, im), d_E (re, im)     part 1: d_T (re, im), w_A, w_E
+  //   part 2: w_T, P (re, im), f_i - f_iv(i)
+  // (d scaled data, w inverse scaled PSD, 0 off the channel mask; P the TDI
+  // generation prefactor)
+  float4* pk;               // [n_det][3][nbins]
   float2* dd;               // [n_det][nbins] sum_c |d|^2 / S in FP64, as a float-float pair (hi, lo)
   int32_t* nsp;             // [B] spline intervals of the sample (nodes 0..nsp)
   int32_t* nch;             // [B] runs with a live bin
@@ -1685,7 +1688,9 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         }
         const int64_t i = (int64_t)kb + lane;
         if (lane < len && i < kcut) {
-          const float t = M.bin_t[i];
+          const float4* pkd = M.pk + (size_t)d * 3 * P.nbins;
+          const float4 pk0 = pkd[i], pk1 = pkd[P.nbins + i], pk2 = pkd[2 * P.nbins + i];
+          const float t = pk2.w;
           const float u = (float)lane;
           const float u2 = u * u, u3 = u2 * u;
           // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike
@@ -1704,10 +1709,9 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           {
             // TDI generation prefactor P(f): its zeros (f L = k/2) stay out of the
             // splines; with h = G (c - i s) the factor multiplies c - i s
-            const float2 pf = M.pbin[(size_t)d * P.nbins + i];
             // explicit FMAs: the lnL and lnL+gradient kernels must round alike
-            const float c2 = fmaf(pf.x, cph, pf.y * sph);
-            const float s2 = fmaf(pf.x, sph, -(pf.y * cph));
+            const float c2 = fmaf(pk2.y, cph, pk2.z * sph);
+            const float s2 = fmaf(pk2.y, sph, -(pk2.z * cph));
             cph = c2;
             sph = s2;
           }
@@ -1735,8 +1739,9 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             const float hr = fmaf(gr, cph, gi * sph);
             const float hi = fmaf(gi, cph, -(gr * sph));
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
-            const float2 dv = M.dat[off];
-            const float w = M.wgt[off];
+            const float2 dv = ch == 0 ? make_float2(pk0.x, pk0.y)
+                                      : (ch == 1 ? make_float2(pk0.z, pk0.w) : make_float2(pk1.x, pk1.y));
+            const float w = ch == 0 ? pk1.z : (ch == 1 ? pk1.w : pk2.x);
             const float er = dv.x - hr, ei = dv.y - hi;
             term = fmaf(fmaf(er, er, ei * ei), w, term);
             const float h2 = fmaf(hr, hr, hi * hi);
@@ -1872,19 +1877,22 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.nbins) return;
   double dd = 0.0;
+  float dr[3], di[3], wf[3];
   for (int ch = 0; ch < 3; ++ch) {
-    const size_t off = ((size_t)det * 3 + ch) * P.nbins + i;
     const double2 v = data[ch * P.nbins + i];
-    M.dat[off] = make_float2((float)(v.x * M.scale), (float)(v.y * M.scale));
+    dr[ch] = (float)(v.x * M.scale);
+    di[ch] = (float)(v.y * M.scale);
     const bool on = (P.chan_mask >> ch) & 1;
-    const double w = on ? 1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale) : 0.0;
-    M.wgt[off] = (float)w;
+    wf[ch] = on ? (float)(1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale)) : 0.0f;
     if (on) dd += (v.x * v.x + v.y * v.y) / psd[ch * P.nbins + i];
   }
   const float hi = (float)dd;
   M.dd[(size_t)det * P.nbins + i] = make_float2(hi, (float)(dd - (double)hi));
   const TdiFactor tf = P.tdi[(size_t)det * P.nbins + i];
-  M.pbin[(size_t)det * P.nbins + i] = make_float2((float)tf.pre, (float)tf.pim);
+  float4* pk = M.pk + (size_t)det * 3 * P.nbins;
+  pk[i] = make_float4(dr[0], di[0], dr[1], di[1]);
+  pk[P.nbins + i] = make_float4(dr[2], di[2], wf[0], wf[1]);
+  pk[2 * P.nbins + i] = make_float4(wf[2], (float)tf.pre, (float)tf.pim, M.bin_t[i]);
 }
 
 // ------------------------------------------------------------------ host side
@@ -2018,7 +2026,6 @@ int mixed_create(PesPlan* p) {
   TdiFactor* tdn;
   float4* tdn_ff;
   float2* node_ff;
-  float2* pbin;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
@@ -2028,20 +2035,18 @@ int mixed_create(PesPlan* p) {
   float* kF;
   float* bin_t;
   float4* runs;
-  float2* dat;
-  float* wgt;
+  float4* pk;
   float2* ddv;
   float4* cg;
   float* cglo;
   const size_t sd = (size_t)B * nd;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) ||
-      (rc = alloc(mb, &runs, (size_t)B * nd * M.nchunks * 3)) || (rc = alloc(mb, &dat, (size_t)nd * 3 * n)) ||
-      (rc = alloc(mb, &wgt, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
+      (rc = alloc(mb, &runs, (size_t)B * nd * M.nchunks * 3)) || (rc = alloc(mb, &pk, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) || (rc = alloc(mb, &pbin, (size_t)nd * n)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -2126,8 +2131,7 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaMemcpy(chl, cl.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(chi, ci.data(), sizeof(int32_t) * M.nchunks, cudaMemcpyHostToDevice));
   PES_CHECK_CUDA(cudaMemcpy(bin_t, bt.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
-  PES_CHECK_CUDA(cudaMemset(dat, 0, sizeof(float2) * nd * 3 * n));
-  PES_CHECK_CUDA(cudaMemset(wgt, 0, sizeof(float) * nd * 3 * n));
+  PES_CHECK_CUDA(cudaMemset(pk, 0, sizeof(float4) * nd * 3 * n));
   PES_CHECK_CUDA(cudaMemset(ddv, 0, sizeof(float2) * nd * n));
   M.node_f = node_f;
   M.ch_begin = chb;
@@ -2135,8 +2139,7 @@ int mixed_create(PesPlan* p) {
   M.ch_iv = chi;
   M.bin_t = bin_t;
   M.runs = runs;
-  M.dat = dat;
-  M.wgt = wgt;
+  M.pk = pk;
   M.dd = ddv;
   M.nsp = nsp;
   M.nch = nch;
@@ -2156,7 +2159,6 @@ int mixed_create(PesPlan* p) {
   M.tdn = tdn;
   M.tdn_ff = tdn_ff;
   M.node_ff = node_ff;
-  M.pbin = pbin;
   M.yv = yv;
   M.scr = scr;
   M.cphi = cphi;
