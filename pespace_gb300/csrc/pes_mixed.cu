@@ -106,8 +106,10 @@ struct MixedDev {
   FF* yv;                   // [B][n_det][7][J] node values (float-float, node fastest)
   double* scr;              // [B][n_det][J][7] spline scratch
   FF* cphi;                 // [B][n_det][J][4] phase spline coefficients (float-float)
-  float4* cg;               // [B][n_det][J][6] transfer spline coefficients (FP32: a_hi, b, c, d)
-  float* cglo;              // [B][n_det][J][6] a - a_hi (the value at the left node in float-float)
+  // [B][n_det][J][8] transfer spline coefficients: slots 0-5 (a_hi, b, c, d) of
+  // quantities 1..6 in FP32, slots 6-7 the six a - a_hi (the value at the left
+  // node in float-float), so one interval is eight 16-byte loads
+  float4* cg;
   float* mom;               // [B][n_det][J][7][4] adjoint moments (FP32 warp sums, FP32 atomics)
   float* ybar;              // [B][n_det][J][7] node adjoints (FP32: the derivative passes run in FP32)
   double* part;             // [B][nblk_dense] lnL partials
@@ -663,8 +665,8 @@ __device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t s
     const float cc = 0.5f * mi;
     const float dc = (mj - mi) * fih[i] * (1.0f / 6.0f);
     const FF a = yq[i];
-    M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(a.hi, bc, cc, dc);
-    M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = a.lo;
+    M.cg[((size_t)sd * M.J + i) * 8 + (q - 1)] = make_float4(a.hi, bc, cc, dc);
+    reinterpret_cast<float*>(M.cg + ((size_t)sd * M.J + i) * 8 + 6)[q - 1] = a.lo;
     mi = mj;
   }
 }
@@ -835,8 +837,8 @@ __global__ void __launch_bounds__(kSplineThreads) k_spline_fit_wide(MixedDev M) 
       o[3] = ff_from(dc);
     } else {
       const float ahi = (float)a;
-      M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(ahi, (float)bc, (float)cc, (float)dc);
-      M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(a - (double)ahi);
+      M.cg[((size_t)sd * M.J + i) * 8 + (q - 1)] = make_float4(ahi, (float)bc, (float)cc, (float)dc);
+      reinterpret_cast<float*>(M.cg + ((size_t)sd * M.J + i) * 8 + 6)[q - 1] = (float)(a - (double)ahi);
     }
     mi = mj;
     a = an;
@@ -1115,8 +1117,8 @@ __device__ __forceinline__ void spline_fit_staged(const MixedDev& M, int64_t sd,
         o[2] = cc;
         o[3] = dc;
       } else {
-        M.cg[((size_t)sd * M.J + i) * 6 + (q - 1)] = make_float4(yc.hi, bc, cc, dc);
-        M.cglo[((size_t)sd * M.J + i) * 6 + (q - 1)] = yc.lo;
+        M.cg[((size_t)sd * M.J + i) * 8 + (q - 1)] = make_float4(yc.hi, bc, cc, dc);
+        reinterpret_cast<float*>(M.cg + ((size_t)sd * M.J + i) * 8 + 6)[q - 1] = yc.lo;
       }
       yc = yn;
     }
@@ -1715,16 +1717,21 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             cph = c2;
             sph = s2;
           }
-          const float4* G = M.cg + (sd * M.J + j) * 6;
-          const float* Glo = M.cglo + (sd * M.J + j) * 6;
+          const float4* G = M.cg + (sd * M.J + j) * 8;
+          const float4 gl0 = G[6], gl1 = G[7];
+          const float Glo[6] = {gl0.x, gl0.y, gl0.z, gl0.w, gl1.x, gl1.y};
           const float xk = fmaf(kSlope, u, r.x0);
           const float x2 = xk > 0.0f ? xk * xk : 0.0f;
           float kink[6];
 #pragma unroll
           for (int q = 0; q < 6; ++q) kink[q] = 0.0f;
           if (xk > 0.0f) {
+            const float4* KF4 = reinterpret_cast<const float4*>(KF);  // 64-byte aligned rows
+            const float4 k0 = KF4[0], k1 = KF4[1], k2 = KF4[2], k3 = KF4[3];
+            const float kfh[6] = {k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+            const float kfl[6] = {k2.x, k2.y, k2.z, k2.w, k3.x, k3.y};
 #pragma unroll
-            for (int q = 0; q < 6; ++q) kink[q] = fmaf(KF[2 + q], x2, KF[8 + q] * x2);
+            for (int q = 0; q < 6; ++q) kink[q] = fmaf(kfh[q], x2, kfl[q] * x2);
           }
           float term = 0.0f;  // |d - h|^2 w
           float cross = 0.0f;  // (|h|^2 - 2 Re(d^* h)) w
@@ -2038,7 +2045,6 @@ int mixed_create(PesPlan* p) {
   float4* pk;
   float2* ddv;
   float4* cg;
-  float* cglo;
   const size_t sd = (size_t)B * nd;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) ||
@@ -2047,7 +2053,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
       (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) ||
-      (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 6)) || (rc = alloc(mb, &cglo, sd * J * 6)) ||
+      (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 8)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
@@ -2163,7 +2169,6 @@ int mixed_create(PesPlan* p) {
   M.scr = scr;
   M.cphi = cphi;
   M.cg = cg;
-  M.cglo = cglo;
   M.mom = mom;
   M.ybar = ybar;
   M.part = part;
