@@ -2,7 +2,7 @@
 
 Mixed plan, kernel class ``dense_mixed`` (one ``k_dense_mixed`` launch per
 call).  Its bins are compute work on data that stays in L2 (125410 bins x
-48 B per detector), so the bound is the FP32 pipe.  FP32 arithmetic per bin
+48 B per detector, three float4 rows per bin), so the bound is the FP32 pipe.  FP32 arithmetic per bin
 and detector, counted from the kernel source (FMA = 2 flops, add/mul = 1):
 
   phase advance: three exact 2 pi reductions and the FP32 tails      38
@@ -28,7 +28,7 @@ the launch's dense bins.
 """
 
 FP32_FLOPS_PER_DENSE_BIN = {"lnl": 244, "grad": 341}
-DRAM_BYTES_PER_DENSE_BIN = 4.97  # (93.04 MB + 4.34 MB) / 19 595 338 bins, ncu --set full, 256 samples
+DRAM_BYTES_PER_DENSE_BIN = 5.14  # (95.76 MB + 4.92 MB) / 19 595 338 bins, ncu --set full, 256 samples
 
 
 def roofline(kernel_class, launches_ms, steps, work, grad, fp32_peak_tflops):
