@@ -33,15 +33,19 @@
 
 namespace pes {
 
+// Trivially default-constructible (usable in shared memory); the explicit
+// conversions let it serve as the value type of the dual numbers (their
+// tangents take the head, FP64 constants are split once).
 struct FF {
   float hi, lo;
+  FF() = default;
+  PES_HD explicit FF(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+  PES_HD explicit operator float() const { return hi; }
+  PES_HD explicit operator double() const { return (double)hi + (double)lo; }
 };
 
 PES_HD FF ff_make(float hi, float lo) { FF r; r.hi = hi; r.lo = lo; return r; }
-PES_HD FF ff_from(double x) {
-  const float h = (float)x;
-  return ff_make(h, (float)(x - (double)h));
-}
+PES_HD FF ff_from(double x) { return FF(x); }
 PES_HD double ff_to(const FF& a) { return (double)a.hi + (double)a.lo; }
 
 PES_HD FF ff_two_sum(float a, float b) {
@@ -271,5 +275,13 @@ PES_HD FF ff_sinc(const FF& x) {
   dsincos(x, &s, &c);
   return s / x;
 }
+
+// value functions of the dual numbers with FF values
+PES_HD FF vsqrt(const FF& x) { return dsqrt(x); }
+PES_HD FF vcbrt(const FF& x) { return dcbrt(x); }
+PES_HD FF vlog(const FF& x) { return dlog(x); }
+PES_HD FF vexp(const FF& x) { return dexp(x); }
+PES_HD FF vatan(const FF& x) { return datan(x); }
+PES_HD void vsincos(const FF& x, FF* s, FF* c) { dsincos(x, s, c); }
 
 }  // namespace pes

@@ -215,6 +215,30 @@ __device__ __forceinline__ void narrow_block_ff(const SampleBlock<double>& a, Sa
   }
 }
 
+// The gradient block (FP64 values, FP32 tangents) with float-float values.
+__device__ __forceinline__ void narrow_block_dual_ff(const SampleBlock<GradScalar>& a,
+                                                     SampleBlock<Dual<kMixNT, float, FF>>& b) {
+  using TE = Dual<kMixNT, float, FF>;
+  static_assert(sizeof(PhenomDCoef<TE>) / sizeof(TE) == sizeof(PhenomDCoef<GradScalar>) / sizeof(GradScalar),
+                "coefficient block must be an array of scalars");
+  static_assert(sizeof(Polar<TE>) / sizeof(TE) == sizeof(Polar<GradScalar>) / sizeof(GradScalar),
+                "polarisation block must be an array of scalars");
+  constexpr int nv = (int)((sizeof(PhenomDCoef<GradScalar>) + sizeof(Polar<GradScalar>)) / sizeof(GradScalar)) + 1;
+  const GradScalar* src = reinterpret_cast<const GradScalar*>(&a);
+  TE* dst = reinterpret_cast<TE*>(&b);
+  for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+    dst[j].v = ff_from(src[j].v);
+#pragma unroll
+    for (int k = 0; k < kMixNT; ++k) dst[j].d[k] = src[j].d[k];
+  }
+  if (threadIdx.x == 0) {
+    b.fcut = a.fcut;
+    b.kcut = a.kcut;
+    b.status = a.status;
+    b.pad = 0;
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void load_block(const SampleBlock<T>* blocks, int s, SampleBlock<T>& sb) {
   const int n8 = sizeof(SampleBlock<T>) / 8;
@@ -1391,9 +1415,11 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
                                                          const SampleBlock<T>* __restrict__ blocks,
                                                          double2* __restrict__ model) {
   constexpr int NV = kMode == 1 ? 11 : 1;
-  constexpr bool kFF = kMode != 1;  // value passes evaluate the bins in float-float arithmetic
+  constexpr bool kFF = kMode != 1;  // value passes: float-float values
+  // the gradient pass evaluates with float-float values and FP32 tangents
+  using TE = std::conditional_t<kMode == 1, Dual<kMixNT, float, FF>, FF>;
   __shared__ SampleBlock<T> sb;
-  __shared__ SampleBlock<FF> sbf;
+  __shared__ SampleBlock<TE> sbf;
   __shared__ double red[kExactThreads / 32][NV];
   const int s = blockIdx.y;
   const int xb = M.xbin[s];
@@ -1402,8 +1428,10 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   __syncthreads();
   if constexpr (kFF) {
     narrow_block_ff(sb, sbf);
-    __syncthreads();
+  } else {
+    narrow_block_dual_ff(sb, sbf);
   }
+  __syncthreads();
   double acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) acc[k] = 0.0;
@@ -1438,35 +1466,38 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
           }
           continue;
         }
-        const double f = (double)(P.k0 + i) * P.f_step;
-        T y[kNodeQ];
-        node_eval<T>(P, M, sb, d, P.tdi[(size_t)d * P.nbins + i], f, y);
-        const T ph = y[0] + (2.0 * kPi * f) * sb.tc;
-        T sn, cs;
-        dsincos(ph, &sn, &cs);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          // h = G exp(-i ph)
-          const T hr = (y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn) * inv_scale;
-          const T hi = (y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn) * inv_scale;
-          const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
-          if constexpr (kMode == 2) {
-            model[off] = make_double2(val(hr), val(hi));
-            continue;
+        if constexpr (kMode == 1) {
+          const double f = (double)(P.k0 + i) * P.f_step;
+          TE y[kNodeQ];
+          node_eval<TE>(P, M, sbf, d, P.tdi[(size_t)d * P.nbins + i], f, y);
+          TE ph = y[0] + (2.0 * kPi * f) * sbf.tc;
+          {  // whole turns removed in FP64 (the phase reaches 1e6 rad); the tangents are unchanged
+            const double phd = ff_to(ph.v);
+            ph.v = ff_from(phd - (2.0 * kPi) * rint(phd * (1.0 / (2.0 * kPi))));
           }
-          const double w = P.w[off];
-          const double2 dv = P.data[off];
-          const double rr = dv.x - val(hr), ri = dv.y - val(hi);
-          if constexpr (kMode == 0) {
-            acc[0] += w * (rr * rr + ri * ri);
-          } else if constexpr (kMode == 1) {
-            // d/dtheta of w |d - h|^2 = -2 w Re((d - h)^* dh)
+          TE sn, cs;
+          dsincos(ph, &sn, &cs);
+          float gk[kMixNT];  // this bin's -2 w Re((d - h)^* dh/dtheta) over the channels (FP32)
 #pragma unroll
-            for (int k = 0; k < kMixNT; ++k)
-              acc[kSlotParam[k]] -= 2.0 * w * (rr * (double)hr.d[k] + ri * (double)hi.d[k]);
-            acc[4] += 2.0 * w * (rr * hr.v + ri * hi.v);  // dh/dlnD_L = -h
-            acc[9] += 4.0 * w * (rr * hi.v - ri * hr.v);  // dh/dphi_c = 2 i h
+          for (int k = 0; k < kMixNT; ++k) gk[k] = 0.0f;
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            // h = G exp(-i ph)
+            const TE hr = (y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn) * inv_scale;
+            const TE hi = (y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn) * inv_scale;
+            const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
+            const double w = P.w[off];
+            const double2 dv = P.data[off];
+            const double hrv = ff_to(hr.v), hiv = ff_to(hi.v);
+            const double rr = dv.x - hrv, ri = dv.y - hiv;
+            const float wr = (float)(-2.0 * w * rr), wi = (float)(-2.0 * w * ri);
+#pragma unroll
+            for (int k = 0; k < kMixNT; ++k) gk[k] = fmaf(wr, hr.d[k], fmaf(wi, hi.d[k], gk[k]));
+            acc[4] += 2.0 * w * (rr * hrv + ri * hiv);  // dh/dlnD_L = -h
+            acc[9] += 4.0 * w * (rr * hiv - ri * hrv);  // dh/dphi_c = 2 i h
           }
+#pragma unroll
+          for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += (double)gk[k];
         }
       }
     }

@@ -175,6 +175,34 @@ PES_HD T sinc_ref(const T& x) {
   return (x.v == 0) ? lift<T>(1.0) : dsin(x) / x;
 }
 PES_HD FF sinc_ref(const FF& x) { return ff_sinc(x); }
+// FF value, FP32 tangents: d/dx sin(x)/x = x sum_k (-1)^k 2k x^(2k-2) / (2k+1)!
+// (k = 1..8, truncation below 2e-9 relative for |x| <= 2), (cos x - sinc x) / x beyond.
+template <int N, class D>
+PES_HD Dual<N, D, FF> sinc_ref(const Dual<N, D, FF>& x) {
+  Dual<N, D, FF> r;
+  r.v = ff_sinc(x.v);
+  const float xf = x.v.hi;
+  float ds;
+  if (fabsf(xf) <= 2.0f) {
+    const float z = xf * xf;
+    float p = 1.0f / 22230464256000.0f;
+    p = fmaf(p, z, -1.0f / 93405312000.0f);
+    p = fmaf(p, z, 1.0f / 518918400.0f);
+    p = fmaf(p, z, -1.0f / 3991680.0f);
+    p = fmaf(p, z, 1.0f / 45360.0f);
+    p = fmaf(p, z, -1.0f / 840.0f);
+    p = fmaf(p, z, 1.0f / 30.0f);
+    p = fmaf(p, z, -1.0f / 3.0f);
+    ds = p * xf;
+  } else {
+    FF sn, cs;
+    dsincos(x.v, &sn, &cs);
+    ds = (cs.hi - r.v.hi) / xf;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * D(ds);
+  return r;
+}
 PES_HD double sinc_ref(const double& x) {
   if (::fabs(x) <= 2.0) {
     double s, ds;
