@@ -148,7 +148,7 @@ extern "C" int pes_fisher_batch(PesPlan* p, const double* theta, int64_t B, doub
     PES_CHECK_CUDA(cudaMalloc(&p->fisher_partial, sizeof(double) * M * kFisherBlocks * kPairs));
   }
   auto* blocks = reinterpret_cast<SampleBlock<FisherScalar>*>(p->fisher_blocks);
-  k_setup<FisherScalar><<<(unsigned)ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B, 0, blocks);
+  k_setup<FisherScalar><<<(unsigned)ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, theta, B, 0, blocks);
   PES_CHECK_LAUNCH();
   k_fisher_bins<<<dim3(kFisherBlocks, (unsigned)B), kFisherThreads, 0, st>>>(p->dev, blocks, p->fisher_partial);
   PES_CHECK_LAUNCH();

@@ -146,6 +146,12 @@ struct MixedBuffers {
   // run on a side stream beside the sparse/spline/dense stages.
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, xready = nullptr;
+  // Second stream of the main sequence: the transfer-spline fit beside the
+  // phase fit and the run anchors, the transfer adjoint beside the phase
+  // adjoint, the second backward tangent pass beside the first.
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_padj = nullptr, ev_tadj = nullptr,
+              ev_bwd = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -1950,22 +1956,24 @@ static int alloc(MixedBuffers* mb, X** ptr, size_t count) {
 // Spline fit of the first B samples: staged register-segment kernels (phase
 // systems in FF, transfer systems in FP32), or the global-scratch kernel for
 // grids beyond 64 x 32 intervals.
-static void launch_spline_fit(const MixedDev& M, int64_t B, cudaStream_t st) {
+// The phase systems on st_phase, the transfer systems on st_transfer (the
+// same stream, or a second one so that the two fits overlap).
+static void launch_spline_fit(const MixedDev& M, int64_t B, cudaStream_t st_phase, cudaStream_t st_transfer) {
   const int64_t nsd = B * M.n_det;
   const int seg = spline_seg(M.J);
   if (seg == 0) {
-    k_spline_fit_wide<<<(unsigned)nsd, kSplineThreads, 0, st>>>(M);
+    k_spline_fit_wide<<<(unsigned)nsd, kSplineThreads, 0, st_phase>>>(M);
     return;
   }
   const unsigned bp = (unsigned)ceil_div(nsd, (int64_t)kFitWarps);
   const unsigned bt = (unsigned)ceil_div(nsd * 6, (int64_t)kFitWarps);
-  const size_t sp = fit_smem_bytes<FF, true>(M.J), sf = fit_smem_bytes<float, true>(M.J);
   if (seg == 32) {
-    k_spline_fit<32, FF><<<bp, kFitWarps * 32, sp, st>>>(M, nsd);
-    k_spline_fit<32, float><<<bt, kFitWarps * 32, sf, st>>>(M, nsd * 6);
+    k_spline_fit<32, FF><<<bp, kFitWarps * 32, fit_smem_bytes<FF, true>(M.J), st_phase>>>(M, nsd);
+    k_spline_fit<32, float><<<bt, kFitWarps * 32, fit_smem_bytes<float, true>(M.J), st_transfer>>>(M, nsd * 6);
   } else {
-    k_spline_fit<kSegMax, FF><<<bp, kFitWarps * 32, fit_smem_bytes<FF, false>(M.J), st>>>(M, nsd);
-    k_spline_fit<kSegMax, float><<<bt, kFitWarps * 32, fit_smem_bytes<float, false>(M.J), st>>>(M, nsd * 6);
+    k_spline_fit<kSegMax, FF><<<bp, kFitWarps * 32, fit_smem_bytes<FF, false>(M.J), st_phase>>>(M, nsd);
+    k_spline_fit<kSegMax, float><<<bt, kFitWarps * 32, fit_smem_bytes<float, false>(M.J), st_transfer>>>(M,
+                                                                                                       nsd * 6);
   }
 }
 
@@ -1987,6 +1995,9 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->fork, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->join, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->xready, cudaEventDisableTiming));
+  PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->aux, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_padj, &mb->ev_tadj, &mb->ev_bwd})
+    PES_CHECK_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
   const int J = d.n_sparse;
@@ -2219,6 +2230,11 @@ int mixed_create(PesPlan* p) {
 void mixed_destroy(PesPlan* p) {
   if (!p->mixed) return;
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
+  if (p->mixed->aux) cudaStreamSynchronize(p->mixed->aux);
+  for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_padj,
+                        p->mixed->ev_tadj, p->mixed->ev_bwd})
+    if (e) cudaEventDestroy(e);
+  if (p->mixed->aux) cudaStreamDestroy(p->mixed->aux);
   for (void* a : p->mixed->allocs) cudaFree(a);
   if (p->mixed->fork) cudaEventDestroy(p->mixed->fork);
   if (p->mixed->join) cudaEventDestroy(p->mixed->join);
@@ -2254,7 +2270,7 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_LAUNCH();
   k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
-  launch_spline_fit(M, 1, st);
+  launch_spline_fit(M, 1, st, st);
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
   k_run_anchors<<<dim3((unsigned)ceil_div(M.nchunks, 128), M.n_det, 1), 128, 0, st>>>(p->dev, M, blocks);
@@ -2295,7 +2311,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
   {
     ProfScope ps(p, kKSetup, st);
-    k_setup<double><<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B, 0, blocks);
+    k_setup<double><<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, theta, B, 0, blocks);
   }
   PES_CHECK_LAUNCH();
   {
@@ -2309,7 +2325,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->fork, 0));
   {
     ProfScope ps(p, kKOther, side);
-    k_mixed_ranges<1><<<ceil_div(B, 64), 64, 0, side>>>(M, blocks, B);
+    k_mixed_ranges<1><<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, side>>>(M, blocks, B);
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->xready, side));
@@ -2321,7 +2337,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (grad) {
     {
       ProfScope ps(p, kKSetup, side);
-      k_setup_grad<<<ceil_div(B, 64), 64, 0, side>>>(p->dev, theta, B,
+      k_setup_grad<<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, side>>>(p->dev, theta, B,
                                                      reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks),
                                                      reinterpret_cast<SampleBlock<NodeGradA>*>(M.gblocksA),
                                                      reinterpret_cast<SampleBlock<NodeGradB>*>(M.gblocksB));
@@ -2337,7 +2353,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
   {
     ProfScope ps(p, kKSparse, st);
-    k_kink<<<ceil_div(B * (int64_t)M.n_det, 64), 64, 0, st>>>(p->dev, M, G, blocks, B);
+    k_kink<<<ceil_div(B * (int64_t)M.n_det, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, M, G, blocks, B);
   }
   PES_CHECK_LAUNCH();
   {
@@ -2347,10 +2363,16 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   {
+    // the phase fit here, the transfer fit on the second stream
+    cudaStream_t aux = p->mixed->aux;
+    PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_nodes, st));
+    PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_nodes, 0));
     ProfScope ps(p, kKSpline, st);
-    launch_spline_fit(M, B, st);
+    ProfScope ps_aux(p, kKSpline, aux);
+    launch_spline_fit(M, B, st, aux);
   }
   PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tfit, p->mixed->aux));
   if (grad) {
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
     PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
@@ -2362,6 +2384,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     k_run_anchors<<<grid, 128, 0, st>>>(p->dev, M, blocks);
   }
   PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_tfit, 0));
   {
     ProfScope ps(p, kKDenseMixed, st);
     dim3 grid(M.nblk_dense, (unsigned)B);
@@ -2371,6 +2394,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
       k_dense_mixed<0><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_dense, st));
   PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->join, 0));
   {
     ProfScope ps(p, kKFinalize, st);
@@ -2378,33 +2402,50 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   if (!grad) return PES_OK;
-  {
-    ProfScope ps(p, kKAdjoint, st);
-    if (spline_seg(M.J) == 32) {
-      const int64_t nsd = B * M.n_det;
+  // node adjoints: phase systems here, transfer systems on the second stream;
+  // then the two tangent passes of the backward node stage side by side
+  cudaStream_t aux = p->mixed->aux;
+  const double ws = 4.0 * p->dev.df;
+  const dim3 sgrid(M.nblk_sparse, M.n_det, (unsigned)B);
+  if (spline_seg(M.J) == 32) {
+    const int64_t nsd = B * M.n_det;
+    {
+      ProfScope ps(p, kKAdjoint, st);
       k_spline_adjoint_staged<double><<<(unsigned)ceil_div(nsd, (int64_t)kFitWarps), kFitWarps * 32,
-                                        adj_smem_bytes<double>(M.J), st>>>(M, nsd, 4.0 * p->dev.df);
-      k_spline_adjoint_staged<float><<<(unsigned)ceil_div(nsd * 6, (int64_t)kFitWarps), kFitWarps * 32,
-                                       adj_smem_bytes<float>(M.J), st>>>(M, nsd * 6, 4.0 * p->dev.df);
-    } else if (spline_seg(M.J) == kSegMax) {
-      k_spline_adjoint<kSegMax><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, 4.0 * p->dev.df);
-    } else {
-      k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, 4.0 * p->dev.df);
+                                        adj_smem_bytes<double>(M.J), st>>>(M, nsd, ws);
     }
+    PES_CHECK_LAUNCH();
+    PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_dense, 0));
+    {
+      ProfScope ps(p, kKAdjoint, aux);
+      k_spline_adjoint_staged<float><<<(unsigned)ceil_div(nsd * 6, (int64_t)kFitWarps), kFitWarps * 32,
+                                       adj_smem_bytes<float>(M.J), aux>>>(M, nsd * 6, ws);
+    }
+    PES_CHECK_LAUNCH();
+  } else {
+    ProfScope ps(p, kKAdjoint, st);
+    if (spline_seg(M.J) == kSegMax)
+      k_spline_adjoint<kSegMax><<<(unsigned)(B * M.n_det * kNodeQ), 32, 0, st>>>(M, ws);
+    else
+      k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, ws);
+    PES_CHECK_LAUNCH();
+  }
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_padj, st));
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tadj, aux));
+  PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_padj, 0));
+  {
+    ProfScope ps(p, kKAdjoint, aux);
+    k_sparse_bwd<kPassB, kPassA><<<sgrid, kSparseThreads, 0, aux>>>(p->dev, M, G, ws);
   }
   PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_bwd, aux));
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_tadj, 0));
   {
     ProfScope ps(p, kKAdjoint, st);
-    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
-    k_sparse_bwd<kPassA, 0><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
+    k_sparse_bwd<kPassA, 0><<<sgrid, kSparseThreads, 0, st>>>(p->dev, M, G, ws);
   }
   PES_CHECK_LAUNCH();
-  {
-    ProfScope ps(p, kKAdjoint, st);
-    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
-    k_sparse_bwd<kPassB, kPassA><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, 4.0 * p->dev.df);
-  }
-  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_bwd, 0));
   {
     ProfScope ps(p, kKFinalize, st);
     k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, B, -2.0 * p->dev.df, grad);

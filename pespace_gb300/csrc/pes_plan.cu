@@ -222,7 +222,7 @@ int run_dense(PesPlan* p, const double* theta, int64_t B, int pass, double* lnl,
   SampleBlock<T>* blocks = reinterpret_cast<SampleBlock<T>*>(p->blocks);
   {
     ProfScope ps(p, kKSetup, st);
-    k_setup<T><<<ceil_div(B, 64), 64, 0, st>>>(p->dev, theta, B, pass, blocks);
+    k_setup<T><<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, theta, B, pass, blocks);
   }
   PES_CHECK_LAUNCH();
   const int nblk = (int)ceil_div(p->desc.nbins, kDenseBinsPerBlock);

@@ -126,6 +126,12 @@ namespace pes {
 
 constexpr int kGradTangents = 4;  // tangents per gradient pass (3 passes for 11 parameters)
 
+// Threads per block of the per-sample kernels (set-up, ranges, kink): each
+// thread runs a long FP64 chain, and GB300 issues FP64 at 2 lanes per cycle
+// per SM, so small blocks spread the samples over all SMs instead of
+// queueing 64 lanes on each SM's FP64 pipe.
+constexpr int kPerSampleThreads = 8;
+
 // ------------------------------------------------------------------ scalar helpers
 template <class T> struct Seed;
 template <> struct Seed<double> {
