@@ -121,6 +121,15 @@ int pes_whittle_lnl_noalloc(const double* data, const double* response, const do
 int pes_phenomd(const double* theta /* host */, const double* freqs, int64_t n, double f_ref, double f_cut_hz,
                 double* hp, double* hc, double* tf, void* stream);
 
+/* Post-Newtonian time-frequency map of the lalsimulation waveform interface:
+ * replaces get_PN_d_phase (pespace/waveform/interface_lalsim.py:297-482),
+ * which fills the `tf` entry of the waveform container for lalsimulation's FD
+ * approximants (interface_lalsim.py:279-281).  params: device, (B, 4) doubles
+ * (mass_1, mass_2 [Msun, detector frame], spin_1z, spin_2z); freqs: device,
+ * (n) [Hz]; tf: device, (B, n) seconds, t(f_ISCO) = 0 and 0 above f_ISCO.
+ * FP64.  1 <= B <= 65535 per call. */
+int pes_pn_tf(const double* params, int64_t B, const double* freqs, int64_t n, double* tf, void* stream);
+
 /* ---------------------------------------------------------------- plans --
  * Batched lnL / lnL+gradient over B parameter samples: the per-sample loop of
  * LikelihoodBilbyInterfaceTaichi.log_likelihood (interface_bilby.py:78-116) and

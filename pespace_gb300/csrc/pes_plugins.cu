@@ -186,6 +186,102 @@ __global__ void k_phenomd(ThetaArg th, double f_ref, double f_cut, const double*
 using namespace pes;
 
 // ------------------------------------------------------------------ C ABI
+// ------------------------------------------------------------------ PN t(f)
+// Post-Newtonian time-frequency map of the reference's lalsimulation interface
+// (pespace/waveform/interface_lalsim.py:297-482): aligned-spin TaylorF2 phase
+// Psi(x) = sum_k (a_k + b_k ln(pi x)) x^((k-5)/3), x = M f, and
+// t(f) = -M/(2 pi) (Psi'(x) - Psi'(x_ISCO)) below x_ISCO = 6^-3/2 / pi, 0 above.
+// The coefficient table is the published expansion the reference uses (its
+// 4PN spin-orbit term carries pi^2, interface_lalsim.py:435-444).
+constexpr double kPnXIsco = 0.021658244478713225;  // M f at the ISCO, 1 / (6^(3/2) pi)
+
+struct PnCoef {
+  double a[9];      // a_0..a_8 (a_5 = 0)
+  double b5, b6, b8;
+  double msec;      // total mass [s]
+  double d_isco;    // Psi'(x_ISCO)
+};
+
+__device__ double pn_dpsi(const PnCoef& c, double x) {
+  // Psi'(x) = sum_k (k-5)/3 a_k x^((k-8)/3) + b5/x + b6 x^(-2/3) (ln(pi x)/3 + 1) + b8 (ln(pi x) + 1):
+  // Horner in w = x^(-1/3) for the power terms (exponents -8/3 .. 0)
+  const double w = 1.0 / cbrt(x);
+  double p = (-5.0 / 3.0) * c.a[0];
+  p = p * w + (-4.0 / 3.0) * c.a[1];
+  p = p * w + (-1.0) * c.a[2];
+  p = p * w + (-2.0 / 3.0) * c.a[3];
+  p = p * w + (-1.0 / 3.0) * c.a[4];
+  p = p * w;                              // k = 5: no power term
+  p = p * w + (1.0 / 3.0) * c.a[6];
+  p = p * w + (2.0 / 3.0) * c.a[7];
+  p = p * w + c.a[8];
+  const double lp = log(kPi * x);
+  const double w2 = w * w;
+  return p + c.b5 * w2 * w + c.b6 * w2 * (lp * (1.0 / 3.0) + 1.0) + c.b8 * (lp + 1.0);
+}
+
+__device__ void pn_coefficients(double m1, double m2, double chi1, double chi2, PnCoef& c) {
+  const double mt = m1 + m2;
+  const double eta = m1 * m2 / (mt * mt), e2 = eta * eta, e3 = e2 * eta;
+  const double dl = sqrt(fmax(0.0, 1.0 - 4.0 * eta));
+  const double xa = 0.5 * (chi1 - chi2), xs = 0.5 * (chi1 + chi2);
+  const double pi = kPi, pi2 = kPi * kPi, pi13 = cbrt(kPi), pi23 = pi13 * pi13;
+  const double pfac = -3.0 / (128.0 * eta);
+  const double c2 = 3715.0 / 756.0 + 55.0 / 9.0 * eta;
+  const double c3 = -16.0 * pi + 113.0 / 3.0 * dl * xa + (113.0 / 3.0 - 76.0 / 3.0 * eta) * xs;
+  const double c4 = 15293365.0 / 508032.0 + 27145.0 / 504.0 * eta + 3085.0 / 72.0 * e2 +
+                    (-405.0 / 8.0 + 200.0 * eta) * xa * xa - 405.0 / 4.0 * dl * xa * xs +
+                    (-405.0 / 8.0 + 5.0 / 2.0 * eta) * xs * xs;
+  const double c5l = (38645.0 / 756.0 - 65.0 / 9.0 * eta) * pi + (-732985.0 / 2268.0 - 140.0 / 9.0 * eta) * dl * xa +
+                     (-732985.0 / 2268.0 + 24260.0 / 81.0 * eta + 340.0 / 9.0 * e2) * xs;
+  const double c6 = 11583231236531.0 / 4694215680.0 - 640.0 / 3.0 * pi2 - 6848.0 / 21.0 * kEulerGamma +
+                    (-15737765635.0 / 3048192.0 + 2255.0 / 12.0 * pi2) * eta + 76055.0 / 1728.0 * e2 -
+                    127825.0 / 1296.0 * e3 - 0.69314718055994531 * 13696.0 / 21.0 + 2270.0 / 3.0 * pi * dl * xa +
+                    (2270.0 / 3.0 - 520.0 * eta) * pi * xs + (75515.0 / 144.0 - 8225.0 / 18.0 * eta) * dl * xs * xa +
+                    (75515.0 / 288.0 - 263245.0 / 252.0 * eta - 480.0 * e2) * xa * xa +
+                    (75515.0 / 288.0 - 232415.0 / 504.0 * eta + 1255.0 / 9.0 * e2) * xs * xs;
+  const double c7 =
+      (77096675.0 / 254016.0 + 378515.0 / 1512.0 * eta - 74045.0 / 756.0 * e2) * pi +
+      (-25150083775.0 / 3048192.0 + 26804935.0 / 6048.0 * eta - 1985.0 / 48.0 * e2) * dl * xa +
+      (-25150083775.0 / 3048192.0 + 10566655595.0 / 762048.0 * eta - 1042165.0 / 3024.0 * e2 + 5345.0 / 36.0 * e3) * xs -
+      1140.0 * pi * dl * xa * xs + (-570.0 + 2240.0 * eta) * pi * xa * xa + (-570.0 + 40.0 * eta) * pi * xs * xs +
+      (14585.0 / 8.0 - 215.0 / 2.0 * eta) * dl * xa * xs * xs + (14585.0 / 8.0 - 7270.0 * eta + 80.0 * e2) * xa * xa * xs +
+      (14585.0 / 24.0 - 2380.0 * eta) * dl * xa * xa * xa +
+      (14585.0 / 24.0 - 475.0 / 6.0 * eta + 100.0 / 3.0 * e2) * xs * xs * xs;
+  const double c8 = (233915.0 / 168.0 - 99185.0 / 252.0 * eta) * dl * xa +
+                    (233915.0 / 168.0 - 3970375.0 / 2268.0 * eta + 19655.0 / 189.0 * e2) * xs;
+  c.a[0] = pfac / (pi * pi23);
+  c.a[1] = 0.0;
+  c.a[2] = pfac * c2 / pi;
+  c.a[3] = pfac * c3 / pi23;
+  c.a[4] = pfac * c4 / pi13;
+  c.a[5] = 0.0;
+  c.a[6] = pfac * c6 * pi13;
+  c.a[7] = pfac * c7 * pi23;
+  c.a[8] = pfac * c8 * pi2;
+  c.b5 = pfac * c5l;
+  c.b6 = pfac * (-6848.0 / 63.0) * pi13;
+  c.b8 = -c.a[8];
+  c.msec = mt * kMTSun;
+  c.d_isco = pn_dpsi(c, kPnXIsco);
+}
+
+// grid (ceil(n / 256), B): thread 0 of each block sets up the sample's coefficients
+__global__ void k_pn_tf(const double* __restrict__ params, int64_t n, const double* __restrict__ freqs,
+                        double* __restrict__ tf) {
+  __shared__ PnCoef c;
+  const int64_t b = blockIdx.y;
+  if (threadIdx.x == 0) {
+    const double* q = params + 4 * b;
+    pn_coefficients(q[0], q[1], q[2], q[3], c);
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = freqs[i] * c.msec;
+  tf[b * n + i] = (x < kPnXIsco && x > 0.0) ? -c.msec / (2.0 * kPi) * (pn_dpsi(c, x) - c.d_isco) : 0.0;
+}
+
 extern "C" {
 
 const char* pes_last_error(void) { return pes::g_error; }
@@ -316,6 +412,16 @@ int pes_phenomd(const double* theta, const double* freqs, int64_t n, double f_re
   k_phenomd<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(th, f_ref, f_cut_hz, freqs, n,
                                                              reinterpret_cast<double2*>(hp),
                                                              reinterpret_cast<double2*>(hc), tf);
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
+int pes_pn_tf(const double* params, int64_t B, const double* freqs, int64_t n, double* tf, void* stream) {
+  PES_REQUIRE(B >= 0 && n >= 0, "pes_pn_tf: negative size (B = %lld, n = %lld)", (long long)B, (long long)n);
+  PES_REQUIRE(B <= 65535, "pes_pn_tf: at most 65535 parameter sets per call, got %lld", (long long)B);
+  if (B == 0 || n == 0) return PES_OK;
+  PES_REQUIRE(params && freqs && tf, "pes_pn_tf: null pointer");
+  k_pn_tf<<<dim3(ceil_div(n, 256), (unsigned)B), 256, 0, as_stream(stream)>>>(params, n, freqs, tf);
   PES_CHECK_LAUNCH();
   return PES_OK;
 }
