@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <type_traits>
 #include <vector>
 
@@ -150,6 +151,9 @@ struct MixedBuffers {
   // phase fit and the run anchors, the transfer adjoint beside the phase
   // adjoint, the second backward tangent pass beside the first.
   cudaStream_t aux = nullptr;
+  // the gradient pass of the dense stage stages its run inputs through shared
+  // memory when they exceed half of L2 (they then stream from DRAM)
+  bool stage_grad = false;
   cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_padj = nullptr, ev_tadj = nullptr,
               ev_bwd = nullptr;
 };
@@ -1666,14 +1670,39 @@ __device__ __forceinline__ void flush_moments(float mq[kNodeQ * kMoments], float
   __syncwarp();
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async, completion by
+// commit/wait groups: a thread's own copies, no spin loop).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(__cvta_generic_to_global(gmem))
+               : "memory");
+}
+// the same through L1 (rows that the next runs of an interval read again)
+__device__ __forceinline__ void cp_async16_l1(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(__cvta_generic_to_global(gmem))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// One run's inputs in shared memory: the three packed rows of its (up to) 32
+// bins, the interval's eight coefficient rows and the run's three anchor rows.
+constexpr int kRunBuf = 3 * 32 + 8 + 3;
+
 // kMode 0: lnL partials; 1: lnL partials + adjoint moments; 2: write the model
 // h (unscaled, complex128 (n_det, 3, nbins)) to `model` (parity/debug path).
-template <int kMode>
+// kStage: the run inputs are copied one run ahead into shared memory (pays
+// off when they stream from DRAM, and in the lnL pass; with L2-resident
+// inputs the gradient pass is faster on plain loads).
+template <int kMode, bool kStage>
 __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev M,
                                                              const SampleBlock<double>* __restrict__ blocks,
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
   __shared__ double red[kMixThreads / 32];
+  // per warp, two run buffers: the next run's inputs are copied while this one is computed
+  __shared__ __align__(16) float4 rbuf[kStage ? kMixThreads / 32 : 1][kStage ? 2 : 1][kStage ? kRunBuf : 1];
   __shared__ float msm[kGrad ? kMixThreads / 32 : 1][kGrad ? kNodeQ * kMoments : 1][kGrad ? kMomPad : 1];
   const int s = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1704,12 +1733,46 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         for (int k = 0; k < kNodeQ * kMoments; ++k) mq[k] = 0.0f;
       }
       const int last = min(nc, first + kChunkMax);
+      // copy run c's inputs into buffer b (nothing for exact runs: runs never
+      // straddle an interval boundary, and bins below xb are evaluated exactly)
+      auto issue = [&](int c, int b) {
+        if (c >= last) return;
+        const int kb = M.ch_begin[c];
+        if (kb < xb) return;
+        float4* dst = &rbuf[wid][b][0];
+        const int64_t i = (int64_t)kb + lane;
+        if (lane < M.ch_len[c] && i < kcut) {
+          const float4* pkd = M.pk + (size_t)d * 3 * P.nbins;
+          cp_async16(dst + lane, pkd + i);
+          cp_async16(dst + 32 + lane, pkd + P.nbins + i);
+          cp_async16(dst + 64 + lane, pkd + 2 * P.nbins + i);
+        }
+        if (lane < 8)
+          cp_async16_l1(dst + 96 + lane, M.cg + (sd * M.J + M.ch_iv[c]) * 8 + lane);
+        else if (lane < 11)
+          cp_async16(dst + 104 + (lane - 8), M.runs + (sd * M.nchunks + c) * 3 + (lane - 8));
+      };
+      if (kStage) {
+        issue(first, 0);
+        cp_async_commit();
+      }
       for (int c = first; c < last; ++c) {
+        const int b = (c - first) & 1;
+        if (kStage) {
+          issue(c + 1, b ^ 1);
+          cp_async_commit();
+          cp_async_wait_one();  // run c's copies have landed
+          __syncwarp();
+        }
         const int j = M.ch_iv[c];
         const int kb = M.ch_begin[c];
         const int len = M.ch_len[c];
-        if (kb < xb) continue;  // exact bins (runs never straddle an interval boundary)
-        const float4* ra = M.runs + (sd * M.nchunks + c) * 3;
+        if (kb < xb) {  // exact bins
+          if (kStage) __syncwarp();
+          continue;
+        }
+        const float4* rb = kStage ? &rbuf[wid][b][0] : nullptr;
+        const float4* ra = kStage ? rb + 104 : M.runs + (sd * M.nchunks + c) * 3;
         const float4 ra0 = ra[0], ra1 = ra[1];
         RunPhase r;
         r.x0 = ra0.x;
@@ -1727,8 +1790,17 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
         }
         const int64_t i = (int64_t)kb + lane;
         if (lane < len && i < kcut) {
-          const float4* pkd = M.pk + (size_t)d * 3 * P.nbins;
-          const float4 pk0 = pkd[i], pk1 = pkd[P.nbins + i], pk2 = pkd[2 * P.nbins + i];
+          float4 pk0, pk1, pk2;
+          if (kStage) {
+            pk0 = rb[lane];
+            pk1 = rb[32 + lane];
+            pk2 = rb[64 + lane];
+          } else {
+            const float4* pkd = M.pk + (size_t)d * 3 * P.nbins;
+            pk0 = pkd[i];
+            pk1 = pkd[P.nbins + i];
+            pk2 = pkd[2 * P.nbins + i];
+          }
           const float t = pk2.w;
           const float u = (float)lane;
           const float u2 = u * u, u3 = u2 * u;
@@ -1754,7 +1826,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             cph = c2;
             sph = s2;
           }
-          const float4* G = M.cg + (sd * M.J + j) * 8;
+          const float4* G = kStage ? rb + 96 : M.cg + (sd * M.J + j) * 8;  // the interval's coefficient rows
           const float4 gl0 = G[6], gl1 = G[7];
           const float Glo[6] = {gl0.x, gl0.y, gl0.z, gl0.w, gl1.x, gl1.y};
           const float xk = fmaf(kSlope, u, r.x0);
@@ -1833,6 +1905,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             }
           }
         }
+        if (kStage) __syncwarp();  // buffer b is refilled two runs on
       }
       if (kGrad && cur_iv >= 0) flush_moments(mq, reinterpret_cast<float (*)[kMomPad]>(&msm[wid][0][0]), M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments, lane);
       if (kGrad && __any_sync(0xffffffffu, kinked)) {
@@ -2022,6 +2095,11 @@ int mixed_create(PesPlan* p) {
   }
   M.scale = 3.085677581491367e16 / (1.476625038050124729627979840144936351e3 * 4.925490947641266978197229498498379006e-6);
   M.scale_ff = ff_from(M.scale);
+  mb->stage_grad = (size_t)nd * (size_t)n * 3 * sizeof(float4) > ((size_t)64 << 20);
+  if (const char* env = std::getenv("PES_DENSE_STAGE")) {  // "1": always stage, "0": never
+    if (env[0] == '1') mb->stage_grad = true;
+    if (env[0] == '0') mb->stage_grad = false;
+  }
   M.scale_f = (float)M.scale;
   M.fstep_ff = ff_from(d.f_step);
   for (int k = 0; k < nd; ++k) mb->gen.gen20[k] = d.det[k].generation == 20;
@@ -2275,7 +2353,7 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
   k_run_anchors<<<dim3((unsigned)ceil_div(M.nchunks, 128), M.n_det, 1), 128, 0, st>>>(p->dev, M, blocks);
   PES_CHECK_LAUNCH();
-  k_dense_mixed<2><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
+  k_dense_mixed<2, false><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
                                                                   reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
   k_exact<2, double><<<dim3(M.xblocks, 1), kExactThreads, 0, st>>>(p->dev, M, G, blocks,
@@ -2389,9 +2467,12 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     ProfScope ps(p, kKDenseMixed, st);
     dim3 grid(M.nblk_dense, (unsigned)B);
     if (grad)
-      k_dense_mixed<1><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+      if (p->mixed->stage_grad)
+        k_dense_mixed<1, true><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+      else
+        k_dense_mixed<1, false><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
     else
-      k_dense_mixed<0><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+      k_dense_mixed<0, true><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_dense, st));

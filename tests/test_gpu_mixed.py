@@ -105,6 +105,26 @@ def test_mixed_gradient(cuda_lib, oracle, dataset):
     assert np.max(np.abs(gg - w_grad) / norm) < 1e-3, (gg, w_grad)
 
 
+def test_mixed_dense_staging_variants(cuda_lib, oracle, dataset, monkeypatch):
+    """The gradient pass of the dense stage with its run inputs copied one run
+    ahead into shared memory (cp.async) and with plain loads: the same lnL bit
+    for bit and the same gradient up to the order of the FP32 moment atomics
+    (LISA + TianQin, so exact runs are skipped in both)."""
+    g, dets, th0 = dataset
+    rng = np.random.default_rng(41)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(2)] + list(random_prior_theta(rng, 3, th0[10])))
+    monkeypatch.setenv("PES_DENSE_STAGE", "1")
+    staged, _ = engines(g, dets, max_batch=8, cut_factor=1.2)
+    monkeypatch.setenv("PES_DENSE_STAGE", "0")
+    plain, _ = engines(g, dets, max_batch=8, cut_factor=1.2)
+    l1, g1 = staged.log_likelihood_and_grad(thetas)
+    l0, g0 = plain.log_likelihood_and_grad(thetas)
+    assert torch.equal(l1, l0)
+    assert torch.equal(staged.log_likelihood_batch(thetas), l0)
+    norm = torch.linalg.norm(g0, dim=1, keepdim=True)
+    assert torch.max(torch.abs(g1 - g0) / norm).item() < 1e-5
+
+
 @pytest.mark.parametrize("n_sparse", [600, 2048, 3000])
 def test_mixed_other_grids(cuda_lib, oracle, dataset, n_sparse):
     """Non-default sparse grids: 600 nodes (register segments of 19 rows),
