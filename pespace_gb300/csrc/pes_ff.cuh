@@ -236,6 +236,24 @@ PES_HD FF ff_wrap_2pi(const FF& x) {
   return ff_addf(r, -kf * kTwoPiC);
 }
 
+// 2 pi = kTwoPiWA + kTwoPiWB + kTwoPiWC + kTwoPiWD (A has 5 significant bits:
+// k * A exact for |k| < 2^19)
+constexpr float kTwoPiWA = 6.25f;
+constexpr float kTwoPiWB = 3.318530693650246e-2f;
+constexpr float kTwoPiWC = 2.430840251310684e-10f;
+constexpr float kTwoPiWD = -4.870820776974614e-18f;
+constexpr float kWrapWideMax = 3.2e6f;  // |x| below 2^19 * 2 pi with margin
+
+// x - 2 pi rint(x / 2 pi) for |x| < kWrapWideMax (x.hi - k A is exact: k A is
+// within a factor two of x.hi for k != 0); error below 1e-9 rad
+PES_HD FF ff_wrap_2pi_wide(const FF& x) {
+  const float kf = rintf(x.hi * 0.15915494309189535f);
+  FF r = ff_addf(x, -kf * kTwoPiWA);
+  r = r - ff_two_prod(kf, kTwoPiWB);
+  r = r - ff_two_prod(kf, kTwoPiWC);
+  return ff_addf(r, -kf * kTwoPiWD);
+}
+
 // x.hi truncated to its leading `bits` significant bits (so that the head
 // times a small integer is exact in FP32), and the FF remainder as a float.
 PES_HD float ff_head(const FF& x, int bits, float* tail) {

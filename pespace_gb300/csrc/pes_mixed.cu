@@ -72,6 +72,9 @@ struct MixedDev {
   OrbitF orbit_f[PES_MAX_DETECTORS];  // FP32 copies for the derivative passes
   FF scale_ff;
   float scale_f;
+  double f_step;            // bin spacing (FP64)
+  float4* sff;              // [B][2] per sample: (t_c, M) and (Mf_peak, -) as float-float pairs
+  unsigned long long* cfrac;  // [B] fraction of f_step t_c in 64-bit fixed point
   FF fstep_ff;              // bin spacing
   const float2* node_ff;    // [J] node frequencies (hi, lo)
   const float4* tdn_ff;     // [n_det][J] node delay factor D (re hi, re lo, im hi, im lo)
@@ -510,6 +513,15 @@ __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
   const SampleBlock<double>& b = blocks[s];
+  if (kPart == 0) {
+    const FF tcf = ff_from(b.tc), msf = ff_from(b.wf.Msec), fpf = ff_from(b.wf.fpeak);
+    M.sff[2 * s] = make_float4(tcf.hi, tcf.lo, msf.hi, msf.lo);
+    M.sff[2 * s + 1] = make_float4(fpf.hi, fpf.lo, 0.0f, 0.0f);
+    // f t_c = (k0 + k) c, c = f_step t_c: its fraction is (k0 + k) frac(c) mod 1
+    const double cyc = M.f_step * b.tc;
+    const double rs = (cyc - floor(cyc)) * 18446744073709551616.0;  // 2^64
+    M.cfrac[s] = (rs >= 0.0 && rs < 18446744073709551616.0) ? (unsigned long long)rs : 0ull;
+  }
   int ns = 0, nc = 0, xb = 0;
   if (b.status == kSampleOk && b.kcut > 0) {
     const int64_t last = b.kcut - 1;
@@ -1616,27 +1628,41 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   const int kb = M.ch_begin[c];
   if (kb < M.xbind[(size_t)s * M.n_det + d]) return;
   const size_t sd = (size_t)s * M.n_det + d;
-  const double tc = blocks[s].tc;
   const int j = M.ch_iv[c];
+  const float4 sa = M.sff[2 * s], sbk = M.sff[2 * s + 1];
+  const FF tcf = ff_make(sa.x, sa.y), msf = ff_make(sa.z, sa.w), fpf = ff_make(sbk.x, sbk.y);
   const FF* co = M.cphi + (sd * M.J + j) * 4;
   const FF a = co[0], b = co[1], cc = co[2], dd = co[3];
   const float2 nfj = M.node_ff[j];
-  const FF t = ff_mulf(M.fstep_ff, (float)(P.k0 + kb)) - ff_make(nfj.x, nfj.y);  // k0 + kb < 2^24
+  const FF fbf = ff_mulf(M.fstep_ff, (float)(P.k0 + kb));  // k0 + kb < 2^24: exact in FP32
+  const FF t = fbf - ff_make(nfj.x, nfj.y);
   const FF ddt = dd * t;
   const FF S0 = a + t * (b + t * (cc + ddt));
   const FF S1 = b + t * (ff_mulf(cc, 2.0f) + ff_mulf(ddt, 3.0f));
   const FF S2 = cc + ff_mulf(ddt, 3.0f);
   const FF D = M.fstep_ff;
-  // anchored phase S0 + 2 pi f t_c: the product's whole cycles removed in FP64
-  // (f t_c reaches 1e6 cycles), the sum wrapped in FP64, the rest in FF
-  const double fb = (double)(P.k0 + kb) * P.f_step;
-  const double cyc = fb * tc;
-  const double ph0d = ff_to(S0) + (2.0 * kPi) * (cyc - rint(cyc));
-  const FF ph0 = ff_from(ph0d - (2.0 * kPi) * rint(ph0d * (1.0 / (2.0 * kPi))));
-  const FF ph1 = ff_wrap_2pi(D * (S1 + ff_from(tc) * (2.0 * kPi)));
+  // anchored phase S0 + 2 pi f t_c.  f t_c reaches 1e6 cycles; its fraction is
+  // (k0 + kb) frac(f_step t_c) mod 1, taken exactly in 64-bit integers and
+  // read out as two 23-bit floats; the sum is wrapped in float-float (FP64
+  // beyond the wide wrap's range).
+  FF ph0;
+  {
+    const unsigned long long pr = (unsigned long long)(P.k0 + kb) * M.cfrac[s];
+    const unsigned h23 = (unsigned)(pr >> 41), l23 = (unsigned)(pr >> 18) & 0x7FFFFFu;
+    const float fh = (__uint_as_float(0x4B000000u | h23) - 8388608.0f) * 1.1920928955078125e-07f;   // / 2^23
+    const float fl = (__uint_as_float(0x4B000000u | l23) - 8388608.0f) * 1.4210854715202004e-14f;  // / 2^46
+    ph0 = S0 + ff_fast_two_sum(fh, fl) * (2.0 * kPi);
+    if (fabsf(ph0.hi) < kWrapWideMax) {
+      ph0 = ff_wrap_2pi_wide(ph0);
+    } else {
+      const double p = ff_to(ph0);
+      ph0 = ff_from(p - (2.0 * kPi) * rint(p * (1.0 / (2.0 * kPi))));
+    }
+  }
+  const FF ph1 = ff_wrap_2pi(D * (S1 + tcf * (2.0 * kPi)));
   const FF ph2 = (D * D) * S2;
   const FF ph3 = (D * D) * (D * dd);
-  const float x0 = (float)fma(blocks[s].wf.Msec, fb, -blocks[s].wf.fpeak);
+  const float x0 = (msf * fbf - fpf).hi;
   // anchor phasor: sincos of the float head, rotated by the (tiny) tail
   float s0f, c0f;
   sincos_poly(ph0.hi, &s0f, &c0f);
@@ -2102,6 +2128,7 @@ int mixed_create(PesPlan* p) {
   }
   M.scale_f = (float)M.scale;
   M.fstep_ff = ff_from(d.f_step);
+  M.f_step = d.f_step;
   for (int k = 0; k < nd; ++k) mb->gen.gen20[k] = d.det[k].generation == 20;
   // shared sparse grid, bin -> interval map, runs
   const double flo = (double)d.k0 * d.f_step, fhi = (double)(d.k0 + n - 1) * d.f_step;
@@ -2152,6 +2179,8 @@ int mixed_create(PesPlan* p) {
   float* gf;
   TdiFactor* tdn;
   float4* tdn_ff;
+  float4* sff;
+  unsigned long long* cfrac;
   float2* node_ff;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
   double *xpart, *xgpart;
@@ -2172,7 +2201,8 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &node_ff, J)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &sff, (size_t)2 * B)) ||
+      (rc = alloc(mb, &cfrac, (size_t)B)) || (rc = alloc(mb, &node_ff, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 8)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
@@ -2284,6 +2314,8 @@ int mixed_create(PesPlan* p) {
   M.gff = gff;
   M.tdn = tdn;
   M.tdn_ff = tdn_ff;
+  M.sff = sff;
+  M.cfrac = cfrac;
   M.node_ff = node_ff;
   M.yv = yv;
   M.scr = scr;
