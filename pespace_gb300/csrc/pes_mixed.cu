@@ -50,12 +50,6 @@ constexpr int kExactBlocksGeo = 64;     // with a geocentric detector most inspi
 constexpr int kExactThreads = 128;
 __device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
 using GradScalar = DualF<kMixNT>;    // exact bins: FP64 values (phases of 1e6 rad), FP32 tangents
-// Sparse nodes: FP32 values (they enter only through the chain rule) and the 9
-// tangents split over two passes (slots 0-4, then 5-8), which halves the live
-// registers of the node evaluation.
-constexpr int kPassA = 5, kPassB = kMixNT - kPassA;
-using NodeGradA = DualS<kPassA>;
-using NodeGradB = DualS<kPassB>;
 
 struct MixedDev {
   int32_t J;                // nodes
@@ -119,8 +113,6 @@ struct MixedDev {
   double* part;             // [B][nblk_dense] lnL partials
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
-  void* gblocksA;           // [B] SampleBlock<NodeGradA> (tangent slots 0-4)
-  void* gblocksB;           // [B] SampleBlock<NodeGradB> (tangent slots 5-8)
   double* gdir;             // [B][n_det] direct t_c term of the gradient
   // Amplitude kink at f_peak: the transfer quantities carry C_q max(0, Mf - Mf_peak)^2
   // (C_q = jump/2 * R_q, R_q = G_q(f_peak)/Ahat(f_peak)); it is removed from the
@@ -152,13 +144,12 @@ struct MixedBuffers {
   cudaEvent_t fork = nullptr, join = nullptr, xready = nullptr;
   // Second stream of the main sequence: the transfer-spline fit beside the
   // phase fit and the run anchors, the transfer adjoint beside the phase
-  // adjoint, the second backward tangent pass beside the first.
+  // adjoint.
   cudaStream_t aux = nullptr;
   // the gradient pass of the dense stage stages its run inputs through shared
   // memory when they exceed half of L2 (they then stream from DRAM)
   bool stage_grad = false;
-  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_padj = nullptr, ev_tadj = nullptr,
-              ev_bwd = nullptr;
+  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -331,30 +322,10 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
 }
 
 // Gradient set-up: per sample, the coefficient block with exact FP64
-// tangents, stored with FP32 tangents for the node kernel.
-// FP32 value and tangents [Off, Off + N) of a coefficient block with FP64 tangents.
-template <int N, int Off, class TD>
-__device__ void narrow_block(const PhenomDCoef<TD>& wf, const Polar<TD>& pol, const TD& tc,
-                             SampleBlock<DualS<N>>& o) {
-  static_assert(sizeof(PhenomDCoef<TD>) / sizeof(TD) == sizeof(PhenomDCoef<DualS<N>>) / sizeof(DualS<N>),
-                "coefficient block must be an array of scalars");
-  static_assert(sizeof(Polar<TD>) / sizeof(TD) == sizeof(Polar<DualS<N>>) / sizeof(DualS<N>),
-                "polarisation block must be an array of scalars");
-  auto narrow = [](const TD* a, DualS<N>* b, int n) {
-    for (int k = 0; k < n; ++k) {
-      b[k].v = (float)a[k].v;
-      for (int i = 0; i < N; ++i) b[k].d[i] = (float)a[k].d[Off + i];
-    }
-  };
-  narrow(reinterpret_cast<const TD*>(&wf), reinterpret_cast<DualS<N>*>(&o.wf), sizeof(PhenomDCoef<TD>) / sizeof(TD));
-  narrow(reinterpret_cast<const TD*>(&pol), reinterpret_cast<DualS<N>*>(&o.pol), sizeof(Polar<TD>) / sizeof(TD));
-  narrow(&tc, &o.tc, 1);
-  o.status = kSampleOk;
-}
-
+// tangents, stored with FP32 tangents (the exact bins and the backward node
+// stage read it).
 __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_t B,
-                             SampleBlock<GradScalar>* __restrict__ out, SampleBlock<NodeGradA>* __restrict__ outA,
-                             SampleBlock<NodeGradB>* __restrict__ outB) {
+                             SampleBlock<GradScalar>* __restrict__ out) {
   using TD = Dual<kMixNT, double>;
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
@@ -363,8 +334,6 @@ __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_
   SampleBlock<GradScalar>& o = out[s];
   if (!theta_in_domain(raw)) {
     o.status = kSampleOutOfDomain;
-    outA[s].status = kSampleOutOfDomain;
-    outB[s].status = kSampleOutOfDomain;
     return;
   }
   TD th[11];
@@ -395,21 +364,72 @@ __global__ void k_setup_grad(PlanDev P, const double* __restrict__ theta, int64_
   narrow(reinterpret_cast<const TD*>(&pol), reinterpret_cast<GradScalar*>(&o.pol), sizeof(Polar<TD>) / sizeof(TD));
   narrow(&th[10], &o.tc, 1);
   o.status = kSampleOk;
-  narrow_block<kPassA, 0>(wf, pol, th[10], outA[s]);
-  narrow_block<kPassB, kPassA>(wf, pol, th[10], outB[s]);
 }
 
-// Backward: recompute the node quantities with tangents and contract with the node adjoints.
-// Pass (N, Off) handles tangent slots [Off, Off + N); the first pass also the
-// analytic ln D_L and phi_c terms.  Each pass writes only its parameters.
-template <int N, int Off>
-__global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, MixedDev M, GenArg G, double wscale) {
-  using GS = DualS<N>;
-  constexpr bool kFirst = Off == 0;
-  __shared__ SampleBlock<GS> sb;
+// Backward node stage in one pass, by the structure of the node values:
+// PhenomD (amplitude A, phase Psi, t(f)) depends on the four mass and spin
+// parameters only, and the transfer values are linear in A,
+//   y_q = A Y_q(T, lambda, sin beta, psi, cos iota) - C_q x^2,  T = t(f) + t_c,
+//   y_0 = Psi + 2 pi f k.x0(T, lambda, sin beta).
+// So PhenomD runs with 4 FP32 tangents (GM) and the response, with A = 1,
+// with 5 (GR: T, lambda, sin beta, psi, cos iota); the chain rule combines
+// them after contracting with the node adjoints W:
+//   dL/dm_k  += G_A dA/dm_k + G_T dt/dm_k + W_0 dPsi/dm_k - sum_q W_q R_q dx2h/dm_k
+//   dL/dt_c  += G_T,   dL/dr_k += G_r[k]
+// with G_A = sum W_q Y_q, G_T = sum W_q A dY_q/dT + W_0 2 pi f dkx0/dT and
+// G_r the same for the response parameters.  Same results as carrying all
+// nine tangents through the whole evaluation, at about half the work.
+using GM = DualS<4>;  // tangent slots 0-3: ln Mc, q, chi_1, chi_2
+using GR = DualS<5>;  // T, lambda, sin beta, psi, cos iota
+
+struct BwdBlock {
+  PhenomDCoef<GM> wf;
+  Polar<GR> pol;
+  GR pfac, cfac;
+  float tc;
+  int status;
+};
+
+__global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd_split(PlanDev P, MixedDev M, GenArg G,
+                                                                      double wscale) {
+  __shared__ BwdBlock sb;
   __shared__ double red[kSparseThreads / 32][11];
   const int s = blockIdx.z, d = blockIdx.y;
-  load_block(reinterpret_cast<const SampleBlock<GS>*>(kFirst ? M.gblocksA : M.gblocksB), s, sb);
+  {
+    // narrow the sample's gradient block (FP64 values, FP32 tangents in slots 0-8)
+    const SampleBlock<GradScalar>& g = reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks)[s];
+    constexpr int nwf = (int)(sizeof(PhenomDCoef<GradScalar>) / sizeof(GradScalar));
+    constexpr int npol = (int)(sizeof(Polar<GradScalar>) / sizeof(GradScalar));
+    static_assert(sizeof(PhenomDCoef<GM>) / sizeof(GM) == nwf, "coefficient block must be an array of scalars");
+    static_assert(sizeof(Polar<GR>) / sizeof(GR) == npol, "polarisation block must be an array of scalars");
+    const GradScalar* wsrc = reinterpret_cast<const GradScalar*>(&g.wf);
+    GM* wdst = reinterpret_cast<GM*>(&sb.wf);
+    for (int k = threadIdx.x; k < nwf; k += blockDim.x) {
+      wdst[k].v = (float)wsrc[k].v;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) wdst[k].d[t] = wsrc[k].d[t];
+    }
+    const GradScalar* psrc = reinterpret_cast<const GradScalar*>(&g.pol);
+    GR* pdst = reinterpret_cast<GR*>(&sb.pol);
+    for (int k = threadIdx.x; k < npol; k += blockDim.x) {
+      pdst[k].v = (float)psrc[k].v;
+      pdst[k].d[0] = 0.0f;
+      pdst[k].d[1] = psrc[k].d[5];  // lambda
+      pdst[k].d[2] = psrc[k].d[6];  // sin beta
+      pdst[k].d[3] = psrc[k].d[7];  // psi
+      pdst[k].d[4] = 0.0f;
+    }
+    if (threadIdx.x == 0) {
+      sb.pfac.v = (float)g.wf.pfac.v;
+      sb.cfac.v = (float)g.wf.cfac.v;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) sb.pfac.d[t] = sb.cfac.d[t] = 0.0f;
+      sb.pfac.d[4] = g.wf.pfac.d[4];  // cos iota
+      sb.cfac.d[4] = g.wf.cfac.d[4];
+      sb.tc = (float)g.tc.v;
+      sb.status = g.status;
+    }
+  }
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
@@ -417,33 +437,81 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, Mix
 #pragma unroll
   for (int k = 0; k < 11; ++k) acc[k] = 0.0f;
   if (sb.status == kSampleOk && ns >= 3 && j <= ns && j < M.J) {
-    GS y[kNodeQ];
     const float fj = M.node_ff[j].x;
-    {
-      const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
-      const Cx<GS> D = cx(lift<GS>(t4.x), lift<GS>(t4.z));
-      node_eval_g<false, GS>(M.orbit_f[d], M.scale_f, sb, D, D, fj, y);
-    }
-    const GS xk = sb.wf.Msec * fj - sb.wf.fpeak;
-    if (xk.v > 0.0) {
-      GS ahat, jump;
-      amp_peak_jump<GS>(sb.wf, ahat, jump);
-      const GS x2h = 0.5 * (xk * xk) * jump;
-      const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
-#pragma unroll
-      for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - R[q] * x2h;  // R_q held fixed
-    }
     const float* yb = M.ybar + (((size_t)s * M.n_det + d) * M.J + j) * kNodeQ;
+    float W[kNodeQ];
 #pragma unroll
-    for (int q = 0; q < kNodeQ; ++q) {
-      const float w = yb[q];
+    for (int q = 0; q < kNodeQ; ++q) W[q] = yb[q];
+    // PhenomD with the mass and spin tangents
+    GM amp, psi, tf;
+    phenomd_eval<GM>(sb.wf, sb.wf.Msec * fj, amp, psi, tf);
+    amp = amp * M.scale_f;
+    // response per unit amplitude with the T and sky/orientation tangents
+    Cx<GR> Y[3];
+    GR kx0;
+    {
+      GR T = lift<GR>(tf.v + sb.tc);
+      T.d[0] = 1.0f;
+      const GR zero = lift<GR>(0.0);
+      const Cx<GR> hp = cx(sb.pfac, zero), hc = cx(zero, -sb.cfac);
+      const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
+      const Cx<GR> D = cx(lift<GR>(t4.x), lift<GR>(t4.z));
+      Cx<GR> L[6];
+      single_links_impl<true, GR>(M.orbit_f[d], fj, hp, hc, T, sb.pol, L, &kx0);
+      tdi_channels_t<false, GR>(D, D, 1, L, Y);
+    }
+    const float tpf = 6.283185307179586f * fj;
+    // contractions over the quantities
+    float GA = 0.0f, GT = W[0] * tpf * kx0.d[0], Gr[4];
 #pragma unroll
-      for (int k = 0; k < N; ++k) acc[kSlotParam[Off + k]] = fmaf(w, y[q].d[k], acc[kSlotParam[Off + k]]);
-      if (kFirst) {
-        if (q > 0) acc[4] = fmaf(-w, y[q].v, acc[4]);  // G ~ 1/D_L
-        else acc[9] = fmaf(-2.0f, w, acc[9]);          // Phi_s = ... - 2 phi_c
+    for (int k = 0; k < 4; ++k) Gr[k] = W[0] * tpf * kx0.d[1 + k];
+    float yv[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const GR* yc[2] = {&Y[c].re, &Y[c].im};
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const int q = 1 + 2 * c + r;
+        const GR& y = *yc[r];
+        GA = fmaf(W[q], y.v, GA);
+        const float wa = W[q] * amp.v;
+        GT = fmaf(wa, y.d[0], GT);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) Gr[k] = fmaf(wa, y.d[1 + k], Gr[k]);
+        yv[2 * c + r] = amp.v * y.v;
       }
     }
+    // peak kink removed from the node data: y_q -= R_q x2h, R_q held fixed
+    float kx[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const GM xk = sb.wf.Msec * fj - sb.wf.fpeak;
+    if (xk.v > 0.0f) {
+      GM ahat, jump;
+      amp_peak_jump<GM>(sb.wf, ahat, jump);
+      const GM x2h = 0.5 * (xk * xk) * jump;
+      const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
+      float WR = 0.0f;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const float Rq = (float)R[q];
+        WR = fmaf(W[1 + q], Rq, WR);
+        yv[q] -= Rq * x2h.v;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) kx[k] = WR * x2h.d[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      acc[k] = GA * amp.d[k] + GT * tf.d[k] + W[0] * psi.d[k] - kx[k];  // ln Mc, q, chi_1, chi_2
+    acc[5] = Gr[3];   // cos iota
+    acc[6] = Gr[0];   // lambda
+    acc[7] = Gr[1];   // sin beta
+    acc[8] = Gr[2];   // psi
+    acc[10] = GT;     // t_c
+    float a4 = 0.0f;  // the transfer values scale as 1/D_L
+#pragma unroll
+    for (int q = 0; q < 6; ++q) a4 = fmaf(-W[1 + q], yv[q], a4);
+    acc[4] = a4;
+    acc[9] = -2.0f * W[0];  // Phi_s = ... - 2 phi_c
   }
   // block sum: float-float across the warp, FP64 across warps
   double accd[11];
@@ -466,19 +534,19 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, Mix
   }
   // dense-side kink term C_q x^2 (x = Msec f - Mf_peak): one thread per (sample, detector)
   if (blockIdx.x == 0 && threadIdx.x == 0 && sb.status == kSampleOk && ns >= 3) {
-    GS ahat, jump;
-    amp_peak_jump<GS>(sb.wf, ahat, jump);
+    GM ahat, jump;
+    amp_peak_jump<GM>(sb.wf, ahat, jump);
     const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
     const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
     const float* K = M.kinkM + ((size_t)s * M.n_det + d) * 12;
     for (int q = 0; q < 6; ++q) {
       // sum A_q x f = (sum A_q x^2 + Mf_peak sum A_q x) / Msec  (f = (x + Mf_peak) / Msec)
       const double K2 = wscale * K[q], K1 = wscale * K[6 + q];
-      const double K1f = (K2 + sb.wf.fpeak.v * K1) / sb.wf.Msec.v;
-      for (int k = 0; k < N; ++k)
-        accd[kSlotParam[Off + k]] += 0.5 * R[q] * K2 * (double)jump.d[k] +
-                                     2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
-      if (kFirst) accd[4] -= C[q] * K2;  // C_q ~ 1/D_L
+      const double K1f = (K2 + (double)sb.wf.fpeak.v * K1) / (double)sb.wf.Msec.v;
+      for (int k = 0; k < 4; ++k)
+        accd[k] += 0.5 * R[q] * K2 * (double)jump.d[k] +
+                   2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
+      accd[4] -= C[q] * K2;  // C_q ~ 1/D_L
     }
   }
   const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -488,15 +556,10 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd(PlanDev P, Mix
   }
   __syncthreads();
   if (threadIdx.x < 11) {
-    bool mine = kFirst && (threadIdx.x == 4 || threadIdx.x == 9);
+    double x = 0.0;
 #pragma unroll
-    for (int k = 0; k < N; ++k) mine = mine || kSlotParam[Off + k] == (int)threadIdx.x;
-    if (mine) {
-      double x = 0.0;
-#pragma unroll
-      for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
-      M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + threadIdx.x] = x;
-    }
+    for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
+    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + threadIdx.x] = x;
   }
 }
 
@@ -2095,7 +2158,7 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->join, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->xready, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->aux, cudaStreamNonBlocking));
-  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_padj, &mb->ev_tadj, &mb->ev_bwd})
+  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_tadj})
     PES_CHECK_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
@@ -2185,8 +2248,6 @@ int mixed_create(PesPlan* p) {
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
   double *xpart, *xgpart;
   SampleBlock<GradScalar>* gblk;
-  SampleBlock<NodeGradA>* gblkA;
-  SampleBlock<NodeGradB>* gblkB;
   double *kR, *kC;
   float* kF;
   float* bin_t;
@@ -2207,7 +2268,7 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
-      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &gblkA, (size_t)B)) || (rc = alloc(mb, &gblkB, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
+      (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
       (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) || (rc = alloc(mb, &xbind, (size_t)B * nd)) ||
       (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * M.xblocks)) ||
       (rc = alloc(mb, &xgpart, (size_t)B * M.xblocks * 11)))
@@ -2327,8 +2388,6 @@ int mixed_create(PesPlan* p) {
   M.gpart = gpart;
   M.gdir = gdir;
   M.gblocks = gblk;
-  M.gblocksA = gblkA;
-  M.gblocksB = gblkB;
   M.kinkR = kR;
   M.kinkC = kC;
   M.kinkF = kF;
@@ -2341,8 +2400,7 @@ void mixed_destroy(PesPlan* p) {
   if (!p->mixed) return;
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
   if (p->mixed->aux) cudaStreamSynchronize(p->mixed->aux);
-  for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_padj,
-                        p->mixed->ev_tadj, p->mixed->ev_bwd})
+  for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_tadj})
     if (e) cudaEventDestroy(e);
   if (p->mixed->aux) cudaStreamDestroy(p->mixed->aux);
   for (void* a : p->mixed->allocs) cudaFree(a);
@@ -2448,9 +2506,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     {
       ProfScope ps(p, kKSetup, side);
       k_setup_grad<<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, side>>>(p->dev, theta, B,
-                                                     reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks),
-                                                     reinterpret_cast<SampleBlock<NodeGradA>*>(M.gblocksA),
-                                                     reinterpret_cast<SampleBlock<NodeGradB>*>(M.gblocksB));
+                                                     reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks));
     }
     PES_CHECK_LAUNCH();
     {
@@ -2516,7 +2572,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   if (!grad) return PES_OK;
   // node adjoints: phase systems here, transfer systems on the second stream;
-  // then the two tangent passes of the backward node stage side by side
+  // then the backward node stage
   cudaStream_t aux = p->mixed->aux;
   const double ws = 4.0 * p->dev.df;
   const dim3 sgrid(M.nblk_sparse, M.n_det, (unsigned)B);
@@ -2543,22 +2599,13 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
       k_spline_adjoint_wide<<<(unsigned)(B * M.n_det), kSplineThreads, 0, st>>>(M, ws);
     PES_CHECK_LAUNCH();
   }
-  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_padj, st));
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tadj, aux));
-  PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_padj, 0));
-  {
-    ProfScope ps(p, kKAdjoint, aux);
-    k_sparse_bwd<kPassB, kPassA><<<sgrid, kSparseThreads, 0, aux>>>(p->dev, M, G, ws);
-  }
-  PES_CHECK_LAUNCH();
-  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_bwd, aux));
   PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_tadj, 0));
   {
     ProfScope ps(p, kKAdjoint, st);
-    k_sparse_bwd<kPassA, 0><<<sgrid, kSparseThreads, 0, st>>>(p->dev, M, G, ws);
+    k_sparse_bwd_split<<<sgrid, kSparseThreads, 0, st>>>(p->dev, M, G, ws);
   }
   PES_CHECK_LAUNCH();
-  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_bwd, 0));
   {
     ProfScope ps(p, kKFinalize, st);
     k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, B, -2.0 * p->dev.df, grad);
