@@ -1,27 +1,33 @@
 // Mixed-precision batched path.
 //
-//  1. sparse stage (FP64): at n_sparse log-spaced nodes f_j shared by all
-//     samples, the phase Phi_s = Psi + 2 pi f k.x0(t_f) and the three TDI
-//     channel transfers G_c (response of the unit-phase waveform with the
-//     constellation-centre delay factored out), per (sample, detector);
-//  2. not-a-knot cubic splines through the nodes (FP64 solve; phase
-//     coefficients kept in FP64, transfer coefficients stored in FP32);
+//  1. sparse stage (float-float on the FP32 pipes, pes_ff.cuh): at n_sparse
+//     log-spaced nodes f_j shared by all samples, the phase
+//     Phi_s = Psi + 2 pi f k.x0(t_f) and the three TDI channel transfers G_c
+//     (response of the unit-phase waveform with the constellation-centre
+//     delay factored out), per (sample, detector);
+//  2. not-a-knot cubic splines through the nodes (phase solved and stored in
+//     float-float, transfer quantities solved in FP32 and stored as FP32
+//     coefficients with float-float values), grid tables and node values
+//     staged through shared memory;
 //  3. dense stage (FP32 bulk): for every bin, h_c = G_c(f) exp(-i (Phi_s(f) +
-//     2 pi f t_c)); the phase of each run of <= 32 bins is anchored in FP64 at
-//     the run start and advanced in FP32 with exact split products; the
-//     residual |d - h|^2 / S is accumulated with compensation, per-block
-//     partials are summed in FP64 in a fixed order;
+//     2 pi f t_c)); the phase of each run of <= 32 bins is anchored at the run
+//     start (float-float, the fraction of f t_c from integer arithmetic) and
+//     advanced in FP32 with exact split products; the residual |d - h|^2 / S
+//     is accumulated with compensation, per-block partials are summed in
+//     FP64 in a fixed order;
 //  4. gradient: the dense stage also accumulates the adjoint moments
 //     sum_bins A_q(f) t^p of each spline interval; a transposed spline solve
-//     turns them into node adjoints, and the sparse stage is recomputed with
-//     dual numbers and contracted with those adjoints (no dense residuals are
-//     stored);
+//     turns them into node adjoints, and one backward pass recomputes the
+//     node values with FP32 dual numbers (PhenomD over the mass and spin
+//     parameters, the response over the others) and contracts them with the
+//     node adjoints (no dense residuals are stored);
 //  5. exact bins: far below merger a light system's time-to-coalescence moves
-//     so fast with f that the constellation's yearly motion advances by more
+//     so fast with f that the constellation's orbital motion advances by more
 //     than kOrbitPhaseMax radians across one node interval; the splines do
-//     not resolve that, so the bins below the first resolved interval are
-//     evaluated directly in FP64 (model, residual, FP32 tangents for the
-//     gradient) and the dense stage skips them.
+//     not resolve that, so each detector's bins below its first resolved
+//     interval are evaluated directly (float-float model, residual against
+//     the FP64 data, FP32 tangents for the gradient) and the dense stage
+//     skips them.
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
