@@ -33,6 +33,13 @@
 
 namespace pes {
 
+// Out-of-line device functions for the float-float routines that a node
+// evaluation calls many times (sin(x)/x six times, sincos four): one copy of
+// their code instead of one per call site keeps the fully inlined node
+// evaluation within the instruction cache (its top stall was instruction
+// fetch; sparse stage 0.45 -> 0.36 ms per step).
+#define PES_HD_OUTLINE static __host__ __device__ __noinline__
+
 // Trivially default-constructible (usable in shared memory); the explicit
 // conversions let it serve as the value type of the dual numbers (their
 // tangents take the head, FP64 constants are split once).
@@ -206,7 +213,7 @@ constexpr float kHalfPiB = 4.838267923332751e-4f;
 constexpr float kHalfPiC = 2.5633440682570896e-12f;
 
 // sin and cos of |x| < 2^15 (reduction error below 2^-48 |k| pi/2)
-PES_HD void dsincos(const FF& x, FF* s, FF* c) {
+PES_HD_OUTLINE void dsincos(const FF& x, FF* s, FF* c) {
   const float kf = rintf(x.hi * 0.63661977236758134f);
   FF r = ff_addf(x, -kf * kHalfPiA);            // exact product, FF sum
   r = r - ff_two_prod(kf, kHalfPiB);
@@ -273,7 +280,7 @@ PES_HD float ff_head(const FF& x, int bits, float* tail) {
 
 // sin(x)/x: Taylor series in z = x^2 for |x| <= 2 (FF for the terms down to
 // z^6/13!, FP32 for those below 2e-8; truncation below 2e-16), else sin(x)/x.
-PES_HD FF ff_sinc(const FF& x) {
+PES_HD_OUTLINE FF ff_sinc(const FF& x) {
   if (fabsf(x.hi) <= 2.0f) {
     const FF z = x * x;
     const float zf = z.hi;
