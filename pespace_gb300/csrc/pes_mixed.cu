@@ -1243,7 +1243,7 @@ __device__ __forceinline__ void spline_fit_staged(const MixedDev& M, int64_t sd,
 // kFitWarps systems per block.  R = FF: the phase systems (one per sample and
 // detector, q = 0); R = float: the six transfer systems (q = 1..6).
 template <int kSeg, class R>
-__global__ void __launch_bounds__(kFitWarps * 32) k_spline_fit(MixedDev M, int64_t n_sys) {
+__global__ void __launch_bounds__(kFitWarps * 32, 3) k_spline_fit(MixedDev M, int64_t n_sys) {
   extern __shared__ __align__(16) unsigned char fit_smem[];
   constexpr bool kPhase = std::is_same<R, FF>::value;
   constexpr bool kStage = kSeg == 32;
