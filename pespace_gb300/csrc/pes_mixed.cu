@@ -225,27 +225,51 @@ __device__ __forceinline__ void narrow_block_ff(const SampleBlock<double>& a, Sa
   }
 }
 
-// The gradient block (FP64 values, FP32 tangents) with float-float values.
-__device__ __forceinline__ void narrow_block_dual_ff(const SampleBlock<GradScalar>& a,
-                                                     SampleBlock<Dual<kMixNT, float, FF>>& b) {
-  using TE = Dual<kMixNT, float, FF>;
-  static_assert(sizeof(PhenomDCoef<TE>) / sizeof(TE) == sizeof(PhenomDCoef<GradScalar>) / sizeof(GradScalar),
-                "coefficient block must be an array of scalars");
-  static_assert(sizeof(Polar<TE>) / sizeof(TE) == sizeof(Polar<GradScalar>) / sizeof(GradScalar),
-                "polarisation block must be an array of scalars");
-  constexpr int nv = (int)((sizeof(PhenomDCoef<GradScalar>) + sizeof(Polar<GradScalar>)) / sizeof(GradScalar)) + 1;
-  const GradScalar* src = reinterpret_cast<const GradScalar*>(&a);
-  TE* dst = reinterpret_cast<TE*>(&b);
-  for (int j = threadIdx.x; j < nv; j += blockDim.x) {
-    dst[j].v = ff_from(src[j].v);
+// Gradient pass of the exact bins, by the same structure as the backward node
+// stage: PhenomD with float-float values and FP32 tangents over the four mass
+// and spin parameters (EM), the response per unit amplitude with five (ER:
+// T = t(f) + t_c, lambda, sin beta, psi, cos iota).
+using EM = Dual<4, float, FF>;
+using ER = Dual<5, float, FF>;
+struct ExactGradBlock {
+  PhenomDCoef<EM> wf;
+  Polar<ER> pol;
+  ER pfac, cfac;
+  FF tc;
+  int32_t status;
+};
+
+__device__ __forceinline__ void narrow_exact_grad(const SampleBlock<GradScalar>& a, ExactGradBlock& b) {
+  constexpr int nwf = (int)(sizeof(PhenomDCoef<GradScalar>) / sizeof(GradScalar));
+  constexpr int npol = (int)(sizeof(Polar<GradScalar>) / sizeof(GradScalar));
+  static_assert(sizeof(PhenomDCoef<EM>) / sizeof(EM) == nwf, "coefficient block must be an array of scalars");
+  static_assert(sizeof(Polar<ER>) / sizeof(ER) == npol, "polarisation block must be an array of scalars");
+  const GradScalar* ws = reinterpret_cast<const GradScalar*>(&a.wf);
+  EM* wd = reinterpret_cast<EM*>(&b.wf);
+  for (int k = threadIdx.x; k < nwf; k += blockDim.x) {
+    wd[k].v = ff_from(ws[k].v);
 #pragma unroll
-    for (int k = 0; k < kMixNT; ++k) dst[j].d[k] = src[j].d[k];
+    for (int t = 0; t < 4; ++t) wd[k].d[t] = ws[k].d[t];
+  }
+  const GradScalar* ps = reinterpret_cast<const GradScalar*>(&a.pol);
+  ER* pd = reinterpret_cast<ER*>(&b.pol);
+  for (int k = threadIdx.x; k < npol; k += blockDim.x) {
+    pd[k].v = ff_from(ps[k].v);
+    pd[k].d[0] = 0.0f;
+    pd[k].d[1] = ps[k].d[5];  // lambda
+    pd[k].d[2] = ps[k].d[6];  // sin beta
+    pd[k].d[3] = ps[k].d[7];  // psi
+    pd[k].d[4] = 0.0f;
   }
   if (threadIdx.x == 0) {
-    b.fcut = a.fcut;
-    b.kcut = a.kcut;
+    b.pfac.v = ff_from(a.wf.pfac.v);
+    b.cfac.v = ff_from(a.wf.cfac.v);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) b.pfac.d[t] = b.cfac.d[t] = 0.0f;
+    b.pfac.d[4] = a.wf.pfac.d[4];  // cos iota
+    b.cfac.d[4] = a.wf.cfac.d[4];
+    b.tc = ff_from(a.tc.v);
     b.status = a.status;
-    b.pad = 0;
   }
 }
 
@@ -1507,10 +1531,11 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
                                                          double2* __restrict__ model) {
   constexpr int NV = kMode == 1 ? 11 : 1;
   constexpr bool kFF = kMode != 1;  // value passes: float-float values
-  // the gradient pass evaluates with float-float values and FP32 tangents
-  using TE = std::conditional_t<kMode == 1, Dual<kMixNT, float, FF>, FF>;
+  // value passes: a float-float copy of the block; gradient pass: the split
+  // float-float block (mass/spin and response tangents)
+  using SBF = std::conditional_t<kMode == 1, ExactGradBlock, SampleBlock<FF>>;
   __shared__ SampleBlock<T> sb;
-  __shared__ SampleBlock<TE> sbf;
+  __shared__ SBF sbf;
   __shared__ double red[kExactThreads / 32][NV];
   const int s = blockIdx.y;
   const int xb = M.xbin[s];
@@ -1520,7 +1545,7 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   if constexpr (kFF) {
     narrow_block_ff(sb, sbf);
   } else {
-    narrow_block_dual_ff(sb, sbf);
+    narrow_exact_grad(sb, sbf);
   }
   __syncthreads();
   double acc[NV];
@@ -1559,36 +1584,69 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
         }
         if constexpr (kMode == 1) {
           const double f = (double)(P.k0 + i) * P.f_step;
-          TE y[kNodeQ];
-          node_eval<TE>(P, M, sbf, d, P.tdi[(size_t)d * P.nbins + i], f, y);
-          TE ph = y[0] + (2.0 * kPi * f) * sbf.tc;
-          {  // whole turns removed in FP64 (the phase reaches 1e6 rad); the tangents are unchanged
-            const double phd = ff_to(ph.v);
-            ph.v = ff_from(phd - (2.0 * kPi) * rint(phd * (1.0 / (2.0 * kPi))));
+          const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
+          // PhenomD with the mass/spin tangents
+          EM amp, psi, tf;
+          phenomd_eval<EM>(sbf.wf, sbf.wf.Msec * f, amp, psi, tf);
+          amp = amp * M.scale;
+          // response per unit amplitude with the T and sky/orientation tangents
+          Cx<ER> Y[3];
+          ER kx0;
+          {
+            ER T = lift<ER>(0.0);
+            T.v = tf.v + sbf.tc;
+            T.d[0] = 1.0f;
+            const ER zero = lift<ER>(0.0);
+            Cx<ER> L[6];
+            single_links_impl<true, ER>(P.orbit[d], f, cx(sbf.pfac, zero), cx(zero, -sbf.cfac), T, sbf.pol, L, &kx0);
+            tdi_channels<ER>(cx(tdb.dre, tdb.dim), cx(tdb.pre, tdb.pim), 1, L, Y);
           }
-          TE sn, cs;
-          dsincos(ph, &sn, &cs);
-          float gk[kMixNT];  // this bin's -2 w Re((d - h)^* dh/dtheta) over the channels (FP32)
-#pragma unroll
-          for (int k = 0; k < kMixNT; ++k) gk[k] = 0.0f;
+          // phase Psi + 2 pi f (k.x0 + t_c), whole turns removed in FP64 (it reaches 1e6 rad)
+          FF sn, cs;
+          {
+            const double phd = ff_to(psi.v + (2.0 * kPi * f) * (kx0.v + sbf.tc));
+            dsincos(ff_from(phd - (2.0 * kPi) * rint(phd * (1.0 / (2.0 * kPi)))), &sn, &cs);
+          }
+          const float csf = cs.hi, snf = sn.hi, ampf = amp.v.hi;
+          // per channel: E = conj(d - h) e^{-i ph} / scale, and with X = Y or a
+          // tangent of Y, Re(E X) and Im(E Y) (the phase derivative's factor)
+          float A0 = 0.0f, A1 = 0.0f, BT = 0.0f, Br[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
-            // h = G exp(-i ph)
-            const TE hr = (y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn) * inv_scale;
-            const TE hi = (y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn) * inv_scale;
+            const FF yr = amp.v * Y[ch].re.v, yi = amp.v * Y[ch].im.v;
+            const double hr = ff_to(yr * cs + yi * sn) * inv_scale;
+            const double hi = ff_to(yi * cs - yr * sn) * inv_scale;
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
             const double w = P.w[off];
             const double2 dv = P.data[off];
-            const double hrv = ff_to(hr.v), hiv = ff_to(hi.v);
-            const double rr = dv.x - hrv, ri = dv.y - hiv;
-            const float wr = (float)(-2.0 * w * rr), wi = (float)(-2.0 * w * ri);
+            const double rr = dv.x - hr, ri = dv.y - hi;
+            acc[4] += 2.0 * w * (rr * hr + ri * hi);  // dh/dlnD_L = -h
+            acc[9] += 4.0 * w * (rr * hi - ri * hr);  // dh/dphi_c = 2 i h
+            // -2 w E in FP64: w / scale alone can exceed the FP32 range (w = 1/S), the product is O(1)
+            const double m2w = -2.0 * w * inv_scale;
+            const double csd = (double)csf, snd = (double)snf;
+            const float er = (float)(m2w * (rr * csd - ri * snd)), ei = (float)(-m2w * (rr * snd + ri * csd));
+            const ER& Yr = Y[ch].re;
+            const ER& Yi = Y[ch].im;
+            A0 = fmaf(er, Yr.v.hi, fmaf(-ei, Yi.v.hi, A0));
+            A1 = fmaf(er, Yi.v.hi, fmaf(ei, Yr.v.hi, A1));
+            BT = fmaf(er, Yr.d[0], fmaf(-ei, Yi.d[0], BT));
 #pragma unroll
-            for (int k = 0; k < kMixNT; ++k) gk[k] = fmaf(wr, hr.d[k], fmaf(wi, hi.d[k], gk[k]));
-            acc[4] += 2.0 * w * (rr * hrv + ri * hiv);  // dh/dlnD_L = -h
-            acc[9] += 4.0 * w * (rr * hiv - ri * hrv);  // dh/dphi_c = 2 i h
+            for (int k = 0; k < 4; ++k) Br[k] = fmaf(er, Yr.d[1 + k], fmaf(-ei, Yi.d[1 + k], Br[k]));
           }
+          A1 *= ampf;
+          BT *= ampf;
+          const float tpf = (float)(2.0 * kPi * f);
+          float g[kMixNT];
 #pragma unroll
-          for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += (double)gk[k];
+          for (int k = 0; k < 4; ++k) g[k] = A0 * amp.d[k] + BT * tf.d[k] + A1 * (psi.d[k] + tpf * kx0.d[0] * tf.d[k]);
+          g[4] = ampf * Br[3] + A1 * tpf * kx0.d[4];  // cos iota
+          g[5] = ampf * Br[0] + A1 * tpf * kx0.d[1];  // lambda
+          g[6] = ampf * Br[1] + A1 * tpf * kx0.d[2];  // sin beta
+          g[7] = ampf * Br[2] + A1 * tpf * kx0.d[3];  // psi
+          g[8] = BT + A1 * tpf * (kx0.d[0] + 1.0f);   // t_c
+#pragma unroll
+          for (int k = 0; k < kMixNT; ++k) acc[kSlotParam[k]] += (double)g[k];
         }
       }
     }
