@@ -35,7 +35,7 @@ struct OrbitF {
   float ck[3], sk[3];
 };
 
-inline OrbitF orbit_f(const PesOrbit& o) {
+PES_HD OrbitF orbit_f(const PesOrbit& o) {
   OrbitF r;
   r.kind = o.kind;
   r.pad = 0;

@@ -33,7 +33,9 @@ def test_fisher_vs_oracle(cuda_lib, oracle, network, precision):
     want = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).fisher(thetas)
     assert np.all(eng.last_status.cpu().numpy() == 0)
     assert np.array_equal(got, np.swapaxes(got, 1, 2))
-    assert _normalised_err(got, want) < 1e-9
+    # FP64 plans: FP64 duals through the model; mixed plans: FP32 structured
+    # derivatives (the bar of the 11x11 Fisher rows is 1e-4 relative)
+    assert _normalised_err(got, want) < (1e-9 if precision == "fp64" else 1e-5)
     # deterministic
     assert np.array_equal(got, eng.fisher_matrix(thetas).cpu().numpy())
 
