@@ -191,8 +191,10 @@ const char* pes_kernel_class_name(int32_t k);
 
 /* Fisher matrices at B parameter sets (row-major (B, 11, 11), parameter order
  * of theta): F_ij = 4 df Re sum_{det, c, f} conj(dh_i) dh_j / S_c(f) over the
- * plan's channels and each sample's live bins, derivatives of the A/E/T model
- * by FP64 forward-mode dual numbers (both precisions of plan).  The data are
+ * plan's channels and each sample's live bins.  FP64 plans take the
+ * derivatives of the A/E/T model by FP64 forward-mode dual numbers; mixed
+ * plans by the model's structure (PhenomD tangents in float-float, response
+ * tangents in FP32; within a few 1e-6 of sqrt(F_ii F_jj) of the FP64 result).  The data are
  * not used, only the PSDs.  Replaces pespace/inference/fisher.py:27-162
  * (fisher_matrix).  Out-of-domain samples get NaN and their status.  The first
  * call allocates the plan's Fisher workspace (about 6 KB + 25 KB per sample of
