@@ -130,6 +130,28 @@ int pes_phenomd(const double* theta /* host */, const double* freqs, int64_t n, 
  * FP64.  1 <= B <= 65535 per call. */
 int pes_pn_tf(const double* params, int64_t B, const double* freqs, int64_t n, double* tf, void* stream);
 
+/* Time-domain Michelson TDI for constant equal arms: replaces
+ * TDMichelsonConstantEqualArm.update_tdi_response() (pespace/detector/tdi.py:
+ * 1460-1600; the reference marks the class incomplete, and its arithmetic is
+ * followed as written).  links: device, (B, 6, n_ext) doubles, the single-link
+ * time series in the order link12, 21, 23, 32, 31, 13 (utils.py:22-29);
+ * out: device, (B, 3, n) doubles, A, E, T (orthogonal != 0) or X, Y, Z.
+ * Output sample i reads link samples i .. i + added; n_ext >= n + added, where
+ * added = int(max_delay * arm_sec // delta_time + 1) (tdi.py:1449-1454),
+ * max_delay 3 (generation 15) or 7 (20).  FP64, bit-identical to the
+ * reference's operation order.  0 <= B <= 65535. */
+int pes_td_tdi_combination(const double* links, int64_t B, int64_t n_ext, int64_t n, double arm_sec,
+                           double delta_time, int32_t generation, int32_t orthogonal, double* out, void* stream);
+
+/* Host only: the delay layout pes_td_tdi_combination uses, the reference's
+ * expressions on Python floats (tdi.py:1449-1454, 1469-1491): added (above),
+ * max_delay, and for delay k = 0 .. max_delay-1 the left sample offset
+ * shifts[k] = (max_delay - k - 1) * arm_sec // delta_time and the weight
+ * fracs[k] = 1 - ((k + 1) * arm_sec % delta_time) / delta_time of the right
+ * sample.  shifts and fracs: host, 7 entries each. */
+int pes_td_tdi_layout(double arm_sec, double delta_time, int32_t generation, int64_t* added, int32_t* max_delay,
+                      int64_t* shifts, double* fracs);
+
 /* ---------------------------------------------------------------- plans --
  * Batched lnL / lnL+gradient over B parameter samples: the per-sample loop of
  * LikelihoodBilbyInterfaceTaichi.log_likelihood (interface_bilby.py:78-116) and

@@ -1,6 +1,7 @@
 // Granular drop-in entry points: one per reference plugin method (orbit
 // vectors, single-link response, TDI combination, Whittle likelihood) plus the
 // IMRPhenomD waveform producer.  FP64 throughout, one thread per frequency.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <mutex>
@@ -282,6 +283,166 @@ __global__ void k_pn_tf(const double* __restrict__ params, int64_t n, const doub
   tf[b * n + i] = (x < kPnXIsco && x > 0.0) ? -c.msec / (2.0 * kPi) * (pn_dpsi(c, x) - c.d_isco) : 0.0;
 }
 
+// ------------------------------------------------ time-domain Michelson TDI
+// TDMichelsonConstantEqualArm.update_tdi_response (pespace/detector/tdi.py:
+// 1460-1600): every output sample i combines the six single-link series at
+// the undelayed sample i + added and, for each delay k = 0..max_delay-1, the
+// linear interpolation left + (right - left) * frac_k between samples
+// i + shift_k and i + shift_k + 1 (utils.py:83-100).  The shifts, fractions and
+// `added` are the reference's expressions on Python floats (tdi.py:1449-1454,
+// 1469-1491), evaluated on the host by td_layout.  The arithmetic keeps the
+// reference's order with no contraction (explicit round-to-nearest adds and
+// multiplies), so the result is bit-identical to a left-to-right evaluation.
+//
+// HBM-bound: each block stages the window [i0, i0 + kTdTile + added + 1) of its
+// six link series in shared memory with coalesced loads and writes kTdTile
+// outputs per channel; per output sample the unique traffic is 6 x 8 B read
+// and 3 x 8 B written.  A window beyond kTdMaxWindow samples (added > 3071,
+// e.g. sub-0.02 s sampling) reads through the L1 instead.
+
+struct TdLayout {
+  int max_delay;
+  int64_t added;
+  int64_t shift[7];
+  double frac[7];
+  double rs2, rs6, rs3;  // sqrt(2), sqrt(6), sqrt(3), correctly rounded
+};
+
+constexpr int kTdThreads = 256;
+constexpr int kTdTile = 1024;
+constexpr int kTdMaxWindow = 4096;  // 6 x 4096 x 8 B = 192 KB of shared memory
+
+// Python's float // and % (CPython's divmod: floor of (a - fmod(a, b)) / b,
+// rounded to the nearest integer when it lands within half of one).
+static void py_divmod(double a, double b, double* floordiv, double* mod) {
+  double m = std::fmod(a, b);
+  double div = (a - m) / b;
+  if (m != 0.0) {
+    if ((b < 0) != (m < 0)) {
+      m += b;
+      div -= 1.0;
+    }
+  } else {
+    m = std::copysign(0.0, b);
+  }
+  double fd;
+  if (div != 0.0) {
+    fd = std::floor(div);
+    if (div - fd > 0.5) fd += 1.0;
+  } else {
+    fd = std::copysign(0.0, a / b);
+  }
+  *floordiv = fd;
+  *mod = m;
+}
+
+static void td_layout(double arm, double dt, int gen20, TdLayout& lay) {
+  lay.max_delay = gen20 ? 7 : 3;
+  double q, r;
+  py_divmod(lay.max_delay * arm, dt, &q, &r);
+  lay.added = (int64_t)(q + 1.0);  // int(max_num_delay * armlength // delta_time + 1)
+  for (int k = 0; k < 7; ++k) {
+    lay.shift[k] = 0;
+    lay.frac[k] = 0.0;
+  }
+  for (int k = 0; k < lay.max_delay; ++k) {
+    const int nd = k + 1;
+    py_divmod(nd * arm, dt, &q, &r);
+    lay.frac[k] = 1.0 - r / dt;  // 1 - (num_delay * armlength % delta_time) / delta_time
+    py_divmod((lay.max_delay - nd) * arm, dt, &q, &r);
+    lay.shift[k] = (int64_t)q;  // (max_num_delay - num_delay) * armlength // delta_time
+  }
+  lay.rs2 = std::sqrt(2.0);
+  lay.rs6 = std::sqrt(6.0);
+  lay.rs3 = std::sqrt(3.0);
+}
+
+// grid (ceil(n / kTdTile), B); links [B][6][n_ext] in the order link12, link21,
+// link23, link32, link31, link13; out [B][3][n].
+template <int kMaxDelay, bool kStaged>
+__global__ void __launch_bounds__(kTdThreads) k_td_tdi(TdLayout lay, const double* __restrict__ links, int64_t n_ext,
+                                                       int64_t n, int orth, double* __restrict__ out) {
+  extern __shared__ double td_win[];  // [6][win]
+  const double* src = links + (int64_t)blockIdx.y * 6 * n_ext;
+  double* dst = out + (int64_t)blockIdx.y * 3 * n;
+  const int64_t i0 = (int64_t)blockIdx.x * kTdTile;
+  const int64_t win = kTdTile + lay.added + 1;
+  if (kStaged) {
+    const int64_t avail = n_ext - i0;
+#pragma unroll 1
+    for (int l = 0; l < 6; ++l) {
+      const double* s = src + (int64_t)l * n_ext + i0;
+      double* w = td_win + l * win;
+#pragma unroll 4
+      for (int64_t j = threadIdx.x; j < win; j += kTdThreads) w[j] = j < avail ? __ldg(s + j) : 0.0;
+    }
+    __syncthreads();
+  }
+  // X = sum of the "plus" terms, then minus the "minus" terms, in the order of
+  // tdi.py:1506-1591 (k = -1: the undelayed sample); Y and Z are the cyclic
+  // relabelling 1 -> 2 -> 3 -> 1, i.e. link index l -> (l + 2) mod 6.
+  constexpr int kTerms = kMaxDelay + 1;
+  constexpr int xp[8] = {5, 4, 0, 1, 0, 1, 5, 4};
+  constexpr int xm[8] = {0, 1, 5, 4, 5, 4, 0, 1};
+#pragma unroll 1
+  for (int r = 0; r < kTdTile / kTdThreads; ++r) {
+    const int64_t t = threadIdx.x + r * kTdThreads;
+    const int64_t i = i0 + t;
+    if (i >= n) break;
+    auto at = [&](int l, int64_t off) -> double {
+      return kStaged ? td_win[l * win + t + off] : __ldg(src + (int64_t)l * n_ext + i + off);
+    };
+    auto term = [&](int l, int k) -> double {
+      if (k < 0) return at(l, lay.added);
+      const double left = at(l, lay.shift[k]), right = at(l, lay.shift[k] + 1);
+      return __dadd_rn(left, __dmul_rn(__dsub_rn(right, left), lay.frac[k]));
+    };
+    double ch[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double acc = term((xp[0] + 2 * c) % 6, -1);
+#pragma unroll
+      for (int j = 1; j < kTerms; ++j) acc = __dadd_rn(acc, term((xp[j] + 2 * c) % 6, j - 1));
+#pragma unroll
+      for (int j = 0; j < kTerms; ++j) acc = __dsub_rn(acc, term((xm[j] + 2 * c) % 6, j - 1));
+      ch[c] = acc;
+    }
+    if (orth) {
+      const double X = ch[0], Y = ch[1], Z = ch[2];
+      dst[i] = __ddiv_rn(__dsub_rn(Z, X), lay.rs2);
+      dst[n + i] = __ddiv_rn(__dadd_rn(__dsub_rn(X, __dmul_rn(2.0, Y)), Z), lay.rs6);
+      dst[2 * n + i] = __ddiv_rn(__dadd_rn(__dadd_rn(X, Y), Z), lay.rs3);
+    } else {
+      dst[i] = ch[0];
+      dst[n + i] = ch[1];
+      dst[2 * n + i] = ch[2];
+    }
+  }
+}
+
+template <int kMaxDelay>
+static int launch_td_tdi(const TdLayout& lay, const double* links, int64_t B, int64_t n_ext, int64_t n, int orth,
+                         double* out, cudaStream_t st) {
+  const dim3 grid((unsigned)((n + kTdTile - 1) / kTdTile), (unsigned)B);
+  const int64_t win = kTdTile + lay.added + 1;
+  if (win <= kTdMaxWindow) {
+    const size_t smem = (size_t)6 * win * sizeof(double);
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_td_tdi<kMaxDelay, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) {
+        set_error("pes_td_tdi_combination: %s", cudaGetErrorString(e));
+        return PES_ECUDA;
+      }
+    }
+    k_td_tdi<kMaxDelay, true><<<grid, kTdThreads, smem, st>>>(lay, links, n_ext, n, orth, out);
+  } else {
+    k_td_tdi<kMaxDelay, false><<<grid, kTdThreads, 0, st>>>(lay, links, n_ext, n, orth, out);
+  }
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
 extern "C" {
 
 const char* pes_last_error(void) { return pes::g_error; }
@@ -424,6 +585,54 @@ int pes_pn_tf(const double* params, int64_t B, const double* freqs, int64_t n, d
   k_pn_tf<<<dim3(ceil_div(n, 256), (unsigned)B), 256, 0, as_stream(stream)>>>(params, n, freqs, tf);
   PES_CHECK_LAUNCH();
   return PES_OK;
+}
+
+int pes_td_tdi_layout(double arm_sec, double delta_time, int32_t generation, int64_t* added, int32_t* max_delay,
+                      int64_t* shifts, double* fracs) {
+  PES_REQUIRE(generation == 15 || generation == 20, "pes_td_tdi_layout: unsupported generation %d", generation);
+  PES_REQUIRE(std::isfinite(arm_sec) && arm_sec > 0.0 && std::isfinite(delta_time) && delta_time > 0.0,
+              "pes_td_tdi_layout: arm length and sampling step must be finite and > 0 (%g, %g)", arm_sec,
+              delta_time);
+  PES_REQUIRE(added && max_delay && shifts && fracs, "pes_td_tdi_layout: null pointer");
+  PES_REQUIRE(7.0 * arm_sec / delta_time < 1e9, "pes_td_tdi_layout: delay of %g samples too long",
+              7.0 * arm_sec / delta_time);
+  TdLayout lay;
+  td_layout(arm_sec, delta_time, generation == 20, lay);
+  *added = lay.added;
+  *max_delay = lay.max_delay;
+  for (int k = 0; k < lay.max_delay; ++k) {
+    shifts[k] = lay.shift[k];
+    fracs[k] = lay.frac[k];
+  }
+  return PES_OK;
+}
+
+int pes_td_tdi_combination(const double* links, int64_t B, int64_t n_ext, int64_t n, double arm_sec,
+                           double delta_time, int32_t generation, int32_t orthogonal, double* out, void* stream) {
+  PES_REQUIRE(generation == 15 || generation == 20, "pes_td_tdi_combination: unsupported generation %d",
+              generation);
+  PES_REQUIRE(std::isfinite(arm_sec) && arm_sec > 0.0 && std::isfinite(delta_time) && delta_time > 0.0,
+              "pes_td_tdi_combination: arm length and sampling step must be finite and > 0 (%g, %g)", arm_sec,
+              delta_time);
+  PES_REQUIRE(B >= 0 && B <= 65535 && n >= 0 && n_ext >= 0,
+              "pes_td_tdi_combination: bad sizes (B = %lld, n = %lld, n_ext = %lld)", (long long)B, (long long)n,
+              (long long)n_ext);
+  PES_REQUIRE(7.0 * arm_sec / delta_time < 1e9, "pes_td_tdi_combination: delay of %g samples too long",
+              7.0 * arm_sec / delta_time);
+  TdLayout lay;
+  td_layout(arm_sec, delta_time, generation == 20, lay);
+  for (int k = 0; k < lay.max_delay; ++k)  // every read stays in [i, i + added]
+    PES_REQUIRE(lay.shift[k] >= 0 && lay.shift[k] + 1 <= lay.added,
+                "pes_td_tdi_combination: delay layout out of range (shift %lld, added %lld)",
+                (long long)lay.shift[k], (long long)lay.added);
+  PES_REQUIRE(n_ext >= n + lay.added,
+              "pes_td_tdi_combination: %lld link samples for %lld outputs, need n + %lld (the longest delay)",
+              (long long)n_ext, (long long)n, (long long)lay.added);
+  if (B == 0 || n == 0) return PES_OK;
+  PES_REQUIRE(links && out, "pes_td_tdi_combination: null pointer");
+  const cudaStream_t st = as_stream(stream);
+  return generation == 20 ? launch_td_tdi<7>(lay, links, B, n_ext, n, orthogonal != 0, out, st)
+                          : launch_td_tdi<3>(lay, links, B, n_ext, n, orthogonal != 0, out, st);
 }
 
 }  // extern "C"

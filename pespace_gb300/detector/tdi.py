@@ -204,3 +204,69 @@ class FDMichelsonConstantEqualArm:
         _lib.check(_lib.load().pes_tdi_combination(
             _lib.ptr(freqs), n, det.orbit_model.arm_length_sec(0.0), self.generation_code, int(self.orthogonal),
             _lib.ptr(det.single_link_response), _lib.ptr(det.tdi_response), _lib.stream_handle()))
+
+
+class TDMichelsonConstantEqualArm:
+    """tdi.py:1388-1600: time-domain Michelson TDI with constant equal arms.
+
+    The reference marks this class incomplete; the combination it defines is
+    kept as written (``pes_td_tdi_combination``): output sample i combines the
+    six single-link time series at sample i + ``added_time_samples_number``
+    and, for k + 1 = 1..max_num_delay arm lengths, their linear interpolation
+    between samples i + shift_k and i + shift_k + 1 with the reference's
+    shifts and weights.  ``detector.single_link_response`` is a (6,
+    ``extended_time_series_length``) float64 CUDA tensor in the order link12,
+    link21, link23, link32, link31, link13; ``detector.tdi_response`` is the
+    (3, ``time_series_length``) float64 result, rows in ``labels`` order.
+    """
+
+    domain = "td"
+
+    def __init__(self, generation="1.5", orthogonal=True, backend="cuda"):
+        self.generation = str(generation)
+        if self.generation == "1.5":
+            self.max_num_delay = 3
+        elif self.generation == "2.0":
+            self.max_num_delay = 7
+        else:
+            raise ValueError(f"Unsupported generation {self.generation}.")
+        if backend != "cuda":
+            raise ValueError(f"Unknown backend: {backend}")
+        self.orthogonal = bool(orthogonal)
+        self.labels = ("A", "E", "T") if self.orthogonal else ("X", "Y", "Z")
+        self.backend = backend
+        self.detector = None
+        self.added_time_samples_number = None
+        self.extended_time_series_length = None
+
+    @property
+    def generation_code(self):
+        return 15 if self.generation == "1.5" else 20
+
+    @staticmethod
+    def _arm_sec(orbit_model):
+        arm = getattr(orbit_model, "armlength_sec", None)
+        if arm is None:
+            arm = orbit_model.arm_length_sec(0.0)
+        return float(arm)
+
+    def init_tdi_combination_model(self, detector):
+        self.detector = detector
+        info = detector.tdi_data.data_info
+        n = int(info.time_series_length)
+        self.added_time_samples_number = int(
+            self.max_num_delay * self._arm_sec(detector.orbit_model) // info.delta_time + 1)
+        self.extended_time_series_length = int(n + self.added_time_samples_number)
+        detector.tdi_response = torch.zeros((3, n), dtype=torch.float64, device="cuda")
+
+    def update_tdi_response(self):
+        det = self.detector
+        links = det.single_link_response
+        out = det.tdi_response
+        n, n_ext = out.shape[-1], links.shape[-1]
+        if links.dtype != torch.float64 or not links.is_cuda or links.shape[-2:] != (6, n_ext) \
+                or not links.is_contiguous():
+            raise ValueError("single_link_response must be a contiguous (6, n_ext) float64 CUDA tensor")
+        _lib.check(_lib.load().pes_td_tdi_combination(
+            _lib.ptr(links), 1, n_ext, n, self._arm_sec(det.orbit_model), float(det.tdi_data.data_info.delta_time),
+            self.generation_code, int(self.orthogonal), _lib.ptr(out), _lib.stream_handle()))
