@@ -314,9 +314,16 @@ def run_td_tdi(args):
     e2e_ms = replicas.reduce_max(float(np.mean(e2e)), "cuda")
     if rank != 0:
         return
+    from pespace_gb300 import census
+
     peaks = measured_peaks() or {}
-    peak = peaks.get("hbm_gbs")
-    achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+    # the reference's operation order leaves every FP64 operation unfused: the FP64 pipe binds
+    ops = census.td_tdi_fp64_ops_per_sample(7) * B * n
+    dgemm = gemm_peak_tflops(torch, torch.float64)
+    op_peak = dgemm * 1e3 / 2.0  # G instructions/s: one DFMA instruction is 2 flops
+    op_achieved = ops / (mean_ms / 1e3) / 1e9
     line = {
         "metric": TD_METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
@@ -327,10 +334,15 @@ def run_td_tdi(args):
         "e2e": {"value": world * B * n / (e2e_ms / 1e3), "unit": "samples/s",
                 "h2d_bytes_per_step": int(B * 6 * n_ext * 8), "d2h_bytes_per_step": int(B * 3 * n * 8)},
         "gpu_launches": args.steps,
-        "roofline": {"kernel": "k_td_tdi<7, staged>", "bound": "hbm", "unit": "GB/s", "achieved": achieved,
-                     "peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)",
-                     "frac": achieved / peak if peak else None, "traffic": None,
-                     "units_per_launch": {"samples": B * n, "algorithmic_bytes": alg_bytes}},
+        "roofline": {"kernel": "k_td_tdi<7, staged>", "bound": "fp64", "unit": "G FP64 op/s",
+                     "achieved": op_achieved, "peak": op_peak,
+                     "peak_source": "measured cuBLAS DGEMM 8192^3 in bench.py, flops / 2 (one DFMA = 2 flops)",
+                     "frac": op_achieved / op_peak,
+                     "traffic": census.TD_TDI_DRAM_BYTES_PER_SAMPLE * B * n,
+                     "units_per_launch": {"samples": B * n, "algorithmic_bytes": alg_bytes, "fp64_ops": ops},
+                     "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)",
+                             "frac": hbm_achieved / hbm_peak if hbm_peak else None}},
         "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:
@@ -463,6 +475,21 @@ def run_native(args):
                      "n_lnl_le_1e6": int(quiet.sum().item()),
                      "n_within_1e-2": int((d <= 1e-2).sum().item()),
                      "max_rel": float((d / b.abs().clamp_min(1.0)).max().item())}
+        # the templates a sampler visits: draws from the Fisher approximation of the posterior
+        # about the injection (covariance F^-1 of the FP64 plan's Fisher matrix)
+        from pespace_gb300.inference.fisher import sample_from_fisher
+
+        try:
+            F = ref.fisher_matrix(torch.as_tensor(th0[None], dtype=torch.float64, device="cuda"))[0]
+            n_post = min(B, 256)
+            post = torch.as_tensor(th0[None] + sample_from_fisher(F, n_post, 2026), device="cuda")
+            bp = ref.log_likelihood_batch(post)
+            dp = (eng.log_likelihood_batch(post) - bp).abs()
+            err_split.update(posterior_draws=n_post, max_abs_posterior=float(dp.max().item()),
+                             median_abs_posterior=float(dp.median().item()),
+                             lnl_range_posterior=[float(bp.min().item()), float(bp.max().item())])
+        except np.linalg.LinAlgError:
+            err_split.update(posterior_draws=0)
         del ref
 
     # ---------------- roofline of the dominant kernel (the dense stage)

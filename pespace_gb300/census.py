@@ -60,3 +60,20 @@ def roofline(kernel_class, launches_ms, steps, work, grad, fp32_peak_tflops):
         if DRAM_BYTES_PER_DENSE_BIN is not None:
             entry["traffic"] = DRAM_BYTES_PER_DENSE_BIN * bins
     return entry
+
+
+# Time-domain TDI (k_td_tdi): FP64 operations per output sample, counted from
+# the kernel source.  For max_delay m: 6 m interpolations of 3 operations
+# (subtract, multiply, add), 3 channels of 2 (m + 1) - 1 signed sums, and the
+# A/E/T combination (7 adds/multiplies and 3 divisions, one operation each).
+# The operation order is the reference's, kept for bit-identical results, so
+# none of them contract into FMAs.
+def td_tdi_fp64_ops_per_sample(max_delay):
+    return 3 * 6 * max_delay + 3 * (2 * (max_delay + 1) - 1) + 10
+
+
+# DRAM bytes of one k_td_tdi<7> launch over 8 388 609 output samples (ncu
+# --set full: 402.81 MB read + 163.36 MB written), per output sample.  The
+# algorithmic figure is 72 B (six 8-byte link samples read, three written);
+# part of the last writes is still in L2 when the kernel ends.
+TD_TDI_DRAM_BYTES_PER_SAMPLE = (402.806784e6 + 163.362816e6) / 8388609
