@@ -63,13 +63,14 @@ def roofline(kernel_class, launches_ms, steps, work, grad, fp32_peak_tflops):
 
 
 # Time-domain TDI (k_td_tdi): FP64 operations per output sample, counted from
-# the kernel source.  For max_delay m: 6 m interpolations of 3 operations
-# (subtract, multiply, add), 3 channels of 2 (m + 1) - 1 signed sums, and the
-# A/E/T combination (7 adds/multiplies and 3 divisions, one operation each).
-# The operation order is the reference's, kept for bit-identical results, so
-# none of them contract into FMAs.
+# the kernel source.  For max_delay m: 6 differences of neighbouring link
+# samples (staged once per sample and shared by the delays), 6 m
+# interpolations of 2 operations (multiply, add), 3 channels of 2 (m + 1) - 1
+# signed sums, and the A/E/T combination (7 adds/multiplies and 3 divisions,
+# one operation each).  The operation order is the reference's, kept for
+# bit-identical results, so none of them contract into FMAs.
 def td_tdi_fp64_ops_per_sample(max_delay):
-    return 3 * 6 * max_delay + 3 * (2 * (max_delay + 1) - 1) + 10
+    return 6 + 2 * 6 * max_delay + 3 * (2 * (max_delay + 1) - 1) + 10
 
 
 # DRAM bytes of one k_td_tdi<7> launch over 8 388 609 output samples (ncu

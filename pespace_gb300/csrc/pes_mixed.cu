@@ -423,8 +423,12 @@ struct BwdBlock {
 __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd_split(PlanDev P, MixedDev M, GenArg G,
                                                                       double wscale) {
   __shared__ BwdBlock sb;
-  __shared__ double red[kSparseThreads / 32][11];
+  __shared__ float2 red[kSparseThreads / 32][11];  // per warp: float-float partial sums
+  __shared__ double kadd[6][5];                     // dense-side kink terms, added in order to warp 0's sums
+  __shared__ int kink_on;
+  __shared__ float kR[6];  // the kink coefficients R_q held fixed, narrowed once
   const int s = blockIdx.z, d = blockIdx.y;
+  if (threadIdx.x < 6) kR[threadIdx.x] = (float)M.kinkR[((size_t)s * M.n_det + d) * 6 + threadIdx.x];
   {
     // narrow the sample's gradient block (FP64 values, FP32 tangents in slots 0-8)
     const SampleBlock<GradScalar>& g = reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks)[s];
@@ -518,11 +522,10 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd_split(PlanDev 
       GM ahat, jump;
       amp_peak_jump<GM>(sb.wf, ahat, jump);
       const GM x2h = 0.5 * (xk * xk) * jump;
-      const double* R = M.kinkR + ((size_t)s * M.n_det + d) * 6;
       float WR = 0.0f;
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
-        const float Rq = (float)R[q];
+        const float Rq = kR[q];
         WR = fmaf(W[1 + q], Rq, WR);
         yv[q] -= Rq * x2h.v;
       }
@@ -543,26 +546,25 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd_split(PlanDev 
     acc[4] = a4;
     acc[9] = -2.0f * W[0];  // Phi_s = ... - 2 phi_c
   }
-  // block sum: float-float across the warp, FP64 across warps
-  double accd[11];
-  {
-    const int l = threadIdx.x & 31;
+  // block sum: float-float across the warp (FP32 pipe); the FP64 pipe (1/64
+  // of the FP32 rate) only in the 11 threads that add the warps' partials
+  const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
-    for (int k = 0; k < 11; ++k) {
-      float hi = acc[k], lo = 0.0f;
+  for (int k = 0; k < 11; ++k) {
+    float hi = acc[k], lo = 0.0f;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float oh = __shfl_down_sync(0xffffffffu, hi, o);
-        const float ol = __shfl_down_sync(0xffffffffu, lo, o);
-        float th, tl;
-        two_sum(hi, oh, th, tl);
-        hi = th;
-        lo += tl + ol;
-      }
-      accd[k] = (l == 0) ? (double)hi + (double)lo : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+      const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+      float th, tl;
+      two_sum(hi, oh, th, tl);
+      hi = th;
+      lo += tl + ol;
     }
+    if (l == 0) red[wid][k] = make_float2(hi, lo);
   }
   // dense-side kink term C_q x^2 (x = Msec f - Mf_peak): one thread per (sample, detector)
+  if (threadIdx.x == 0) kink_on = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0 && sb.status == kSampleOk && ns >= 3) {
     GM ahat, jump;
     amp_peak_jump<GM>(sb.wf, ahat, jump);
@@ -574,22 +576,24 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd_split(PlanDev 
       const double K2 = wscale * K[q], K1 = wscale * K[6 + q];
       const double K1f = (K2 + (double)sb.wf.fpeak.v * K1) / (double)sb.wf.Msec.v;
       for (int k = 0; k < 4; ++k)
-        accd[k] += 0.5 * R[q] * K2 * (double)jump.d[k] +
-                   2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
-      accd[4] -= C[q] * K2;  // C_q ~ 1/D_L
+        kadd[q][k] = 0.5 * R[q] * K2 * (double)jump.d[k] +
+                     2.0 * C[q] * (K1f * (double)sb.wf.Msec.d[k] - K1 * (double)sb.wf.fpeak.d[k]);
+      kadd[q][4] = -(C[q] * K2);  // C_q ~ 1/D_L
     }
-  }
-  const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) {
-#pragma unroll
-    for (int k = 0; k < 11; ++k) red[wid][k] = accd[k];
+    kink_on = 1;
   }
   __syncthreads();
   if (threadIdx.x < 11) {
+    const int k = threadIdx.x;
     double x = 0.0;
 #pragma unroll
-    for (int w = 0; w < kSparseThreads / 32; ++w) x += red[w][threadIdx.x];
-    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + threadIdx.x] = x;
+    for (int w = 0; w < kSparseThreads / 32; ++w) {
+      double v = (double)red[w][k].x + (double)red[w][k].y;
+      if (w == 0 && kink_on && k < 5)
+        for (int q = 0; q < 6; ++q) v += kadd[q][k];
+      x += v;
+    }
+    M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + blockIdx.x) * 11 + k] = x;
   }
 }
 

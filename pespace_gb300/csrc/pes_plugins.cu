@@ -294,11 +294,16 @@ __global__ void k_pn_tf(const double* __restrict__ params, int64_t n, const doub
 // reference's order with no contraction (explicit round-to-nearest adds and
 // multiplies), so the result is bit-identical to a left-to-right evaluation.
 //
-// HBM-bound: each block stages the window [i0, i0 + kTdTile + added + 1) of its
-// six link series in shared memory with coalesced loads and writes kTdTile
-// outputs per channel; per output sample the unique traffic is 6 x 8 B read
-// and 3 x 8 B written.  A window beyond kTdMaxWindow samples (added > 3071,
-// e.g. sub-0.02 s sampling) reads through the L1 instead.
+// Each block stages the window [i0, i0 + kTdTile + added + 1) of its six link
+// series in shared memory with coalesced loads, and beside it the differences
+// right - left of neighbouring samples: every delay that reads a sample pair
+// reuses its difference (the same subtraction of the same operands), which
+// takes 6 instead of 6 max_delay FP64 subtractions per output sample.  Per
+// output sample the unique traffic is 6 x 8 B read and 3 x 8 B written, but
+// the reference's operation order leaves about 145 unfused FP64 operations,
+// so the FP64 pipe (1/64 of the FP32 rate) binds, not HBM.  A window beyond
+// kTdMaxWindow samples (added > 1535, e.g. sub-0.04 s sampling) reads
+// through the L1 and subtracts per delay instead.
 
 struct TdLayout {
   int max_delay;
@@ -309,8 +314,8 @@ struct TdLayout {
 };
 
 constexpr int kTdThreads = 256;
-constexpr int kTdTile = 1024;
-constexpr int kTdMaxWindow = 4096;  // 6 x 4096 x 8 B = 192 KB of shared memory
+constexpr int kTdTile = 512;
+constexpr int kTdMaxWindow = 2048;  // values and differences: 12 x 2048 x 8 B = 192 KB of shared memory
 
 // Python's float // and % (CPython's divmod: floor of (a - fmod(a, b)) / b,
 // rounded to the nearest integer when it lands within half of one).
@@ -362,11 +367,12 @@ static void td_layout(double arm, double dt, int gen20, TdLayout& lay) {
 template <int kMaxDelay, bool kStaged>
 __global__ void __launch_bounds__(kTdThreads) k_td_tdi(TdLayout lay, const double* __restrict__ links, int64_t n_ext,
                                                        int64_t n, int orth, double* __restrict__ out) {
-  extern __shared__ double td_win[];  // [6][win]
+  extern __shared__ double td_win[];  // [6][win] values, then [6][win] differences
   const double* src = links + (int64_t)blockIdx.y * 6 * n_ext;
   double* dst = out + (int64_t)blockIdx.y * 3 * n;
   const int64_t i0 = (int64_t)blockIdx.x * kTdTile;
   const int64_t win = kTdTile + lay.added + 1;
+  double* td_dif = td_win + 6 * win;
   if (kStaged) {
     const int64_t avail = n_ext - i0;
 #pragma unroll 1
@@ -375,6 +381,14 @@ __global__ void __launch_bounds__(kTdThreads) k_td_tdi(TdLayout lay, const doubl
       double* w = td_win + l * win;
 #pragma unroll 4
       for (int64_t j = threadIdx.x; j < win; j += kTdThreads) w[j] = j < avail ? __ldg(s + j) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int l = 0; l < 6; ++l) {
+      const double* w = td_win + l * win;
+      double* df = td_dif + l * win;
+#pragma unroll 4
+      for (int64_t j = threadIdx.x; j + 1 < win; j += kTdThreads) df[j] = __dsub_rn(w[j + 1], w[j]);
     }
     __syncthreads();
   }
@@ -394,8 +408,9 @@ __global__ void __launch_bounds__(kTdThreads) k_td_tdi(TdLayout lay, const doubl
     };
     auto term = [&](int l, int k) -> double {
       if (k < 0) return at(l, lay.added);
-      const double left = at(l, lay.shift[k]), right = at(l, lay.shift[k] + 1);
-      return __dadd_rn(left, __dmul_rn(__dsub_rn(right, left), lay.frac[k]));
+      const double left = at(l, lay.shift[k]);
+      const double dif = kStaged ? td_dif[l * win + t + lay.shift[k]] : __dsub_rn(at(l, lay.shift[k] + 1), left);
+      return __dadd_rn(left, __dmul_rn(dif, lay.frac[k]));
     };
     double ch[3];
 #pragma unroll
@@ -426,7 +441,7 @@ static int launch_td_tdi(const TdLayout& lay, const double* links, int64_t B, in
   const dim3 grid((unsigned)((n + kTdTile - 1) / kTdTile), (unsigned)B);
   const int64_t win = kTdTile + lay.added + 1;
   if (win <= kTdMaxWindow) {
-    const size_t smem = (size_t)6 * win * sizeof(double);
+    const size_t smem = (size_t)12 * win * sizeof(double);
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(k_td_tdi<kMaxDelay, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);

@@ -39,7 +39,7 @@ def test_layout_follows_python_float_semantics():
     lib = _lib.load()
     rng = np.random.default_rng(11)
     cases = [(1.0, 0.1), (0.3, 0.1), (8.0, 1.0), (8.0, 0.25), (LISA_ARM_SEC, 5.0), (LISA_ARM_SEC, 0.25),
-             (10.0, 4.0), (0.5773502691896258, 0.1), (438.6, 1.0), (438.8, 1.0), (2.0, 3.0)]
+             (10.0, 4.0), (0.5773502691896258, 0.1), (219.2, 1.0), (219.4, 1.0), (2.0, 3.0)]
     cases += [(float(a), float(d)) for a, d in zip(rng.uniform(0.1, 40.0, 200), rng.uniform(0.01, 10.0, 200))]
     cases += [(k * d, d) for k in (1, 3, 7, 9) for d in (0.1, 0.2, 0.3, 0.7, 1.1)]  # exact-multiple edges
     for arm, dt in cases:
@@ -160,8 +160,8 @@ def _run_gpu(links, n, arm, dt, gen, orth):
     (3e9 / 299792458.0, 0.25, 4096),    # Taiji, whole tiles
     (0.5773502691896258, 0.1, 1),       # TianQin, one sample
     (4.0, 0.5, 2049),                   # whole-sample delays
-    (438.6, 1.0, 3000),                 # 2.0: window of 4096 samples, the largest staged
-    (438.8, 1.0, 3000),                 # 2.0: 4097 samples, read through the L1
+    (219.2, 1.0, 3000),                 # 2.0: window of 2048 samples, the largest staged
+    (219.4, 1.0, 3000),                 # 2.0: 2049 samples, read through the L1
     (LISA_ARM_SEC, 0.002, 3000),        # long delays: L1 path for both generations
 ])
 def test_gpu_matches_oracle(cuda_lib, gen, orth, arm, dt, n):
