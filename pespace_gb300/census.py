@@ -74,7 +74,7 @@ def td_tdi_fp64_ops_per_sample(max_delay):
 
 
 # DRAM bytes of one k_td_tdi<7> launch over 8 388 609 output samples (ncu
-# --set full: 402.81 MB read + 163.36 MB written), per output sample.  The
+# --set full: 402.73 MB read + 167.52 MB written), per output sample.  The
 # algorithmic figure is 72 B (six 8-byte link samples read, three written);
 # part of the last writes is still in L2 when the kernel ends.
-TD_TDI_DRAM_BYTES_PER_SAMPLE = (402.806784e6 + 163.362816e6) / 8388609
+TD_TDI_DRAM_BYTES_PER_SAMPLE = (402.726144e6 + 167.52e6) / 8388609
