@@ -295,6 +295,28 @@ def run_td_tdi(args):
     value = world * B * n / (mean_ms / 1e3)
     alg_bytes = B * (6 * n_ext + 3 * n) * 8
 
+    # the float-float entry point on the same series, against the exact result
+    out_ff = torch.empty_like(out)
+
+    def call_ff(x, y):
+        _lib.check(lib.pes_td_tdi_combination_mixed(_lib.ptr(x), B, n_ext, n, arm, DT, 20, 1, _lib.ptr(y),
+                                                    _lib.stream_handle()))
+
+    for _ in range(max(3, args.warmup)):
+        call_ff(links, out_ff)
+    ev_ff = []
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        call_ff(links, out_ff)
+        e.record()
+        ev_ff.append((s, e))
+    barrier()
+    ff_ms = replicas.reduce_max(float(np.mean([s.elapsed_time(e) for s, e in ev_ff])), "cuda")
+    ff_err = float(((out_ff - out).abs().max() / links.abs().max()).item())
+
     # e2e: links from pinned host memory, channels back to pinned host memory
     links_host = links.cpu().pin_memory()
     out_host = torch.empty((B, 3, n), dtype=torch.float64).pin_memory()
@@ -344,6 +366,11 @@ def run_td_tdi(args):
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, burst)",
                              "frac": hbm_achieved / hbm_peak if hbm_peak else None}},
         "clocks": clocks.summary(),
+        "float_float": {"entry": "pes_td_tdi_combination_mixed", "value": world * B * n / (ff_ms / 1e3),
+                        "unit": "samples/s", "ms_per_step": ff_ms,
+                        "hbm": {"achieved_gbs": alg_bytes / (ff_ms / 1e3) / 1e9, "peak_gbs": hbm_peak,
+                                "frac": alg_bytes / (ff_ms / 1e3) / 1e9 / hbm_peak if hbm_peak else None},
+                        "max_abs_err_over_max_link": ff_err},
     }
     if not args.no_cpu_baseline:
         v, done, dt = td_cpu_baseline(arm)

@@ -143,6 +143,16 @@ int pes_pn_tf(const double* params, int64_t B, const double* freqs, int64_t n, d
 int pes_td_tdi_combination(const double* links, int64_t B, int64_t n_ext, int64_t n, double arm_sec,
                            double delta_time, int32_t generation, int32_t orthogonal, double* out, void* stream);
 
+/* The same combination in float-float arithmetic on the FP32 pipe (no
+ * counterpart in the reference; the FP64 entry point above is the drop-in).
+ * Same arguments and layouts.  Each output is within about 2^-46 of the
+ * magnitudes it combines: |out - exact| <= 2e-12 max |link| over the
+ * samples it reads (the exact path is bit-identical).  Requires
+ * added <= 1535 (e.g. sampling steps >= 0.04 s for LISA at generation 20). */
+int pes_td_tdi_combination_mixed(const double* links, int64_t B, int64_t n_ext, int64_t n, double arm_sec,
+                                 double delta_time, int32_t generation, int32_t orthogonal, double* out,
+                                 void* stream);
+
 /* Host only: the delay layout pes_td_tdi_combination uses, the reference's
  * expressions on Python floats (tdi.py:1449-1454, 1469-1491): added (above),
  * max_delay, and for delay k = 0 .. max_delay-1 the left sample offset

@@ -88,6 +88,7 @@ SIGNATURES = {
     "pes_pn_tf": (ctypes.c_int, [_vp, _i64, _vp, _i64, _vp, _vp]),
     "pes_td_tdi_combination": (ctypes.c_int, [_vp, _i64, _i64, _i64, _d, _d, _i32, _i32, _vp, _vp]),
     "pes_td_tdi_layout": (ctypes.c_int, [_d, _d, _i32, _vp, _vp, _vp, _vp]),
+    "pes_td_tdi_combination_mixed": (ctypes.c_int, [_vp, _i64, _i64, _i64, _d, _d, _i32, _i32, _vp, _vp]),
     "pes_plan_create": (ctypes.c_int, [ctypes.POINTER(PesPlanDesc), ctypes.POINTER(_vp)]),
     "pes_plan_destroy": (ctypes.c_int, [_vp]),
     "pes_plan_set_data": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp]),

@@ -458,6 +458,194 @@ static int launch_td_tdi(const TdLayout& lay, const double* links, int64_t B, in
   return PES_OK;
 }
 
+// Float-float variant (pes_td_tdi_combination_mixed): the same combination on
+// the FP32 pipe.  Each block scales its window by a power of two (its largest
+// exponent to 2^0, exact) and splits every double into a float-float pair from
+// the bits alone (integer operations: the FP64 pipe is not used on the way
+// in); interpolations, sums and the A/E/T combination run in float-float
+// (about 2^-46 of the operands per operation); each channel goes back to a
+// double from the bits and one FP64 add.  Scaled magnitudes below 2^-126
+// (2^-126 of the window's largest link sample) flush to zero; a NaN or an
+// infinity among the inputs gives NaN in the outputs that read it.
+struct TdLayoutFF {
+  int max_delay;
+  int64_t added;
+  int64_t shift[7];
+  float2 frac[7];      // the weights as float-float pairs
+  float2 rs2, rs6, rs3;  // 1/sqrt(2), 1/sqrt(6), 1/sqrt(3) as float-float pairs
+};
+
+static float2 ff_pair(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
+
+static void td_layout_ff(const TdLayout& lay, TdLayoutFF& out) {
+  out.max_delay = lay.max_delay;
+  out.added = lay.added;
+  for (int k = 0; k < 7; ++k) {
+    out.shift[k] = lay.shift[k];
+    out.frac[k] = ff_pair(lay.frac[k]);
+  }
+  out.rs2 = ff_pair(1.0 / std::sqrt(2.0));
+  out.rs6 = ff_pair(1.0 / std::sqrt(6.0));
+  out.rs3 = ff_pair(1.0 / std::sqrt(3.0));
+}
+
+// x * 2^-scale as a float-float pair: head = sign, exponent and the top 23
+// fraction bits; tail = the other 29 fraction bits, normalised (truncated to
+// 24 significant bits).
+__device__ __forceinline__ FF td_split(double x, int scale) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int E = (int)((b >> 52) & 0x7FF);
+  if (E == 0x7FF) return ff_make(__uint_as_float(0x7fc00000u), 0.0f);
+  const int e = E - 1023 - scale;
+  if (E == 0 || e < -126) return ff_make(0.0f, 0.0f);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29));
+  const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+  float lo = 0.0f;
+  if (r != 0u) {
+    const int lz = __clz((int)r);    // r < 2^29: 3 <= lz <= 31
+    const int el = e - 52 + 31 - lz;  // exponent of r's leading bit
+    if (el >= -126) {
+      const unsigned frac = (unsigned)((((unsigned long long)r << (lz + 1)) & 0xFFFFFFFFull) >> 9);
+      lo = __uint_as_float(sign | ((unsigned)(el + 127) << 23) | frac);
+    }
+  }
+  return ff_make(hi, lo);
+}
+
+// float f * 2^scale as a double, from the bits
+__device__ __forceinline__ double td_widen(float f, int scale) {
+  const unsigned u = __float_as_uint(f);
+  const int ef = (int)((u >> 23) & 0xFF);
+  if (ef == 0xFF) return __longlong_as_double(0x7ff8000000000000ll);
+  const int ed = ef - 127 + 1023 + scale;
+  if (ef == 0 || ed <= 0) return 0.0;
+  if (ed >= 0x7FF) return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | 0x7ff0000000000000ull));
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  return __longlong_as_double((long long)(sign | ((unsigned long long)ed << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
+template <int kMaxDelay>
+__global__ void __launch_bounds__(kTdThreads) k_td_tdi_ff(TdLayoutFF lay, const double* __restrict__ links,
+                                                          int64_t n_ext, int64_t n, int orth,
+                                                          double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char td_raw[];
+  const int64_t win = kTdTile + lay.added + 1;
+  FF* val = reinterpret_cast<FF*>(td_raw);  // [6][win]: the doubles first, then their float-float pairs
+  FF* dif = val + 6 * win;                  // [6][win]: right - left
+  double* raw = reinterpret_cast<double*>(td_raw);
+  __shared__ int wmax[kTdThreads / 32];
+  const double* src = links + (int64_t)blockIdx.y * 6 * n_ext;
+  double* dst = out + (int64_t)blockIdx.y * 3 * n;
+  const int64_t i0 = (int64_t)blockIdx.x * kTdTile;
+  const int64_t avail = n_ext - i0;
+  int emax = 0;  // largest finite biased exponent in the window
+#pragma unroll 1
+  for (int l = 0; l < 6; ++l) {
+    const double* s = src + (int64_t)l * n_ext + i0;
+    double* w = raw + l * win;
+#pragma unroll 4
+    for (int64_t j = threadIdx.x; j < win; j += kTdThreads) {
+      const double x = j < avail ? __ldg(s + j) : 0.0;
+      w[j] = x;
+      const int E = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FF);
+      if (E != 0x7FF) emax = max(emax, E);
+    }
+  }
+  emax = __reduce_max_sync(0xffffffffu, emax);
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = emax;
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < kTdThreads / 32; ++w) emax = max(emax, wmax[w]);
+  const int scale = emax - 1023;  // the window's largest magnitude maps into [1, 2)
+  // each thread rewrites the slots it loaded: doubles -> float-float pairs in place
+#pragma unroll 1
+  for (int l = 0; l < 6; ++l) {
+    double* w = raw + l * win;
+    FF* v = val + l * win;
+#pragma unroll 4
+    for (int64_t j = threadIdx.x; j < win; j += kTdThreads) v[j] = td_split(w[j], scale);
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int l = 0; l < 6; ++l) {
+    const FF* v = val + l * win;
+    FF* df = dif + l * win;
+#pragma unroll 4
+    for (int64_t j = threadIdx.x; j + 1 < win; j += kTdThreads) df[j] = v[j + 1] - v[j];
+  }
+  __syncthreads();
+  constexpr int kTerms = kMaxDelay + 1;
+  constexpr int xp[8] = {5, 4, 0, 1, 0, 1, 5, 4};
+  constexpr int xm[8] = {0, 1, 5, 4, 5, 4, 0, 1};
+#pragma unroll 1
+  for (int r = 0; r < kTdTile / kTdThreads; ++r) {
+    const int64_t t = threadIdx.x + r * kTdThreads;
+    const int64_t i = i0 + t;
+    if (i >= n) break;
+    auto term = [&](int l, int k) -> FF {
+      if (k < 0) return val[l * win + t + lay.added];
+      const int64_t o = l * win + t + lay.shift[k];
+      const float2 f = lay.frac[k];
+      return val[o] + dif[o] * ff_make(f.x, f.y);
+    };
+    FF ch[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      FF acc = term((xp[0] + 2 * c) % 6, -1);
+#pragma unroll
+      for (int j = 1; j < kTerms; ++j) acc = acc + term((xp[j] + 2 * c) % 6, j - 1);
+#pragma unroll
+      for (int j = 0; j < kTerms; ++j) acc = acc - term((xm[j] + 2 * c) % 6, j - 1);
+      ch[c] = acc;
+    }
+    FF o3[3];
+    if (orth) {
+      const FF X = ch[0], Y = ch[1], Z = ch[2];
+      o3[0] = (Z - X) * ff_make(lay.rs2.x, lay.rs2.y);
+      o3[1] = (X - ff_mulf(Y, 2.0f) + Z) * ff_make(lay.rs6.x, lay.rs6.y);
+      o3[2] = (X + Y + Z) * ff_make(lay.rs3.x, lay.rs3.y);
+    } else {
+      o3[0] = ch[0];
+      o3[1] = ch[1];
+      o3[2] = ch[2];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dst[(int64_t)c * n + i] = __dadd_rn(td_widen(o3[c].hi, scale), td_widen(o3[c].lo, scale));
+  }
+}
+
+template <int kMaxDelay>
+static int launch_td_tdi_ff(const TdLayout& lay, const double* links, int64_t B, int64_t n_ext, int64_t n, int orth,
+                            double* out, cudaStream_t st) {
+  TdLayoutFF lf;
+  td_layout_ff(lay, lf);
+  const dim3 grid((unsigned)((n + kTdTile - 1) / kTdTile), (unsigned)B);
+  const int64_t win = kTdTile + lay.added + 1;
+  const size_t smem = (size_t)12 * win * sizeof(FF);  // [6][win] values + [6][win] differences, float pairs
+  if (win > kTdMaxWindow) {
+    set_error("pes_td_tdi_combination_mixed: the longest delay (%lld samples) exceeds %d",
+              (long long)lay.added, kTdMaxWindow - kTdTile - 1);
+    return PES_EINVAL;
+  }
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_td_tdi_ff<kMaxDelay>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) {
+      set_error("pes_td_tdi_combination_mixed: %s", cudaGetErrorString(e));
+      return PES_ECUDA;
+    }
+  }
+  k_td_tdi_ff<kMaxDelay><<<grid, kTdThreads, smem, st>>>(lf, links, n_ext, n, orth, out);
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
 extern "C" {
 
 const char* pes_last_error(void) { return pes::g_error; }
@@ -648,6 +836,38 @@ int pes_td_tdi_combination(const double* links, int64_t B, int64_t n_ext, int64_
   const cudaStream_t st = as_stream(stream);
   return generation == 20 ? launch_td_tdi<7>(lay, links, B, n_ext, n, orthogonal != 0, out, st)
                           : launch_td_tdi<3>(lay, links, B, n_ext, n, orthogonal != 0, out, st);
+}
+
+int pes_td_tdi_combination_mixed(const double* links, int64_t B, int64_t n_ext, int64_t n, double arm_sec,
+                                 double delta_time, int32_t generation, int32_t orthogonal, double* out,
+                                 void* stream) {
+  PES_REQUIRE(generation == 15 || generation == 20, "pes_td_tdi_combination_mixed: unsupported generation %d",
+              generation);
+  PES_REQUIRE(std::isfinite(arm_sec) && arm_sec > 0.0 && std::isfinite(delta_time) && delta_time > 0.0,
+              "pes_td_tdi_combination_mixed: arm length and sampling step must be finite and > 0 (%g, %g)",
+              arm_sec, delta_time);
+  PES_REQUIRE(B >= 0 && B <= 65535 && n >= 0 && n_ext >= 0,
+              "pes_td_tdi_combination_mixed: bad sizes (B = %lld, n = %lld, n_ext = %lld)", (long long)B,
+              (long long)n, (long long)n_ext);
+  PES_REQUIRE(7.0 * arm_sec / delta_time < 1e9, "pes_td_tdi_combination_mixed: delay of %g samples too long",
+              7.0 * arm_sec / delta_time);
+  TdLayout lay;
+  td_layout(arm_sec, delta_time, generation == 20, lay);
+  for (int k = 0; k < lay.max_delay; ++k)  // every read stays in [i, i + added]
+    PES_REQUIRE(lay.shift[k] >= 0 && lay.shift[k] + 1 <= lay.added,
+                "pes_td_tdi_combination_mixed: delay layout out of range (shift %lld, added %lld)",
+                (long long)lay.shift[k], (long long)lay.added);
+  PES_REQUIRE(n_ext >= n + lay.added,
+              "pes_td_tdi_combination_mixed: %lld link samples for %lld outputs, need n + %lld (the longest delay)",
+              (long long)n_ext, (long long)n, (long long)lay.added);
+  PES_REQUIRE(kTdTile + lay.added + 1 <= kTdMaxWindow,
+              "pes_td_tdi_combination_mixed: the longest delay (%lld samples) exceeds %d", (long long)lay.added,
+              kTdMaxWindow - kTdTile - 1);
+  if (B == 0 || n == 0) return PES_OK;
+  PES_REQUIRE(links && out, "pes_td_tdi_combination_mixed: null pointer");
+  const cudaStream_t st = as_stream(stream);
+  return generation == 20 ? launch_td_tdi_ff<7>(lay, links, B, n_ext, n, orthogonal != 0, out, st)
+                          : launch_td_tdi_ff<3>(lay, links, B, n_ext, n, orthogonal != 0, out, st);
 }
 
 }  // extern "C"

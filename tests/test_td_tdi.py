@@ -6,9 +6,11 @@ as written and is pinned by known answers.  With an arm length that is a whole
 number of samples every interpolation weight is 1, and the combination is the
 textbook TDI with delays of 1..max_num_delay arm lengths, checked here sample
 by sample.  CPU: the oracle, the C layout helper against Python's own float
-operators, the entry point's argument checks.  GPU: ``pes_td_tdi_combination``
+operators, the entry points' argument checks.  GPU: ``pes_td_tdi_combination``
 bit-identical to the oracle (staged and L1 paths, both generations, both
-channel sets, batched, full size).
+channel sets, batched, full size); ``pes_td_tdi_combination_mixed``
+(float-float) within 2e-12 of the largest link magnitude, with NaN inputs
+reaching the same outputs as in the oracle.
 """
 
 import ctypes
@@ -123,6 +125,20 @@ def test_entry_point_argument_checks():
     assert f(None, 1, added, 0, LISA_ARM_SEC, 5.0, 20, 1, None, None) == 0  # empty series
 
 
+def test_mixed_entry_point_argument_checks():
+    from pespace_gb300 import _lib
+
+    lib = _lib.load()
+    f = lib.pes_td_tdi_combination_mixed
+    added = td_tdi.layout(LISA_ARM_SEC, 5.0, "2.0")[0]
+    assert f(None, 1, 100 + added, 100, LISA_ARM_SEC, 5.0, 16, 1, None, None) != 0  # generation
+    assert f(None, 1, 99 + added, 100, LISA_ARM_SEC, 5.0, 20, 1, None, None) != 0  # series too short
+    long_added = td_tdi.layout(219.4, 1.0, "2.0")[0]  # 1536: beyond the staged window
+    assert f(None, 1, 100 + long_added, 100, 219.4, 1.0, 20, 1, None, None) != 0
+    assert b"longest delay" in lib.pes_last_error()
+    assert f(None, 0, 100 + added, 100, LISA_ARM_SEC, 5.0, 20, 1, None, None) == 0  # empty batch
+
+
 def test_class_constructor():
     from pespace_gb300.detector.tdi import TDMichelsonConstantEqualArm
 
@@ -133,12 +149,15 @@ def test_class_constructor():
         TDMichelsonConstantEqualArm("1.0")
     with pytest.raises(ValueError):
         TDMichelsonConstantEqualArm(backend="taichi")
+    with pytest.raises(ValueError):
+        TDMichelsonConstantEqualArm(precision="fp32")
+    assert TDMichelsonConstantEqualArm(precision="mixed").precision == "mixed"
 
 
 # ----------------------------------------------------------------------------- GPU
 
 
-def _run_gpu(links, n, arm, dt, gen, orth):
+def _run_gpu(links, n, arm, dt, gen, orth, mixed=False):
     import torch
 
     from pespace_gb300 import _lib
@@ -146,10 +165,14 @@ def _run_gpu(links, n, arm, dt, gen, orth):
     x = torch.as_tensor(links, device="cuda").contiguous()
     B = x.shape[0]
     out = torch.full((B, 3, n), float("nan"), dtype=torch.float64, device="cuda")
-    _lib.check(_lib.load().pes_td_tdi_combination(_lib.ptr(x), B, x.shape[-1], n, arm, dt,
-                                                  15 if gen == "1.5" else 20, int(orth), _lib.ptr(out),
-                                                  _lib.stream_handle()))
+    lib = _lib.load()
+    fn = lib.pes_td_tdi_combination_mixed if mixed else lib.pes_td_tdi_combination
+    _lib.check(fn(_lib.ptr(x), B, x.shape[-1], n, arm, dt, 15 if gen == "1.5" else 20, int(orth), _lib.ptr(out),
+                  _lib.stream_handle()))
     return out.cpu().numpy()
+
+
+MIXED_TOL = 2e-12  # of the largest link magnitude: float-float, about 2^-46 per operation
 
 
 @pytest.mark.gpu
@@ -219,3 +242,68 @@ def test_gpu_through_detector_class(cuda_lib):
     det.single_link_response = torch.zeros((6, 10), dtype=torch.float64, device="cuda")
     with pytest.raises(Exception):
         tdi.update_tdi_response()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("gen", ["1.5", "2.0"])
+@pytest.mark.parametrize("orth", [True, False])
+@pytest.mark.parametrize("arm,dt,n", [
+    (LISA_ARM_SEC, 5.0, 5000),
+    (3e9 / 299792458.0, 0.25, 4096),
+    (0.5773502691896258, 0.1, 1),
+    (219.2, 1.0, 3000),                 # 2.0: the largest window
+])
+def test_gpu_mixed_within_tolerance(cuda_lib, gen, orth, arm, dt, n):
+    added = td_tdi.layout(arm, dt, gen)[0]
+    if 512 + added + 1 > 2048:
+        pytest.skip("delay beyond the float-float kernel's window")
+    rng = np.random.default_rng(19)
+    B = 2
+    links = rng.standard_normal((B, 6, n + added)) * 1e-21
+    links[1] *= 10.0 ** rng.uniform(-12, 0, (6, n + added))  # wide dynamic range in the second series
+    got = _run_gpu(links, n, arm, dt, gen, orth, mixed=True)
+    for b in range(B):
+        want = td_tdi.combine(links[b], n, arm, dt, gen, orth)
+        err = np.max(np.abs(got[b] - want)) / np.max(np.abs(links[b]))
+        assert err <= MIXED_TOL, (b, err)
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_full_size_and_nan(cuda_lib):
+    arm, dt, gen = LISA_ARM_SEC, 4.0, "2.0"
+    n = int(2.0 ** 25 // dt + 1)
+    added = td_tdi.layout(arm, dt, gen)[0]
+    rng = np.random.default_rng(23)
+    links = rng.standard_normal((1, 6, n + added)) * 3e-20
+    links[0, 2, 777_777] = np.nan
+    got = _run_gpu(links, n, arm, dt, gen, True, mixed=True)[0]
+    scale = np.nanmax(np.abs(links))
+    step = 1 << 20
+    for s in range(0, n, step):
+        e = min(n, s + step)
+        want = td_tdi.combine(links[0][:, s:e + added], e - s, arm, dt, gen, True)
+        assert np.array_equal(np.isnan(got[:, s:e]), np.isnan(want)), s
+        ok = ~np.isnan(want)
+        assert np.max(np.abs(got[:, s:e][ok] - want[ok])) <= MIXED_TOL * scale, s
+    assert np.isnan(got).any()
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_through_detector_class(cuda_lib):
+    import torch
+
+    from pespace_gb300.detector.orbit import KaplerianHeliocentric
+    from pespace_gb300.detector.tdi import TDMichelsonConstantEqualArm
+
+    dt, n = 5.0, 3001
+    orbit = KaplerianHeliocentric(2.5e9, 0.0, -math.pi / 9)
+    det = types.SimpleNamespace(
+        tdi_data=types.SimpleNamespace(data_info=types.SimpleNamespace(time_series_length=n, delta_time=dt)),
+        orbit_model=orbit)
+    tdi = TDMichelsonConstantEqualArm("2.0", False, precision="mixed")
+    tdi.init_tdi_combination_model(det)
+    links = np.random.default_rng(29).standard_normal((6, tdi.extended_time_series_length))
+    det.single_link_response = torch.as_tensor(links, device="cuda")
+    tdi.update_tdi_response()
+    want = td_tdi.combine(links, n, orbit.arm_length_sec(0.0), dt, "2.0", False)
+    assert np.max(np.abs(det.tdi_response.cpu().numpy() - want)) <= MIXED_TOL * np.max(np.abs(links))
