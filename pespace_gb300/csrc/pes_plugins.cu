@@ -820,6 +820,8 @@ int pes_td_tdi_combination(const double* links, int64_t B, int64_t n_ext, int64_
   PES_REQUIRE(B >= 0 && B <= 65535 && n >= 0 && n_ext >= 0,
               "pes_td_tdi_combination: bad sizes (B = %lld, n = %lld, n_ext = %lld)", (long long)B, (long long)n,
               (long long)n_ext);
+  PES_REQUIRE(n <= (int64_t)kTdTile * 0x7FFFFFFF, "pes_td_tdi_combination: %lld samples exceed the launch grid",
+              (long long)n);
   PES_REQUIRE(7.0 * arm_sec / delta_time < 1e9, "pes_td_tdi_combination: delay of %g samples too long",
               7.0 * arm_sec / delta_time);
   TdLayout lay;
@@ -849,6 +851,8 @@ int pes_td_tdi_combination_mixed(const double* links, int64_t B, int64_t n_ext, 
   PES_REQUIRE(B >= 0 && B <= 65535 && n >= 0 && n_ext >= 0,
               "pes_td_tdi_combination_mixed: bad sizes (B = %lld, n = %lld, n_ext = %lld)", (long long)B,
               (long long)n, (long long)n_ext);
+  PES_REQUIRE(n <= (int64_t)kTdTile * 0x7FFFFFFF, "pes_td_tdi_combination_mixed: %lld samples exceed the launch grid",
+              (long long)n);
   PES_REQUIRE(7.0 * arm_sec / delta_time < 1e9, "pes_td_tdi_combination_mixed: delay of %g samples too long",
               7.0 * arm_sec / delta_time);
   TdLayout lay;

@@ -123,6 +123,9 @@ def test_entry_point_argument_checks():
     assert f(None, 1, 100 + added, 100, LISA_ARM_SEC, 5.0, 20, 1, None, None) != 0  # null pointers
     assert f(None, 0, 100 + added, 100, LISA_ARM_SEC, 5.0, 20, 1, None, None) == 0  # empty batch
     assert f(None, 1, added, 0, LISA_ARM_SEC, 5.0, 20, 1, None, None) == 0  # empty series
+    huge = 512 * 0x7FFFFFFF + 1
+    assert f(None, 1, huge + added, huge, LISA_ARM_SEC, 5.0, 20, 1, None, None) != 0  # beyond the grid
+    assert b"launch grid" in lib.pes_last_error()
 
 
 def test_mixed_entry_point_argument_checks():
