@@ -221,6 +221,23 @@ int pes_plan_profile(PesPlan* plan, int32_t enable);
 int pes_plan_stats(PesPlan* plan, int64_t* launches /* host [8] */, double* device_ms /* host [8] */);
 const char* pes_kernel_class_name(int32_t k);
 
+/* Launch options of a plan (no counterpart in the reference).  They change
+ * speed only: results agree bit for bit, except the gradient, whose FP32
+ * moment atomics may sum in another order.  The Python autotuner
+ * (pespace_gb300.inference.autotune) times the candidates on a caller's
+ * batch and keeps the fastest.
+ *   PES_OPT_DENSE_STAGE (mixed plans; FP64 plans read 0 and ignore it):
+ *     1 = the gradient pass of the dense stage copies each run's inputs one
+ *     run ahead into shared memory (cp.async), 0 = plain loads.  Default: 1
+ *     when the packed dense inputs exceed 64 MB (they stream from DRAM).
+ *   PES_OPT_SAMPLE_THREADS: threads per block of the per-sample kernels of
+ *     the lnL calls (set-up, ranges, peak kink), 1..128 (the gradient
+ *     set-up uses up to 255 registers per thread); default 8. */
+#define PES_OPT_DENSE_STAGE 1
+#define PES_OPT_SAMPLE_THREADS 2
+int pes_plan_set_option(PesPlan* plan, int32_t option, int64_t value);
+int pes_plan_get_option(PesPlan* plan, int32_t option, int64_t* value /* host */);
+
 /* Fisher matrices at B parameter sets (row-major (B, 11, 11), parameter order
  * of theta): F_ij = 4 df Re sum_{det, c, f} conj(dh_i) dh_j / S_c(f) over the
  * plan's channels and each sample's live bins.  FP64 plans take the

@@ -14,6 +14,8 @@ PES_EINVAL = 1
 PES_ENOMEM = 2
 PES_ECUDA = 3
 PES_ETIMEOUT = 4
+PES_OPT_DENSE_STAGE = 1
+PES_OPT_SAMPLE_THREADS = 2
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 MAX_DETECTORS = 4
@@ -97,6 +99,8 @@ SIGNATURES = {
     "pes_plan_model_tdi": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "pes_plan_profile": (ctypes.c_int, [_vp, _i32]),
     "pes_plan_stats": (ctypes.c_int, [_vp, _vp, _vp]),
+    "pes_plan_set_option": (ctypes.c_int, [_vp, _i32, _i64]),
+    "pes_plan_get_option": (ctypes.c_int, [_vp, _i32, _vp]),
     "pes_kernel_class_name": (ctypes.c_char_p, [_i32]),
     "pes_plan_work": (ctypes.c_int, [_vp, _i64, _vp, _vp]),
     "pes_fisher_batch": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),

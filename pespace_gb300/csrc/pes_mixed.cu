@@ -2464,6 +2464,13 @@ int mixed_create(PesPlan* p) {
   return PES_OK;
 }
 
+void mixed_stage_option(PesPlan* p, int set, int64_t* value) {
+  if (set)
+    p->mixed->stage_grad = *value != 0;
+  else
+    *value = p->mixed->stage_grad ? 1 : 0;
+}
+
 void mixed_destroy(PesPlan* p) {
   if (!p->mixed) return;
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
@@ -2547,7 +2554,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
   {
     ProfScope ps(p, kKSetup, st);
-    k_setup<double><<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, theta, B, 0, blocks);
+    k_setup<double><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, 0, blocks);
   }
   PES_CHECK_LAUNCH();
   {
@@ -2561,7 +2568,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->fork, 0));
   {
     ProfScope ps(p, kKOther, side);
-    k_mixed_ranges<1><<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, side>>>(M, blocks, B);
+    k_mixed_ranges<1><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, side>>>(M, blocks, B);
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->xready, side));
@@ -2573,7 +2580,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (grad) {
     {
       ProfScope ps(p, kKSetup, side);
-      k_setup_grad<<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, side>>>(p->dev, theta, B,
+      k_setup_grad<<<ceil_div(B, p->sample_threads), p->sample_threads, 0, side>>>(p->dev, theta, B,
                                                      reinterpret_cast<SampleBlock<GradScalar>*>(M.gblocks));
     }
     PES_CHECK_LAUNCH();
@@ -2587,7 +2594,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
   {
     ProfScope ps(p, kKSparse, st);
-    k_kink<<<ceil_div(B * (int64_t)M.n_det, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, M, G, blocks, B);
+    k_kink<<<ceil_div(B * (int64_t)M.n_det, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, M, G, blocks, B);
   }
   PES_CHECK_LAUNCH();
   {

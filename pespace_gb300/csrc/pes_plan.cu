@@ -222,7 +222,7 @@ int run_dense(PesPlan* p, const double* theta, int64_t B, int pass, double* lnl,
   SampleBlock<T>* blocks = reinterpret_cast<SampleBlock<T>*>(p->blocks);
   {
     ProfScope ps(p, kKSetup, st);
-    k_setup<T><<<ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, theta, B, pass, blocks);
+    k_setup<T><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, pass, blocks);
   }
   PES_CHECK_LAUNCH();
   const int nblk = (int)ceil_div(p->desc.nbins, kDenseBinsPerBlock);
@@ -429,6 +429,43 @@ int pes_plan_profile(PesPlan* p, int32_t enable) {
   PES_REQUIRE(p, "pes_plan_profile: null plan");
   p->prof.enabled = enable != 0;
   return PES_OK;
+}
+
+int pes_plan_set_option(PesPlan* p, int32_t option, int64_t value) {
+  PES_REQUIRE(p, "pes_plan_set_option: null plan");
+  switch (option) {
+    case PES_OPT_DENSE_STAGE:
+      PES_REQUIRE(value == 0 || value == 1, "pes_plan_set_option: PES_OPT_DENSE_STAGE takes 0 or 1, got %lld",
+                  (long long)value);
+      if (p->mixed) mixed_stage_option(p, 1, &value);
+      return PES_OK;
+    case PES_OPT_SAMPLE_THREADS:
+      PES_REQUIRE(value >= 1 && value <= 128, "pes_plan_set_option: PES_OPT_SAMPLE_THREADS takes 1..128, got %lld",
+                  (long long)value);
+      p->sample_threads = (int)value;
+      return PES_OK;
+    default:
+      break;
+  }
+  ::pes::set_error("pes_plan_set_option: unknown option %d", option);
+  return PES_EINVAL;
+}
+
+int pes_plan_get_option(PesPlan* p, int32_t option, int64_t* value) {
+  PES_REQUIRE(p && value, "pes_plan_get_option: null pointer");
+  switch (option) {
+    case PES_OPT_DENSE_STAGE:
+      *value = 0;
+      if (p->mixed) mixed_stage_option(p, 0, value);
+      return PES_OK;
+    case PES_OPT_SAMPLE_THREADS:
+      *value = p->sample_threads;
+      return PES_OK;
+    default:
+      break;
+  }
+  ::pes::set_error("pes_plan_get_option: unknown option %d", option);
+  return PES_EINVAL;
 }
 
 int pes_plan_stats(PesPlan* p, int64_t* launches, double* device_ms) {

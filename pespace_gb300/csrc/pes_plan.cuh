@@ -58,6 +58,14 @@ enum KernelClass : int {
   kKOther = 7,
 };
 
+// Threads per block of the per-sample kernels (set-up, ranges, kink): each
+// thread runs a long FP64 chain, and GB300 issues FP64 at 2 lanes per cycle
+// per SM, so small blocks spread the samples over all SMs instead of
+// queueing 64 lanes on each SM's FP64 pipe.
+// The default; a plan's lnL launches use PesPlan::sample_threads, which
+// PES_OPT_SAMPLE_THREADS (the autotuner) may change.
+constexpr int kPerSampleThreads = 8;
+
 struct Profiler {
   bool enabled = false;
   int64_t launches[PES_KERNEL_CLASSES] = {};
@@ -93,6 +101,7 @@ struct PesPlan {
   int32_t* status = nullptr;   // [max_batch] internal status when the caller passes NULL
   unsigned data_set_mask = 0;
   pes::MixedBuffers* mixed = nullptr;
+  int sample_threads = pes::kPerSampleThreads;  // block size of the per-sample lnL kernels (PES_OPT_SAMPLE_THREADS)
   void* fisher_blocks = nullptr;     // [max_batch] SampleBlock<Dual<11>> (first Fisher call)
   double* fisher_partial = nullptr;  // [max_batch][blocks][66]
   pes::Profiler prof;
@@ -126,11 +135,6 @@ namespace pes {
 
 constexpr int kGradTangents = 4;  // tangents per gradient pass (3 passes for 11 parameters)
 
-// Threads per block of the per-sample kernels (set-up, ranges, kink): each
-// thread runs a long FP64 chain, and GB300 issues FP64 at 2 lanes per cycle
-// per SM, so small blocks spread the samples over all SMs instead of
-// queueing 64 lanes on each SM's FP64 pipe.
-constexpr int kPerSampleThreads = 8;
 
 // ------------------------------------------------------------------ scalar helpers
 template <class T> struct Seed;
@@ -218,4 +222,6 @@ int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const st
                int64_t* out, cudaStream_t st);
 int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* grad, int32_t* status,
               cudaStream_t st);
+// read (set == 0) or write the dense stage's staging choice of the gradient pass
+void mixed_stage_option(PesPlan* p, int set, int64_t* value);
 }  // namespace pes

@@ -194,6 +194,20 @@ class WhittleLikelihood:
         self.last_status = status
         return out, grad
 
+    @property
+    def launch_options(self):
+        """The plan's launch options: {"dense_stage": 0 | 1, "sample_threads": n}."""
+        from .autotune import OPTIONS, get_option
+
+        return {name: get_option(self, name) for name in OPTIONS}
+
+    def autotune(self, theta, grad=True, reps=5, candidates=None):
+        """Time the plan's launch options on the batch ``theta`` and keep the
+        fastest (``pespace_gb300.inference.autotune.autotune``)."""
+        from .autotune import autotune
+
+        return autotune(self, theta, grad=grad, reps=reps, candidates=candidates)
+
     def fisher_matrix(self, theta):
         """(B, 11, 11) Fisher matrices at the rows of a (B, 11) parameter tensor
         (fisher.py:27-162 over this engine's detectors, channels and per-sample

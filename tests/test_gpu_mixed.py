@@ -224,3 +224,36 @@ def test_mixed_edge_cases_and_status(cuda_lib, oracle, dataset):
         plan = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets[:1]], 1e-4, channels=chans)
         want = plan.lnl(thetas)
         assert np.all(np.abs(got - want) <= 1e-2 + 1e-8 * np.abs(want)), (chans, got - want)
+
+
+def test_launch_options_and_autotune(cuda_lib, oracle, dataset):
+    """Launch options change speed only: every staging choice and per-sample
+    block size gives the same lnL bit for bit (gradient up to the order of
+    the FP32 moment atomics); the autotuner keeps one of its candidates."""
+    from pespace_gb300.inference.autotune import CANDIDATES, set_option
+
+    g, dets, th0 = dataset
+    rng = np.random.default_rng(43)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(2)] + list(random_prior_theta(rng, 3, th0[10])))
+    mixed, fp64 = engines(g, dets, max_batch=8, cut_factor=1.2)
+    assert mixed.launch_options == {"dense_stage": 0, "sample_threads": 8}  # small inputs: direct loads
+    l0, g0 = mixed.log_likelihood_and_grad(thetas)
+    norm = torch.linalg.norm(g0, dim=1, keepdim=True)
+    for stage in CANDIDATES["dense_stage"]:
+        for threads in CANDIDATES["sample_threads"] + (1, 128):
+            set_option(mixed, "dense_stage", stage)
+            set_option(mixed, "sample_threads", threads)
+            l1, g1 = mixed.log_likelihood_and_grad(thetas)
+            assert torch.equal(l1, l0), (stage, threads)
+            assert torch.equal(mixed.log_likelihood_batch(thetas), l0), (stage, threads)
+            assert torch.max(torch.abs(g1 - g0) / norm).item() < 1e-5, (stage, threads)
+    report = mixed.autotune(thetas, reps=2)
+    assert set(report) == {"dense_stage", "sample_threads"}
+    assert mixed.launch_options == {k: v["chosen"] for k, v in report.items()}
+    assert all(v["chosen"] in CANDIDATES[k] and v["ms"][v["chosen"]] > 0 for k, v in report.items())
+    assert torch.equal(mixed.log_likelihood_batch(thetas), l0)
+    # FP64 plans: only the per-sample block size
+    w0 = fp64.log_likelihood_batch(thetas)
+    report = fp64.autotune(thetas, grad=False, reps=1)
+    assert set(report) == {"sample_threads"} and fp64.launch_options["dense_stage"] == 0
+    assert torch.equal(fp64.log_likelihood_batch(thetas), w0)
