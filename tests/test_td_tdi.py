@@ -99,6 +99,55 @@ def test_oracle_whole_sample_arm_is_textbook_tdi(gen):
             assert out[c, i] == want, (c, i)
 
 
+def _scalar_reference_loop(links, n, arm, dt, generation, orthogonal):
+    """The loop body of tdi.py:1482-1600 for one sample at a time, on Python floats."""
+    m = td_tdi.max_num_delay(generation)
+    added = int(m * arm // dt + 1)
+    t_frac = [1.0 - ((i + 1) * arm % dt) / dt for i in range(m)]
+    y = dict(zip(td_tdi.LINKS, (list(map(float, row)) for row in links)))
+    out = [[], [], []]
+    for i in range(n):
+        d = {name: [0.0] * m for name in td_tdi.LINKS}
+        for num_delay in range(m, 0, -1):
+            i_shift = int((m - num_delay) * arm // dt)
+            for name in td_tdi.LINKS:
+                left, right = y[name][i + i_shift], y[name][i + i_shift + 1]
+                d[name][num_delay - 1] = left + (right - left) * t_frac[num_delay - 1]
+        c = {name: y[name][i + added] for name in td_tdi.LINKS}
+        d12, d21, d23, d32, d31, d13 = (d[k] for k in td_tdi.LINKS)
+        X = c["link13"] + d31[0] + d12[1] + d21[2]
+        Y = c["link21"] + d12[0] + d23[1] + d32[2]
+        Z = c["link32"] + d23[0] + d31[1] + d13[2]
+        if m == 7:
+            X = X + d12[3] + d21[4] + d13[5] + d31[6]
+            Y = Y + d23[3] + d32[4] + d21[5] + d12[6]
+            Z = Z + d31[3] + d13[4] + d32[5] + d23[6]
+        X = X - c["link12"] - d21[0] - d13[1] - d31[2]
+        Y = Y - c["link23"] - d32[0] - d21[1] - d12[2]
+        Z = Z - c["link31"] - d13[0] - d32[1] - d23[2]
+        if m == 7:
+            X = X - d13[3] - d31[4] - d12[5] - d21[6]
+            Y = Y - d21[3] - d12[4] - d23[5] - d32[6]
+            Z = Z - d32[3] - d23[4] - d31[5] - d13[6]
+        if orthogonal:
+            vals = ((Z - X) / math.sqrt(2.0), (X - 2.0 * Y + Z) / math.sqrt(6.0), (X + Y + Z) / math.sqrt(3.0))
+        else:
+            vals = (X, Y, Z)
+        for k in range(3):
+            out[k].append(vals[k])
+    return np.array(out)
+
+
+@pytest.mark.parametrize("gen", ["1.5", "2.0"])
+@pytest.mark.parametrize("orth", [True, False])
+def test_oracle_equals_scalar_loop(gen, orth):
+    arm, dt, n = LISA_ARM_SEC, 0.7, 40
+    added = td_tdi.layout(arm, dt, gen)[0]
+    links = np.random.default_rng(13).standard_normal((6, n + added)) * 1e-20
+    assert np.array_equal(td_tdi.combine(links, n, arm, dt, gen, orth),
+                          _scalar_reference_loop(links, n, arm, dt, gen, orth))
+
+
 def test_oracle_rejects_short_series_and_generation():
     with pytest.raises(ValueError):
         td_tdi.combine(np.zeros((6, 10)), 10, LISA_ARM_SEC, 5.0, "1.5")
