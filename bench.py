@@ -173,14 +173,19 @@ def cpu_baseline_run(n_samples, threads, precision_note, grad=True):
     oracle.build()
     g = oracle.grid(DUR, DT, FMIN, FMAX)
     th0 = config0_theta(DUR - 86400.0)
-    orb = oracle.heliocentric(2.5e9, 0.0, -math.pi / 9)
-    psd = oracle.psd(g["freqs"], "AET", False, GEN, **oracle.PSD_PRESETS["LISA_SciRDv1"])
-    noise = oracle.noise_realization(g, psd, "AET", 2026)
-    data = np.stack([noise[c] for c in "AET"])
-    psd_arr = np.stack([psd[c] for c in "AET"])
-    plan = oracle.Plan(g, [(orb, GEN, data, psd_arr)], 1e-4, cut_factor=1.2)
-    data = data + plan.model_tdi(0, th0)
-    plan = oracle.Plan(g, [(orb, GEN, data, psd_arr)], 1e-4, cut_factor=1.2)
+    # the workload's detectors: LISA, or LISA + Taiji + TianQin for network-d (seeded noise per detector)
+    specs = [(oracle.heliocentric(2.5e9, 0.0, -math.pi / 9), "LISA_SciRDv1")]
+    if WORKLOAD.startswith("network-d"):
+        specs += [(oracle.heliocentric(3.0e9, 0.0, math.pi / 9), "Taiji_TDC"),
+                  (oracle.geocentric(math.sqrt(3.0) * 1e8), "Tianqin_GWSpace")]
+    dets = []
+    for k, (orb, model) in enumerate(specs):
+        psd = oracle.psd(g["freqs"], "AET", False, GEN, **oracle.PSD_PRESETS[model])
+        noise = oracle.noise_realization(g, psd, "AET", 2026 + k)
+        dets.append((orb, GEN, np.stack([noise[c] for c in "AET"]), np.stack([psd[c] for c in "AET"])))
+    plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2)
+    dets = [(orb, gen, data + plan.model_tdi(k, th0), psd_arr) for k, (orb, gen, data, psd_arr) in enumerate(dets)]
+    plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2)
     thetas = prior_samples(np.random.default_rng(2026), n_samples, th0[10])
     t0 = time.perf_counter()
     plan.lnl(thetas, grad=grad, nthreads=threads)
@@ -210,10 +215,11 @@ def run_reference(args):
         print(json.dumps(line), flush=True)
         return
     threads = os.cpu_count() or 1
-    n = max(threads, 16)
+    # network-d: about 9 s of FP64 work per sample and core (three detectors, 3.35 M bins each)
+    n = max(4, threads // 4) if WORKLOAD.startswith("network-d") else max(threads, 16)
     rates = []
     for _ in range(args.warmup):
-        cpu_baseline_run(threads, threads, "")
+        cpu_baseline_run(min(n, threads), threads, "")
     for _ in range(args.steps):
         r, _ = cpu_baseline_run(n, threads, "")
         rates.append(r)
