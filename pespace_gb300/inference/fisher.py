@@ -5,8 +5,11 @@ batch_size) and its definition
 
     F_ij = 4 df Re sum_{det, c, f} conj(ds_i(f)) ds_j(f) / S_c(f),
 
-computed on the GPU by ``pes_fisher_batch`` (FP64 forward-mode derivatives at
-every live bin of the engine's grid, over its detectors and channels).  The
+computed on the GPU by ``pes_fisher_batch`` at every live bin of the engine's
+grid, over its detectors and channels.  FP64 plans use FP64 forward-mode
+derivatives.  Mixed plans use the model's structure: PhenomD tangents in
+float-float and response tangents in FP32, within 1e-5 of the FP64 matrices
+normalised by their diagonal.  The
 rows and columns follow the engine's 11-parameter vector (ln Mc, q, chi_1,
 chi_2, ln D_L [Mpc], cos iota, lambda, sin beta, psi, phi_c, t_c), not the
 fields of the reference's parameter tuple.  ``sample_from_fisher`` and
@@ -28,7 +31,10 @@ PARAMETERS = ("ln_chirp_mass", "mass_ratio", "chi_1", "chi_2", "ln_luminosity_di
 def _as_theta(fiducial_params):
     """(theta (B, 11), single) from an (11,) / (B, 11) array or a reference-style
     parameter mapping whose entries are scalars or equal-length 1-D arrays."""
-    if isinstance(fiducial_params, (np.ndarray, torch.Tensor, list, tuple)) and not hasattr(fiducial_params, "_fields"):
+    if isinstance(fiducial_params, torch.Tensor):
+        th = fiducial_params.detach().to(device="cpu", dtype=torch.float64)
+        return (th[None], True) if th.dim() == 1 else (th, False)
+    if isinstance(fiducial_params, (np.ndarray, list, tuple)) and not hasattr(fiducial_params, "_fields"):
         th = torch.as_tensor(np.asarray(fiducial_params, dtype=np.float64))
         return (th[None], True) if th.dim() == 1 else (th, False)
     get = fiducial_params.get if isinstance(fiducial_params, dict) else (lambda k, d=None: getattr(fiducial_params, k, d))

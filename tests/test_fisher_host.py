@@ -59,3 +59,18 @@ def test_wrap_angle_params():
     assert np.all((w["polarization"] >= 0) & (w["polarization"] < np.pi))
     assert w["chirp_mass"] is s["chirp_mass"]
     assert np.array_equal(s["ecliptic_longitude"], [-0.5, 7.0])  # input untouched
+
+
+def test_fiducial_parameter_forms():
+    """Arrays, lists and tensors (any device) give the same (B, 11) rows."""
+    import torch
+
+    from pespace_gb300.inference.fisher import _as_theta
+
+    row = np.linspace(0.1, 1.1, 11)
+    for x in (row, list(row), torch.as_tensor(row)):
+        th, single = _as_theta(x)
+        assert single and th.shape == (1, 11) and th.dtype == torch.float64
+        assert np.array_equal(th[0].numpy(), row)
+    th, single = _as_theta(torch.as_tensor(np.stack([row, 2 * row])))
+    assert not single and th.shape == (2, 11)
