@@ -63,8 +63,33 @@ class DataInformation:
         return np.arange(self.time_series_length) * self.delta_time + self.start_time
 
 
+def fd_from_td(td_array, info, window=None):
+    """tdi.py:661-726 (set_fd_data_from_td): per channel, rfft of the windowed
+    series divided by the sampling frequency, cropped to the frequency mask.
+
+    td_array : (C, time_series_length) real array; info : DataInformation;
+    window : None (no window), an array of time_series_length weights, or a
+        ``scipy.signal.get_window`` specification.  Host NumPy, like the
+        reference (a one-time set-up step).
+    """
+    n = info.time_series_length
+    if window is None:
+        weight = np.ones(n)
+    elif isinstance(window, np.ndarray):
+        weight = window
+    else:
+        from scipy import signal
+
+        weight = signal.get_window(window, n)
+    out = [np.fft.rfft(np.asarray(row, dtype=np.float64) * weight) / info.sampling_frequency for row in td_array]
+    return np.stack([row[info.frequency_mask_array] for row in out]).astype(np.complex128)
+
+
 class TDIChannelData:
-    """tdi.py:162-1376 (frequency-domain part) with CUDA tensors."""
+    """tdi.py:162-1376 with CUDA tensors: ``td_data`` (C, time_series_length)
+    float64, ``fd_data`` (C, frequency_series_length) complex128; the
+    wavelet domain and the conversions the reference leaves unimplemented
+    raise NotImplementedError as there."""
 
     def __init__(self, scaling=False, backend="cuda"):
         if backend != "cuda":
@@ -74,7 +99,9 @@ class TDIChannelData:
         self._reset()
 
     def _reset(self):
+        self.time_samples = None
         self.frequency_samples = None
+        self.td_data = None
         self.fd_data = None
         self.fd_noise_power_density = None
         self._data_info = None
@@ -110,6 +137,68 @@ class TDIChannelData:
             raise ValueError(f"tdi_data_array must have shape {tuple(self.fd_data.shape)}, got {tuple(arr.shape)}; "
                              "crop it with `data_info.frequency_mask_array` first")
         self.fd_data.copy_(arr)
+
+    def set_td_data_from_input(self, channels, duration, delta_time, tdi_data_array, start_time=0.0,
+                               minimum_frequency=1e-5, maximum_frequency=0.1):
+        """tdi.py:330-414: time-domain data from a (len(channels), time_series_length) array."""
+        if self._reset_flag:
+            warnings.warn("You are setting `td_data` with input array, but you have set TDI data of current "
+                          "instance previously; the instance is reset.")
+            self._reset()
+        self.set_data_info(channels, duration, delta_time, start_time, minimum_frequency, maximum_frequency)
+        arr = np.asarray(tdi_data_array, dtype=np.float64)
+        channels_num, samples_num = arr.shape
+        if len(channels) != channels_num:
+            raise ValueError(f"You set channels with {channels}, while the length of first dimension "
+                             f"of input tdi_data_array is {channels_num}.")
+        if self.data_info.time_series_length != samples_num:
+            raise ValueError(f"The length of second dimension of input array is {samples_num}. It is different "
+                             f"with the `time_series_length={self.data_info.time_series_length}` which is set "
+                             "according to the duration and delta_time by `int(duration//delta_time + 1)`.")
+        self.time_samples = torch.as_tensor(self.data_info.time_samples_array, dtype=torch.float64, device="cuda")
+        self.td_data = torch.as_tensor(arr, device="cuda")
+        self._reset_flag = True
+
+    def set_td_data_from_zero(self, channels, duration, delta_time, start_time=0.0, minimum_frequency=1e-5,
+                              maximum_frequency=0.1):
+        """tdi.py:521-583: time-domain data of zeros."""
+        if self._reset_flag:
+            warnings.warn("You are setting `td_data` with zero value; the instance is reset.")
+            self._reset()
+        self.set_data_info(channels, duration, delta_time, start_time, minimum_frequency, maximum_frequency)
+        self.time_samples = torch.as_tensor(self.data_info.time_samples_array, dtype=torch.float64, device="cuda")
+        self.td_data = torch.zeros((len(channels), self.data_info.time_series_length), dtype=torch.float64,
+                                   device="cuda")
+        self._reset_flag = True
+
+    def set_fd_data_from_td(self, window=None):
+        """tdi.py:661-726: ``fd_data`` from ``td_data`` (``fd_from_td``); the start
+        time is not applied as a phase shift, as in the reference."""
+        if self.td_data is None or self.fd_data is not None:
+            raise ValueError("Fourier transform cannot be executed since the `td_data` is not set or "
+                             "`fd_data` has been set previously.")
+        arr = fd_from_td(self.td_data.cpu().numpy(), self.data_info, window)
+        self.frequency_samples = torch.as_tensor(self.data_info.frequency_samples_array, dtype=torch.float64,
+                                                 device="cuda")
+        self.fd_data = torch.as_tensor(arr, device="cuda")
+
+    def set_td_data_from_fd(self, window=None):
+        raise NotImplementedError()
+
+    def set_wd_data_from_zero(self):
+        raise NotImplementedError()
+
+    def set_wd_data_from_td(self):
+        raise NotImplementedError()
+
+    def set_wd_data_from_fd(self):
+        raise NotImplementedError()
+
+    def set_fd_noise_power_density_from_td_data(self):
+        raise NotImplementedError()
+
+    def get_td_noise_realization(self):
+        raise NotImplementedError()
 
     def set_fd_noise_power_density_from_model(self, noise_model, **model_kwargs):
         if isinstance(noise_model, str):
@@ -158,6 +247,12 @@ class TDIChannelData:
         if tuple(arr.shape) != tuple(self.fd_data.shape):
             raise ValueError("Cannot add the input into the `fd_data`: shape differs from the TDI data")
         self.fd_data += arr.to(self.fd_data.dtype)
+
+    @property
+    def td_data_numpy(self):
+        if self.td_data is None:
+            return None
+        return namedtuple("DataContent", self.data_info.channels)(*self.td_data.cpu().numpy())
 
     @property
     def fd_data_numpy(self):
