@@ -4,6 +4,7 @@ from .likelihood import (  # noqa: F401
     CapturedStep,
     LikelihoodBilbyInterface,
     WhittleLikelihood,
+    WhittleLikelihoodCuda,
     compute_whittle_likelihood,
     log_likelihood,
     noise_weighted_inner_product,

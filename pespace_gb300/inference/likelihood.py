@@ -256,6 +256,39 @@ class WhittleLikelihood:
         return out
 
 
+class WhittleLikelihoodCuda(WhittleLikelihood):
+    """``WhittleLikelihoodJax`` (likelihood_jax.py:45-260) with the reference's
+    constructor ``(waveform, detector, channels)``.
+
+    The waveform must be this package's ``IMRPhenomD``, and its frequencies
+    must equal every detector's frequency samples (the reference's checks,
+    likelihood_jax.py:84-112).  Its reference frequency becomes the plan's.
+    ``likelihood_param_type`` is built from the waveform's ``required_params``
+    and the response's four parameters.  ``log_likelihood(params)`` takes that
+    tuple.  The GPU options (``precision``, ``cut_factor``, ``max_batch``,
+    ``n_sparse``) are keyword-only.
+    """
+
+    def __init__(self, waveform, detector, channels, *, precision="fp64", cut_factor=0.0, max_batch=1024,
+                 n_sparse=1024):
+        if not isinstance(waveform, IMRPhenomD):
+            raise TypeError("WhittleLikelihoodCuda requires the waveform to be an IMRPhenomD instance, but got "
+                            f"{type(waveform).__name__}.")
+        dets = detector if isinstance(detector, tuple) else (detector,)
+        for det in dets:
+            if det.backend != "cuda":
+                raise ValueError("WhittleLikelihoodCuda requires all detectors configured with backend='cuda', "
+                                 f"but got backend={det.backend} for detector={det.name}.")
+            fs = det.tdi_data.frequency_samples
+            if fs is None or fs.shape != waveform.frequencies.shape or not torch.equal(
+                    fs.to(waveform.frequencies.device), waveform.frequencies):
+                raise ValueError("The waveform frequencies should match the frequency samples of the TDI data "
+                                 f"for detector={det.name}.")
+        super().__init__(dets, channels, precision=precision, reference_frequency=waveform.reference_frequency,
+                         cut_factor=cut_factor, max_batch=max_batch, n_sparse=n_sparse)
+        self.waveform = waveform
+
+
 class CapturedStep:
     """One batched lnL (+ gradient) call of an engine captured in a CUDA graph.
 

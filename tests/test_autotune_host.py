@@ -26,3 +26,10 @@ def test_autotune_argument_checks():
         autotune(fake, None, reps=0)
     with pytest.raises(ValueError):
         autotune(fake, None, candidates={"tile": (1, 2)})
+
+
+def test_reference_constructor_rejects_other_waveforms():
+    from pespace_gb300.inference import WhittleLikelihoodCuda
+
+    with pytest.raises(TypeError):
+        WhittleLikelihoodCuda("IMRPhenomXAS", None, ("A", "E", "T"))

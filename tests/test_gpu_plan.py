@@ -208,3 +208,25 @@ def test_reference_parameter_tuple_calls(cuda_lib, oracle, dataset):
     assert np.allclose(got, want, rtol=1e-12, atol=1e-9)
     one = eng.log_likelihood(P(*[np.asarray(f)[0] for f in batch]))
     assert isinstance(one, float) and abs(one - want[0]) <= 1e-9 + 1e-12 * abs(want[0])
+
+
+def test_reference_constructor_signature(cuda_lib, oracle, dataset):
+    """WhittleLikelihoodCuda(waveform, detector, channels), the reference's
+    WhittleLikelihoodJax constructor: the same plan as WhittleLikelihood with
+    the waveform's reference frequency, and the reference's argument checks."""
+    from pespace_gb300.inference import WhittleLikelihood, WhittleLikelihoodCuda
+    from pespace_gb300.waveform import IMRPhenomD
+
+    g, dets, th0 = dataset
+    cdets = cuda_detectors(g, dets[:1])
+    freqs = cdets[0].tdi_data.data_info.frequency_samples_array
+    like = WhittleLikelihoodCuda(IMRPhenomD(freqs, 1e-4), cdets, ("A", "E", "T"), max_batch=8)
+    ref = WhittleLikelihood(cdets, precision="fp64", reference_frequency=1e-4, max_batch=8)
+    rng = np.random.default_rng(31)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(3)])
+    assert torch.equal(like.log_likelihood_batch(thetas), ref.log_likelihood_batch(thetas))
+    assert like.likelihood_param_type._fields == ref.likelihood_param_type._fields
+    with pytest.raises(ValueError):
+        WhittleLikelihoodCuda(IMRPhenomD(freqs[:-1], 1e-4), cdets, ("A", "E", "T"))
+    with pytest.raises(ValueError):
+        WhittleLikelihoodCuda(IMRPhenomD(freqs, 1e-4), cdets, ("A", "X"))
