@@ -6,6 +6,8 @@ frequency grid.  The waveform container is a dict ``{"plus", "cross", "tf"}``
 of CUDA tensors, or a mode-keyed dict of such dicts (antenna.py:438-458).
 """
 
+from abc import ABC, abstractmethod
+
 import torch
 
 from .. import _lib
@@ -42,7 +44,19 @@ def _modes(waveform):
     return list(waveform.values())
 
 
-class FDResponseModelMarset2018:
+class SingleLinkResponseModel(ABC):
+    """antenna.py:326-344: the response plugin interface."""
+
+    @abstractmethod
+    def init_single_link_response_model(self, detector):
+        pass
+
+    @abstractmethod
+    def update_single_link_response(self, waveform, lam, beta, psi, tc):
+        pass
+
+
+class FDResponseModelMarset2018(SingleLinkResponseModel):
     """antenna.py:347-543: Marsat et al. (2018) FD response, CUDA backend."""
 
     def __init__(self, backend="cuda"):
@@ -71,6 +85,16 @@ class FDResponseModelMarset2018:
             det.orbit_model.to_c(), _lib.ptr(freqs), n, len(modes), _lib.ptr(hp), _lib.ptr(hc), _lib.ptr(tf),
             float(lam), float(beta), float(psi), float(tc), _lib.ptr(det.single_link_response),
             _lib.stream_handle()))
+
+
+class FDResponseModelLongWavelength(SingleLinkResponseModel):
+    """antenna.py:546-553: a placeholder in the reference, as here (abstract:
+    instantiating it raises TypeError, as there)."""
+
+
+class FDResponseModelStaticLongWavelength(SingleLinkResponseModel):
+    """antenna.py:556-563: a placeholder in the reference, as here (abstract:
+    instantiating it raises TypeError, as there)."""
 
 
 class InterferometerAntenna:
@@ -111,6 +135,34 @@ class InterferometerAntenna:
         if self.tdi_combination.domain != "fd":
             raise NotImplementedError(f"Unsupported domain {self.tdi_combination.domain}")
         self.tdi_data.add_into_fd_data(self.tdi_response)
+
+    def get_optimal_snr(self, waveform, lam, beta, psi, tc):
+        """Optimal SNR per TDI channel and in total (antenna.py:273-303, a
+        placeholder in the reference, which documents this return value).
+
+        rho_c^2 = 4 df sum_f |h_c(f)|^2 / S_c(f) over the data's channels: the
+        normalisation of the reference's likelihood, lnL = -2 df sum |d - h|^2
+        / S.  Bins where S = 0 (the TDI zeros) contribute nothing.  The
+        detector's response buffers hold this waveform's response afterwards.
+        Returns {channel: rho_c, ..., "total": sqrt(sum_c rho_c^2)}.
+        """
+        if self.tdi_combination.domain != "fd":
+            raise NotImplementedError(f"Unsupported domain {self.tdi_combination.domain}")
+        psd = self.tdi_data.fd_noise_power_density
+        if psd is None:
+            raise ValueError("Setting `fd_noise_power_density` before computing the optimal SNR.")
+        self.update_detector_response(waveform, lam, beta, psi, tc)
+        df = float(self.tdi_data.data_info.delta_frequency)
+        out, total = {}, 0.0
+        for c_i, chan in enumerate(self.tdi_data.data_info.channels):
+            h = self.tdi_response[self.tdi_combination.labels.index(chan)]
+            S = psd[c_i]
+            w = torch.where(S > 0, 1.0 / torch.where(S > 0, S, torch.ones_like(S)), torch.zeros_like(S))
+            rho2 = 4.0 * df * float(torch.sum((h.real ** 2 + h.imag ** 2) * w).item())
+            out[chan] = rho2 ** 0.5
+            total += rho2
+        out["total"] = total ** 0.5
+        return out
 
     @property
     def tdi_response_numpy(self):

@@ -5,6 +5,7 @@ Storage is channel-major: ``fd_data`` is a (C, N) complex128 CUDA tensor and
 """
 
 import warnings
+from abc import ABC, abstractmethod
 from collections import namedtuple
 from dataclasses import dataclass, field
 
@@ -242,6 +243,16 @@ class TDIChannelData:
             return torch.as_tensor(arr, dtype=torch.complex128, device="cuda")
         raise ValueError(f"Unknown output_type: {output_type}")
 
+    def add_into_td_data(self):
+        raise NotImplementedError()
+
+    def add_into_wd_data(self):
+        raise NotImplementedError()
+
+    @property
+    def wd_data_numpy(self):
+        return None  # no wavelet-domain data (not implemented, as in the reference)
+
     def add_into_fd_data(self, input):
         arr = input if torch.is_tensor(input) else torch.as_tensor(np.stack(list(input)), device="cuda")
         if tuple(arr.shape) != tuple(self.fd_data.shape):
@@ -267,7 +278,20 @@ class TDIChannelData:
         return namedtuple("DataContent", self.data_info.channels)(*self.fd_noise_power_density.cpu().numpy())
 
 
-class FDMichelsonConstantEqualArm:
+class TDICombinationModel(ABC):
+    """tdi.py:1379-1385: the TDI plugin interface."""
+
+    @abstractmethod
+    def update_tdi_response(self):
+        pass
+
+
+class FDMichelsonConstantEqualArmFFT(TDICombinationModel):
+    """tdi.py:1797-1810: a placeholder in the reference, as here (abstract:
+    instantiating it raises TypeError, as there)."""
+
+
+class FDMichelsonConstantEqualArm(TDICombinationModel):
     """tdi.py:1603-1793: FD Michelson TDI with constant equal arms."""
 
     domain = "fd"
@@ -301,7 +325,7 @@ class FDMichelsonConstantEqualArm:
             _lib.ptr(det.single_link_response), _lib.ptr(det.tdi_response), _lib.stream_handle()))
 
 
-class TDMichelsonConstantEqualArm:
+class TDMichelsonConstantEqualArm(TDICombinationModel):
     """tdi.py:1388-1600: time-domain Michelson TDI with constant equal arms.
 
     The reference marks this class incomplete; the combination it defines is

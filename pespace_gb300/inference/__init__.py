@@ -6,6 +6,7 @@ from .likelihood import (  # noqa: F401
     WhittleLikelihood,
     WhittleLikelihoodCuda,
     compute_whittle_likelihood,
+    compute_whittle_likelihood_ti,
     log_likelihood,
     noise_weighted_inner_product,
 )

@@ -50,6 +50,10 @@ def compute_whittle_likelihood(channels, observed_data, response_data, psd, df, 
                                         _rows(psd, labels, channels), df)
 
 
+# the reference's name for the same call (likelihood_ti.py:17)
+compute_whittle_likelihood_ti = compute_whittle_likelihood
+
+
 class LikelihoodBilbyInterface:
     """interface_bilby.py:21-116 without the bilby base class (bilby is optional)."""
 

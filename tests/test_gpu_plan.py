@@ -230,3 +230,22 @@ def test_reference_constructor_signature(cuda_lib, oracle, dataset):
         WhittleLikelihoodCuda(IMRPhenomD(freqs[:-1], 1e-4), cdets, ("A", "E", "T"))
     with pytest.raises(ValueError):
         WhittleLikelihoodCuda(IMRPhenomD(freqs, 1e-4), cdets, ("A", "X"))
+
+
+def test_optimal_snr(cuda_lib, oracle, dataset):
+    """InterferometerAntenna.get_optimal_snr: rho_c^2 = 4 df sum |h_c|^2 / S_c
+    of the plugin response, against the oracle's A/E/T model."""
+    from pespace_gb300.waveform import IMRPhenomD
+
+    g, dets, th0 = dataset
+    det = cuda_detectors(g, dets[:1])[0]
+    wf = IMRPhenomD(det.tdi_data.data_info.frequency_samples_array, 1e-4)
+    snr = det.get_optimal_snr(wf.from_theta(th0), th0[6], np.arcsin(th0[7]), th0[8], th0[10])
+    h = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets[:1]], 1e-4).model_tdi(0, th0)
+    S = np.asarray(dets[0][4])
+    w = np.where(S > 0, 1.0 / np.where(S > 0, S, 1.0), 0.0)
+    want = 4.0 * g["df"] * np.sum(np.abs(h) ** 2 * w, axis=1)
+    for k, c in enumerate("AET"):
+        assert abs(snr[c] ** 2 - want[k]) <= 1e-8 * want.sum(), c
+    assert abs(snr["total"] ** 2 - want.sum()) <= 1e-8 * want.sum()
+    assert snr["total"] > 0
