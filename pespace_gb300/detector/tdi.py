@@ -86,6 +86,93 @@ def fd_from_td(td_array, info, window=None):
     return np.stack([row[info.frequency_mask_array] for row in out]).astype(np.complex128)
 
 
+# data_info keys of the HDF5 file, in the reference's DataInformation field order (tdi.py:64-101)
+_INFO_KEYS = ("channels", "duration", "delta_time", "start_time", "minimum_frequency", "maximum_frequency",
+              "sampling_frequency", "delta_frequency", "time_series_length", "time_samples_array",
+              "full_frequency_series_length", "full_frequency_samples_array", "frequency_mask_array",
+              "frequency_samples_array", "frequency_series_length")
+
+
+def _h5py():
+    try:
+        import h5py
+    except ImportError as error:
+        raise ImportError("HDF5 save/recover needs h5py, which is not installed") from error
+    return h5py
+
+
+def _as_str(x):
+    x = x[()] if isinstance(x, np.ndarray) and x.ndim == 0 else x
+    return x.decode("utf-8") if isinstance(x, (bytes, np.bytes_)) else str(x)
+
+
+def _info_values(info):
+    values = {k: getattr(info, k) for k in _INFO_KEYS if k not in ("time_samples_array",
+                                                                    "full_frequency_samples_array")}
+    values["time_samples_array"] = info.time_samples_array
+    values["full_frequency_samples_array"] = np.fft.rfftfreq(info.time_series_length, info.delta_time)
+    return values
+
+
+def _hdf5_write(filename, scaling, backend, info, arrays):
+    """tdi.py:1022-1097 layout: class_attrs/{scaling, backend, _np_fp, _np_cp},
+    data_info/<field>, tdi_data/{td_data, fd_data}/<chan>,
+    noise_data/fd_noise_power_density/<chan>.  ``arrays``: {key: (C, n) array or None}."""
+    h5py = _h5py()
+    string = h5py.string_dtype(encoding="utf-8")
+    with h5py.File(filename, "x") as file:
+        file.create_dataset("class_attrs/scaling", data=np.array(scaling))
+        file.create_dataset("class_attrs/backend", data=np.array(backend, dtype=string))
+        file.create_dataset("class_attrs/_np_fp", data=np.array("float64", dtype=string))
+        file.create_dataset("class_attrs/_np_cp", data=np.array("complex128", dtype=string))
+        values = _info_values(info)
+        for key in _INFO_KEYS:
+            if key == "channels":
+                file.create_dataset(f"data_info/{key}", data=np.array(values[key], dtype=string))
+            else:
+                file.create_dataset(f"data_info/{key}", data=np.array(values[key]))
+        for group, keys in (("tdi_data", ("td_data", "fd_data")), ("noise_data", ("fd_noise_power_density",))):
+            for key in keys:
+                data = arrays.get(key)
+                if data is not None:
+                    for c_i, chan in enumerate(info.channels):
+                        file.create_dataset(f"{group}/{key}/{chan}", data=np.asarray(data[c_i]))
+
+
+def _hdf5_read(filename):
+    """tdi.py:1099-1292: (scaling, DataInformation, {key: (C, n) array}) with
+    the reference's checks of the stored precision and derived quantities
+    (AssertionError on a mismatch).  The stored backend is not used: the
+    data are recovered onto this package's CUDA backend."""
+    h5py = _h5py()
+    with h5py.File(filename, "r") as file:
+        scaling = bool(file["class_attrs/scaling"][()])
+        fp, cp = _as_str(file["class_attrs/_np_fp"][()]), _as_str(file["class_attrs/_np_cp"][()])
+        assert fp == "float64" and cp == "complex128", (
+            f"Failed to recover TDIChannelData from file {filename}.\nThe numerical precision of stored data "
+            f"does not match the settings of the current environment.\nThe stored data have _np_fp={fp}, and "
+            f"_np_cp={cp}.\nWhile TDIChannelData in the current environment is initialized with "
+            "_np_fp=float64, and _np_cp=complex128.")
+        channels = tuple(_as_str(c) for c in file["data_info/channels"][()])
+        args = [float(file[f"data_info/{k}"][()]) for k in ("duration", "delta_time", "start_time",
+                                                            "minimum_frequency", "maximum_frequency")]
+        info = DataInformation(channels, *args)
+        values = _info_values(info)
+        for key in _INFO_KEYS[6:]:
+            stored = file[f"data_info/{key}"][()]
+            same = np.array_equal(values[key], stored) if np.ndim(stored) else values[key] == stored
+            assert same, (f"Failed to recover TDIChannelData from file {filename}, the `{key}` is different "
+                          "from the stored value.")
+        arrays = {}
+        for group, keys in (("tdi_data", ("td_data", "fd_data")), ("noise_data", ("fd_noise_power_density",))):
+            if group not in file:
+                continue
+            for key in keys:
+                if key in file[group]:
+                    arrays[key] = np.stack([np.asarray(file[f"{group}/{key}/{chan}"][()]) for chan in channels])
+    return scaling, info, arrays
+
+
 class TDIChannelData:
     """tdi.py:162-1376 with CUDA tensors: ``td_data`` (C, time_series_length)
     float64, ``fd_data`` (C, frequency_series_length) complex128; the
@@ -242,6 +329,35 @@ class TDIChannelData:
         if output_type == "cuda":
             return torch.as_tensor(arr, dtype=torch.complex128, device="cuda")
         raise ValueError(f"Unknown output_type: {output_type}")
+
+    def save_to_file(self, filename):
+        """tdi.py:1022-1097: the instance's data as an HDF5 file (h5py; the
+        file must not exist)."""
+        _hdf5_write(filename, self.scaling, self.backend, self.data_info,
+                    {"td_data": None if self.td_data is None else self.td_data.cpu().numpy(),
+                     "fd_data": None if self.fd_data is None else self.fd_data.cpu().numpy(),
+                     "fd_noise_power_density": None if self.fd_noise_power_density is None
+                     else self.fd_noise_power_density.cpu().numpy()})
+
+    @staticmethod
+    def recover_from_file(filename):
+        """tdi.py:1099-1292: a TDIChannelData from a file written by
+        ``save_to_file`` (here or by the reference), on the CUDA backend."""
+        scaling, info, arrays = _hdf5_read(filename)
+        ret = TDIChannelData(scaling=scaling)
+        ret._data_info = info
+        if "td_data" in arrays:
+            ret.time_samples = torch.as_tensor(info.time_samples_array, dtype=torch.float64, device="cuda")
+            ret.td_data = torch.as_tensor(arrays["td_data"], dtype=torch.float64, device="cuda")
+        if "fd_data" in arrays:
+            ret.frequency_samples = torch.as_tensor(info.frequency_samples_array, dtype=torch.float64,
+                                                    device="cuda")
+            ret.fd_data = torch.as_tensor(arrays["fd_data"], dtype=torch.complex128, device="cuda")
+        if "fd_noise_power_density" in arrays:
+            ret.fd_noise_power_density = torch.as_tensor(arrays["fd_noise_power_density"], dtype=torch.float64,
+                                                         device="cuda")
+        ret._reset_flag = True
+        return ret
 
     def add_into_td_data(self):
         raise NotImplementedError()
