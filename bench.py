@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="adjoint", choices=sorted(WORKLOADS))
+    ap.add_argument("--n-sparse", type=int, default=None, help="sparse nodes of the mixed plan (default per workload)")
     args = ap.parse_args()
     global DUR, DT, FMIN, FMAX, GEN, WORKLOAD
     DUR, DT, FMIN, FMAX, GEN, WORKLOAD = WORKLOADS[args.workload]
@@ -165,10 +166,33 @@ def gemm_peak_tflops(torch, dtype):
     return 2 * 8192 ** 3 / best / 1e12
 
 
-def cpu_baseline_run(n_samples, threads, precision_note, grad=True):
-    """The reference's CPU path (oracle port, FP64 dense, OpenMP over samples)."""
+def stratified(B, n):
+    """Indices of n samples spread evenly over a batch of B (the CPU arms' subsets)."""
+    return np.unique(np.linspace(0, B - 1, max(1, min(n, B))).round().astype(int))
+
+
+def workload_config(B, world):
+    """The `config` of both arms' lines: the workload and its sizes."""
+    g_nbins = int(np.count_nonzero((np.fft.rfftfreq(int(DUR // DT + 1), DT) >= FMIN) *
+                                   (np.fft.rfftfreq(int(DUR // DT + 1), DT) <= FMAX)))
+    return {"workload": WORKLOAD, "global_batch": B * world, "per_gpu_batch": B, "nbins": g_nbins}
+
+
+def td_config():
+    """The `config` of both arms' time-domain TDI lines."""
+    arm = LISA_ARM_M / C_SI
+    n = int(DUR // DT + 1)
+    return {"workload": WORKLOAD, "samples": n, "link_samples": n + int(7 * arm // DT + 1), "batch": 1,
+            "generation": GEN}
+
+
+def cpu_baseline_run(n_samples, threads, precision_note, grad=True, batch=None):
+    """The reference's CPU path (oracle port, FP64 dense, OpenMP over samples) on
+    n_samples of the GPU arm's seeded batch of `batch` samples, spread evenly
+    over it (rank 0's batch)."""
     from oracle import fdpath as oracle
-    from pespace_gb300.workloads import config0_theta, prior_samples
+    from pespace_gb300.replicas import rank_theta
+    from pespace_gb300.workloads import config0_theta
 
     oracle.build()
     g = oracle.grid(DUR, DT, FMIN, FMAX)
@@ -186,11 +210,12 @@ def cpu_baseline_run(n_samples, threads, precision_note, grad=True):
     plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2)
     dets = [(orb, gen, data + plan.model_tdi(k, th0), psd_arr) for k, (orb, gen, data, psd_arr) in enumerate(dets)]
     plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2)
-    thetas = prior_samples(np.random.default_rng(2026), n_samples, th0[10])
+    batch = BATCH if batch is None else batch
+    thetas = rank_theta(0, batch, th0[10])[stratified(batch, n_samples)]
     t0 = time.perf_counter()
     plan.lnl(thetas, grad=grad, nthreads=threads)
     dt = time.perf_counter() - t0
-    return n_samples / dt, dt
+    return len(thetas) / dt, dt
 
 
 def run_reference(args):
@@ -208,30 +233,35 @@ def run_reference(args):
         line = {"impl": "reference", "metric": TD_METRIC, "value": v, "unit": "samples/s", "n_gpus": 0,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (1 << 20) / v,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": WORKLOAD},
+                "data": "synthetic", "config": td_config(),
                 "cpu_baseline": {"value": v, "unit": "samples/s", "cores": 1, "kind": "port",
                                  "sample": "2^20-sample blocks for 1 s per step (numpy); taichi absent on this host"},
                 "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
     threads = os.cpu_count() or 1
-    # network-d: about 9 s of FP64 work per sample and core (three detectors, 3.35 M bins each)
-    n = max(4, threads // 4) if WORKLOAD.startswith("network-d") else max(threads, 16)
+    B = args.batch
+    # a bounded sample of the GPU arm's seeded batch, spread evenly over it:
+    # 64 of the 1024 samples (every 16th); network-d (three detectors, 3.35 M
+    # bins each, about 9 s of FP64 work per sample and core) a quarter of the cores
+    n = max(4, threads // 4) if WORKLOAD.startswith("network-d") else 64
+    n = len(stratified(B, n))
     rates = []
     for _ in range(args.warmup):
-        cpu_baseline_run(min(n, threads), threads, "")
+        cpu_baseline_run(n, threads, "", batch=B)
     for _ in range(args.steps):
-        r, _ = cpu_baseline_run(n, threads, "")
+        r, _ = cpu_baseline_run(n, threads, "", batch=B)
         rates.append(r)
     v = float(np.mean(rates))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "lnL+grad evals/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "global_batch": BATCH, "sample_per_step": n},
+        "config": workload_config(B, world),
         "cpu_baseline": {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} prior samples per step, full grid, FP64 dense with "
-                                   "forward-mode gradient; taichi/jax absent on this host"},
+                         "sample": f"{n} of the {B} seeded samples per step (evenly spread over the batch), "
+                                   "full grid, FP64 dense with forward-mode gradient, OpenMP over samples; "
+                                   "taichi/jax absent on this host"},
         "e2e": {"value": v, "unit": "lnL+grad evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -356,9 +386,8 @@ def run_td_tdi(args):
         "metric": TD_METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded normal link series)",
-        "config": {"workload": WORKLOAD, "samples": n, "link_samples": n_ext, "batch": B, "generation": GEN,
-                   "l2": "flushed between steps (512 MB write outside the timed events); inputs 403 MB",
-                   "parallelism": f"replicas x{world}"},
+        "config": td_config(), "l2": "flushed between steps (512 MB write outside the timed events); inputs 403 MB",
+        "parallelism": f"replicas x{world}",
         "e2e": {"value": world * B * n / (e2e_ms / 1e3), "unit": "samples/s",
                 "h2d_bytes_per_step": int(B * 6 * n_ext * 8), "d2h_bytes_per_step": int(B * 3 * n * 8)},
         "gpu_launches": args.steps,
@@ -406,7 +435,7 @@ def run_native(args):
     else:
         det = lisa_dataset(DUR, DT, FMIN, FMAX, th0, GEN, seed=2026)
     eng = WhittleLikelihood(det, precision=args.precision, reference_frequency=1e-4, cut_factor=1.2, max_batch=B,
-                            n_sparse=N_SPARSE.get(args.workload, 1024))
+                            n_sparse=args.n_sparse or N_SPARSE.get(args.workload, 1024))
     theta_host = torch.as_tensor(replicas.rank_theta(rank, B, th0[10])).pin_memory()
     theta = theta_host.to("cuda")
     lib = _lib.load()
@@ -494,7 +523,7 @@ def run_native(args):
     del graph_step
 
     # ---------------- accuracy against the FP64 path on this workload
-    err = err_split = None
+    err = err_split = fp64_gpu = None
     err_samples = B if args.workload != "network-d" else min(B, 128)  # FP64 over 10 M bins x 3: a subset
     if args.precision == "mixed":
         ref = WhittleLikelihood(det, precision="fp64", reference_frequency=1e-4, cut_factor=1.2, max_batch=B)
@@ -523,6 +552,14 @@ def run_native(args):
                              lnl_range_posterior=[float(bp.min().item()), float(bp.max().item())])
         except np.linalg.LinAlgError:
             err_split.update(posterior_draws=0)
+        # the plain FP64 GPU path timed on the same batch: the metric's comparison
+        fp64_n = err_samples
+        th64 = theta[:fp64_n]
+        ref.log_likelihood_and_grad(th64)
+        ms64 = replicas.reduce_max(timed(lambda: ref.log_likelihood_and_grad(th64), 2), "cuda")
+        fp64_gpu = {"value": replicas.job_rate(world, fp64_n, ms64), "unit": "lnL+grad evals/s",
+                    "ms_per_step": ms64, "steps": 2, "warmup": 1, "samples": fp64_n,
+                    "path": "FP64 plan: dense FP64 evaluation of every live bin, forward-mode gradient"}
         del ref
 
     # ---------------- roofline of the dominant kernel (the dense stage)
@@ -534,15 +571,16 @@ def run_native(args):
         roofline = census.roofline(dom, kern[dom], args.steps, work, True, gemm_peak_tflops(torch, torch.float32))
         roofline["fp64_peak_tflops"] = gemm_peak_tflops(torch, torch.float64)
 
+    config = workload_config(B, world)
+    assert config["nbins"] == int(eng.desc.nbins), (config, eng.desc.nbins)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "lnL+grad evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": args.precision,
-                       "global_batch": B * world, "per_gpu_batch": B, "nbins": int(eng.desc.nbins),
-                       "l2": "flushed between steps (512 MB write outside the timed events)",
-                       "parallelism": f"replicas x{world}"},
+            "config": config, "precision": args.precision,
+            "l2": "flushed between steps (512 MB write outside the timed events)",
+            "parallelism": f"replicas x{world}",
             "e2e": {"value": e2e_value, "unit": "lnL+grad evals/s", "h2d_bytes_per_step": int(B * 11 * 8),
                     "d2h_bytes_per_step": int(B * 12 * 8)},
             "gpu_launches": int(gpu_launches),
@@ -555,22 +593,26 @@ def run_native(args):
             "roofline": roofline,
             "clocks": clocks.summary(),
         }
+        if fp64_gpu is not None:
+            line["fp64_gpu"] = fp64_gpu
+            line["vs_fp64"] = value / fp64_gpu["value"]
         if err is not None:
             line["max_abs_dlnl_vs_fp64"] = err
             line["dlnl_samples"] = err_samples
             line["dlnl_vs_fp64"] = err_split
         if not args.no_cpu_baseline and args.workload != "network-d":
             threads = os.cpu_count() or 1
-            n = 20 * threads  # about 10 s of the 16-core host
-            v, dt = cpu_baseline_run(n, threads, "")
+            n = min(B, 20 * threads)  # about 10 s of the 16-core host
+            v, dt = cpu_baseline_run(n, threads, "", batch=B)
             line["cpu_baseline"] = {"value": v, "unit": "lnL+grad evals/s", "cores": threads, "kind": "port",
-                                    "sample": f"{n} prior samples, full grid, FP64 dense + forward-mode gradient "
-                                              f"({dt:.1f} s)"}
+                                    "sample": f"{n} of the {B} samples (evenly spread over the batch), full grid, "
+                                              f"FP64 dense + forward-mode gradient ({dt:.1f} s)"}
             # lnL only on one core: the setting of the reference's published single-core figure
             n1 = 32
-            v1, dt1 = cpu_baseline_run(n1, 1, "", grad=False)
+            v1, dt1 = cpu_baseline_run(n1, 1, "", grad=False, batch=B)
             line["cpu_baseline_1core_lnl"] = {"value": v1, "unit": "lnL evals/s", "cores": 1, "kind": "port",
-                                              "sample": f"{n1} prior samples, full grid, FP64 dense ({dt1:.1f} s)"}
+                                              "sample": f"{n1} of the {B} samples, full grid, FP64 dense "
+                                                        f"({dt1:.1f} s)"}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

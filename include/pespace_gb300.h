@@ -121,6 +121,16 @@ int pes_whittle_lnl_noalloc(const double* data, const double* response, const do
 int pes_phenomd(const double* theta /* host */, const double* freqs, int64_t n, double f_ref, double f_cut_hz,
                 double* hp, double* hc, double* tf, void* stream);
 
+/* Higher-mode waveform producer: the mode-keyed container of the reference's
+ * higher-mode producers (pespace/waveform/interface_ripple.py:155-235; consumed
+ * mode by mode at antenna.py:446-458), with IMRPhenomHM (London et al. 2018)
+ * in place of the absent IMRPhenomXHM.  Modes, in this order: (2,2), (2,1),
+ * (3,3), (3,2), (4,4), (4,3).  hp, hc: (6, n) complex; tf: (6, n) seconds,
+ * t_c = 0; each mode zero above f_cut_hz and above its mapped Mf = 0.2.
+ * theta: host, 11 doubles. */
+int pes_phenomhm(const double* theta /* host */, const double* freqs, int64_t n, double f_ref, double f_cut_hz,
+                 double* hp, double* hc, double* tf, void* stream);
+
 /* Post-Newtonian time-frequency map of the lalsimulation waveform interface:
  * replaces get_PN_d_phase (pespace/waveform/interface_lalsim.py:297-482),
  * which fills the `tf` entry of the waveform container for lalsimulation's FD
@@ -171,6 +181,8 @@ int pes_td_tdi_layout(double arm_sec, double delta_time, int32_t generation, int
 #define PES_MAX_DETECTORS 4
 #define PES_PRECISION_FP64 0 /* dense FP64 evaluation on every bin             */
 #define PES_PRECISION_MIXED 1 /* FP64 sparse grid + FP32 dense spline bulk      */
+#define PES_APPROX_PHENOMD 0  /* IMRPhenomD, the (2,2) mode                       */
+#define PES_APPROX_PHENOMHM 1 /* IMRPhenomHM, modes (2,2),(2,1),(3,3),(3,2),(4,4),(4,3) */
 
 typedef struct PesDetectorDesc {
   PesOrbit orbit;
@@ -190,7 +202,7 @@ typedef struct PesPlanDesc {
   int32_t precision;  /* PES_PRECISION_*                                         */
   int32_t n_sparse;   /* mixed: sparse log-spaced nodes in [fmin, fmax]          */
   int32_t max_batch;  /* largest B passed to the batch calls                     */
-  int32_t pad;
+  int32_t approximant; /* PES_APPROX_*: the waveform of the plan's samples         */
   PesDetectorDesc det[PES_MAX_DETECTORS];
 } PesPlanDesc;
 

@@ -82,7 +82,13 @@ class OraclePlan(ctypes.Structure):
         ("n_det", ctypes.c_int32),
         ("chan_mask", ctypes.c_int32),
         ("dets", ctypes.c_void_p),
+        ("approximant", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
     ]
+
+
+APPROXIMANTS = {"IMRPhenomD": 0, "IMRPhenomHM": 1}
+HM_MODES = ((2, 2), (2, 1), (3, 3), (3, 2), (4, 4), (4, 3))
 
 
 def lib():
@@ -102,6 +108,7 @@ def lib():
         L.oracle_whittle.argtypes = [vp, vp, vp, ctypes.c_int, i64, d]
         L.oracle_whittle.restype = d
         L.oracle_phenomd.argtypes = [vp, vp, i64, d, d, vp, vp, vp, vp, vp]
+        L.oracle_phenomhm.argtypes = [vp, vp, i64, d, d, vp, vp, vp, vp, vp]
         L.oracle_model_tdi.argtypes = [P(OraclePlan), ctypes.c_int, ctypes.c_int, vp, vp]
         L.oracle_lnl_batch.argtypes = [P(OraclePlan), vp, i64, vp, vp, ctypes.c_int]
         L.oracle_fisher_batch.argtypes = [P(OraclePlan), vp, i64, vp, ctypes.c_int]
@@ -213,6 +220,24 @@ def phenomd(theta, freqs, f_ref, f_cut_hz=np.inf, amp_psi=False):
     return hp, hc, tf, dict(zip(keys, info))
 
 
+def phenomhm(theta, freqs, f_ref, f_cut_hz=np.inf):
+    """IMRPhenomHM container: hp, hc (6, n) complex, tf (6, n), amplitude and
+    phase (6, n) (h_lm = A exp(-i Psi)) in mode order HM_MODES, and per mode
+    (fRD_lm [Mf], Rholm, amplitude-map inspiral corner [Mf], phase-map
+    ringdown corner [Mf])."""
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64)
+    n = freqs.size
+    hp = np.zeros((6, n), dtype=np.complex128)
+    hc = np.zeros((6, n), dtype=np.complex128)
+    tf = np.zeros((6, n))
+    ap = np.zeros((6, n, 2))
+    info = np.zeros((6, 4))
+    lib().oracle_phenomhm(_p(theta), _p(freqs), n, f_ref, float(min(f_cut_hz, 1e300)), _p(hp), _p(hc), _p(tf),
+                          _p(ap), _p(info))
+    return hp, hc, tf, ap[..., 0], ap[..., 1], info
+
+
 # ------------------------------------------------------------------ grid
 def grid(duration, delta_time, minimum_frequency, maximum_frequency):
     """pespace/detector/tdi.py:120-159 semantics, as index arithmetic.
@@ -311,7 +336,7 @@ def noise_realization(g, psd_by_channel, channels, seed):
 class Plan:
     """Keeps the ctypes plan and the arrays it points to alive."""
 
-    def __init__(self, g, detectors, f_ref, cut_factor=0.0, channels=("A", "E", "T")):
+    def __init__(self, g, detectors, f_ref, cut_factor=0.0, channels=("A", "E", "T"), approximant="IMRPhenomD"):
         self.g = g
         self._keep = []
         dets = (OracleDet * len(detectors))()
@@ -334,6 +359,7 @@ class Plan:
         p.n_det = len(detectors)
         p.chan_mask = sum(1 << "AET".index(c) for c in channels)
         p.dets = ctypes.addressof(dets)
+        p.approximant = APPROXIMANTS[approximant]
         self.plan = p
 
     def lnl(self, theta, grad=False, nthreads=0):

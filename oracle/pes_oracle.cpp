@@ -17,6 +17,10 @@
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
+
+// Kerr quasi-normal-mode table (model data shared with the CUDA kernels)
+#define PES_QNM_STORAGE static const
+#include "../pespace_gb300/csrc/pes_qnm_table.h"
 #endif
 
 namespace orc {
@@ -280,7 +284,7 @@ void tdi_at_f(double f, double arm, int gen20, int orth, const Cx<T> L[6], Cx<T>
 // value = l00 + l10 eta + xi (l01 + l11 eta + l21 eta^2) + xi^2 (l02 + l12 eta + l22 eta^2)
 //       + xi^3 (l03 + l13 eta + l23 eta^2), with xi = chi_PN - 1.
 enum { F_V2, F_G1, F_G2, F_G3, F_S1, F_S2, F_S3, F_S4,
-       F_B1, F_B2, F_B3, F_A1, F_A2, F_A3, F_A4, F_A5, F_COUNT };
+       F_B1, F_B2, F_B3, F_A1, F_A2, F_A3, F_A4, F_A5, F_R1, F_R2, F_R3, F_COUNT };
 static const double kFit[F_COUNT][11] = {
   {0.8149838730507785, 2.5747553517454658, 1.1610198035496786, -2.3627771785551537, 6.771038707057573, 0.7570782938606834, -2.7256896890432474, 7.1140380397149965, 0.1766934149293479, -0.7978690983168183, 2.1162391502005153},
   {0.006927402739328343, 0.03020474290328911, 0.006308024337706171, -0.12074130661131138, 0.26271598905781324, 0.0034151773647198794, -0.10779338611188374, 0.27098966966891747, 0.0007374185938559283, -0.02749621038376281, 0.0733150789135702},
@@ -298,6 +302,10 @@ static const double kFit[F_COUNT][11] = {
   {9.5988072383479, -397.05438595557433, 16.202126189517813, -1574.8286986717037, 3600.3410843831093, 27.092429659075467, -1786.482357315139, 5152.919378666511, 11.175710130033895, -577.7999423177481, 1808.730762932043},
   {-0.02989487384493607, 1.4022106448583738, -0.07356049468633846, 0.8337006542278661, 0.2240008282397391, -0.055202870001177226, 0.5667186343606578, 0.7186931973380503, -0.015507437354325743, 0.15750322779277187, 0.21076815715176228},
   {0.9974408278363099, -0.007884449714907203, -0.059046901195591035, 1.3958712396764088, -4.516631601676276, -0.05585343136869692, 1.7516580039343603, -5.990208965347804, -0.017945336522161195, 0.5965097794825992, -2.0608879367971804},
+  // rho1..rho3: the calibrated inspiral amplitude terms (coefficients of Mf^{7/3}, Mf^{8/3}, Mf^3)
+  {3931.8979897196614, -17395.758706812805, 3132.375545898835, 343965.86092361377, -1.2162565819981997e6, -70698.00600428853, 1.383907177859705e6, -3.9662761890979446e6, -60017.52423652596, 803515.1181825735, -2.091710365941658e6},
+  {-40105.47653771657, 112253.0169706701, 23561.696065836168, -3.476180699403351e6, 1.137593670849482e7, 754313.1127166454, -1.308476044625268e7, 3.6444584853928134e7, 596226.612472288, -7.4277901143564405e6, 1.8928977514040343e7},
+  {83208.35471266537, -191237.7264145924, -210916.2454782992, 8.71797508352568e6, -2.6914942420669552e7, -1.9889806527362722e6, 3.0888029960154563e7, -8.390870279256162e7, -1.4535031953446497e6, 1.7063528990822166e7, -4.2748659731120914e7},
 };
 
 template <class T>
@@ -308,6 +316,32 @@ T fit_eval(int which, const T& eta, const T& xi) {
   T xi3 = xi2 * xi;
   return c[0] + c[1] * eta + xi * (c[2] + c[3] * eta + c[4] * eta2) + xi2 * (c[5] + c[6] * eta + c[7] * eta2) +
          xi3 * (c[8] + c[9] * eta + c[10] * eta2);
+}
+
+// Kerr quasi-normal modes: M omega = wR - i wI of mode `mode` (table order
+// (2,2), (2,1), (3,3), (3,2), (4,4), (4,3)) at dimensionless spin a, from the
+// natural cubic spline in u = sqrt(1 - a) through the tabulated frequencies
+// (computed by Leaver's continued fractions, pespace_gb300/csrc/gen_qnm_table.py);
+// a is clamped to +-PES_QNM_A_MAX.
+template <class T>
+void qnm_interp(int mode, const T& a, T& wR, T& wI) {
+  T ac = a;
+  if (val(ac) > PES_QNM_A_MAX) ac = T(PES_QNM_A_MAX);
+  if (val(ac) < -PES_QNM_A_MAX) ac = T(-PES_QNM_A_MAX);
+  T u = sqrt(1.0 - ac);
+  int i = (int)std::floor((val(u) - PES_QNM_U0) / PES_QNM_DU);
+  if (i < 0) i = 0;
+  if (i > PES_QNM_NODES - 2) i = PES_QNM_NODES - 2;
+  const double h = PES_QNM_DU;
+  T t = (u - (PES_QNM_U0 + i * h)) / h;
+  T s = 1.0 - t;
+  T cA = (s * s * s - s) * (h * h / 6.0), cB = (t * t * t - t) * (h * h / 6.0);
+  const double* re = kQnmTable[mode][0];
+  const double* re2 = kQnmTable[mode][1];
+  const double* im = kQnmTable[mode][2];
+  const double* im2 = kQnmTable[mode][3];
+  wR = s * re[i] + t * re[i + 1] + cA * re2[i] + cB * re2[i + 1];
+  wI = s * im[i] + t * im[i + 1] + cA * im2[i] + cB * im2[i + 1];
 }
 
 // Phenomenological constants of IMRPhenomD.
@@ -328,6 +362,8 @@ struct PhenomD {
   T t0, MfRef, phi_shift;  // Psi = Phi(Mf) - t0 (Mf - MfRef) - phi_shift
   T amp_scale;              // h22 = amp_scale * Mf^{-7/6} * Ahat(Mf)
   T pfac, cfac;             // (1 + cos^2 i)/2, cos i
+  T af, erad;               // remnant spin and radiated energy (fraction of M)
+  T v2c;                    // intermediate amplitude collocation value
 };
 
 template <class T>
@@ -483,20 +519,23 @@ void phenomd_setup(const T* th, double f_ref, PhenomD<T>& p) {
                      (0.1014665242971878 - 2.0967746996832157 * eta) * s +
                      (-1.3546806617824356 + 4.108962025369336 * eta) * s2 +
                      (-0.8676969352555539 + 2.064046835273906 * eta) * s3));
+  p.af = af;
   T sn = s / (m1 * m1 + m2 * m2);
   T eta4 = eta3 * eta;
   T erad = ((0.055974469826360077 * eta + 0.5809510763115132 * eta2 - 0.9606726679372312 * eta3 +
              3.352411249771192 * eta4) *
             (1.0 + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * eta2) * sn)) /
            (1.0 + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * eta2) * sn);
-  // (2,2,0) quasi-normal mode from the Berti, Cardoso & Will (2006) fits
-  T oneminus = 1.0 - af;
-  T wR = 1.5251 - 1.1568 * pow(oneminus, 0.1292);
-  T Q = 0.7 + 1.4187 * pow(oneminus, -0.4990);
+  p.erad = erad;
+  // (2,2,0) quasi-normal mode of the remnant (mass 1 - E_rad, spin af): the
+  // Kerr frequency M omega = wR - i wI interpolated from the mode table
+  T wR, wI;
+  qnm_interp(0, af, wR, wI);
   p.fRD = wR / (2.0 * PI) / (1.0 - erad);
-  p.fDM = wR / (2.0 * Q) / (2.0 * PI) / (1.0 - erad);
+  p.fDM = wI / (2.0 * PI) / (1.0 - erad);
   // fits
   T v2c = fit_eval(F_V2, eta, xi);
+  p.v2c = v2c;
   p.g1 = fit_eval(F_G1, eta, xi);
   p.g2 = fit_eval(F_G2, eta, xi);
   p.g3 = fit_eval(F_G3, eta, xi);
@@ -541,11 +580,10 @@ void phenomd_setup(const T* th, double f_ref, PhenomD<T>& p) {
                     77616.0 * c12 * (2610335.0 + 995766.0 * seta) - 77287373856.0 * c22 * seta +
                     5841690624.0 * (chi1 + chi2) * PI + 21384760320.0 * pi2))) /
       60085960704.0;
-  // The calibrated inspiral terms rho1..rho3 (Mf^{7/3}, Mf^{8/3}, Mf^3) are not
-  // used: the inspiral amplitude is the 3PN SPA amplitude alone.
-  p.ampc[5] = T(0.0);
-  p.ampc[6] = T(0.0);
-  p.ampc[7] = T(0.0);
+  // the calibrated inspiral terms rho1 Mf^{7/3} + rho2 Mf^{8/3} + rho3 Mf^3 (Khan et al. 2016 eq. 29)
+  p.ampc[5] = fit_eval(F_R1, eta, xi);
+  p.ampc[6] = fit_eval(F_R2, eta, xi);
+  p.ampc[7] = fit_eval(F_R3, eta, xi);
   // intermediate amplitude: match value/derivative at 0.014 and fpeak, value v2 in between
   {
     T f1 = T(AMP_F_JOIN_INS), f3 = p.fpeak, f2 = 0.5 * (f1 + f3);
@@ -646,6 +684,285 @@ bool phenomd_eval(const PhenomD<T>& p, double f, double f_cut_hz, Cx<T>& hp, Cx<
   return true;
 }
 
+// ----------------------------------------------------------------- IMRPhenomHM
+// The higher-multipole model of London et al. 2018 (arXiv:1708.00404), built
+// from the (2,2) IMRPhenomD as the paper does:
+//  * each mode's frequency maps onto the (2,2) frequency f22: f22 = 2 f / m
+//    in the inspiral (same orbital frequency), f22 = Rholm f in the ringdown
+//    (Rholm = fRD22 / fRD_lm, so the mode's ringdown sits at its own Kerr QNM
+//    frequency); between the corners the phase map is linear (the paper's),
+//    the amplitude map the cubic Hermite blend of the two lines (value and
+//    slope matched, so that the amplitude stays C1); the amplitude map's
+//    corners are the (2,2) amplitude joins Mf = 0.014 and f_peak, the phase
+//    map's the (2,2) phase joins Mf = 0.018 and fRD22 / 2;
+//  * amplitude A_lm(f) = beta_lm A22(f22): beta_lm the ratio of the
+//    post-Newtonian mode amplitudes |H_lm| / |H_22| sqrt(2/m) at the
+//    orbital velocity v = (2 pi M f_b / m)^{1/3} (leading order with the 1PN
+//    corrections of the l = m modes and the leading spin term of (2,1);
+//    Blanchet, Living Rev. Rel. 17, 2 (2014) eq. 327; Arun et al. 2009),
+//    f_b = f below the amplitude map's inspiral corner f_i and
+//    f_i (2 - exp(1 - f/f_i)) above it (C1, saturating at 2 f_i); A22 the
+//    PhenomD amplitude whose merger-ringdown Lorentzian width is the mode's,
+//    in mapped frequency Rholm fDM_lm (intermediate collocation re-solved);
+//  * phase Psi_lm(f) = (m/2) Psi22(2 f / m) in the inspiral,
+//    (1/a) Psi22(a f + b) + c0 + c1 f between the corners and
+//    (1/Rholm) Psi22^MRD(Rholm f) + c0' + c1' f in the ringdown, with the
+//    damping of the arctangent the mode's (Rholm fDM_lm in mapped
+//    frequency) and c0, c1, c0', c1' making Psi_lm C1; plus the constant
+//    phase of H_lm (k quarter turns).  t_lm(f) = dPsi_lm/df / (2 pi).
+//  * polarisations: hp = sum P_lm h_lm, hc = i sum C_lm h_lm with
+//    P_lm = [(-1)^l Y_{l,-m} + Y_lm] / (2 N), C_lm = [(-1)^l Y_{l,-m} - Y_lm] / (2 N),
+//    Y the s = -2 spherical harmonics at azimuth 0 (Wigner d^l_{m,2}) and
+//    N = sqrt(5 / (16 pi)), so that (2,2) gives PhenomD's (1 + cos^2 i)/2, -cos i.
+// Modes (in this order): (2,2), (2,1), (3,3), (3,2), (4,4), (4,3) (also the
+// order of the quasi-normal-mode table).
+constexpr int HM_MODES = 6;
+static const int kHMlm[HM_MODES][2] = {{2, 2}, {2, 1}, {3, 3}, {3, 2}, {4, 4}, {4, 3}};
+
+static double factorial(int n) {
+  double r = 1.0;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+
+// s = -2 spin-weighted spherical harmonic at azimuth 0 from cos(iota):
+// sqrt((2l+1)/(4 pi)) d^l_{m,2}(iota)
+template <class T>
+T sylm_m2(int l, int m, const T& cosi) {
+  T ch = sqrt(0.5 * (1.0 + cosi)), sh = sqrt(0.5 * (1.0 - cosi));
+  T sum = T(0.0);
+  for (int k = 0; k <= l + m; ++k) {
+    if (l + m - k < 0 || l - 2 - k < 0 || k + 2 - m < 0) continue;
+    const double c = ((k & 1) ? -1.0 : 1.0) *
+                     std::sqrt(factorial(l + m) * factorial(l - m) * factorial(l + 2) * factorial(l - 2)) /
+                     (factorial(l + m - k) * factorial(l - 2 - k) * factorial(k) * factorial(k + 2 - m));
+    T term = T(c);
+    for (int e = 0; e < 2 * l + m - 2 * k - 2; ++e) term = term * ch;
+    for (int e = 0; e < 2 * k + 2 - m; ++e) term = term * sh;
+    sum = sum + term;
+  }
+  return std::sqrt((2.0 * l + 1.0) / (4.0 * PI)) * sum;
+}
+
+// Signed post-Newtonian amplitude ratio beta_lm(v) and the quarter turns of
+// H_lm's phase (H_lm = i^k |.|).
+template <class T>
+T hm_pn_ratio(int l, int m, const T& v, const T& eta, const T& dlt, const T& chis, const T& chia, int* kq) {
+  T v2 = v * v;
+  T h22 = 1.0 + v2 * (-107.0 / 42.0 + 55.0 / 42.0 * eta) + 2.0 * PI * v2 * v;
+  T r;
+  if (l == 2 && m == 2) { *kq = 0; return T(1.0); }
+  if (l == 2 && m == 1) {
+    *kq = 1;
+    r = (1.0 / 3.0) * (dlt * v * (1.0 + v2 * (-17.0 / 28.0 + 5.0 / 7.0 * eta)) - 1.5 * (chia + dlt * chis) * v2);
+  } else if (l == 3 && m == 3) {
+    *kq = 3;
+    r = 0.75 * std::sqrt(15.0 / 14.0) * dlt * v * (1.0 + v2 * (-4.0 + 2.0 * eta));
+  } else if (l == 3 && m == 2) {
+    *kq = 0;
+    r = (1.0 / 3.0) * std::sqrt(5.0 / 7.0) * v2 * (1.0 - 3.0 * eta);
+  } else if (l == 4 && m == 4) {
+    *kq = 2;
+    r = (8.0 / 9.0) * std::sqrt(5.0 / 7.0) * v2 * (1.0 - 3.0 * eta);
+  } else {  // (4,3)
+    *kq = 3;
+    r = 9.0 / (4.0 * std::sqrt(70.0)) * dlt * v2 * v * (1.0 - 2.0 * eta);
+  }
+  return r / h22 * std::sqrt(2.0 / m);
+}
+
+template <class T>
+struct PhenomHMMode {
+  int l, m, kq;
+  T P, C;                          // polarisation factors
+  T Rholm, fRD, fDMeff, g3fDMeff;  // fRD: the mode's ringdown frequency (Mf)
+  T fpeak, dl[5];                  // amplitude in mapped frequency: peak, intermediate polynomial
+  T fiA, frA;                      // amplitude map corners (Mf)
+  T fiP, frP, aP, bP;              // phase map
+  T cI0, cI1, cR0, cR1;            // C1 constants of the phase
+};
+
+template <class T>
+struct PhenomHM {
+  PhenomD<T> d;
+  PhenomHMMode<T> md[HM_MODES];
+  T eta, dlt, chis, chia;
+  T fRD_max;  // largest ringdown frequency of the modes (Mf)
+};
+
+// the amplitude's frequency map: 2 f / m below fiA, Rholm f above frA, the
+// cubic Hermite blend of the two (values and slopes) between
+template <class T>
+T hm_amp_map(const PhenomHMMode<T>& md, const T& Mf) {
+  if (md.l == 2 && md.m == 2) return Mf;  // the identity for (2,2), exactly
+  if (Mf <= md.fiA) return (2.0 / md.m) * Mf;
+  if (Mf >= md.frA) return md.Rholm * Mf;
+  const T h = md.frA - md.fiA, s = (Mf - md.fiA) / h;
+  const T s2 = s * s, s3 = s2 * s;
+  return (2.0 * s3 - 3.0 * s2 + 1.0) * ((2.0 / md.m) * md.fiA) + (s3 - 2.0 * s2 + s) * (h * (2.0 / md.m)) +
+         (3.0 * s2 - 2.0 * s3) * (md.Rholm * md.frA) + (s3 - s2) * (h * md.Rholm);
+}
+
+// mapped (2,2) amplitude hat with the mode's merger-ringdown width
+template <class T>
+T hm_amp_hat(const PhenomHM<T>& h, const PhenomHMMode<T>& md, const T& Mf22) {
+  const PhenomD<T>& p = h.d;
+  if (Mf22 < AMP_F_JOIN_INS) return amp_ins(p, Mf22);
+  if (Mf22 >= md.fpeak) {
+    T x = Mf22 - p.fRD;
+    return p.g1 * md.g3fDMeff / (x * x + md.g3fDMeff * md.g3fDMeff) * exp(-p.g2 * x / md.g3fDMeff);
+  }
+  return md.dl[0] + Mf22 * (md.dl[1] + Mf22 * (md.dl[2] + Mf22 * (md.dl[3] + Mf22 * md.dl[4])));
+}
+
+// (2,2) phase and its Mf-derivative (aligned: Psi = Phi - t0 (Mf - MfRef) - shift)
+template <class T>
+void hm_psi22(const PhenomD<T>& p, const T& Mf, T& psi, T& dpsi) {
+  psi = phi_full(p, Mf) - p.t0 * (Mf - p.MfRef) - p.phi_shift;
+  dpsi = dphi_full(p, Mf) - p.t0;
+}
+// the (2,2) merger-ringdown phase ansatz with damping fdm
+template <class T>
+void hm_psi22_mrd(const PhenomD<T>& p, const T& fdm, const T& Mf, T& psi, T& dpsi) {
+  T sq = sqrt(sqrt(Mf));
+  T x = Mf - p.a5 * p.fRD;
+  psi = (p.a1 * Mf - p.a2 / Mf + (4.0 / 3.0) * p.a3 * sq * sq * sq + p.a4 * atan(x / fdm)) / p.eta + p.C1MRD +
+        p.C2MRD * Mf - p.t0 * (Mf - p.MfRef) - p.phi_shift;
+  dpsi = (p.a1 + p.a2 / (Mf * Mf) + p.a3 / sq + p.a4 * fdm / (fdm * fdm + x * x)) / p.eta + p.C2MRD - p.t0;
+}
+
+// Psi_lm and dPsi_lm/dMf without the constant quarter turns; region by Mf
+template <class T>
+void hm_phase(const PhenomHM<T>& h, const PhenomHMMode<T>& md, const T& Mf, T& psi, T& dpsi) {
+  if (Mf < md.fiP) {
+    hm_psi22(h.d, (2.0 / md.m) * Mf, psi, dpsi);
+    psi = (0.5 * md.m) * psi;
+  } else if (Mf < md.frP) {
+    hm_psi22(h.d, md.aP * Mf + md.bP, psi, dpsi);
+    psi = psi / md.aP + md.cI0 + md.cI1 * Mf;
+    dpsi = dpsi + md.cI1;
+  } else {
+    hm_psi22_mrd(h.d, md.fDMeff, md.Rholm * Mf, psi, dpsi);
+    psi = psi / md.Rholm + md.cR0 + md.cR1 * Mf;
+    dpsi = dpsi + md.cR1;
+  }
+}
+
+template <class T>
+void phenomhm_setup(const T* th, double f_ref, PhenomHM<T>& h) {
+  PhenomD<T>& p = h.d;
+  phenomd_setup(th, f_ref, p);
+  T q = th[1];
+  h.eta = p.eta;
+  h.dlt = (q - 1.0) / (q + 1.0);
+  h.chis = 0.5 * (th[2] + th[3]);
+  h.chia = 0.5 * (th[2] - th[3]);
+  const double nrm = 2.0 * std::sqrt(5.0 / (64.0 * PI));
+  h.fRD_max = p.fRD;
+  for (int k = 0; k < HM_MODES; ++k) {
+    PhenomHMMode<T>& md = h.md[k];
+    md.l = kHMlm[k][0];
+    md.m = kHMlm[k][1];
+    const int l = md.l, m = md.m;
+    T Yp = sylm_m2(l, m, th[5]), Ym = sylm_m2(l, -m, th[5]);
+    const double sg = (l & 1) ? -1.0 : 1.0;
+    md.P = (sg * Ym + Yp) / (2.0 * nrm);
+    md.C = (sg * Ym - Yp) / (2.0 * nrm);
+    // the mode's Kerr quasi-normal mode
+    T wR, wI;
+    qnm_interp(k, p.af, wR, wI);
+    md.fRD = wR / (2.0 * PI) / (1.0 - p.erad);
+    T fDMlm = wI / (2.0 * PI) / (1.0 - p.erad);
+    if (val(md.fRD) > val(h.fRD_max)) h.fRD_max = md.fRD;
+    md.Rholm = p.fRD / md.fRD;
+    md.fDMeff = md.Rholm * fDMlm;
+    md.g3fDMeff = p.g3 * md.fDMeff;
+    if (p.g2 <= 1.0)
+      md.fpeak = fabs(p.fRD + (md.fDMeff * (-1.0 + sqrt(1.0 - p.g2 * p.g2)) * p.g3) / p.g2);
+    else
+      md.fpeak = fabs(p.fRD + (-md.fDMeff * p.g3) / p.g2);
+    // intermediate amplitude with the mode's merger-ringdown: value/derivative at 0.014 and fpeak, v2 midway
+    {
+      T f1 = T(AMP_F_JOIN_INS), f3 = md.fpeak, f2 = 0.5 * (f1 + f3);
+      T A[5][5], b[5];
+      T fs[3] = {f1, f2, f3};
+      for (int r = 0; r < 3; ++r) {
+        T pw = T(1.0);
+        for (int j = 0; j < 5; ++j) { A[r][j] = pw; pw = pw * fs[r]; }
+      }
+      T fd[2] = {f1, f3};
+      for (int r = 0; r < 2; ++r) {
+        A[3 + r][0] = T(0.0);
+        A[3 + r][1] = T(1.0);
+        A[3 + r][2] = 2.0 * fd[r];
+        A[3 + r][3] = 3.0 * fd[r] * fd[r];
+        A[3 + r][4] = 4.0 * fd[r] * fd[r] * fd[r];
+      }
+      T x3 = f3 - p.fRD, den = x3 * x3 + md.g3fDMeff * md.g3fDMeff;
+      T Amrd = p.g1 * md.g3fDMeff / den * exp(-p.g2 * x3 / md.g3fDMeff);
+      b[0] = amp_ins(p, f1);
+      b[1] = p.v2c;
+      b[2] = Amrd;
+      b[3] = damp_ins(p, f1);
+      b[4] = Amrd * (-p.g2 / md.g3fDMeff - 2.0 * x3 / den);
+      solve5(A, b, md.dl);
+    }
+    // maps: corners at the (2,2) joins, inspiral slope 2/m, ringdown slope Rholm
+    md.fiA = (0.5 * m) * AMP_F_JOIN_INS;
+    md.frA = md.fpeak / md.Rholm;
+    int kq;
+    hm_pn_ratio(l, m, T(0.1), h.eta, h.dlt, h.chis, h.chia, &kq);
+    md.kq = kq;
+    md.fiP = (0.5 * m) * PHI_F_JOIN_INS;
+    md.frP = (0.5 * p.fRD) / md.Rholm;
+    md.aP = (0.5 * p.fRD - PHI_F_JOIN_INS) / (md.frP - md.fiP);
+    md.bP = PHI_F_JOIN_INS - md.aP * md.fiP;
+    // C1 matching of the phase at fiP and frP
+    md.cI0 = md.cI1 = md.cR0 = md.cR1 = T(0.0);
+    T v1, d1, v2_, d2;
+    hm_psi22(p, (2.0 / m) * md.fiP, v1, d1);
+    v1 = (0.5 * m) * v1;
+    hm_psi22(p, md.aP * md.fiP + md.bP, v2_, d2);
+    v2_ = v2_ / md.aP;
+    md.cI1 = d1 - d2;
+    md.cI0 = v1 - v2_ - md.cI1 * md.fiP;
+    T v3, d3;
+    hm_psi22(p, md.aP * md.frP + md.bP, v2_, d2);
+    v2_ = v2_ / md.aP + md.cI0 + md.cI1 * md.frP;
+    d2 = d2 + md.cI1;
+    hm_psi22_mrd(p, md.fDMeff, md.Rholm * md.frP, v3, d3);
+    v3 = v3 / md.Rholm;
+    md.cR1 = d2 - d3;
+    md.cR0 = v2_ - v3 - md.cR1 * md.frP;
+  }
+}
+
+// Mode k: amplitude, phase (including the quarter turns) and t(f) at f [Hz];
+// false where the mode is zero (above f_cut_hz or above mapped Mf = 0.2).
+template <class T>
+bool phenomhm_mode(const PhenomHM<T>& h, int k, double f, double f_cut_hz, T& amp, T& psi, T& tf) {
+  const PhenomD<T>& p = h.d;
+  const PhenomHMMode<T>& md = h.md[k];
+  T Mf = p.M_sec * f;
+  T f22A = hm_amp_map(md, Mf);
+  if (f > f_cut_hz || f22A > MF_CUT) {
+    amp = T(0.0);
+    psi = T(0.0);
+    tf = T(0.0);
+    return false;
+  }
+  int kq;
+  const T fb = (Mf <= md.fiA) ? Mf : md.fiA * (2.0 - exp(1.0 - Mf / md.fiA));
+  const T beta = hm_pn_ratio(md.l, md.m, cbrt(2.0 * PI * fb / md.m), h.eta, h.dlt, h.chis, h.chia, &kq);
+  T v = cbrt(f22A);
+  amp = beta * (p.amp_scale / (f22A * sqrt(v)) * hm_amp_hat(h, md, f22A));
+  T dpsi;
+  hm_phase(h, md, Mf, psi, dpsi);
+  psi = psi + md.kq * (0.5 * PI);
+  tf = p.M_sec / (2.0 * PI) * dpsi;
+  return true;
+}
+
 // ----------------------------------------------------------------- batch lnL
 struct OracleDet {
   OrbitDesc orbit;
@@ -665,6 +982,8 @@ struct OraclePlan {
   int32_t n_det;
   int32_t chan_mask; // bit c set: channel c (A=0, E=1, T=2) enters the likelihood
   const OracleDet* dets;
+  int32_t approximant;  // 0: IMRPhenomD (2,2); 1: IMRPhenomHM (six modes)
+  int32_t pad;
 };
 
 template <class T>
@@ -674,31 +993,82 @@ double sample_cut_hz(const PhenomD<T>& p, double cut_factor, double fmax) {
   return fc;
 }
 
+// The plan's waveform: IMRPhenomD, or IMRPhenomHM with its six modes.
+template <class T>
+struct OracleWave {
+  int approx;
+  PhenomHM<T> hm;  // hm.d is the PhenomD of either approximant
+};
+
+template <class T>
+void wave_setup(int approx, const T* th, double f_ref, OracleWave<T>& w) {
+  w.approx = approx;
+  if (approx == 1)
+    phenomhm_setup(th, f_ref, w.hm);
+  else
+    phenomd_setup(th, f_ref, w.hm.d);
+}
+
+template <class T>
+double wave_cut_hz(const OracleWave<T>& w, double cut_factor, double fmax) {
+  double fc = fmax;
+  const double frd = val(w.approx == 1 ? w.hm.fRD_max : w.hm.d.fRD);
+  if (cut_factor > 0.0) fc = std::min(fmax, cut_factor * frd / val(w.hm.d.M_sec));
+  return fc;
+}
+
+// The waveform container's modes at f: hp, hc, tf per mode; returns the
+// number of modes (zero containers for modes that are cut) and sets *live.
+template <class T>
+int wave_eval(const OracleWave<T>& w, double f, double fcut, Cx<T>* hp, Cx<T>* hc, T* tf, bool* live) {
+  if (w.approx != 1) {
+    *live = phenomd_eval(w.hm.d, f, fcut, hp[0], hc[0], tf[0]);
+    return 1;
+  }
+  *live = false;
+  for (int k = 0; k < HM_MODES; ++k) {
+    T amp, psi;
+    if (phenomhm_mode(w.hm, k, f, fcut, amp, psi, tf[k])) {
+      *live = true;
+      const T c = cos(psi), sn = sin(psi);
+      const PhenomHMMode<T>& md = w.hm.md[k];
+      // h_lm = amp e^{-i psi}; hp = P h_lm, hc = i C h_lm
+      hp[k] = Cx<T>{md.P * amp * c, -(md.P * amp * sn)};
+      hc[k] = Cx<T>{md.C * amp * sn, md.C * amp * c};
+    } else {
+      hp[k] = Cx<T>{T(0.0), T(0.0)};
+      hc[k] = Cx<T>{T(0.0), T(0.0)};
+    }
+  }
+  return HM_MODES;
+}
+
 template <class T>
 T lnl_one(const OraclePlan& pl, const T* th) {
-  PhenomD<T> wf;
-  phenomd_setup(th, pl.f_ref, wf);
+  OracleWave<T> wv;
+  wave_setup(pl.approximant, th, pl.f_ref, wv);
   T sb = th[7];
   T cb = sqrt((1.0 - sb) * (1.0 + sb));
   T P[3][3], X[3][3], k[3];
   polarization(th[6], sb, cb, th[8], P, X, k);
   double fmax = double(pl.k0 + pl.nbins - 1) * pl.f_step + 1.0;
-  double fcut = sample_cut_hz(wf, pl.cut_factor, fmax);
+  double fcut = wave_cut_hz(wv, pl.cut_factor, fmax);
   // Neumaier-compensated sums in FP64
   T acc = T(0.0);
   double comp = 0.0;
   for (int64_t i = 0; i < pl.nbins; ++i) {
     double f = double(pl.k0 + i) * pl.f_step;
-    Cx<T> hp, hc;
-    T tf;
-    bool live = phenomd_eval(wf, f, fcut, hp, hc, tf);
+    Cx<T> hp[HM_MODES], hc[HM_MODES];
+    T tf[HM_MODES];
+    bool live;
+    const int nm = wave_eval(wv, f, fcut, hp, hc, tf, &live);
     T bin = T(0.0);
     for (int d = 0; d < pl.n_det; ++d) {
       const OracleDet& det = pl.dets[d];
       Cx<T> h[3] = {{T(0.0), T(0.0)}, {T(0.0), T(0.0)}, {T(0.0), T(0.0)}};
       if (live) {
         Cx<T> L[6];
-        response_at_f(det.orbit, f, 1, &hp, &hc, &tf, th[10], P, X, k, L);
+        response_at_f(det.orbit, f, nm, hp, hc, tf, th[10], P, X, k, L);
         tdi_at_f(f, det.orbit.arm_sec, det.gen20, 1, L, h);
       }
       for (int c = 0; c < 3; ++c) {
@@ -729,24 +1099,26 @@ void fisher_one(const OraclePlan& pl, const double* t, double* F) {
     th[j] = D11(t[j]);
     th[j].d[j] = 1.0;
   }
-  PhenomD<D11> wf;
-  phenomd_setup(th, pl.f_ref, wf);
+  OracleWave<D11> wv;
+  wave_setup(pl.approximant, th, pl.f_ref, wv);
   D11 sb = th[7];
   D11 cb = sqrt((1.0 - sb) * (1.0 + sb));
   D11 P[3][3], X[3][3], k[3];
   polarization(th[6], sb, cb, th[8], P, X, k);
   double fmax = double(pl.k0 + pl.nbins - 1) * pl.f_step + 1.0;
-  double fcut = sample_cut_hz(wf, pl.cut_factor, fmax);
+  double fcut = wave_cut_hz(wv, pl.cut_factor, fmax);
   double acc[11][11] = {};
   for (int64_t i = 0; i < pl.nbins; ++i) {
     double f = double(pl.k0 + i) * pl.f_step;
-    Cx<D11> hp, hc;
-    D11 tf;
-    if (!phenomd_eval(wf, f, fcut, hp, hc, tf)) continue;
+    Cx<D11> hp[HM_MODES], hc[HM_MODES];
+    D11 tf[HM_MODES];
+    bool live;
+    const int nm = wave_eval(wv, f, fcut, hp, hc, tf, &live);
+    if (!live) continue;
     for (int d = 0; d < pl.n_det; ++d) {
       const OracleDet& det = pl.dets[d];
       Cx<D11> L[6], h[3];
-      response_at_f(det.orbit, f, 1, &hp, &hc, &tf, th[10], P, X, k, L);
+      response_at_f(det.orbit, f, nm, hp, hc, tf, th[10], P, X, k, L);
       tdi_at_f(f, det.orbit.arm_sec, det.gen20, 1, L, h);
       for (int c = 0; c < 3; ++c) {
         if (!((pl.chan_mask >> c) & 1)) continue;
@@ -860,23 +1232,59 @@ int oracle_phenomd(const double* th, const double* f, int64_t n, double f_ref, d
   return 0;
 }
 
+// IMRPhenomHM container on arbitrary frequencies: mode-major (6, n) hp, hc
+// (complex interleaved) and tf, modes (2,2), (2,1), (3,3), (3,2), (4,4), (4,3);
+// amp_psi (optional): (6, n, 2) amplitude and phase (h_lm = A exp(-i Psi));
+// info (optional, 6 x 4): per mode fRD_lm, Rholm, the amplitude and phase map corners' Mf.
+int oracle_phenomhm(const double* th, const double* f, int64_t n, double f_ref, double f_cut_hz, double* hp,
+                    double* hc, double* tf, double* amp_psi, double* info) {
+  PhenomHM<double> h;
+  phenomhm_setup<double>(th, f_ref, h);
+  for (int k = 0; k < HM_MODES; ++k) {
+    for (int64_t i = 0; i < n; ++i) {
+      double amp = 0.0, psi = 0.0, t = 0.0;
+      const size_t o = (size_t)k * n + i;
+      if (phenomhm_mode<double>(h, k, f[i], f_cut_hz, amp, psi, t)) {
+        const double c = std::cos(psi), sn = std::sin(psi);
+        hp[2 * o] = h.md[k].P * amp * c;
+        hp[2 * o + 1] = -(h.md[k].P * amp * sn);
+        hc[2 * o] = h.md[k].C * amp * sn;
+        hc[2 * o + 1] = h.md[k].C * amp * c;
+      } else {
+        hp[2 * o] = hp[2 * o + 1] = hc[2 * o] = hc[2 * o + 1] = 0.0;
+      }
+      tf[o] = t;
+      if (amp_psi) { amp_psi[2 * o] = amp; amp_psi[2 * o + 1] = psi; }
+    }
+    if (info) {
+      info[4 * k] = h.md[k].fRD;
+      info[4 * k + 1] = h.md[k].Rholm;
+      info[4 * k + 2] = h.md[k].fiA;
+      info[4 * k + 3] = h.md[k].frP;
+    }
+  }
+  return 0;
+}
+
 // Dense A/E/T (or X/Y/Z) model of one detector for one parameter set.
 int oracle_model_tdi(const OraclePlan* pl, int det, int orth, const double* th, double* out) {
-  PhenomD<double> wf;
-  phenomd_setup<double>(th, pl->f_ref, wf);
+  OracleWave<double> wv;
+  wave_setup<double>(pl->approximant, th, pl->f_ref, wv);
   double sb = th[7], cb = std::sqrt((1.0 - sb) * (1.0 + sb));
   double P[3][3], X[3][3], k[3];
   polarization<double>(th[6], sb, cb, th[8], P, X, k);
   double fmax = double(pl->k0 + pl->nbins - 1) * pl->f_step + 1.0;
-  double fcut = sample_cut_hz(wf, pl->cut_factor, fmax);
+  double fcut = wave_cut_hz(wv, pl->cut_factor, fmax);
   const OracleDet& d = pl->dets[det];
   for (int64_t i = 0; i < pl->nbins; ++i) {
     double f = double(pl->k0 + i) * pl->f_step;
-    Cx<double> hp, hc, h[3] = {{0, 0}, {0, 0}, {0, 0}};
-    double tf;
-    if (phenomd_eval(wf, f, fcut, hp, hc, tf)) {
+    Cx<double> hp[HM_MODES], hc[HM_MODES], h[3] = {{0, 0}, {0, 0}, {0, 0}};
+    double tf[HM_MODES];
+    bool live;
+    const int nm = wave_eval(wv, f, fcut, hp, hc, tf, &live);
+    if (live) {
       Cx<double> L[6];
-      response_at_f<double>(d.orbit, f, 1, &hp, &hc, &tf, th[10], P, X, k, L);
+      response_at_f<double>(d.orbit, f, nm, hp, hc, tf, th[10], P, X, k, L);
       tdi_at_f<double>(f, d.orbit.arm_sec, d.gen20, orth, L, h);
     }
     for (int c = 0; c < 3; ++c) { out[2 * (c * pl->nbins + i)] = h[c].re; out[2 * (c * pl->nbins + i) + 1] = h[c].im; }

@@ -18,6 +18,8 @@ PES_OPT_DENSE_STAGE = 1
 PES_OPT_SAMPLE_THREADS = 2
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+APPROX_PHENOMD = 0
+APPROX_PHENOMHM = 1
 MAX_DETECTORS = 4
 
 
@@ -65,7 +67,7 @@ class PesPlanDesc(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("n_sparse", ctypes.c_int32),
         ("max_batch", ctypes.c_int32),
-        ("pad", ctypes.c_int32),
+        ("approximant", ctypes.c_int32),
         ("det", PesDetectorDesc * MAX_DETECTORS),
     ]
 
@@ -87,6 +89,7 @@ SIGNATURES = {
     "pes_whittle_lnl": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i64, _d, _vp, _i64, _vp, _vp]),
     "pes_whittle_lnl_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i64, _d, _vp, _vp]),
     "pes_phenomd": (ctypes.c_int, [_vp, _vp, _i64, _d, _d, _vp, _vp, _vp, _vp]),
+    "pes_phenomhm": (ctypes.c_int, [_vp, _vp, _i64, _d, _d, _vp, _vp, _vp, _vp]),
     "pes_pn_tf": (ctypes.c_int, [_vp, _i64, _vp, _i64, _vp, _vp]),
     "pes_td_tdi_combination": (ctypes.c_int, [_vp, _i64, _i64, _i64, _d, _d, _i32, _i32, _vp, _vp]),
     "pes_td_tdi_layout": (ctypes.c_int, [_d, _d, _i32, _vp, _vp, _vp, _vp]),

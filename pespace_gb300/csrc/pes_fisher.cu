@@ -314,7 +314,8 @@ extern "C" int pes_fisher_batch(PesPlan* p, const double* theta, int64_t B, doub
     PES_CHECK_CUDA(cudaMalloc(&p->fisher_partial, sizeof(double) * M * kFisherBlocks * kPairs));
   }
   auto* blocks = reinterpret_cast<SampleBlock<FisherScalar>*>(p->fisher_blocks);
-  k_setup<FisherScalar><<<(unsigned)ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(p->dev, theta, B, 0, blocks);
+  k_setup<FisherScalar><<<(unsigned)ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(
+      p->dev, theta, B, 0, blocks, hm_blocks<FisherScalar>(p));
   PES_CHECK_LAUNCH();
   if (p->mixed)  // mixed plans: FP32 structured derivatives
     k_fisher_fast<<<dim3(kFisherBlocks, (unsigned)B), kFastThreads, 0, st>>>(p->dev, blocks, p->fisher_partial);

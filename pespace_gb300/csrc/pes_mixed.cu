@@ -116,7 +116,7 @@ struct MixedDev {
   float4* cg;
   float* mom;               // [B][n_det][J][7][4] adjoint moments (FP32 warp sums, FP32 atomics)
   float* ybar;              // [B][n_det][J][7] node adjoints (FP32: the derivative passes run in FP32)
-  double* part;             // [B][nblk_dense] lnL partials
+  double* part;             // [B][nblk_dense][2] partials: sum |d - h|^2 w (direct form), sum -2 Re(d^* h) w
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
   double* gdir;             // [B][n_det] direct t_c term of the gradient
@@ -127,7 +127,34 @@ struct MixedDev {
   double* kinkC;            // [B][n_det][6] C_q
   float* kinkF;             // [B][n_det][16] Msec f_step, -, C_0..C_5 as float-float (hi x6, lo x6), -, -
   float* kinkM;             // [B][n_det][12] dense adjoint moments: sum A_q x^2, sum A_q x
+  // The split form of the dense sum, sum |d - h|^2 w = sum |d|^2 w - 2 Re sum d^* h w
+  // + sum |h|^2 w, for templates far from the data: |d|^2 w from FP64 suffix
+  // sums, |h|^2 w from the transfer splines' coefficients against the data's
+  // weight moments (the model's squared modulus is a polynomial in t on each
+  // interval), so that only the cross term carries per-bin FP32 rounding.
+  const double* wmom;       // [n_det][nbins][2][3][7] sums over the bins of k's interval before k of
+                            //   t^p W_c and of t^p V_c (W_c = w_c |P|^2 / scale^2, V_c = W_c |d_c|^2 w_c,
+                            //   t = f - f_j)
+  const double* wtot;       // [n_det][J][2][3][7] the same over each whole interval
+  const double* dsuf;       // [n_det][nbins + 1] sum_{i >= k} sum_c |d_c|^2 w_c (FP64)
+  double* wrow;             // [nbins] set-up scratch: one detector's sum_c |d_c|^2 w_c per bin
+  float* cgb;               // [B][n_det][J][6] tails b - b_hi of the transfer splines' slope coefficients
+  double* hd;               // [B][n_det][kHdOut] per detector's dense range: sum |h|^2 w, sum |d|^2 w,
+                            //   sum |d|^2 |h|^2 w^2, and the splines' error estimate of sum |h|^2 w
+                            //   from the exact model at the interval midpoints (signed, absolute)
+  // Samples whose FP32 or spline error could exceed the accuracy target are
+  // re-evaluated exactly over their dense range: the error estimates above
+  // use the exact transfer quantities at the interval midpoints.
+  const float2* mid_ff;     // [J] interval midpoints (hi, lo)
+  const float4* tdm_ff;     // [n_det][J] TDI delay factor at the midpoints
+  FF* ym;                   // [B][n_det][6][J] transfer quantities at the midpoints (kink removed)
+  int32_t rblocks;          // blocks per sample of the exact re-evaluation
+  int32_t rpad;
+  double* rpart;            // [B][rblocks] exact dense-range partials of re-evaluated samples
 };
+constexpr int kHdOut = 6;
+constexpr int kMomStride = 42;  // doubles per bin (and interval) of wmom / wtot
+constexpr int kRefineBlocks = 32;  // blocks per sample of the exact re-evaluation
 
 // Error-free transformation: s + e == a + b exactly (Knuth's two-sum).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -155,7 +182,7 @@ struct MixedBuffers {
   // the gradient pass of the dense stage stages its run inputs through shared
   // memory when they exceed half of L2 (they then stream from DRAM)
   bool stage_grad = false;
-  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr;
+  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr, ev_hd = nullptr, ev_pfit = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -320,6 +347,9 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
 }
 
 // Forward: node values in float-float arithmetic.  grid (ceil(J/128), n_det, B)
+// kMid: the six transfer quantities at the midpoints of intervals 0..nsp-1
+// instead (the exact model that the splines' error estimates compare with).
+template <bool kMid>
 __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedDev M, GenArg G,
                                                                const SampleBlock<double>* __restrict__ blocks) {
   __shared__ SampleBlock<double> sb;
@@ -331,11 +361,11 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int ns = M.nsp[s];
-  if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J) return;
+  if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J || (kMid && j >= ns)) return;
   FF y[kNodeQ];
   {
-    const float2 fn = M.node_ff[j];
-    const float4 t4 = M.tdn_ff[(size_t)d * M.J + j];
+    const float2 fn = kMid ? M.mid_ff[j] : M.node_ff[j];
+    const float4 t4 = kMid ? M.tdm_ff[(size_t)d * M.J + j] : M.tdn_ff[(size_t)d * M.J + j];
     const Cx<FF> D = cx(ff_make(t4.x, t4.y), ff_make(t4.z, t4.w));
     node_eval_g<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, D, D, ff_make(fn.x, fn.y), y);
     const FF xk = sbf.wf.Msec * ff_make(fn.x, fn.y) - sbf.wf.fpeak;
@@ -345,6 +375,12 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
 #pragma unroll
       for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - ff_from(C[q]) * x2;
     }
+  }
+  if (kMid) {
+    FF* out = M.ym + ((size_t)s * M.n_det + d) * 6 * M.J + j;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) out[(size_t)q * M.J] = y[1 + q];
+    return;
   }
   FF* out = M.yv + ((size_t)s * M.n_det + d) * kNodeQ * M.J + j;
 #pragma unroll
@@ -804,12 +840,16 @@ __device__ __forceinline__ void spline_fit_transfer(const MixedDev& M, int64_t s
   for (int i = i0; i < i1; ++i) {
     const float mj = (i + 1 == n) ? mn : S[(i + 1) * kNodeQ].x;
     const float sl = S[i * kNodeQ].y;
-    const float bc = sl - fh[i] * (2.0f * mi + mj) * (1.0f / 6.0f);
+    (void)sl;
+    // b = slope - h (2 m_i + m_j) / 6 with the FP64 slope: stored as FP32 head and tail
+    const double bd = (y(i + 1) - y(i)) * M.ginvh[i] - (double)(fh[i] * (2.0f * mi + mj) * (1.0f / 6.0f));
+    const float bc = (float)bd;
     const float cc = 0.5f * mi;
     const float dc = (mj - mi) * fih[i] * (1.0f / 6.0f);
     const FF a = yq[i];
     M.cg[((size_t)sd * M.J + i) * 8 + (q - 1)] = make_float4(a.hi, bc, cc, dc);
     reinterpret_cast<float*>(M.cg + ((size_t)sd * M.J + i) * 8 + 6)[q - 1] = a.lo;
+    M.cgb[((size_t)sd * M.J + i) * 6 + (q - 1)] = (float)(bd - (double)bc);
     mi = mj;
   }
 }
@@ -1249,19 +1289,22 @@ __device__ __forceinline__ void spline_fit_staged(const MixedDev& M, int64_t sd,
       else if (k + 1 < cnt) mj = x[(k + 1) < kSeg ? k + 1 : k];
       else mj = next_first;
       const FF yn = y[fit_pad(i + 1)];
-      const R sl = ff_to_r<R>((yn - yc) * t_gih[tp(i)]);
-      const R bc = sl - t_h[tp(i)] * (two * mi + mj) * sixth;
+      const FF slf = (yn - yc) * t_gih[tp(i)];
+      const R corr = t_h[tp(i)] * (two * mi + mj) * sixth;
       const R cc = half * mi;
       const R dc = (mj - mi) * t_ih[tp(i)] * sixth;
       if constexpr (std::is_same<R, FF>::value) {
         FF* o = M.cphi + ((size_t)sd * M.J + i) * 4;
         o[0] = yc;
-        o[1] = bc;
+        o[1] = slf - corr;
         o[2] = cc;
         o[3] = dc;
       } else {
-        M.cg[((size_t)sd * M.J + i) * 8 + (q - 1)] = make_float4(yc.hi, bc, cc, dc);
+        // b = slope - h (2 m_i + m_j) / 6 from the float-float slope: FP32 head and tail
+        const FF bf = ff_addf(slf, -corr);
+        M.cg[((size_t)sd * M.J + i) * 8 + (q - 1)] = make_float4(yc.hi, bf.hi, cc, dc);
         reinterpret_cast<float*>(M.cg + ((size_t)sd * M.J + i) * 8 + 6)[q - 1] = yc.lo;
+        M.cgb[((size_t)sd * M.J + i) * 6 + (q - 1)] = bf.lo;
       }
       yc = yn;
     }
@@ -1525,16 +1568,46 @@ __global__ void __launch_bounds__(kFitWarps * 32) k_spline_adjoint_staged(MixedD
 }
 
 // ------------------------------------------------------------------ exact bins
+// Accuracy target of a mixed lnL (|dlnL| against the FP64 evaluation) and the
+// error model that decides which samples are re-evaluated exactly over their
+// dense range: the FP32 rounding of the model in the cross term,
+// kCrossRel sqrt(sum |d|^2 |h|^2 w^2) (a few ulps of the phase and modulus
+// per bin, independent between bins), plus the splines' interpolation error
+// of sum |h|^2 w estimated from the exact model at the interval midpoints
+// (kSplineSafety times its estimate, for the part of the error that the
+// midpoint bump does not capture).  Both in units of lnL (times 2 df).
+// The midpoint estimate corrects sum |h|^2 w (it predicts the splines' error
+// there to a few per cent); what remains is modelled as kSplineRel times the
+// sum of the intervals' absolute estimates (the splines' phase error enters
+// the cross term where the model is steep).
+constexpr double kRefineTarget = 2e-3;
+constexpr double kCrossRel = 4e-7;
+constexpr double kSplineRel = 0.02;
+
+__device__ __forceinline__ bool refine_sample(const PlanDev& P, const MixedDev& M, int64_t s) {
+  double sv = 0.0, eha = 0.0;
+  for (int d = 0; d < M.n_det; ++d) {
+    const double* h = M.hd + ((size_t)s * M.n_det + d) * kHdOut;
+    sv += h[2];
+    eha += h[4];
+  }
+  const double e = 2.0 * P.df * (kCrossRel * sqrt(fmax(sv, 0.0)) + kSplineRel * eha);
+  return e > kRefineTarget;
+}
+
 // Bins [0, xbind[s][d]) of each detector evaluated directly (FP64 model and residual against the
 // FP64 data).  kMode 0: lnL partials (T = double); 1: gradient partials
-// (T = GradScalar, FP64 values with FP32 tangents); 2: write the model.
-// grid (xblocks, B); threads stride over the sample's exact bins.
+// (T = GradScalar, FP64 values with FP32 tangents); 2: write the model;
+// 3: lnL partials of bins [xbind[s][d], kcut) of the samples that
+// refine_sample selects (the exact re-evaluation of their dense range).
+// grid (xblocks or rblocks, B); threads stride over the sample's exact bins.
 template <int kMode, class T>
 __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, GenArg G,
                                                          const SampleBlock<T>* __restrict__ blocks,
                                                          double2* __restrict__ model) {
   constexpr int NV = kMode == 1 ? 11 : 1;
   constexpr bool kFF = kMode != 1;  // value passes: float-float values
+  constexpr bool kRefine = kMode == 3;
   // value passes: a float-float copy of the block; gradient pass: the split
   // float-float block (mass/spin and response tangents)
   using SBF = std::conditional_t<kMode == 1, ExactGradBlock, SampleBlock<FF>>;
@@ -1543,7 +1616,8 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   __shared__ double red[kExactThreads / 32][NV];
   const int s = blockIdx.y;
   const int xb = M.xbin[s];
-  if (xb == 0) return;  // uniform per block; the finalizers skip such samples
+  if (!kRefine && xb == 0) return;  // uniform per block; the finalizers skip such samples
+  if (kRefine && (blocks[s].status != kSampleOk || !refine_sample(P, M, s))) return;
   load_block(blocks, s, sb);
   __syncthreads();
   if constexpr (kFF) {
@@ -1559,7 +1633,8 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   if (sb.status == kSampleOk) {
     for (int d = 0; d < M.n_det; ++d) {
       const int xbd = M.xbind[(size_t)s * M.n_det + d];
-      for (int i = blockIdx.x * kExactThreads + threadIdx.x; i < xbd; i += gridDim.x * kExactThreads) {
+      const int i0 = kRefine ? xbd : 0, i1 = kRefine ? (int)sb.kcut : xbd;
+      for (int i = i0 + blockIdx.x * kExactThreads + threadIdx.x; i < i1; i += gridDim.x * kExactThreads) {
         if constexpr (kFF) {
           const FF f = ff_mulf(M.fstep_ff, (float)(P.k0 + i));  // k0 + i < 2^24: exact in FP32
           const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
@@ -1671,6 +1746,8 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
     for (int w = 0; w < kExactThreads / 32; ++w) x += red[w][threadIdx.x];
     if (kMode == 0)
       M.xpart[(size_t)s * gridDim.x + blockIdx.x] = x;
+    else if (kMode == 3)
+      M.rpart[(size_t)s * gridDim.x + blockIdx.x] = x;
     else
       M.xgpart[((size_t)s * gridDim.x + blockIdx.x) * 11 + threadIdx.x] = x;
   }
@@ -1692,6 +1769,20 @@ __device__ __forceinline__ float reduce_exact(float x) {
   r = fmaf(-k, kTwoPiMid, r);
   r = fmaf(-k, kTwoPiLo, r);
   return r;
+}
+
+// The same reduction with its rounding kept: x - 2 pi k = r + *e to about
+// 2^-46 of |r| (the first subtraction is exact; the errors of the two
+// rounded ones are recovered with FMAs, r0 - r1 being exact).
+__device__ __forceinline__ float reduce_exact_ff(float x, float* e) {
+  const float k = fmaf(x, kInvTwoPi, kRoundMagic) - kRoundMagic;
+  const float r0 = fmaf(-k, kTwoPiHi, x);
+  const float r1 = fmaf(-k, kTwoPiMid, r0);
+  const float e1 = fmaf(-k, kTwoPiMid, r0 - r1);
+  const float r2 = fmaf(-k, kTwoPiLo, r1);
+  const float e2 = fmaf(-k, kTwoPiLo, r1 - r2);
+  *e = e1 + e2;
+  return r2;
 }
 
 // sin and cos of |x| < 2^21 in FP32 FMA arithmetic only: x = k pi/2 + r with
@@ -1857,7 +1948,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
                                                              const SampleBlock<double>* __restrict__ blocks,
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
-  __shared__ double red[kMixThreads / 32];
+  __shared__ double red[kMixThreads / 32][2];
   // per warp, two run buffers: the next run's inputs are copied while this one is computed
   __shared__ __align__(16) float4 rbuf[kStage ? kMixThreads / 32 : 1][kStage ? 2 : 1][kStage ? kRunBuf : 1];
   __shared__ float msm[kGrad ? kMixThreads / 32 : 1][kGrad ? kNodeQ * kMoments : 1][kGrad ? kMomPad : 1];
@@ -1869,6 +1960,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   const int first = g * kChunkMax;
   float acc = 0.0f, comp = 0.0f;
   float dsh = 0.0f, dsl = 0.0f;  // float-float sum of the FP64 |d|^2/S of the weak-template bins
+  float xacc = 0.0f, xcomp = 0.0f;  // compensated sum of the cross term -2 Re(d^* h) w
   if (blocks[s].status == kSampleOk && first < nc) {
     for (int d = 0; d < M.n_det; ++d) {
       const size_t sd = (size_t)s * M.n_det + d;
@@ -1961,11 +2053,29 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float t = pk2.w;
           const float u = (float)lane;
           const float u2 = u * u, u3 = u2 * u;
-          // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike
-          const float del = reduce_exact(r.p1h * u) + reduce_exact(r.p2h * u2) + reduce_exact(r.p3h * u3) +
-                            fmaf(r.p1l, u, fmaf(r.p2l, u2, r.p3l * u3));
+          // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike.
+          // The phase advance is summed error-free (reductions and sums keep their
+          // roundings), its sine and cosine taken of the head and corrected to
+          // first order in the tail.
+          float del, dlo;
+          {
+            float ea, eb, ec;
+            const float a = reduce_exact_ff(r.p1h * u, &ea), b = reduce_exact_ff(r.p2h * u2, &eb),
+                        c = reduce_exact_ff(r.p3h * u3, &ec);
+            float s1, t1, s2, t2, s3, t3;
+            two_sum(a, b, s1, t1);
+            two_sum(s1, c, s2, t2);
+            two_sum(s2, fmaf(r.p1l, u, fmaf(r.p2l, u2, r.p3l * u3)), s3, t3);
+            del = s3;
+            dlo = ((ea + eb) + ec) + ((t1 + t2) + t3);
+          }
           float sd_, cd_;
           sincos_poly(del, &sd_, &cd_);
+          {
+            const float sdc = fmaf(dlo, cd_, sd_);
+            cd_ = fmaf(-dlo, sd_, cd_);
+            sd_ = sdc;
+          }
           float cph = fmaf(r.c0, cd_, -(r.s0 * sd_));
           float sph = fmaf(r.s0, cd_, r.c0 * sd_);
           // Renormalise the rotated phasor with one Newton step for 1/|e|
@@ -2002,6 +2112,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           float term = 0.0f;  // |d - h|^2 w
           float cross = 0.0f;  // (|h|^2 - 2 Re(d^* h)) w
           float hh = 0.0f;     // |h|^2 w
+          float xdh = 0.0f;    // Re(d^* h) w
           float aphi = 0.0f;
           float ag[6];
 #pragma unroll
@@ -2019,7 +2130,9 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             term = fmaf(fmaf(er, er, ei * ei), w, term);
             const float h2 = fmaf(hr, hr, hi * hi);
             hh = fmaf(h2, w, hh);
-            cross = fmaf(fmaf(-2.0f, fmaf(dv.x, hr, dv.y * hi), h2), w, cross);
+            const float dh = fmaf(dv.x, hr, dv.y * hi);
+            cross = fmaf(fmaf(-2.0f, dh, h2), w, cross);
+            xdh = fmaf(dh, w, xdh);
             if (kMode == 2) model[off] = make_double2((double)hr / M.scale, (double)hi / M.scale);
             if (kGrad) {
               ag[2 * ch] = w * (er * cph - ei * sph);
@@ -2044,6 +2157,12 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float tk = acc + yk;
           comp = (tk - acc) - yk;
           acc = tk;
+          {
+            const float yx = -2.0f * xdh - xcomp;
+            const float tx = xacc + yx;
+            xcomp = (tx - xacc) - yx;
+            xacc = tx;
+          }
           if (kGrad && xk > 0.0f) {
             kinked = true;
 #pragma unroll
@@ -2076,9 +2195,11 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
       }
     }
   }
-  // deterministic reduction: lanes (float-float) -> warps (FP64) -> block partial
-  float vh, vl;
+  // deterministic reduction: lanes (float-float) -> warps (FP64) -> block partial,
+  // for the direct sum and the cross-term sum
+  float vh, vl, xh, xl;
   two_sum(acc, -comp, vh, vl);
+  two_sum(xacc, -xcomp, xh, xl);
   {
     float th, tl;
     two_sum(vh, dsh, th, tl);
@@ -2089,18 +2210,187 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   for (int o = 16; o > 0; o >>= 1) {
     const float oh = __shfl_down_sync(0xffffffffu, vh, o);
     const float ol = __shfl_down_sync(0xffffffffu, vl, o);
+    const float ph = __shfl_down_sync(0xffffffffu, xh, o);
+    const float pl = __shfl_down_sync(0xffffffffu, xl, o);
     float th, tl;
     two_sum(vh, oh, th, tl);
     vh = th;
     vl += tl + ol;
+    two_sum(xh, ph, th, tl);
+    xh = th;
+    xl += tl + pl;
   }
-  if (lane == 0) red[wid] = (double)vh + (double)vl;
+  if (lane == 0) {
+    red[wid][0] = (double)vh + (double)vl;
+    red[wid][1] = (double)xh + (double)xl;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 2) {
     double x = 0.0;
 #pragma unroll
-    for (int w = 0; w < kMixThreads / 32; ++w) x += red[w];
-    M.part[(size_t)s * M.nblk_dense + blockIdx.x] = x;
+    for (int w = 0; w < kMixThreads / 32; ++w) x += red[w][threadIdx.x];
+    M.part[((size_t)s * M.nblk_dense + blockIdx.x) * 2 + threadIdx.x] = x;
+  }
+}
+
+// sum |h|^2 w and sum |d|^2 w over the dense range [xbind, kcut) of each
+// (sample, detector), one warp each.  On interval j the model's channel c is
+// h_c = G_c(t) P(f) e^{-i phase} with G_c = a + b t + c t^2 + d t^3 (the
+// transfer splines, re and im), plus C (X0 + Msec t)^2 past the amplitude
+// peak (X0 = Msec f_j - Mf_peak), so |h_c|^2 w_c = |G_c(t)|^2 W_c and its sum
+// over the interval's bins is sum_p g_p sum_k t_k^p W_c with g the
+// coefficients of |G_c|^2: FP64 throughout, no per-bin rounding of the model.
+constexpr int kHdThreads = 128;  // one block per (sample, detector), threads over its intervals
+__device__ __forceinline__ double hd_piece(const double (&A)[6], const double (&Bc)[6], const double (&Cc)[6],
+                                           const double (&Dc)[6], const double* Sm) {
+  double acc = 0.0;
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    const int r = 2 * ch, i = 2 * ch + 1;
+    const double g0 = A[r] * A[r] + A[i] * A[i];
+    const double g1 = 2.0 * (A[r] * Bc[r] + A[i] * Bc[i]);
+    const double g2 = Bc[r] * Bc[r] + Bc[i] * Bc[i] + 2.0 * (A[r] * Cc[r] + A[i] * Cc[i]);
+    const double g3 = 2.0 * (A[r] * Dc[r] + A[i] * Dc[i] + Bc[r] * Cc[r] + Bc[i] * Cc[i]);
+    const double g4 = Cc[r] * Cc[r] + Cc[i] * Cc[i] + 2.0 * (Bc[r] * Dc[r] + Bc[i] * Dc[i]);
+    const double g5 = 2.0 * (Cc[r] * Dc[r] + Cc[i] * Dc[i]);
+    const double g6 = Dc[r] * Dc[r] + Dc[i] * Dc[i];
+    const double* m = Sm + ch * 7;
+    acc += g0 * m[0] + g1 * m[1] + g2 * m[2] + g3 * m[3] + g4 * m[4] + g5 * m[5] + g6 * m[6];
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
+                                                  const SampleBlock<double>* __restrict__ blocks, int64_t B) {
+  __shared__ double red[kHdThreads / 32][4];
+  const int lane = threadIdx.x;
+  const int64_t sd = blockIdx.x;
+  if (sd >= B * M.n_det) return;
+  const int64_t s = sd / M.n_det;
+  const int d = (int)(sd % M.n_det);
+  const SampleBlock<double>& b = blocks[s];
+  double* out = M.hd + sd * kHdOut;
+  const int64_t kcut = b.kcut;
+  const int64_t lo = M.xbind[sd];
+  if (b.status != kSampleOk || M.nsp[s] < 3 || lo >= kcut) {
+    if (lane < kHdOut) out[lane] = 0.0;
+    return;  // uniform per block
+  }
+  const double Msec = b.wf.Msec, fpk = b.wf.fpeak;
+  // first bin with x = Msec f - Mf_peak > 0
+  int64_t kpk = (int64_t)floor(fpk / (Msec * P.f_step)) - P.k0;
+  for (int it = 0; it < 2 && kpk > 0 && Msec * ((double)(P.k0 + kpk - 1) * P.f_step) > fpk; ++it) --kpk;
+  for (int it = 0; it < 2 && Msec * ((double)(P.k0 + kpk) * P.f_step) <= fpk; ++it) ++kpk;
+  // intervals holding bins lo and kcut - 1
+  auto iv_of = [&](int64_t k) {
+    int a = 0, z = M.J - 2;
+    while (a < z) {
+      const int mid = (a + z + 1) >> 1;
+      if (M.iv_first[mid] <= k) a = mid; else z = mid - 1;
+    }
+    return a;
+  };
+  const int jlo = iv_of(lo), jhi = iv_of(kcut - 1);
+  const double* KC = M.kinkC + sd * 6;
+  const double* wm = M.wmom + (size_t)d * P.nbins * kMomStride;
+  const FF* ym = M.ym + (size_t)sd * 6 * M.J;
+  double sum = 0.0, sumv = 0.0, eh = 0.0, eha = 0.0;
+  for (int j = jlo + lane; j <= jhi; j += kHdThreads) {
+    const int64_t e1 = M.iv_first[j], e2 = M.iv_first[j + 1];
+    const int64_t k1 = max(e1, lo), k2 = min(e2, kcut);
+    if (k1 >= k2) continue;
+    const double* tot = M.wtot + ((size_t)d * M.J + j) * kMomStride;
+    auto F = [&](int64_t k, int idx) { return k >= e2 ? tot[idx] : wm[(size_t)k * kMomStride + idx]; };
+    double A[6], Bc[6], Cc[6], Dc[6];
+    const float4* cg = M.cg + ((size_t)sd * M.J + j) * 8;
+    const float* alo = reinterpret_cast<const float*>(cg + 6);
+    const float* blo = M.cgb + ((size_t)sd * M.J + j) * 6;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const float4 c4 = cg[q];
+      A[q] = (double)c4.x + (double)alo[q];
+      Bc[q] = (double)c4.y + (double)blo[q];
+      Cc[q] = (double)c4.z;
+      Dc[q] = (double)c4.w;
+    }
+    // the splines' error at the midpoint (kink-free values on both sides)
+    const double h = M.gh[j], tm = 0.5 * h;
+    double delta[6], gm[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const double sp = A[q] + tm * (Bc[q] + tm * (Cc[q] + tm * Dc[q]));
+      const double ex = ff_to(ym[(size_t)q * M.J + j]);
+      delta[q] = ex - sp;
+      gm[q] = ex;
+    }
+    const double Xm = Msec * (M.node_f[j] + tm) - fpk;
+    if (Xm > 0.0) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) gm[q] += KC[q] * Xm * Xm;
+    }
+    double Sm[42];
+    const int64_t ks = min(max(kpk, k1), k2);  // [k1, ks) before the peak, [ks, k2) past it
+    if (ks > k1) {
+#pragma unroll
+      for (int x = 0; x < 42; ++x) Sm[x] = F(ks, x) - F(k1, x);
+      sum += hd_piece(A, Bc, Cc, Dc, Sm);
+      sumv += hd_piece(A, Bc, Cc, Dc, Sm + 21);
+    }
+    if (ks < k2) {
+      const double X0 = Msec * M.node_f[j] - fpk;
+      double A2[6], B2[6], C2[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        A2[q] = A[q] + KC[q] * X0 * X0;
+        B2[q] = Bc[q] + 2.0 * KC[q] * X0 * Msec;
+        C2[q] = Cc[q] + KC[q] * Msec * Msec;
+      }
+#pragma unroll
+      for (int x = 0; x < 42; ++x) Sm[x] = F(k2, x) - F(ks, x);
+      sum += hd_piece(A2, B2, C2, Dc, Sm);
+      sumv += hd_piece(A2, B2, C2, Dc, Sm + 21);
+    }
+    // first-order change of sum |h|^2 w over the interval if the splines' error
+    // had the shape 16 t^2 (h - t)^2 / h^4 times its midpoint value
+    {
+      const double ih2 = 1.0 / (h * h);
+      double e = 0.0;
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const double m2 = F(k2, ch * 7 + 2) - F(k1, ch * 7 + 2), m3 = F(k2, ch * 7 + 3) - F(k1, ch * 7 + 3),
+                     m4 = F(k2, ch * 7 + 4) - F(k1, ch * 7 + 4);
+        const double bump = 16.0 * ih2 * (m2 - 2.0 * m3 / h + m4 * ih2);
+        e += 2.0 * (gm[2 * ch] * delta[2 * ch] + gm[2 * ch + 1] * delta[2 * ch + 1]) * bump;
+      }
+      eh += e;
+      eha += fabs(e);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    sumv += __shfl_xor_sync(0xffffffffu, sumv, o);
+    eh += __shfl_xor_sync(0xffffffffu, eh, o);
+    eha += __shfl_xor_sync(0xffffffffu, eha, o);
+  }
+  if ((lane & 31) == 0) {
+    red[lane >> 5][0] = sum;
+    red[lane >> 5][1] = sumv;
+    red[lane >> 5][2] = eh;
+    red[lane >> 5][3] = eha;
+  }
+  __syncthreads();
+  if (lane == 0) {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < kHdThreads / 32; ++w)
+      for (int q = 0; q < 4; ++q) t[q] += red[w][q];
+    const double* ds = M.dsuf + (size_t)d * (P.nbins + 1);
+    out[0] = t[0];
+    out[1] = ds[lo] - ds[kcut];
+    out[2] = t[1];
+    out[3] = t[2];
+    out[4] = t[3];
+    out[5] = 0.0;
   }
 }
 
@@ -2114,8 +2404,24 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
     if (status) status[s] = b.status;
     return;
   }
-  double acc = 0.0;
-  for (int k = 0; k < M.nblk_dense; ++k) acc += M.part[(size_t)s * M.nblk_dense + k];
+  // dense bins: the direct sum of |d - h|^2 w, or the split form for templates
+  // far from the data (residual above 2 sqrt(<h|h> <d|d>)), where the FP32
+  // rounding of the model enters only the cross term
+  double R = 0.0, X = 0.0, H = 0.0, Dd = 0.0;
+  for (int k = 0; k < M.nblk_dense; ++k) {
+    R += M.part[((size_t)s * M.nblk_dense + k) * 2];
+    X += M.part[((size_t)s * M.nblk_dense + k) * 2 + 1];
+  }
+  for (int d = 0; d < M.n_det; ++d) {
+    // sum |h|^2 w from the splines, corrected by the midpoint estimate of their error
+    H += M.hd[((size_t)s * M.n_det + d) * kHdOut] + M.hd[((size_t)s * M.n_det + d) * kHdOut + 3];
+    Dd += M.hd[((size_t)s * M.n_det + d) * kHdOut + 1];
+  }
+  double acc = (R > 2.0 * sqrt(H * Dd)) ? (Dd + X) + H : R;
+  if (refine_sample(P, M, s)) {  // the exact re-evaluation of the dense range
+    acc = 0.0;
+    for (int k = 0; k < M.rblocks; ++k) acc += M.rpart[(size_t)s * M.rblocks + k];
+  }
   if (M.xbin[s] > 0)
     for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
   const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
@@ -2162,11 +2468,49 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
   }
   const float hi = (float)dd;
   M.dd[(size_t)det * P.nbins + i] = make_float2(hi, (float)(dd - (double)hi));
+  M.wrow[i] = dd;
   const TdiFactor tf = P.tdi[(size_t)det * P.nbins + i];
   float4* pk = M.pk + (size_t)det * 3 * P.nbins;
   pk[i] = make_float4(dr[0], di[0], dr[1], di[1]);
   pk[P.nbins + i] = make_float4(dr[2], di[2], wf[0], wf[1]);
   pk[2 * P.nbins + i] = make_float4(wf[2], (float)tf.pre, (float)tf.pim, M.bin_t[i]);
+}
+
+// Within-interval weight moments of detector det (set-up): one thread per
+// (interval, channel) runs over the interval's bins in order, writing the
+// exclusive prefix sums of t^p W_c (p = 0..6) at every bin and the interval's
+// totals; W_c = w_c |P|^2 / scale^2 in FP64, t = f_k - f_j.
+__global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ wmom, double* __restrict__ wtot) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (M.J - 1) * 6) return;
+  const int j = t / 6, c = t % 3, v = (t % 6) / 3;  // v = 1: data-weighted moments
+  const int64_t k1 = M.iv_first[j], k2 = M.iv_first[j + 1];
+  const double fj = M.node_f[j];
+  const double is2 = 1.0 / (M.scale * M.scale);
+  double acc[7];
+#pragma unroll
+  for (int p = 0; p < 7; ++p) acc[p] = 0.0;
+  double* pm = wmom + (size_t)det * P.nbins * kMomStride + v * 21 + c * 7;
+  for (int64_t k = k1; k < k2; ++k) {
+    const double tk = (double)(P.k0 + k) * P.f_step - fj;
+    const TdiFactor tf = P.tdi[(size_t)det * P.nbins + k];
+    const size_t off = ((size_t)det * 3 + c) * P.nbins + k;
+    const double w = P.w[off];
+    double tp = w * (tf.pre * tf.pre + tf.pim * tf.pim) * is2;
+    if (v) {
+      const double2 dv = P.data[off];
+      tp *= (dv.x * dv.x + dv.y * dv.y) * w;
+    }
+#pragma unroll
+    for (int p = 0; p < 7; ++p) {
+      pm[(size_t)k * kMomStride + p] = acc[p];
+      acc[p] += tp;
+      tp *= tk;
+    }
+  }
+  double* tot = wtot + ((size_t)det * M.J + j) * kMomStride + v * 21 + c * 7;
+#pragma unroll
+  for (int p = 0; p < 7; ++p) tot[p] = acc[p];
 }
 
 // ------------------------------------------------------------------ host side
@@ -2209,6 +2553,7 @@ static void launch_spline_fit(const MixedDev& M, int64_t B, cudaStream_t st_phas
 
 int mixed_create(PesPlan* p) {
   const PesPlanDesc& d = p->desc;
+  PES_REQUIRE(d.approximant == PES_APPROX_PHENOMD, "mixed plan: only IMRPhenomD is supported by the mixed precision path");
   PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
   PES_REQUIRE(d.k0 >= 1, "mixed plan: the grid must start above 0 Hz (k0 >= 1)");
   PES_REQUIRE(d.k0 + d.nbins < (int64_t)1 << 24, "mixed plan: bin indices k0 + i must stay below 2^24");
@@ -2226,7 +2571,7 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->join, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->xready, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->aux, cudaStreamNonBlocking));
-  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_tadj})
+  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_tadj, &mb->ev_hd, &mb->ev_pfit})
     PES_CHECK_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
@@ -2315,6 +2660,11 @@ int mixed_create(PesPlan* p) {
   float2* node_ff;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
   double *xpart, *xgpart;
+  double *wmom, *wtot, *dsuf, *wrow, *hdv, *rpart;
+  float* cgb;
+  float2* mid_ff;
+  float4* tdm_ff;
+  FF* ymv;
   SampleBlock<GradScalar>* gblk;
   double *kR, *kC;
   float* kF;
@@ -2334,7 +2684,12 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &cfrac, (size_t)B)) || (rc = alloc(mb, &node_ff, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 8)) ||
       (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
-      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense)) ||
+      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense * 2)) ||
+      (rc = alloc(mb, &wmom, (size_t)nd * n * kMomStride)) || (rc = alloc(mb, &wtot, (size_t)nd * J * kMomStride)) ||
+      (rc = alloc(mb, &dsuf, (size_t)nd * (n + 1))) || (rc = alloc(mb, &wrow, (size_t)n)) ||
+      (rc = alloc(mb, &cgb, sd * J * 6)) || (rc = alloc(mb, &hdv, sd * kHdOut)) ||
+      (rc = alloc(mb, &mid_ff, J)) || (rc = alloc(mb, &tdm_ff, (size_t)nd * J)) || (rc = alloc(mb, &ymv, sd * 6 * J)) ||
+      (rc = alloc(mb, &rpart, (size_t)B * kRefineBlocks)) ||
       (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
       (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) || (rc = alloc(mb, &xbind, (size_t)B * nd)) ||
@@ -2460,6 +2815,38 @@ int mixed_create(PesPlan* p) {
   M.kinkC = kC;
   M.kinkF = kF;
   M.kinkM = kM;
+  M.wmom = wmom;
+  M.wtot = wtot;
+  M.dsuf = dsuf;
+  M.wrow = wrow;
+  M.cgb = cgb;
+  M.hd = hdv;
+  M.ym = ymv;
+  M.rpart = rpart;
+  M.rblocks = kRefineBlocks;
+  {
+    // interval midpoints and their TDI delay factors (the last node has no interval)
+    std::vector<float2> mff(J);
+    std::vector<float4> tmf((size_t)nd * J);
+    for (int jj = 0; jj < J; ++jj) {
+      const double fm = jj + 1 < J ? 0.5 * (nf[jj] + nf[jj + 1]) : nf[jj];
+      const FF v = ff_from(fm);
+      mff[jj] = make_float2(v.hi, v.lo);
+      for (int k = 0; k < nd; ++k) {
+        Cx<double> D, Pf;
+        tdi_factors(fm, d.det[k].orbit.arm_sec, d.det[k].generation == 20, D, Pf);
+        const FF re = ff_from(D.re), im = ff_from(D.im);
+        tmf[(size_t)k * J + jj] = make_float4(re.hi, re.lo, im.hi, im.lo);
+      }
+    }
+    PES_CHECK_CUDA(cudaMemcpy(mid_ff, mff.data(), sizeof(float2) * J, cudaMemcpyHostToDevice));
+    PES_CHECK_CUDA(cudaMemcpy(tdm_ff, tmf.data(), sizeof(float4) * tmf.size(), cudaMemcpyHostToDevice));
+  }
+  M.mid_ff = mid_ff;
+  M.tdm_ff = tdm_ff;
+  PES_CHECK_CUDA(cudaMemset(wmom, 0, sizeof(double) * nd * n * kMomStride));
+  PES_CHECK_CUDA(cudaMemset(wtot, 0, sizeof(double) * nd * J * kMomStride));
+  PES_CHECK_CUDA(cudaMemset(dsuf, 0, sizeof(double) * nd * (n + 1)));
   // the dense-path partial buffer is not needed; gradient set-up blocks are shared
   return PES_OK;
 }
@@ -2475,7 +2862,8 @@ void mixed_destroy(PesPlan* p) {
   if (!p->mixed) return;
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
   if (p->mixed->aux) cudaStreamSynchronize(p->mixed->aux);
-  for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_tadj})
+  for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_tadj, p->mixed->ev_hd,
+                        p->mixed->ev_pfit})
     if (e) cudaEventDestroy(e);
   if (p->mixed->aux) cudaStreamDestroy(p->mixed->aux);
   for (void* a : p->mixed->allocs) cudaFree(a);
@@ -2496,6 +2884,11 @@ int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cud
   k_mixed_ingest<<<ceil_div(p->desc.nbins, 256), 256, 0, st>>>(p->dev, M, det,
                                                                reinterpret_cast<const double2*>(data), psd);
   PES_CHECK_LAUNCH();
+  suffix_sum(p->desc.nbins, M.wrow, const_cast<double*>(M.dsuf) + (size_t)det * (p->desc.nbins + 1), st);
+  PES_CHECK_LAUNCH();
+  k_wmoments<<<ceil_div((M.J - 1) * 6, 128), 128, 0, st>>>(p->dev, M, det, const_cast<double*>(M.wmom),
+                                                            const_cast<double*>(M.wtot));
+  PES_CHECK_LAUNCH();
   return PES_OK;
 }
 
@@ -2504,14 +2897,14 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   MixedDev& M = p->mixed->dev;
   const GenArg& G = p->mixed->gen;
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
-  k_setup<double><<<1, 64, 0, st>>>(p->dev, theta_dev, 1, 0, blocks);
+  k_setup<double><<<1, 64, 0, st>>>(p->dev, theta_dev, 1, 0, blocks, hm_blocks<double>(p));
   PES_CHECK_LAUNCH();
   k_mixed_ranges<0><<<1, 64, 0, st>>>(M, blocks, 1);
   k_mixed_ranges<1><<<1, 64, 0, st>>>(M, blocks, 1);
   PES_CHECK_LAUNCH();
   k_kink<<<1, 64, 0, st>>>(p->dev, M, G, blocks, 1);
   PES_CHECK_LAUNCH();
-  k_sparse_fwd<<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
+  k_sparse_fwd<false><<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
   launch_spline_fit(M, 1, st, st);
   PES_CHECK_LAUNCH();
@@ -2554,7 +2947,8 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
   {
     ProfScope ps(p, kKSetup, st);
-    k_setup<double><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, 0, blocks);
+    k_setup<double><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, 0, blocks,
+                                                                                  hm_blocks<double>(p));
   }
   PES_CHECK_LAUNCH();
   {
@@ -2591,7 +2985,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     }
     PES_CHECK_LAUNCH();
   }
-  PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
+  // (the side stream's completion is recorded after the exact re-evaluation below)
   {
     ProfScope ps(p, kKSparse, st);
     k_kink<<<ceil_div(B * (int64_t)M.n_det, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, M, G, blocks, B);
@@ -2600,7 +2994,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   {
     ProfScope ps(p, kKSparse, st);
     dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
-    k_sparse_fwd<<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
+    k_sparse_fwd<false><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   }
   PES_CHECK_LAUNCH();
   {
@@ -2614,6 +3008,31 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tfit, p->mixed->aux));
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_pfit, st));
+  {
+    // <h|h> and <d|d> of the dense ranges, beside the anchors and the dense stage
+    // (after both fits: grids beyond 64 x 32 intervals fit every quantity on the main stream)
+    cudaStream_t aux = p->mixed->aux;
+    {
+      ProfScope ps(p, kKSparse, aux);
+      k_sparse_fwd<true><<<dim3(M.nblk_sparse, M.n_det, (unsigned)B), kSparseThreads, 0, aux>>>(p->dev, M, G, blocks);
+    }
+    PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_pfit, 0));
+    PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->xready, 0));
+    ProfScope ps(p, kKOther, aux);
+    k_hd<<<(unsigned)(B * (int64_t)M.n_det), kHdThreads, 0, aux>>>(p->dev, M, blocks, B);
+  }
+  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_hd, p->mixed->aux));
+  // the exact re-evaluation of the samples that the error estimates select,
+  // on the side stream after its exact low-frequency bins
+  PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_hd, 0));
+  {
+    ProfScope ps(p, kKDenseFp64, side);
+    k_exact<3, double><<<dim3(M.rblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+  }
+  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
   if (grad) {
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
     PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
@@ -2640,6 +3059,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_dense, st));
   PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->join, 0));
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_hd, 0));
   {
     ProfScope ps(p, kKFinalize, st);
     k_mixed_finalize<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, M, blocks, B, lnl, status);

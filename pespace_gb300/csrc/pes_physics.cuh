@@ -327,14 +327,45 @@ PES_HD void tdi_channels(const Cx<double>& D, const Cx<double>& P, int orth, con
   tdi_channels_t<true, T>(cx(lift<T>(D.re), lift<T>(D.im)), cx(lift<T>(P.re), lift<T>(P.im)), orth, L, out);
 }
 
+// ------------------------------------------------------------------ Kerr quasi-normal modes
+// M omega = wR - i wI of a Kerr black hole of dimensionless spin a for mode
+// `mode` (table order (2,2), (2,1), (3,3), (3,2), (4,4), (4,3); s = -2,
+// overtone 0), from the natural cubic spline in u = sqrt(1 - a) through the
+// frequencies that gen_qnm_table.py computes by Leaver's continued fractions
+// (negative a: the retrograde continuation).  a is clamped to +-PES_QNM_A_MAX.
+#define PES_QNM_STORAGE __device__ static const
+#include "pes_qnm_table.h"
+
+template <class T>
+PES_HD void qnm_interp(int mode, const T& a, T& wR, T& wI) {
+  T ac = a;
+  if (val(ac) > PES_QNM_A_MAX) ac = lift<T>(PES_QNM_A_MAX);
+  if (val(ac) < -PES_QNM_A_MAX) ac = lift<T>(-PES_QNM_A_MAX);
+  const T u = dsqrt(1.0 - ac);
+  int i = (int)floor((val(u) - PES_QNM_U0) / PES_QNM_DU);
+  i = i < 0 ? 0 : (i > PES_QNM_NODES - 2 ? PES_QNM_NODES - 2 : i);
+  const double h = PES_QNM_DU;
+  const T t = (u - (PES_QNM_U0 + i * h)) / h;
+  const T s = 1.0 - t;
+  const T cA = (s * s * s - s) * (h * h / 6.0), cB = (t * t * t - t) * (h * h / 6.0);
+  const double* re = kQnmTable[mode][0];
+  const double* re2 = kQnmTable[mode][1];
+  const double* im = kQnmTable[mode][2];
+  const double* im2 = kQnmTable[mode][3];
+  wR = s * re[i] + t * re[i + 1] + cA * re2[i] + cB * re2[i + 1];
+  wI = s * im[i] + t * im[i + 1] + cA * im2[i] + cB * im2[i + 1];
+}
+
 // ------------------------------------------------------------------ IMRPhenomD
 constexpr double kAmpJoinIns = 0.014;  // Mf of the inspiral/intermediate amplitude join
 constexpr double kPhiJoinIns = 0.018;  // Mf of the inspiral/intermediate phase join
 constexpr double kMfCut = 0.2;         // PhenomD is zero above Mf = 0.2
 
-// Coefficient fits (Khan et al. 2016 Table V): v2, gamma1..3, sigma1..4, beta1..3, alpha1..5;
-// value = c0 + c1 eta + xi (c2 + c3 eta + c4 eta^2) + xi^2 (c5 + ...) + xi^3 (c8 + ...), xi = chi_PN - 1.
-enum { kFV2, kFG1, kFG2, kFG3, kFS1, kFS2, kFS3, kFS4, kFB1, kFB2, kFB3, kFA1, kFA2, kFA3, kFA4, kFA5, kFCount };
+// Coefficient fits (Khan et al. 2016 Table V): v2, gamma1..3, sigma1..4, beta1..3, alpha1..5,
+// rho1..3; value = c0 + c1 eta + xi (c2 + c3 eta + c4 eta^2) + xi^2 (c5 + ...) + xi^3 (c8 + ...),
+// xi = chi_PN - 1.
+enum { kFV2, kFG1, kFG2, kFG3, kFS1, kFS2, kFS3, kFS4, kFB1, kFB2, kFB3, kFA1, kFA2, kFA3, kFA4, kFA5,
+       kFR1, kFR2, kFR3, kFCount };
 __device__ __constant__ static const double kPhenomFits[kFCount][11] = {
   {0.8149838730507785, 2.5747553517454658, 1.1610198035496786, -2.3627771785551537, 6.771038707057573, 0.7570782938606834, -2.7256896890432474, 7.1140380397149965, 0.1766934149293479, -0.7978690983168183, 2.1162391502005153},
   {0.006927402739328343, 0.03020474290328911, 0.006308024337706171, -0.12074130661131138, 0.26271598905781324, 0.0034151773647198794, -0.10779338611188374, 0.27098966966891747, 0.0007374185938559283, -0.02749621038376281, 0.0733150789135702},
@@ -352,6 +383,9 @@ __device__ __constant__ static const double kPhenomFits[kFCount][11] = {
   {9.5988072383479, -397.05438595557433, 16.202126189517813, -1574.8286986717037, 3600.3410843831093, 27.092429659075467, -1786.482357315139, 5152.919378666511, 11.175710130033895, -577.7999423177481, 1808.730762932043},
   {-0.02989487384493607, 1.4022106448583738, -0.07356049468633846, 0.8337006542278661, 0.2240008282397391, -0.055202870001177226, 0.5667186343606578, 0.7186931973380503, -0.015507437354325743, 0.15750322779277187, 0.21076815715176228},
   {0.9974408278363099, -0.007884449714907203, -0.059046901195591035, 1.3958712396764088, -4.516631601676276, -0.05585343136869692, 1.7516580039343603, -5.990208965347804, -0.017945336522161195, 0.5965097794825992, -2.0608879367971804},
+  {3931.8979897196614, -17395.758706812805, 3132.375545898835, 343965.86092361377, -1.2162565819981997e6, -70698.00600428853, 1.383907177859705e6, -3.9662761890979446e6, -60017.52423652596, 803515.1181825735, -2.091710365941658e6},
+  {-40105.47653771657, 112253.0169706701, 23561.696065836168, -3.476180699403351e6, 1.137593670849482e7, 754313.1127166454, -1.308476044625268e7, 3.6444584853928134e7, 596226.612472288, -7.4277901143564405e6, 1.8928977514040343e7},
+  {83208.35471266537, -191237.7264145924, -210916.2454782992, 8.71797508352568e6, -2.6914942420669552e7, -1.9889806527362722e6, 3.0888029960154563e7, -8.390870279256162e7, -1.4535031953446497e6, 1.7063528990822166e7, -4.2748659731120914e7},
 };
 
 // Per-sample coefficient block.  Psi is the full phase in h22 = A e^{-i Psi}
@@ -361,7 +395,7 @@ struct PhenomDCoef {
   T Msec;               // total mass [s]
   T fRD, fDM, fpeak;    // Mf units
   T amp_scale;          // A = amp_scale * Mf^{-7/6} * Ahat(Mf)
-  T ai[5];              // Ahat_ins = 1 + ai0 u^2 + ai1 u^3 + ai2 u^4 + ai3 u^5 + ai4 u^6
+  T ai[8];              // Ahat_ins = 1 + sum_j ai_j u^(j+2): 3PN SPA terms (j < 5), rho1..rho3 (j = 5..7)
   T dl[5];              // Ahat_int = sum dl_j Mf^j
   T g1, g2, g3fDM;      // Ahat_mrd = g1 g3fDM / ((Mf-fRD)^2 + g3fDM^2) exp(-g2 (Mf-fRD)/g3fDM)
   T pin[12];            // Psi_ins = u^-5 sum pin_j u^j + (lg0 + lg1 u) ln u
@@ -370,6 +404,7 @@ struct PhenomDCoef {
   T pm[6];              // Psi_mrd = pm0 + pm1 Mf + pm2/Mf + pm3 Mf^{3/4} + pm4 atan((Mf - pm5)/fDM)
   T tscale;             // Msec / (2 pi)
   T pfac, cfac;         // (1 + cos^2 i)/2, cos i
+  T af, erad, eta, v2;  // remnant spin, radiated energy, symmetric mass ratio, amplitude collocation value
 };
 
 template <class T>
@@ -416,7 +451,8 @@ template <class T>
 PES_HD T phenomd_amphat(const PhenomDCoef<T>& c, const T& Mf, const T& u) {
   if (Mf < kAmpJoinIns) {
     T u2 = u * u;
-    return 1.0 + u2 * (c.ai[0] + u * (c.ai[1] + u * (c.ai[2] + u * (c.ai[3] + u * c.ai[4]))));
+    return 1.0 + u2 * (c.ai[0] + u * (c.ai[1] + u * (c.ai[2] + u * (c.ai[3] + u * (c.ai[4] +
+                       u * (c.ai[5] + u * (c.ai[6] + u * c.ai[7])))))));
   }
   if (Mf >= c.fpeak) {
     T x = Mf - c.fRD;
@@ -504,14 +540,16 @@ PES_HD void phenomd_setup(const T* th, double f_ref, PhenomDCoef<T>& c) {
              3.352411249771192 * eta3) * eta *
             (1.0 + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * eta2) * sn)) /
            (1.0 + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * eta2) * sn);
-  // (2,2,0) quasi-normal mode: Berti, Cardoso & Will (2006) fits
-  T om = one - af;
-  T wR = 1.5251 - 1.1568 * dpow(om, 0.1292);
-  T Qf = 0.7 + 1.4187 * dpow(om, -0.4990);
-  T mscale = 1.0 / ((2.0 * kPi) * (one - erad));
-  c.fRD = wR * mscale;
-  c.fDM = wR / (2.0 * Qf) * mscale;
+  // (2,2,0) quasi-normal mode of the remnant (mass 1 - E_rad, spin af)
+  T wR, wI;
+  qnm_interp<T>(0, af, wR, wI);
+  c.fRD = wR / (2.0 * kPi) / (one - erad);
+  c.fDM = wI / (2.0 * kPi) / (one - erad);
   T v2 = phenom_fit(kFV2, eta, xi);
+  c.af = af;
+  c.erad = erad;
+  c.eta = eta;
+  c.v2 = v2;
   c.g1 = phenom_fit(kFG1, eta, xi);
   c.g2 = phenom_fit(kFG2, eta, xi);
   T g3 = phenom_fit(kFG3, eta, xi);
@@ -542,6 +580,10 @@ PES_HD void phenomd_setup(const T* th, double f_ref, PhenomDCoef<T>& c) {
                   77616.0 * 995766.0 * seta * (c12 - c22) + 5841690624.0 * kPi * (chi1 + chi2) +
                   21384760320.0 * pi2)) *
             (pi2 / 60085960704.0);
+  // calibrated terms rho1 Mf^{7/3} + rho2 Mf^{8/3} + rho3 Mf^3 (Khan et al. 2016 eq. 29)
+  c.ai[5] = phenom_fit(kFR1, eta, xi);
+  c.ai[6] = phenom_fit(kFR2, eta, xi);
+  c.ai[7] = phenom_fit(kFR3, eta, xi);
   // TaylorF2 aligned-spin phasing (3.5PN, spin-orbit to 3.5PN, 2PN spin-spin,
   // no 3PN spin-spin) plus the sigma terms, as a series in u.
   T SL = m1 * m1 * chi1 + m2 * m2 * chi2;
@@ -637,9 +679,11 @@ PES_HD void phenomd_setup(const T* th, double f_ref, PhenomDCoef<T>& c) {
     T f1 = lift<T>(kAmpJoinIns), f3 = c.fpeak, f2 = 0.5 * (f1 + f3);
     T u1 = dcbrt(f1);
     T u12 = u1 * u1;
-    T Ains = one + u12 * (c.ai[0] + u1 * (c.ai[1] + u1 * (c.ai[2] + u1 * (c.ai[3] + u1 * c.ai[4]))));
+    T Ains = one + u12 * (c.ai[0] + u1 * (c.ai[1] + u1 * (c.ai[2] + u1 * (c.ai[3] + u1 * (c.ai[4] +
+                   u1 * (c.ai[5] + u1 * (c.ai[6] + u1 * c.ai[7])))))));
     // dAhat/dMf = (1/(3u^2)) dAhat/du
-    T dAdu = u1 * (2.0 * c.ai[0] + u1 * (3.0 * c.ai[1] + u1 * (4.0 * c.ai[2] + u1 * (5.0 * c.ai[3] + u1 * 6.0 * c.ai[4]))));
+    T dAdu = u1 * (2.0 * c.ai[0] + u1 * (3.0 * c.ai[1] + u1 * (4.0 * c.ai[2] + u1 * (5.0 * c.ai[3] + u1 * (6.0 * c.ai[4] +
+                   u1 * (7.0 * c.ai[5] + u1 * (8.0 * c.ai[6] + u1 * 9.0 * c.ai[7])))))));
     T dAins = dAdu / (3.0 * u12);
     T x3 = f3 - c.fRD;
     T den = x3 * x3 + c.g3fDM * c.g3fDM;
@@ -691,6 +735,294 @@ PES_HD void phenomd_setup(const T* th, double f_ref, PhenomDCoef<T>& c) {
   c.amp_scale = amp_norm * (M * kMRSun) * (M * kMTSun) / DLm * dsqrt(eta * (2.0 / 3.0));
   c.pfac = 0.5 * (one + th[5] * th[5]);
   c.cfac = th[5];
+}
+
+// ------------------------------------------------------------------ IMRPhenomHM
+// The six-mode model of London et al. 2018 (arXiv:1708.00404) built on the
+// (2,2) IMRPhenomD block above: modes (2,2), (2,1), (3,3), (3,2), (4,4), (4,3)
+// (the quasi-normal-mode table's order).  Each mode maps onto the (2,2)
+// frequency f22: 2 f / m in the inspiral, Rholm f (Rholm = fRD22 / fRD_lm)
+// in the ringdown; between corners at the (2,2) joins (amplitude: Mf = 0.014
+// and f_peak; phase: Mf = 0.018 and fRD22 / 2) the phase map is linear and
+// the amplitude map the cubic Hermite blend of the two lines (C1).
+// Amplitude: beta_lm A22(f22) with beta_lm the post-Newtonian mode ratio
+// |H_lm| / |H_22| sqrt(2/m) at v = (2 pi M f_b / m)^{1/3}, f_b = f below the
+// amplitude map's inspiral corner f_i and f_i (2 - exp(1 - f/f_i)) above it,
+// and the (2,2) amplitude's merger-ringdown width set to the mode's (Rholm
+// fDM_lm in mapped frequency; intermediate collocation re-solved).  Phase: (m/2) Psi22(2f/m) below the phase map's
+// first corner, (1/a) Psi22(a f + b) + c0 + c1 f between the corners,
+// (1/Rholm) Psi22_MRD(Rholm f) + c0' + c1' f above (arctangent width the
+// mode's), C1 throughout; plus k_lm quarter turns (the phase of H_lm).
+// Polarisations: hp = sum P_lm h_lm, hc = i sum C_lm h_lm (s = -2 spherical
+// harmonics at azimuth 0; (2,2) gives (1 + cos^2 i)/2 and -cos i).
+constexpr int kHMModes = 6;
+__device__ __constant__ static const int kHMlm[kHMModes][3] = {  // l, m, quarter turns of H_lm
+    {2, 2, 0}, {2, 1, 1}, {3, 3, 3}, {3, 2, 0}, {4, 4, 2}, {4, 3, 3}};
+
+template <class T>
+struct HMMode {
+  T P, C;                       // polarisation factors
+  T Rholm, fDMeff, g3fDMeff;    // ringdown map slope, the mode's damping in mapped frequency
+  T fpeak, dl[5];               // mapped amplitude: peak, intermediate polynomial
+  T fiA, frA;                   // amplitude map corners (Mf)
+  T fiP, frP, aP, bP;           // phase map
+  T cI0, cI1, cR0, cR1;         // C1 constants of the phase
+  T fRD;                        // the mode's ringdown frequency (Mf)
+};
+
+template <class T>
+struct PhenomHMCoef {
+  T eta, dlt, chis, chia;  // for the PN amplitude ratios
+  T fRDmax;                // largest ringdown frequency of the modes (Mf)
+  T v2;                    // the (2,2) intermediate amplitude collocation value
+  T ainsf1, dainsf1;       // the (2,2) inspiral amplitude and its Mf-derivative at Mf = 0.014
+  HMMode<T> md[kHMModes];
+};
+
+PES_HD double hm_fact(int n) {
+  double r = 1.0;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+
+// s = -2 spherical harmonic at azimuth 0 from cos(iota): sqrt((2l+1)/4pi) d^l_{m,2}
+template <class T>
+PES_HD T hm_sylm(int l, int m, const T& cosi) {
+  const T ch = dsqrt(0.5 * (1.0 + cosi)), sh = dsqrt(0.5 * (1.0 - cosi));
+  T sum = lift<T>(0.0);
+  for (int k = 0; k <= l + m; ++k) {
+    if (l + m - k < 0 || l - 2 - k < 0 || k + 2 - m < 0) continue;
+    const double c = ((k & 1) ? -1.0 : 1.0) *
+                     ::sqrt(hm_fact(l + m) * hm_fact(l - m) * hm_fact(l + 2) * hm_fact(l - 2)) /
+                     (hm_fact(l + m - k) * hm_fact(l - 2 - k) * hm_fact(k) * hm_fact(k + 2 - m));
+    T term = lift<T>(c);
+    for (int e = 0; e < 2 * l + m - 2 * k - 2; ++e) term = term * ch;
+    for (int e = 0; e < 2 * k + 2 - m; ++e) term = term * sh;
+    sum = sum + term;
+  }
+  return ::sqrt((2.0 * l + 1.0) / (4.0 * kPi)) * sum;
+}
+
+// Signed PN amplitude ratio beta_lm(v) (Blanchet 2014 eq. 327; leading spin term of (2,1))
+template <class T>
+PES_HD T hm_pn_ratio(int k, const T& v, const PhenomHMCoef<T>& h) {
+  const T v2 = v * v;
+  const T h22 = 1.0 + v2 * (-107.0 / 42.0 + (55.0 / 42.0) * h.eta) + (2.0 * kPi) * (v2 * v);
+  T r;
+  switch (k) {
+    case 0: return lift<T>(1.0);
+    case 1:
+      r = (1.0 / 3.0) * (h.dlt * v * (1.0 + v2 * (-17.0 / 28.0 + (5.0 / 7.0) * h.eta)) - 1.5 * (h.chia + h.dlt * h.chis) * v2);
+      return r / h22 * ::sqrt(2.0);
+    case 2:
+      r = (0.75 * 1.0350983390135313) * h.dlt * v * (1.0 + v2 * (-4.0 + 2.0 * h.eta));  // sqrt(15/14)
+      return r / h22 * ::sqrt(2.0 / 3.0);
+    case 3:
+      r = (0.84515425472851657 / 3.0) * v2 * (1.0 - 3.0 * h.eta);  // sqrt(5/7)
+      return r / h22 * ::sqrt(2.0 / 2.0);
+    case 4:
+      r = (8.0 / 9.0 * 0.84515425472851657) * v2 * (1.0 - 3.0 * h.eta);
+      return r / h22 * ::sqrt(2.0 / 4.0);
+    default:
+      r = (9.0 / (4.0 * 8.3666002653407556)) * h.dlt * v2 * v * (1.0 - 2.0 * h.eta);  // sqrt(70)
+      return r / h22 * ::sqrt(2.0 / 3.0);
+  }
+}
+
+// the (2,2) merger-ringdown phase ansatz (aligned coefficients) with damping fdm
+template <class T>
+PES_HD void hm_psi_mrd(const PhenomDCoef<T>& c, const T& fdm, const T& Mf, T& psi, T& dpsi) {
+  const T iMf = 1.0 / Mf;
+  const T q = dsqrt(dsqrt(Mf));
+  const T x = Mf - c.pm[5];
+  psi = c.pm[0] + c.pm[1] * Mf + c.pm[2] * iMf + c.pm[3] * (q * q * q) + c.pm[4] * datan(x / fdm);
+  dpsi = c.pm[1] - c.pm[2] * iMf * iMf + 0.75 * c.pm[3] / q + c.pm[4] * fdm / (fdm * fdm + x * x);
+}
+
+// mode k's phase (without the quarter turns) and dPsi/dMf
+template <class T>
+PES_HD void hm_phase(const PhenomDCoef<T>& c, const HMMode<T>& md, int m, const T& Mf, T& psi, T& dpsi) {
+  if (Mf < md.fiP) {
+    const T f22 = (2.0 / m) * Mf;
+    phenomd_phase<T>(c, f22, dcbrt(f22), psi, dpsi);
+    psi = (0.5 * m) * psi;
+  } else if (Mf < md.frP) {
+    const T f22 = md.aP * Mf + md.bP;
+    phenomd_phase<T>(c, f22, dcbrt(f22), psi, dpsi);
+    psi = psi / md.aP + md.cI0 + md.cI1 * Mf;
+    dpsi = dpsi + md.cI1;
+  } else {
+    hm_psi_mrd<T>(c, md.fDMeff, md.Rholm * Mf, psi, dpsi);
+    psi = psi / md.Rholm + md.cR0 + md.cR1 * Mf;
+    dpsi = dpsi + md.cR1;
+  }
+}
+
+// mapped (2,2) amplitude hat with the mode's merger-ringdown width
+template <class T>
+PES_HD T hm_amphat(const PhenomDCoef<T>& c, const HMMode<T>& md, const T& Mf22, const T& u) {
+  if (Mf22 < kAmpJoinIns) return phenomd_amphat<T>(c, Mf22, u);
+  if (Mf22 >= md.fpeak) {
+    const T x = Mf22 - c.fRD;
+    return c.g1 * md.g3fDMeff / (x * x + md.g3fDMeff * md.g3fDMeff) * dexp(-c.g2 * x / md.g3fDMeff);
+  }
+  return md.dl[0] + Mf22 * (md.dl[1] + Mf22 * (md.dl[2] + Mf22 * (md.dl[3] + Mf22 * md.dl[4])));
+}
+
+// the amplitude's frequency map: 2 f / m below fiA, Rholm f above frA, the
+// cubic Hermite blend of the two (values and slopes) between
+template <class T>
+PES_HD T hm_amp_map(const HMMode<T>& md, int m, const T& Mf) {
+  if (val(Mf) <= val(md.fiA)) return (2.0 / m) * Mf;
+  if (val(Mf) >= val(md.frA)) return md.Rholm * Mf;
+  const T h = md.frA - md.fiA, s = (Mf - md.fiA) / h;
+  const T s2 = s * s, s3 = s2 * s;
+  return (2.0 * s3 - 3.0 * s2 + 1.0) * ((2.0 / m) * md.fiA) + (s3 - 2.0 * s2 + s) * (h * (2.0 / m)) +
+         (3.0 * s2 - 2.0 * s3) * (md.Rholm * md.frA) + (s3 - s2) * (h * md.Rholm);
+}
+
+// Mode k at Mf: amplitude, phase (with the quarter turns) and t(f) [s]; the
+// mapped (amplitude) frequency in *f22 for the caller's Mf = 0.2 cut.
+template <class T>
+PES_HD void phenomhm_eval(const PhenomDCoef<T>& c, const PhenomHMCoef<T>& h, int k, const T& Mf, T& amp, T& psi,
+                          T& tf, T* f22_out) {
+  const HMMode<T>& md = h.md[k];
+  const int m = kHMlm[k][1];
+  const T f22 = k == 0 ? Mf : hm_amp_map<T>(md, m, Mf);
+  if (f22_out) *f22_out = f22;
+  const T u = dcbrt(f22);
+  T beta = lift<T>(1.0);
+  if (k != 0) {
+    const T fb = (val(Mf) <= val(md.fiA)) ? Mf : md.fiA * (2.0 - dexp(1.0 - Mf / md.fiA));
+    beta = hm_pn_ratio<T>(k, dcbrt((2.0 * kPi / m) * fb), h);
+  }
+  amp = beta * (c.amp_scale / (f22 * dsqrt(u)) * hm_amphat<T>(c, md, f22, u));
+  T dpsi;
+  hm_phase<T>(c, md, m, Mf, psi, dpsi);
+  psi = psi + kHMlm[k][2] * (0.5 * kPi);
+  tf = c.tscale * dpsi;
+}
+
+// The modes' coefficients from the (2,2) block c (already set up from th)
+// and the remnant spin af and radiated energy erad of that set-up.
+template <class T>
+PES_HD void phenomhm_setup(const T* th, const PhenomDCoef<T>& c, PhenomHMCoef<T>& h) {
+  const T one = lift<T>(1.0);
+  const T af = c.af, erad = c.erad, eta = c.eta, v2 = c.v2;
+  const T q = th[1];
+  h.eta = eta;
+  h.dlt = (q - 1.0) / (q + 1.0);
+  h.chis = 0.5 * (th[2] + th[3]);
+  h.chia = 0.5 * (th[2] - th[3]);
+  h.v2 = v2;
+  h.fRDmax = c.fRD;
+  const double nrm = 2.0 * ::sqrt(5.0 / (64.0 * kPi));
+  const T f1 = lift<T>(kAmpJoinIns);
+  const T u1 = dcbrt(f1);
+  for (int k = 0; k < kHMModes; ++k) {
+    HMMode<T>& md = h.md[k];
+    const int l = kHMlm[k][0], m = kHMlm[k][1];
+    const T Yp = hm_sylm<T>(l, m, th[5]), Ym = hm_sylm<T>(l, -m, th[5]);
+    const double sg = (l & 1) ? -1.0 : 1.0;
+    md.P = (sg * Ym + Yp) * (1.0 / (2.0 * nrm));
+    md.C = (sg * Ym - Yp) * (1.0 / (2.0 * nrm));
+    T wR, wI;
+    qnm_interp<T>(k, af, wR, wI);
+    md.fRD = wR / (2.0 * kPi) / (one - erad);
+    const T fDMlm = wI / (2.0 * kPi) / (one - erad);
+    if (val(md.fRD) > val(h.fRDmax)) h.fRDmax = md.fRD;
+    if (k == 0) {  // the (2,2) mode is PhenomD's, bit for bit
+      md.fRD = c.fRD;
+      md.Rholm = one;
+      md.fDMeff = c.fDM;
+      md.g3fDMeff = c.g3fDM;
+      md.fpeak = c.fpeak;
+      for (int j = 0; j < 5; ++j) md.dl[j] = c.dl[j];
+      md.fiA = f1;
+      md.frA = c.fpeak;
+      md.fiP = lift<T>(kPhiJoinIns);
+      md.frP = 0.5 * c.fRD;
+      md.aP = one;
+      md.bP = lift<T>(0.0);
+      md.cI0 = md.cI1 = md.cR0 = md.cR1 = lift<T>(0.0);
+      continue;
+    }
+    md.Rholm = c.fRD / md.fRD;
+    md.fDMeff = md.Rholm * fDMlm;
+    const T g3 = c.g3fDM / c.fDM;
+    md.g3fDMeff = g3 * md.fDMeff;
+    if (val(c.g2) <= 1.0)
+      md.fpeak = dabs(c.fRD + md.fDMeff * g3 * (dsqrt(one - c.g2 * c.g2) - 1.0) / c.g2);
+    else
+      md.fpeak = dabs(c.fRD - md.fDMeff * g3 / c.g2);
+    // intermediate amplitude with the mode's merger-ringdown
+    {
+      const T f3 = md.fpeak, f2 = 0.5 * (f1 + f3);
+      const T u12 = u1 * u1;
+      const T Ains = one + u12 * (c.ai[0] + u1 * (c.ai[1] + u1 * (c.ai[2] + u1 * (c.ai[3] + u1 * (c.ai[4] +
+                     u1 * (c.ai[5] + u1 * (c.ai[6] + u1 * c.ai[7])))))));
+      const T dAdu = u1 * (2.0 * c.ai[0] + u1 * (3.0 * c.ai[1] + u1 * (4.0 * c.ai[2] + u1 * (5.0 * c.ai[3] + u1 * (6.0 * c.ai[4] +
+                     u1 * (7.0 * c.ai[5] + u1 * (8.0 * c.ai[6] + u1 * 9.0 * c.ai[7])))))));
+      const T dAins = dAdu / (3.0 * u12);
+      const T x3 = f3 - c.fRD;
+      const T den = x3 * x3 + md.g3fDMeff * md.g3fDMeff;
+      const T Amrd = c.g1 * md.g3fDMeff / den * dexp(-c.g2 * x3 / md.g3fDMeff);
+      const T dAmrd = Amrd * (-c.g2 / md.g3fDMeff - 2.0 * x3 / den);
+      T A[5][5], b[5];
+      const T fs[3] = {f1, f2, f3};
+      for (int r = 0; r < 3; ++r) {
+        T pw = one;
+        for (int j = 0; j < 5; ++j) { A[r][j] = pw; pw = pw * fs[r]; }
+      }
+      const T fd[2] = {f1, f3};
+      for (int r = 0; r < 2; ++r) {
+        A[3 + r][0] = lift<T>(0.0);
+        A[3 + r][1] = one;
+        A[3 + r][2] = 2.0 * fd[r];
+        A[3 + r][3] = 3.0 * fd[r] * fd[r];
+        A[3 + r][4] = 4.0 * fd[r] * fd[r] * fd[r];
+      }
+      b[0] = Ains;
+      b[1] = v2;
+      b[2] = Amrd;
+      b[3] = dAins;
+      b[4] = dAmrd;
+      solve5(A, b, md.dl);
+    }
+    // maps
+    md.fiA = (0.5 * m) * f1;
+    md.frA = md.fpeak / md.Rholm;
+    md.fiP = lift<T>((0.5 * m) * kPhiJoinIns);
+    md.frP = (0.5 * c.fRD) / md.Rholm;
+    md.aP = (0.5 * c.fRD - kPhiJoinIns) / (md.frP - md.fiP);
+    md.bP = kPhiJoinIns - md.aP * md.fiP;
+    // C1 matching of the phase at fiP and frP
+    md.cI0 = md.cI1 = md.cR0 = md.cR1 = lift<T>(0.0);
+    T v1, d1, va, da;
+    {
+      const T f22 = (2.0 / m) * md.fiP;
+      phenomd_phase<T>(c, f22, dcbrt(f22), v1, d1);
+      v1 = (0.5 * m) * v1;
+    }
+    {
+      const T f22 = md.aP * md.fiP + md.bP;
+      phenomd_phase<T>(c, f22, dcbrt(f22), va, da);
+      va = va / md.aP;
+    }
+    md.cI1 = d1 - da;
+    md.cI0 = v1 - va - md.cI1 * md.fiP;
+    T vb, db, vr, dr;
+    {
+      const T f22 = md.aP * md.frP + md.bP;
+      phenomd_phase<T>(c, f22, dcbrt(f22), vb, db);
+      vb = vb / md.aP + md.cI0 + md.cI1 * md.frP;
+      db = db + md.cI1;
+    }
+    hm_psi_mrd<T>(c, md.fDMeff, md.Rholm * md.frP, vr, dr);
+    vr = vr / md.Rholm;
+    md.cR1 = db - dr;
+    md.cR0 = vb - vr - md.cR1 * md.frP;
+  }
 }
 
 }  // namespace pes

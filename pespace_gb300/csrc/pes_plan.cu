@@ -14,10 +14,69 @@ constexpr int kDenseThreads = 128;
 constexpr int kDenseBinsPerThread = 4;
 constexpr int kDenseBinsPerBlock = kDenseThreads * kDenseBinsPerThread;
 
+// IMRPhenomHM container of mode k at f, time-shifted by t_c as the reference
+// does (antenna.py:435-441): hp, hc times exp(-2 pi i f t_c), tf + t_c.
+// False when the mode is above its mapped Mf = 0.2.
+template <class T>
+__device__ __forceinline__ bool hm_mode_container(const SampleBlock<T>& b, const PhenomHMCoef<T>& h, int k, double f,
+                                                  const Cx<T>& ts, Cx<T>& hp, Cx<T>& hc, T& tft) {
+  const T Mf = b.wf.Msec * f;
+  T amp, psi, tf, f22;
+  phenomhm_eval<T>(b.wf, h, k, Mf, amp, psi, tf, &f22);
+  if (val(f22) > kMfCut) return false;
+  T s, c;
+  dsincos(psi, &s, &c);
+  // h_lm = amp e^{-i psi}; hp = P h_lm, hc = i C h_lm
+  const T ap = h.md[k].P * amp, ac = h.md[k].C * amp;
+  hp = cmul(cx(ap * c, -(ap * s)), ts);
+  hc = cmul(cx(ac * s, ac * c), ts);
+  tft = tf + b.tc;
+  return true;
+}
+
+// IMRPhenomHM: the six modes' links summed per detector (antenna.py:446-458),
+// then TDI; residual sum over detectors and channels.
+template <class T>
+__device__ __forceinline__ T bin_residual_hm(const PlanDev& P, const SampleBlock<T>& b, const PhenomHMCoef<T>& h,
+                                             int64_t i) {
+  const double f = (double)(P.k0 + i) * P.f_step;
+  Cx<T> ts;
+  dsincos((-2.0 * kPi * f) * b.tc, &ts.im, &ts.re);
+  T sum = lift<T>(0.0);
+  for (int d = 0; d < P.n_det; ++d) {
+    Cx<T> La[6];
+#pragma unroll
+    for (int l = 0; l < 6; ++l) La[l] = cx(lift<T>(0.0), lift<T>(0.0));
+#pragma unroll 1
+    for (int k = 0; k < kHMModes; ++k) {
+      Cx<T> hp, hc, L[6];
+      T tft;
+      if (!hm_mode_container<T>(b, h, k, f, ts, hp, hc, tft)) continue;
+      single_links<T>(P.orbit[d], f, hp, hc, tft, b.pol, L);
+#pragma unroll
+      for (int l = 0; l < 6; ++l) La[l] = La[l] + L[l];
+    }
+    Cx<T> C[3];
+    const TdiFactor dp = P.tdi[d * P.nbins + i];
+    tdi_channels<T>(cx(dp.dre, dp.dim), cx(dp.pre, dp.pim), 1, La, C);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      if (!((P.chan_mask >> ch) & 1)) continue;
+      const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
+      const double2 dv = P.data[off];
+      T rr = dv.x - C[ch].re, ri = dv.y - C[ch].im;
+      sum = sum + (rr * rr + ri * ri) * P.w[off];
+    }
+  }
+  return sum;
+}
+
 // Model (A/E/T) of every detector at one dense bin, accumulated into the
 // residual sum sum_det sum_c |d - h|^2 w.
 template <class T>
-__device__ __forceinline__ T bin_residual(const PlanDev& P, const SampleBlock<T>& b, int64_t i) {
+__device__ __forceinline__ T bin_residual(const PlanDev& P, const SampleBlock<T>& b, const PhenomHMCoef<T>* h,
+                                          int64_t i) {
+  if (P.approximant == PES_APPROX_PHENOMHM) return bin_residual_hm<T>(P, b, *h, i);
   const double f = (double)(P.k0 + i) * P.f_step;
   T Mf = b.wf.Msec * f;
   T amp, psi, tf;
@@ -52,7 +111,8 @@ __device__ __forceinline__ T bin_residual(const PlanDev& P, const SampleBlock<T>
 
 template <class T>
 __global__ void __launch_bounds__(kDenseThreads) k_dense_fp64(PlanDev P, const SampleBlock<T>* __restrict__ blocks,
-                                                              int nblk, double* __restrict__ partial) {
+                                                              const PhenomHMCoef<T>* __restrict__ hmb, int nblk,
+                                                              double* __restrict__ partial) {
   constexpr int NV = 1 + NumTangents<T>::value;
   __shared__ SampleBlock<T> sb;
   __shared__ double red[kDenseThreads / 32][NV];
@@ -70,7 +130,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense_fp64(PlanDev P, const S
 #pragma unroll 1
     for (int j = 0; j < kDenseBinsPerThread; ++j) {
       const int64_t i = base + (int64_t)j * kDenseThreads;
-      if (i < sb.kcut) acc = acc + bin_residual<T>(P, sb, i);
+      if (i < sb.kcut) acc = acc + bin_residual<T>(P, sb, hmb ? hmb + s : nullptr, i);
     }
   }
   double v[NV];
@@ -127,15 +187,29 @@ __global__ void k_finalize(PlanDev P, const SampleBlock<T>* __restrict__ blocks,
 }
 
 // Dense A/E/T (or X/Y/Z) model of one detector (parity/debug path).
-__global__ void k_model_tdi(PlanDev P, const SampleBlock<double>* __restrict__ blocks, int det, int orth,
-                            double2* __restrict__ out) {
+__global__ void k_model_tdi(PlanDev P, const SampleBlock<double>* __restrict__ blocks,
+                            const PhenomHMCoef<double>* __restrict__ hmb, int det, int orth, double2* __restrict__ out) {
   __shared__ SampleBlock<double> sb;
   if (threadIdx.x == 0) sb = blocks[0];
   __syncthreads();
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.nbins) return;
   Cx<double> C[3] = {cx(0.0, 0.0), cx(0.0, 0.0), cx(0.0, 0.0)};
-  if (sb.status == kSampleOk && i < sb.kcut) {
+  if (sb.status == kSampleOk && i < sb.kcut && P.approximant == PES_APPROX_PHENOMHM) {
+    const double f = (double)(P.k0 + i) * P.f_step;
+    Cx<double> ts, La[6];
+    dsincos((-2.0 * kPi * f) * sb.tc, &ts.im, &ts.re);
+    for (int l = 0; l < 6; ++l) La[l] = cx(0.0, 0.0);
+    for (int k = 0; k < kHMModes; ++k) {
+      Cx<double> hp, hc, L[6];
+      double tft;
+      if (!hm_mode_container<double>(sb, hmb[0], k, f, ts, hp, hc, tft)) continue;
+      single_links<double>(P.orbit[det], f, hp, hc, tft, sb.pol, L);
+      for (int l = 0; l < 6; ++l) La[l] = La[l] + L[l];
+    }
+    const TdiFactor dp = P.tdi[det * P.nbins + i];
+    tdi_channels<double>(cx(dp.dre, dp.dim), cx(dp.pre, dp.pim), orth, La, C);
+  } else if (sb.status == kSampleOk && i < sb.kcut) {
     const double f = (double)(P.k0 + i) * P.f_step;
     double Mf = sb.wf.Msec * f;
     double amp, psi, tf, s, c;
@@ -215,6 +289,10 @@ __global__ void __launch_bounds__(kSuffixThreads) k_suffix(int64_t n, const doub
   }
 }
 
+void suffix_sum(int64_t n, const double* row, double* out, cudaStream_t st) {
+  k_suffix<<<1, kSuffixThreads, 0, st>>>(n, row, out);
+}
+
 // ------------------------------------------------------------------ host driver
 template <class T>
 int run_dense(PesPlan* p, const double* theta, int64_t B, int pass, double* lnl, double* grad, int32_t* status,
@@ -222,14 +300,15 @@ int run_dense(PesPlan* p, const double* theta, int64_t B, int pass, double* lnl,
   SampleBlock<T>* blocks = reinterpret_cast<SampleBlock<T>*>(p->blocks);
   {
     ProfScope ps(p, kKSetup, st);
-    k_setup<T><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, pass, blocks);
+    k_setup<T><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, pass, blocks,
+                                                                            hm_blocks<T>(p));
   }
   PES_CHECK_LAUNCH();
   const int nblk = (int)ceil_div(p->desc.nbins, kDenseBinsPerBlock);
   dim3 grid(nblk, (unsigned)B);
   {
     ProfScope ps(p, kKDenseFp64, st);
-    k_dense_fp64<T><<<grid, kDenseThreads, 0, st>>>(p->dev, blocks, nblk, p->partial);
+    k_dense_fp64<T><<<grid, kDenseThreads, 0, st>>>(p->dev, blocks, hm_blocks<T>(p), nblk, p->partial);
   }
   PES_CHECK_LAUNCH();
   {
@@ -256,6 +335,8 @@ int pes_plan_create(const PesPlanDesc* desc, PesPlan** out) {
   PES_REQUIRE(desc->precision == PES_PRECISION_FP64 || desc->precision == PES_PRECISION_MIXED,
               "pes_plan_create: unknown precision %d", desc->precision);
   PES_REQUIRE(desc->max_batch >= 1 && desc->max_batch <= 65535, "pes_plan_create: max_batch must be 1..65535");
+  PES_REQUIRE(desc->approximant == PES_APPROX_PHENOMD || desc->approximant == PES_APPROX_PHENOMHM,
+              "pes_plan_create: unknown approximant %d", desc->approximant);
   PES_REQUIRE(desc->f_step > 0 && desc->df > 0, "pes_plan_create: f_step and df must be positive");
   for (int d = 0; d < desc->n_det; ++d) {
     PES_REQUIRE(desc->det[d].generation == 15 || desc->det[d].generation == 20,
@@ -276,6 +357,8 @@ int pes_plan_create(const PesPlanDesc* desc, PesPlan** out) {
   D.cut_factor = desc->cut_factor;
   D.n_det = desc->n_det;
   D.chan_mask = desc->chan_mask;
+  D.approximant = desc->approximant;
+  D.pad = 0;
   for (int d = 0; d < desc->n_det; ++d) D.orbit[d] = desc->det[d].orbit;
   const int64_t n = desc->nbins;
   const int nd = desc->n_det;
@@ -290,6 +373,8 @@ int pes_plan_create(const PesPlanDesc* desc, PesPlan** out) {
   if (e == cudaSuccess) e = cudaMalloc(&p->suffix, sizeof(double) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&p->d_row, sizeof(double) * n);
   if (e == cudaSuccess) e = cudaMalloc(&p->blocks, p->blocks_bytes);
+  if (e == cudaSuccess && desc->approximant == PES_APPROX_PHENOMHM)  // the largest scalar: the Fisher duals
+    e = cudaMalloc(&p->hm_blocks, (size_t)B * sizeof(PhenomHMCoef<Dual<11>>));
   if (e == cudaSuccess && desc->precision == PES_PRECISION_FP64)
     e = cudaMalloc(&p->partial, sizeof(double) * p->partial_len);
   if (e == cudaSuccess) e = cudaMalloc(&p->status, sizeof(int32_t) * B);
@@ -331,6 +416,7 @@ int pes_plan_destroy(PesPlan* p) {
   cudaFree(p->suffix);
   cudaFree(p->d_row);
   cudaFree(p->blocks);
+  if (p->hm_blocks) cudaFree(p->hm_blocks);
   cudaFree(p->partial);
   cudaFree(p->status);
   delete p;
@@ -416,9 +502,9 @@ int pes_plan_model_tdi(PesPlan* p, int32_t det, int32_t orthogonal, const double
     return PES_OK;
   }
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
-  k_setup<double><<<1, 1, 0, st>>>(p->dev, d_theta, 1, 0, blocks);
+  k_setup<double><<<1, 1, 0, st>>>(p->dev, d_theta, 1, 0, blocks, hm_blocks<double>(p));
   PES_CHECK_LAUNCH();
-  k_model_tdi<<<ceil_div(p->desc.nbins, 128), 128, 0, st>>>(p->dev, blocks, det, orthogonal != 0,
+  k_model_tdi<<<ceil_div(p->desc.nbins, 128), 128, 0, st>>>(p->dev, blocks, hm_blocks<double>(p), det, orthogonal != 0,
                                                             reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaFreeAsync(d_theta, st));

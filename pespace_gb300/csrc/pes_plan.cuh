@@ -24,6 +24,8 @@ struct PlanDev {
   double cut_factor;
   int32_t n_det;
   int32_t chan_mask;
+  int32_t approximant;  // PES_APPROX_*
+  int32_t pad;
   PesOrbit orbit[PES_MAX_DETECTORS];
   const double2* data;   // [n_det][3][nbins]
   const double* w;       // [n_det][3][nbins] inverse PSD, zero on channels outside chan_mask
@@ -95,6 +97,7 @@ struct PesPlan {
   double* suffix = nullptr;
   double* d_row = nullptr;     // [nbins] per-bin sum_det sum_c |d|^2 w (suffix source)
   void* blocks = nullptr;      // per-sample SampleBlock<T> (largest T)
+  void* hm_blocks = nullptr;   // per-sample PhenomHMCoef<T> (IMRPhenomHM plans; largest T)
   size_t blocks_bytes = 0;
   double* partial = nullptr;   // [max_batch][nblk][1 + NT]
   size_t partial_len = 0;
@@ -108,6 +111,12 @@ struct PesPlan {
 };
 
 namespace pes {
+// the plan's per-sample IMRPhenomHM mode coefficients in scalar type T (null for IMRPhenomD plans)
+template <class T>
+inline PhenomHMCoef<T>* hm_blocks(PesPlan* p) {
+  return reinterpret_cast<PhenomHMCoef<T>*>(p->hm_blocks);
+}
+
 // Brackets one kernel launch for the measurement hooks (a no-op unless enabled).
 struct ProfScope {
   PesPlan* p;
@@ -169,22 +178,23 @@ PES_HD bool theta_in_domain(const double* t) {
          fabs(t[7]) <= 1.0;
 }
 
-// bins [0, kcut) satisfy f <= fcut and Msec f <= 0.2 (both monotone in f)
-PES_HD int64_t find_kcut(const PlanDev& P, double Msec, double fcut) {
+// bins [0, kcut) satisfy f <= fcut and Msec f <= mf_max (both monotone in f)
+PES_HD int64_t find_kcut(const PlanDev& P, double Msec, double fcut, double mf_max = kMfCut) {
   int64_t lo = 0, hi = P.nbins;  // invariant: live(i) for i < lo, !live(i) for i >= hi
   while (lo < hi) {
     int64_t mid = (lo + hi) >> 1;
     double f = (double)(P.k0 + mid) * P.f_step;
-    bool live = (f <= fcut) && (Msec * f <= kMfCut);
+    bool live = (f <= fcut) && (Msec * f <= mf_max);
     if (live) lo = mid + 1; else hi = mid;
   }
   return lo;
 }
 
 // ------------------------------------------------------------------ kernels
+// hmb: the samples' IMRPhenomHM mode coefficients (IMRPhenomHM plans; may be null otherwise)
 template <class T>
 __global__ void k_setup(PlanDev P, const double* __restrict__ theta, int64_t B, int pass,
-                        SampleBlock<T>* __restrict__ blocks) {
+                        SampleBlock<T>* __restrict__ blocks, PhenomHMCoef<T>* __restrict__ hmb) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= B) return;
   constexpr int NT = NumTangents<T>::value;
@@ -200,6 +210,8 @@ __global__ void k_setup(PlanDev P, const double* __restrict__ theta, int64_t B, 
   T th[11];
   for (int j = 0; j < 11; ++j) th[j] = Seed<T>::make(raw[j], NT > 0 ? j - pass * NT : -1);
   phenomd_setup<T>(th, P.f_ref, b.wf);
+  const bool hm = P.approximant == PES_APPROX_PHENOMHM;
+  if (hm) phenomhm_setup<T>(th, b.wf, hmb[s]);
   T sb = th[7];
   T cb = dsqrt((1.0 - sb) * (1.0 + sb));
   make_polar<T>(th[6], sb, cb, th[8], b.pol);
@@ -207,12 +219,23 @@ __global__ void k_setup(PlanDev P, const double* __restrict__ theta, int64_t B, 
   const double Msec = val(b.wf.Msec);
   const double fmax = (double)(P.k0 + P.nbins - 1) * P.f_step + 1.0;
   double fcut = fmax;
-  if (P.cut_factor > 0.0) fcut = fmin(fmax, P.cut_factor * val(b.wf.fRD) / Msec);
+  // the model's cut: cut_factor times the largest ringdown frequency of its modes
+  const double frd = hm ? val(hmb[s].fRDmax) : val(b.wf.fRD);
+  if (P.cut_factor > 0.0) fcut = fmin(fmax, P.cut_factor * frd / Msec);
   b.fcut = fcut;
-  b.kcut = find_kcut(P, Msec, fcut);
+  double mf_max = kMfCut;  // PhenomD: zero above Mf = 0.2; HM: each mode above its mapped Mf = 0.2
+  if (hm)
+    for (int k = 1; k < kHMModes; ++k) {
+      const double mk = kMfCut / val(hmb[s].md[k].Rholm);
+      mf_max = mk > mf_max ? mk : mf_max;
+    }
+  b.kcut = find_kcut(P, Msec, fcut, mf_max);
   b.status = kSampleOk;
 }
 
+
+// out[k] = sum_{i >= k} row[i] for k = 0..n (FP64, fixed order; set-up only)
+void suffix_sum(int64_t n, const double* row, double* out, cudaStream_t st);
 
 int mixed_create(PesPlan* p);
 void mixed_destroy(PesPlan* p);

@@ -182,6 +182,39 @@ __global__ void k_phenomd(ThetaArg th, double f_ref, double f_cut, const double*
   tf[i] = t;
 }
 
+// IMRPhenomHM modes on a frequency array: block (x, mode); h_lm = A e^{-i Psi},
+// hp = P_lm h_lm, hc = i C_lm h_lm, t(f) = dPsi_lm/df / (2 pi); zero above the
+// cut and above the mode's mapped Mf = 0.2.  Outputs mode-major (6, n).
+__global__ void k_phenomhm(ThetaArg th, double f_ref, double f_cut, const double* __restrict__ freqs, int64_t n,
+                           double2* __restrict__ hp, double2* __restrict__ hc, double* __restrict__ tf) {
+  __shared__ PhenomDCoef<double> c;
+  __shared__ PhenomHMCoef<double> h;
+  if (threadIdx.x == 0) {
+    phenomd_setup<double>(th.v, f_ref, c);
+    phenomhm_setup<double>(th.v, c, h);
+  }
+  __syncthreads();
+  const int k = blockIdx.y;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = (int64_t)k * n + i;
+  const double f = freqs[i];
+  double amp = 0.0, psi = 0.0, t = 0.0, f22 = 0.0;
+  if (f <= f_cut) phenomhm_eval<double>(c, h, k, c.Msec * f, amp, psi, t, &f22);
+  if (f > f_cut || f22 > kMfCut) {
+    hp[o] = make_double2(0.0, 0.0);
+    hc[o] = make_double2(0.0, 0.0);
+    tf[o] = 0.0;
+    return;
+  }
+  double s, co;
+  dsincos(psi, &s, &co);
+  const double ap = h.md[k].P * amp, ac = h.md[k].C * amp;
+  hp[o] = make_double2(ap * co, -(ap * s));
+  hc[o] = make_double2(ac * s, ac * co);
+  tf[o] = t;
+}
+
 }  // namespace pes
 
 using namespace pes;
@@ -776,6 +809,20 @@ int pes_phenomd(const double* theta, const double* freqs, int64_t n, double f_re
   k_phenomd<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(th, f_ref, f_cut_hz, freqs, n,
                                                              reinterpret_cast<double2*>(hp),
                                                              reinterpret_cast<double2*>(hc), tf);
+  PES_CHECK_LAUNCH();
+  return PES_OK;
+}
+
+int pes_phenomhm(const double* theta, const double* freqs, int64_t n, double f_ref, double f_cut_hz, double* hp,
+                 double* hc, double* tf, void* stream) {
+  PES_REQUIRE(theta, "pes_phenomhm: null theta");
+  PES_REQUIRE(n >= 0, "pes_phenomhm: n < 0");
+  if (n == 0) return PES_OK;
+  PES_REQUIRE(freqs && hp && hc && tf, "pes_phenomhm: null pointer");
+  ThetaArg th;
+  for (int j = 0; j < 11; ++j) th.v[j] = theta[j];
+  k_phenomhm<<<dim3(ceil_div(n, 128), kHMModes), 128, 0, as_stream(stream)>>>(
+      th, f_ref, f_cut_hz, freqs, n, reinterpret_cast<double2*>(hp), reinterpret_cast<double2*>(hc), tf);
   PES_CHECK_LAUNCH();
   return PES_OK;
 }

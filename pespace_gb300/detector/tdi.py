@@ -86,6 +86,28 @@ def fd_from_td(td_array, info, window=None):
     return np.stack([row[info.frequency_mask_array] for row in out]).astype(np.complex128)
 
 
+def fd_noise_realization_array(info, psd, seed=None):
+    """tdi.py:896-916 on the host: per channel, one draw of
+    ``default_rng(seed).normal(0, 0.5 / sqrt(delta_frequency), (2, full length))``
+    as real and imaginary parts, zero at DC (and at Nyquist for an even number
+    of time samples), cropped to the frequency mask and scaled by sqrt(PSD).
+    info : DataInformation; psd : (C, frequency_series_length) array.
+    Returns a (C, frequency_series_length) complex128 array."""
+    rng = np.random.default_rng(seed=seed)
+    var = 0.5 / (info.delta_frequency) ** 0.5
+    psd = np.asarray(psd, dtype=np.float64)
+    out = []
+    for c_i, _ in enumerate(info.channels):
+        re, im = rng.normal(0, var, (2, info.full_frequency_series_length))
+        re[0] = 0.0
+        im[0] = 0.0
+        if np.mod(info.time_series_length, 2) == 0:
+            im[-1] = 0.0
+            re[-1] = 0.0
+        out.append((re + 1j * im)[info.frequency_mask_array] * psd[c_i] ** 0.5)
+    return np.stack(out)
+
+
 # data_info keys of the HDF5 file, in the reference's DataInformation field order (tdi.py:64-101)
 _INFO_KEYS = ("channels", "duration", "delta_time", "start_time", "minimum_frequency", "maximum_frequency",
               "sampling_frequency", "delta_frequency", "time_series_length", "time_samples_array",
@@ -311,19 +333,7 @@ class TDIChannelData:
         if self.fd_noise_power_density is None:
             raise ValueError("Setting `fd_noise_power_density` before generating noise realization.")
         info = self.data_info
-        rng = np.random.default_rng(seed=seed)
-        var = 0.5 / (info.delta_frequency) ** 0.5
-        psd = self.fd_noise_power_density.cpu().numpy()
-        out = []
-        for c_i, _ in enumerate(info.channels):
-            re, im = rng.normal(0, var, (2, info.full_frequency_series_length))
-            re[0] = 0.0
-            im[0] = 0.0
-            if np.mod(info.time_series_length, 2) == 0:
-                im[-1] = 0.0
-                re[-1] = 0.0
-            out.append((re + 1j * im)[info.frequency_mask_array] * psd[c_i] ** 0.5)
-        arr = np.stack(out)
+        arr = fd_noise_realization_array(info, self.fd_noise_power_density.cpu().numpy(), seed)
         if output_type == "numpy":
             return namedtuple("DataContent", info.channels)(*arr)
         if output_type == "cuda":

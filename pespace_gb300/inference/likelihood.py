@@ -96,11 +96,16 @@ class WhittleLikelihood:
     precision : "fp64" (dense FP64, every bin) or "mixed" (FP64 sparse grid,
         FP32 dense bulk).
     cut_factor : per-sample model cutoff in units of the ringdown frequency
-        (0 keeps the IMRPhenomD Mf = 0.2 cut only).
+        (the largest of the modes' for IMRPhenomHM; 0 keeps the model's own
+        Mf = 0.2 cut only).
+    approximant : "IMRPhenomD" (the (2,2) mode) or "IMRPhenomHM" (modes
+        (2,2), (2,1), (3,3), (3,2), (4,4), (4,3); FP64 plans).
     """
 
+    APPROXIMANTS = {"IMRPhenomD": _lib.APPROX_PHENOMD, "IMRPhenomHM": _lib.APPROX_PHENOMHM}
+
     def __init__(self, detector, channels=("A", "E", "T"), precision="fp64", reference_frequency=None,
-                 cut_factor=0.0, max_batch=1024, n_sparse=1024):
+                 cut_factor=0.0, max_batch=1024, n_sparse=1024, approximant="IMRPhenomD"):
         if not isinstance(detector, tuple):
             detector = (detector,)
         if len(detector) > _lib.MAX_DETECTORS:
@@ -139,6 +144,10 @@ class WhittleLikelihood:
         desc.precision = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
         desc.n_sparse = int(n_sparse)
         desc.max_batch = self.max_batch
+        if approximant not in self.APPROXIMANTS:
+            raise ValueError(f"unknown approximant {approximant}; available: {sorted(self.APPROXIMANTS)}")
+        desc.approximant = self.APPROXIMANTS[approximant]
+        self.approximant = approximant
         for i, det in enumerate(detector):
             desc.det[i].orbit = det.orbit_model.to_c()
             desc.det[i].generation = det.tdi_combination.generation_code
@@ -340,18 +349,26 @@ class CapturedStep:
 
 
 class _LogLikelihoodFn(torch.autograd.Function):
-    """lnL(theta) with the gradient from the plan's derivative kernels."""
+    """lnL(theta) with the gradient from the plan's adjoint kernels.
+
+    The forward pass runs the lnL-only call and keeps nothing but the
+    parameters.  The backward pass runs the lnL+gradient call, which
+    recomputes the sparse-grid waveform and transfer, the splines and the
+    dense stage (accumulating the interval moments), then the transposed
+    spline solve and the backward node pass: no dense residuals are stored
+    between the two passes."""
 
     @staticmethod
     def forward(ctx, theta, engine):
-        lnl, grad = engine.log_likelihood_and_grad(theta)
-        ctx.save_for_backward(grad)
-        return lnl
+        ctx.engine = engine
+        ctx.save_for_backward(theta)
+        return engine.log_likelihood_batch(theta)
 
     @staticmethod
     def backward(ctx, g):
-        (grad,) = ctx.saved_tensors
-        return g[:, None] * grad, None
+        (theta,) = ctx.saved_tensors
+        _, grad = ctx.engine.log_likelihood_and_grad(theta)
+        return (g[:, None] * grad).reshape(theta.shape), None
 
 
 def log_likelihood(theta, engine):

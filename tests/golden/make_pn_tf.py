@@ -63,4 +63,6 @@ def _refshim_mtsun():
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {os.path.basename(__file__)} <path to the pespace checkout>")
+    main(sys.argv[1])
