@@ -2,8 +2,9 @@
 // F_ij = 4 df Re sum_{det, c, f} conj(dh_i) dh_j / S_c(f).  FP64 plans take
 // the derivatives of the A/E/T model with respect to the 11 parameters by
 // forward-mode dual numbers in FP64 at every live bin (the same per-bin model
-// as the FP64 plan); mixed plans by FP32 duals with the model's structure
-// (k_fisher_fast below).
+// as the FP64 plan; IMRPhenomHM: the six modes' links summed per detector);
+// mixed IMRPhenomD plans by FP32 duals with the model's structure
+// (k_fisher_fast below), mixed IMRPhenomHM plans as the FP64 ones.
 // A block of 64 threads evaluates 64 bins of one detector, stores
 // sqrt(w) dh in shared memory, and its threads then form the 66 pair sums of
 // those bins; per-block partials are summed in a fixed order.
@@ -25,8 +26,11 @@ __device__ __forceinline__ void pair_of(int p, int& a, int& b) {
   b = a + p;
 }
 
+// hmb: the samples' IMRPhenomHM mode coefficients (IMRPhenomHM plans: the
+// six modes' links summed per detector, antenna.py:446-458), else null.
 __global__ void __launch_bounds__(kFisherThreads) k_fisher_bins(PlanDev P,
                                                                 const SampleBlock<FisherScalar>* __restrict__ blocks,
+                                                                const PhenomHMCoef<FisherScalar>* __restrict__ hmb,
                                                                 double* __restrict__ partial) {
   using T = FisherScalar;
   __shared__ SampleBlock<T> sb;
@@ -54,27 +58,42 @@ __global__ void __launch_bounds__(kFisherThreads) k_fisher_bins(PlanDev P,
       const int64_t i = base + t;
       const bool live = i < sb.kcut;
       const double f = (double)(P.k0 + (live ? i : 0)) * P.f_step;
-      Cx<T> hp, hc;
+      Cx<T> hp, hc, ts;
       T tft;
       if (live) {
-        T Mf = sb.wf.Msec * f;
-        T amp, psi, tf;
-        phenomd_eval<T>(sb.wf, Mf, amp, psi, tf);
-        T sn, cs;
-        dsincos(psi, &sn, &cs);
-        T ap = sb.wf.pfac * amp, ac = sb.wf.cfac * amp;
-        hp = cx(ap * cs, -(ap * sn));
-        hc = cx(-(ac * sn), -(ac * cs));
-        Cx<T> ts;
         dsincos((-2.0 * kPi * f) * sb.tc, &ts.im, &ts.re);
-        hp = cmul(hp, ts);
-        hc = cmul(hc, ts);
-        tft = tf + sb.tc;
+        if (!hmb) {
+          T Mf = sb.wf.Msec * f;
+          T amp, psi, tf;
+          phenomd_eval<T>(sb.wf, Mf, amp, psi, tf);
+          T sn, cs;
+          dsincos(psi, &sn, &cs);
+          T ap = sb.wf.pfac * amp, ac = sb.wf.cfac * amp;
+          hp = cx(ap * cs, -(ap * sn));
+          hc = cx(-(ac * sn), -(ac * cs));
+          hp = cmul(hp, ts);
+          hc = cmul(hc, ts);
+          tft = tf + sb.tc;
+        }
       }
       for (int d = 0; d < P.n_det; ++d) {
         if (live) {
           Cx<T> L[6], C[3];
-          single_links<T>(P.orbit[d], f, hp, hc, tft, sb.pol, L);
+          if (hmb) {
+#pragma unroll
+            for (int l = 0; l < 6; ++l) L[l] = cx(lift<T>(0.0), lift<T>(0.0));
+#pragma unroll 1
+            for (int k = 0; k < kHMModes; ++k) {
+              Cx<T> mhp, mhc, Lk[6];
+              T mtft;
+              if (!hm_mode_container<T>(sb, hmb[s], k, f, ts, mhp, mhc, mtft)) continue;
+              single_links<T>(P.orbit[d], f, mhp, mhc, mtft, sb.pol, Lk);
+#pragma unroll
+              for (int l = 0; l < 6; ++l) L[l] = L[l] + Lk[l];
+            }
+          } else {
+            single_links<T>(P.orbit[d], f, hp, hc, tft, sb.pol, L);
+          }
           const TdiFactor dp = P.tdi[d * P.nbins + i];
           tdi_channels<T>(cx(dp.dre, dp.dim), cx(dp.pre, dp.pim), 1, L, C);
 #pragma unroll
@@ -317,10 +336,12 @@ extern "C" int pes_fisher_batch(PesPlan* p, const double* theta, int64_t B, doub
   k_setup<FisherScalar><<<(unsigned)ceil_div(B, kPerSampleThreads), kPerSampleThreads, 0, st>>>(
       p->dev, theta, B, 0, blocks, hm_blocks<FisherScalar>(p));
   PES_CHECK_LAUNCH();
-  if (p->mixed)  // mixed plans: FP32 structured derivatives
+  const bool hm = p->desc.approximant == PES_APPROX_PHENOMHM;
+  if (p->mixed && !hm)  // mixed IMRPhenomD plans: FP32 structured derivatives
     k_fisher_fast<<<dim3(kFisherBlocks, (unsigned)B), kFastThreads, 0, st>>>(p->dev, blocks, p->fisher_partial);
-  else  // FP64 plans: FP64 dual numbers through the whole model
-    k_fisher_bins<<<dim3(kFisherBlocks, (unsigned)B), kFisherThreads, 0, st>>>(p->dev, blocks, p->fisher_partial);
+  else  // FP64 plans and IMRPhenomHM: FP64 dual numbers through the whole model
+    k_fisher_bins<<<dim3(kFisherBlocks, (unsigned)B), kFisherThreads, 0, st>>>(
+        p->dev, blocks, hm ? hm_blocks<FisherScalar>(p) : nullptr, p->fisher_partial);
   PES_CHECK_LAUNCH();
   k_fisher_final<<<(unsigned)ceil_div(B * kPairs, 128), 128, 0, st>>>(blocks, B, kFisherBlocks, 4.0 * p->dev.df,
                                                                        p->fisher_partial, fisher, status);

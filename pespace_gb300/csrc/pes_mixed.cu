@@ -57,8 +57,16 @@ constexpr int kExactThreads = 128;
 __device__ __constant__ static const int kSlotParam[kMixNT] = {0, 1, 2, 3, 5, 6, 7, 8, 10};
 using GradScalar = DualF<kMixNT>;    // exact bins: FP64 values (phases of 1e6 rad), FP32 tangents
 
+// Plans of several modes (IMRPhenomHM) keep every sparse-grid, spline, anchor,
+// kink and midpoint buffer, and the per-sample range arrays nsp, nch, sff,
+// cfrac, xbind and xbin, per virtual sample v = s * n_modes + k (sample s,
+// mode k); the dense stage sums the modes of a bin before forming its
+// residual.  n_modes = 1 (IMRPhenomD): v = s.
 struct MixedDev {
   int32_t J;                // nodes
+  int32_t n_modes;          // 1 (IMRPhenomD) or kHMModes (IMRPhenomHM)
+  const PhenomHMCoef<double>* hm;  // [B] the samples' mode coefficients (IMRPhenomHM plans), else null
+  int32_t* vcut;            // [B * n_modes] first bin past the mode's range (its mapped Mf = 0.2, or kcut)
   int32_t nchunks;
   int32_t n_det;
   int32_t nblk_dense;
@@ -147,7 +155,11 @@ struct MixedDev {
   // use the exact transfer quantities at the interval midpoints.
   const float2* mid_ff;     // [J] interval midpoints (hi, lo)
   const float4* tdm_ff;     // [n_det][J] TDI delay factor at the midpoints
-  FF* ym;                   // [B][n_det][6][J] transfer quantities at the midpoints (kink removed)
+  FF* ym;                   // [B][n_det][7][J] transfer quantities (rows 0-5, kink removed) and the
+                            //   phase (row 6) at the midpoints
+  // The splines' error at the midpoints, added back per bin with the shape of
+  // the leading error term of cubic interpolation:
+  float4* cbump;            // [B][n_det][J][2] delta_0..delta_5, h, 4 / h^2
   int32_t rblocks;          // blocks per sample of the exact re-evaluation
   int32_t rpad;
   double* rpart;            // [B][rblocks] exact dense-range partials of re-evaluated samples
@@ -182,46 +194,42 @@ struct MixedBuffers {
   // the gradient pass of the dense stage stages its run inputs through shared
   // memory when they exceed half of L2 (they then stream from DRAM)
   bool stage_grad = false;
-  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr, ev_hd = nullptr, ev_pfit = nullptr;
+  cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr, ev_hd = nullptr, ev_pfit = nullptr,
+              ev_kink = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
-template <class T>
-__device__ __forceinline__ void node_eval(const PlanDev& P, const MixedDev& M, const SampleBlock<T>& b, int d,
-                                          const TdiFactor& td, double f, T y[kNodeQ]) {
-  T Mf = b.wf.Msec * f;
-  T amp, psi, tf;
-  phenomd_eval<T>(b.wf, Mf, amp, psi, tf);
-  amp = amp * M.scale;
-  const T zero = lift<T>(0.0);
-  Cx<T> hp = cx(b.wf.pfac * amp, zero);
-  Cx<T> hc = cx(zero, -(b.wf.cfac * amp));
-  Cx<T> L[6], C[3];
-  T kx0;
-  single_links_impl<true, T>(P.orbit[d], f, hp, hc, tf + b.tc, b.pol, L, &kx0);
-  tdi_channels<T>(cx(td.dre, td.dim), cx(td.pre, td.pim), 1, L, C);
-  y[0] = psi + (2.0 * kPi * f) * kx0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    y[1 + 2 * c] = C[c].re;
-    y[2 + 2 * c] = C[c].im;
-  }
-}
-
-// node_eval with the orbit, frequency and TDI factors in the scalar types of
-// the caller's pass: FF orbit and frequency for the float-float value passes,
-// FP32 ones for the FP32 derivative passes (no FP64 on the way).  kPre
-// applies the TDI generation prefactor Pf (exact bins); nodes take it as 1.
+// Node values of mode k of a multi-mode (IMRPhenomHM) sample, or of the
+// IMRPhenomD model when hm is null: the phase Phi = Psi_k + 2 pi f k.x0 at the
+// mode's t(f) and the three channels' transfer of the mode (response of the
+// unit-phase mode, centre delay factored out; h_k = A_k e^{-i Psi_k},
+// hp = P_k h_k, hc = i C_k h_k).  The orbit, frequency and TDI factors come
+// in the scalar types of the caller's pass (float-float for the value
+// passes).  kPre applies the TDI generation prefactor Pf (exact bins); nodes
+// take it as 1.  The modes continue past their mapped Mf = 0.2 here (smooth
+// splines); the dense stage and the exact bins cut them per bin.
 template <bool kPre, class T, class O, class Fq>
-__device__ __forceinline__ void node_eval_g(const O& orbit, const Fq& scale, const SampleBlock<T>& b,
-                                            const Cx<T>& D, const Cx<T>& Pf, const Fq& f, T y[kNodeQ]) {
+__device__ __forceinline__ void node_eval_mode(const O& orbit, const Fq& scale, const SampleBlock<T>& b,
+                                               const PhenomHMCoef<T>* hm, int k, const Cx<T>& D, const Cx<T>& Pf,
+                                               const Fq& f, T y[kNodeQ], bool* live = nullptr) {
   const T Mf = b.wf.Msec * f;
   T amp, psi, tf;
-  phenomd_eval<T>(b.wf, Mf, amp, psi, tf);
-  amp = amp * scale;
   const T zero = lift<T>(0.0);
-  Cx<T> hp = cx(b.wf.pfac * amp, zero);
-  Cx<T> hc = cx(zero, -(b.wf.cfac * amp));
+  Cx<T> hp, hc;
+  if (hm) {
+    T f22;
+    phenomhm_eval<T>(b.wf, *hm, k, Mf, amp, psi, tf, &f22);
+    if (live) *live = val(f22) <= kMfCut;
+    amp = amp * scale;
+    hp = cx(hm->md[k].P * amp, zero);
+    hc = cx(zero, hm->md[k].C * amp);
+  } else {
+    phenomd_eval<T>(b.wf, Mf, amp, psi, tf);
+    if (live) *live = true;
+    amp = amp * scale;
+    hp = cx(b.wf.pfac * amp, zero);
+    hc = cx(zero, -(b.wf.cfac * amp));
+  }
   Cx<T> L[6], C[3];
   T kx0;
   single_links_impl<true, T>(orbit, f, hp, hc, tf + b.tc, b.pol, L, &kx0);
@@ -232,6 +240,21 @@ __device__ __forceinline__ void node_eval_g(const O& orbit, const Fq& scale, con
     y[1 + 2 * c] = C[c].re;
     y[2 + 2 * c] = C[c].im;
   }
+}
+
+// float-float copy of a sample's mode coefficients, written cooperatively
+__device__ __forceinline__ void narrow_hm_ff(const PhenomHMCoef<double>& a, PhenomHMCoef<FF>& b) {
+  static_assert(sizeof(PhenomHMCoef<FF>) == sizeof(PhenomHMCoef<double>), "FF mode block layout");
+  constexpr int nv = (int)(sizeof(PhenomHMCoef<double>) / sizeof(double));
+  const double* src = reinterpret_cast<const double*>(&a);
+  FF* dst = reinterpret_cast<FF*>(&b);
+  for (int j = threadIdx.x; j < nv; j += blockDim.x) dst[j] = ff_from(src[j]);
+}
+__device__ __forceinline__ void load_hm(const PhenomHMCoef<double>* hm, int64_t s, PhenomHMCoef<double>& out) {
+  constexpr int n8 = (int)(sizeof(PhenomHMCoef<double>) / 8);
+  const double* src = reinterpret_cast<const double*>(hm + s);
+  double* dst = reinterpret_cast<double*>(&out);
+  for (int j = threadIdx.x; j < n8; j += blockDim.x) dst[j] = src[j];
 }
 
 // FF copy of a sample block (wf, pol, tc converted; cut and status copied),
@@ -308,12 +331,15 @@ __device__ __forceinline__ void load_block(const SampleBlock<T>* blocks, int s, 
   for (int j = threadIdx.x; j < n8; j += blockDim.x) dst[j] = src[j];
 }
 
-// Kink coefficients per (sample, detector).
+// Kink coefficients per (virtual sample, detector): the amplitude kink of
+// the sample's model (IMRPhenomD), or of mode k (IMRPhenomHM: hm_kink).
 __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= B * (int64_t)M.n_det) return;
-  const int64_t s = t / M.n_det;
+  if (t >= B * M.n_modes * (int64_t)M.n_det) return;
+  const int64_t v = t / M.n_det;
   const int d = (int)(t % M.n_det);
+  const int64_t s = v / M.n_modes;
+  const int k = (int)(v % M.n_modes);
   const SampleBlock<double>& b = blocks[s];
   double* R = M.kinkR + (size_t)t * 6;
   double* C = M.kinkC + (size_t)t * 6;
@@ -324,18 +350,22 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
     C[q] = 0.0;
   }
   if (b.status != kSampleOk) return;
-  double y[kNodeQ], ahat, jump;
-  TdiFactor td;
+  const PhenomHMCoef<double>* hm = M.hm ? M.hm + s : nullptr;
+  double mf_pk, ahat, jump;
+  if (hm)
+    hm_kink<double>(b.wf, *hm, k, mf_pk, ahat, jump);
+  else {
+    mf_pk = b.wf.fpeak;
+    amp_peak_jump<double>(b.wf, ahat, jump);
+  }
+  const double fpk = mf_pk / b.wf.Msec;
+  double y[kNodeQ];
   {
     Cx<double> D, Pf;
-    tdi_factors(b.wf.fpeak / b.wf.Msec, P.orbit[d].arm_sec, G.gen20[d], D, Pf);
-    td.dre = D.re;
-    td.dim = D.im;
-    td.pre = 1.0;  // the generation prefactor is applied per bin, outside the splines
-    td.pim = 0.0;
+    tdi_factors(fpk, P.orbit[d].arm_sec, G.gen20[d], D, Pf);
+    // the generation prefactor is applied per bin, outside the splines
+    node_eval_mode<false, double>(P.orbit[d], M.scale, b, hm, k, D, cx(1.0, 0.0), fpk, y);
   }
-  node_eval<double>(P, M, b, d, td, b.wf.fpeak / b.wf.Msec, y);
-  amp_peak_jump<double>(b.wf, ahat, jump);
   F[0] = (float)(b.wf.Msec * P.f_step);
   for (int q = 0; q < 6; ++q) {
     R[q] = y[1 + q] / ahat;
@@ -354,35 +384,44 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
                                                                const SampleBlock<double>* __restrict__ blocks) {
   __shared__ SampleBlock<double> sb;
   __shared__ SampleBlock<FF> sbf;
-  const int s = blockIdx.z, d = blockIdx.y;
+  __shared__ PhenomHMCoef<double> hmd;
+  __shared__ PhenomHMCoef<FF> hmf;
+  const int v = blockIdx.z, d = blockIdx.y;  // virtual sample (sample, mode), detector
+  const int s = v / M.n_modes, k = v % M.n_modes;
   load_block(blocks, s, sb);
+  if (M.hm) load_hm(M.hm, s, hmd);
   __syncthreads();
   narrow_block_ff(sb, sbf);
+  if (M.hm) narrow_hm_ff(hmd, hmf);
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ns = M.nsp[s];
+  const int ns = M.nsp[v];
   if (sb.status != kSampleOk || ns < 3 || j > ns || j >= M.J || (kMid && j >= ns)) return;
+  const size_t vd = (size_t)v * M.n_det + d;
   FF y[kNodeQ];
   {
     const float2 fn = kMid ? M.mid_ff[j] : M.node_ff[j];
     const float4 t4 = kMid ? M.tdm_ff[(size_t)d * M.J + j] : M.tdn_ff[(size_t)d * M.J + j];
     const Cx<FF> D = cx(ff_make(t4.x, t4.y), ff_make(t4.z, t4.w));
-    node_eval_g<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, D, D, ff_make(fn.x, fn.y), y);
-    const FF xk = sbf.wf.Msec * ff_make(fn.x, fn.y) - sbf.wf.fpeak;
+    node_eval_mode<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, M.hm ? &hmf : nullptr, k, D, D, ff_make(fn.x, fn.y),
+                              y);
+    const float4 pk = M.sff[2 * v + 1];  // the model's (mode's) amplitude kink point, Mf
+    const FF xk = sbf.wf.Msec * ff_make(fn.x, fn.y) - ff_make(pk.x, pk.y);
     if (xk.hi > 0.0f) {
-      const double* C = M.kinkC + ((size_t)s * M.n_det + d) * 6;
+      const double* C = M.kinkC + vd * 6;
       const FF x2 = xk * xk;
 #pragma unroll
       for (int q = 0; q < 6; ++q) y[1 + q] = y[1 + q] - ff_from(C[q]) * x2;
     }
   }
   if (kMid) {
-    FF* out = M.ym + ((size_t)s * M.n_det + d) * 6 * M.J + j;
+    FF* out = M.ym + vd * 7 * M.J + j;
 #pragma unroll
     for (int q = 0; q < 6; ++q) out[(size_t)q * M.J] = y[1 + q];
+    out[(size_t)6 * M.J] = y[0];
     return;
   }
-  FF* out = M.yv + ((size_t)s * M.n_det + d) * kNodeQ * M.J + j;
+  FF* out = M.yv + vd * kNodeQ * M.J + j;
 #pragma unroll
   for (int q = 0; q < kNodeQ; ++q) out[(size_t)q * M.J] = y[q];
 }
@@ -642,22 +681,46 @@ __global__ void __launch_bounds__(kSparseThreads, 3) k_sparse_bwd_split(PlanDev 
 // from the exact bins and the run anchors on), so the bisection can run on the
 // side stream.
 template <int kPart>
-__global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= B) return;
+__global__ void k_mixed_ranges(PlanDev P, MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
+  // kPart 0: one thread per virtual sample v; kPart 1: one thread per sample
+  const int nm = M.n_modes;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (kPart == 0 ? B * nm : B)) return;
+  const int64_t s = kPart == 0 ? t / nm : t;
+  const int kmode = kPart == 0 ? (int)(t % nm) : 0;
   const SampleBlock<double>& b = blocks[s];
+  const PhenomHMCoef<double>* hm = M.hm ? M.hm + s : nullptr;
+  // the range's last live bin: the sample's cut, and for mode k of a
+  // multi-mode model its mapped Mf = 0.2 (the mode's own cut)
+  int64_t kc = b.status == kSampleOk ? b.kcut : 0;
   if (kPart == 0) {
-    const FF tcf = ff_from(b.tc), msf = ff_from(b.wf.Msec), fpf = ff_from(b.wf.fpeak);
-    M.sff[2 * s] = make_float4(tcf.hi, tcf.lo, msf.hi, msf.lo);
-    M.sff[2 * s + 1] = make_float4(fpf.hi, fpf.lo, 0.0f, 0.0f);
+    // the model's (the mode's) amplitude kink point: PhenomD's f_peak, or
+    // where the mode's amplitude map turns linear at its mapped f_peak
+    const double mfpk = (hm && kmode > 0) ? hm->md[kmode].frA : b.wf.fpeak;
+    const FF tcf = ff_from(b.tc), msf = ff_from(b.wf.Msec), fpf = ff_from(mfpk);
+    M.sff[2 * t] = make_float4(tcf.hi, tcf.lo, msf.hi, msf.lo);
+    M.sff[2 * t + 1] = make_float4(fpf.hi, fpf.lo, 0.0f, 0.0f);
     // f t_c = (k0 + k) c, c = f_step t_c: its fraction is (k0 + k) frac(c) mod 1
     const double cyc = M.f_step * b.tc;
     const double rs = (cyc - floor(cyc)) * 18446744073709551616.0;  // 2^64
-    M.cfrac[s] = (rs >= 0.0 && rs < 18446744073709551616.0) ? (unsigned long long)rs : 0ull;
+    M.cfrac[t] = (rs >= 0.0 && rs < 18446744073709551616.0) ? (unsigned long long)rs : 0ull;
+    if (hm && kc > 0) {
+      // first bin whose mapped frequency passes Mf = 0.2 (the linear map, as
+      // the mode's model evaluates it past its amplitude corner)
+      const double Rk = hm->md[kmode].Rholm;
+      int64_t lo = 0, hi = kc;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        const double Mf = b.wf.Msec * ((double)(P.k0 + mid) * P.f_step);
+        if ((kmode == 0 ? Mf : Rk * Mf) <= kMfCut) lo = mid + 1; else hi = mid;
+      }
+      kc = lo;
+    }
+    M.vcut[t] = (int32_t)kc;
   }
   int ns = 0, nc = 0, xb = 0;
-  if (b.status == kSampleOk && b.kcut > 0) {
-    const int64_t last = b.kcut - 1;
+  if (kc > 0) {
+    const int64_t last = kc - 1;
     int lo = 0, hi = M.nchunks - 1;  // last run whose first bin is <= last
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
@@ -668,38 +731,47 @@ __global__ void k_mixed_ranges(MixedDev M, const SampleBlock<double>* __restrict
     if (ns < 3) ns = 3;
     if (ns > M.J - 1) ns = M.J - 1;
     if (kPart == 0) {
-      M.nsp[s] = ns;
-      M.nch[s] = nc;
+      M.nsp[t] = ns;
+      M.nch[t] = nc;
       return;
     }
     for (int d = 0; d < M.n_det; ++d) {
-      auto unresolved = [&](int j) {
-        double a, ps, t0, t1;
-        phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j], a, ps, t0);
-        phenomd_eval<double>(b.wf, b.wf.Msec * M.node_f[j + 1], a, ps, t1);
-        return M.omega[d] * fabs(t1 - t0) > kOrbitPhaseMax;
-      };
       int xbd = 0;
-      if (unresolved(0)) {
-        int lo2 = 0, hi2 = ns - 1;  // last unresolved interval
-        while (lo2 < hi2) {
-          int mid = (lo2 + hi2 + 1) >> 1;
-          if (unresolved(mid)) lo2 = mid; else hi2 = mid - 1;
+      // the exact range: the largest over the modes (each mode's own t(f))
+      for (int k = 0; k < nm; ++k) {
+        auto tfk = [&](int j) {
+          double a, ps, tt;
+          const double Mf = b.wf.Msec * M.node_f[j];
+          if (hm)
+            phenomhm_eval<double>(b.wf, *hm, k, Mf, a, ps, tt, nullptr);
+          else
+            phenomd_eval<double>(b.wf, Mf, a, ps, tt);
+          return tt;
+        };
+        auto unresolved = [&](int j) { return M.omega[d] * fabs(tfk(j + 1) - tfk(j)) > kOrbitPhaseMax; };
+        if (unresolved(0)) {
+          int lo2 = 0, hi2 = ns - 1;  // last unresolved interval
+          while (lo2 < hi2) {
+            int mid = (lo2 + hi2 + 1) >> 1;
+            if (unresolved(mid)) lo2 = mid; else hi2 = mid - 1;
+          }
+          const int64_t first = M.iv_first[lo2 + 1];
+          const int x = (int)(first < kc ? first : kc);
+          xbd = x > xbd ? x : xbd;
         }
-        const int64_t first = M.iv_first[lo2 + 1];
-        xbd = (int)(first < b.kcut ? first : b.kcut);
       }
-      M.xbind[s * M.n_det + d] = xbd;
+      for (int k = 0; k < nm; ++k) M.xbind[(s * nm + k) * M.n_det + d] = xbd;
       xb = xbd > xb ? xbd : xb;
     }
   } else if (kPart == 1) {
-    for (int d = 0; d < M.n_det; ++d) M.xbind[s * M.n_det + d] = 0;
+    for (int d = 0; d < M.n_det; ++d)
+      for (int k = 0; k < nm; ++k) M.xbind[(s * nm + k) * M.n_det + d] = 0;
   }
   if (kPart == 0) {
-    M.nsp[s] = ns;
-    M.nch[s] = nc;
+    M.nsp[t] = ns;
+    M.nch[t] = nc;
   } else {
-    M.xbin[s] = xb;
+    for (int k = 0; k < nm; ++k) M.xbin[s * nm + k] = xb;
   }
 }
 
@@ -1568,21 +1640,20 @@ __global__ void __launch_bounds__(kFitWarps * 32) k_spline_adjoint_staged(MixedD
 }
 
 // ------------------------------------------------------------------ exact bins
-// Accuracy target of a mixed lnL (|dlnL| against the FP64 evaluation) and the
-// error model that decides which samples are re-evaluated exactly over their
-// dense range: the FP32 rounding of the model in the cross term,
-// kCrossRel sqrt(sum |d|^2 |h|^2 w^2) (a few ulps of the phase and modulus
-// per bin, independent between bins), plus the splines' interpolation error
-// of sum |h|^2 w estimated from the exact model at the interval midpoints
-// (kSplineSafety times its estimate, for the part of the error that the
-// midpoint bump does not capture).  Both in units of lnL (times 2 df).
-// The midpoint estimate corrects sum |h|^2 w (it predicts the splines' error
-// there to a few per cent); what remains is modelled as kSplineRel times the
-// sum of the intervals' absolute estimates (the splines' phase error enters
-// the cross term where the model is steep).
-constexpr double kRefineTarget = 2e-3;
+// Error model that decides which samples are re-evaluated exactly over their
+// dense range (the bar is |dlnL| <= 1e-2 against the FP64 evaluation).  The
+// dense stage adds back the splines' midpoint error (k_bump), so what is left
+// is (a) the FP32 rounding of the model in the cross term, a sum of
+// independent per-bin errors whose spread is about 2.2e-7 sqrt(sum |d|^2 |h|^2
+// w^2) (times 2 df, in lnL), modelled as kCrossRel = 4e-7 times that root
+// sum; and (b) the part of the splines' error that the midpoint bump does not
+// capture, modelled as kSplineRel of the intervals' absolute midpoint
+// estimates of sum |h|^2 w.  A sample is refined when the two exceed
+// kRefineTarget: the unrefined ones then have a rounding spread below
+// 2.2e-3, which puts the 1e-2 bar at 4.5 of those spreads.
+constexpr double kRefineTarget = 4e-3;
 constexpr double kCrossRel = 4e-7;
-constexpr double kSplineRel = 0.02;
+constexpr double kSplineRel = 0.01;
 
 __device__ __forceinline__ bool refine_sample(const PlanDev& P, const MixedDev& M, int64_t s) {
   double sv = 0.0, eha = 0.0;
@@ -1614,14 +1685,19 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   __shared__ SampleBlock<T> sb;
   __shared__ SBF sbf;
   __shared__ double red[kExactThreads / 32][NV];
+  __shared__ PhenomHMCoef<double> hmd;  // multi-mode plans (value passes)
+  __shared__ PhenomHMCoef<FF> hmf;
   const int s = blockIdx.y;
-  const int xb = M.xbin[s];
+  const int nm = M.n_modes;
+  const int xb = M.xbin[(size_t)s * nm];
   if (!kRefine && xb == 0) return;  // uniform per block; the finalizers skip such samples
   if (kRefine && (blocks[s].status != kSampleOk || !refine_sample(P, M, s))) return;
   load_block(blocks, s, sb);
+  if (kFF && M.hm) load_hm(M.hm, s, hmd);
   __syncthreads();
   if constexpr (kFF) {
     narrow_block_ff(sb, sbf);
+    if (M.hm) narrow_hm_ff(hmd, hmf);
   } else {
     narrow_exact_grad(sb, sbf);
   }
@@ -1632,23 +1708,37 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   const double inv_scale = 1.0 / M.scale;
   if (sb.status == kSampleOk) {
     for (int d = 0; d < M.n_det; ++d) {
-      const int xbd = M.xbind[(size_t)s * M.n_det + d];
+      const int xbd = M.xbind[(size_t)s * nm * M.n_det + d];
       const int i0 = kRefine ? xbd : 0, i1 = kRefine ? (int)sb.kcut : xbd;
       for (int i = i0 + blockIdx.x * kExactThreads + threadIdx.x; i < i1; i += gridDim.x * kExactThreads) {
         if constexpr (kFF) {
           const FF f = ff_mulf(M.fstep_ff, (float)(P.k0 + i));  // k0 + i < 2^24: exact in FP32
           const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
-          FF y[kNodeQ];
-          node_eval_g<true, FF>(M.orbit_ff[d], M.scale_ff, sbf, cx(ff_from(tdb.dre), ff_from(tdb.dim)),
-                                cx(ff_from(tdb.pre), ff_from(tdb.pim)), f, y);
-          // phase reduced modulo 2 pi in FP64, then its sine and cosine in FF
-          const double phd = ff_to(y[0] + (2.0 * kPi * f) * sbf.tc);
-          FF sn, cs;
-          dsincos(ff_from(phd - (2.0 * kPi) * rint(phd * (1.0 / (2.0 * kPi)))), &sn, &cs);
+          // the modes' channels in float-float, summed
+          FF hsr[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
+          FF hsi[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
+#pragma unroll 1
+          for (int k = 0; k < nm; ++k) {
+            FF y[kNodeQ];
+            bool live = true;
+            node_eval_mode<true, FF>(M.orbit_ff[d], M.scale_ff, sbf, M.hm ? &hmf : nullptr, k,
+                                     cx(ff_from(tdb.dre), ff_from(tdb.dim)), cx(ff_from(tdb.pre), ff_from(tdb.pim)),
+                                     f, y, &live);
+            if (!live) continue;  // the mode above its mapped Mf = 0.2
+            // phase reduced modulo 2 pi in FP64, then its sine and cosine in FF
+            const double phd = ff_to(y[0] + (2.0 * kPi * f) * sbf.tc);
+            FF sn, cs;
+            dsincos(ff_from(phd - (2.0 * kPi) * rint(phd * (1.0 / (2.0 * kPi)))), &sn, &cs);
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              hsr[ch] = hsr[ch] + (y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn);
+              hsi[ch] = hsi[ch] + (y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn);
+            }
+          }
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
-            const double hr = ff_to(y[1 + 2 * ch] * cs + y[2 + 2 * ch] * sn) * inv_scale;
-            const double hi = ff_to(y[2 + 2 * ch] * cs - y[1 + 2 * ch] * sn) * inv_scale;
+            const double hr = ff_to(hsr[ch]) * inv_scale;
+            const double hi = ff_to(hsi[ch]) * inv_scale;
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
             if constexpr (kMode == 2) {
               model[off] = make_double2(hr, hi);
@@ -1844,9 +1934,9 @@ struct RunPhase {
 // peak-kink coordinate Msec f - Mf_peak at the run start.
 __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
                                                       const SampleBlock<double>* __restrict__ blocks) {
-  const int s = blockIdx.z, d = blockIdx.y;
+  const int s = blockIdx.z, d = blockIdx.y;  // s: virtual sample (sample, mode)
   const int c = blockIdx.x * 128 + threadIdx.x;
-  if (blocks[s].status != kSampleOk || c >= M.nch[s]) return;
+  if (blocks[s / M.n_modes].status != kSampleOk || c >= M.nch[s]) return;
   const int kb = M.ch_begin[c];
   if (kb < M.xbind[(size_t)s * M.n_det + d]) return;
   const size_t sd = (size_t)s * M.n_det + d;
@@ -1936,18 +2026,69 @@ __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wai
 
 // One run's inputs in shared memory: the three packed rows of its (up to) 32
 // bins, the interval's eight coefficient rows and the run's three anchor rows.
-constexpr int kRunBuf = 3 * 32 + 8 + 3;
+constexpr int kRunBuf = 3 * 32 + 8 + 3 + 2;  // packed bins, coefficient rows, anchor, midpoint corrections
+
+// The splines' error at each interval's midpoint, against the exact model
+// there, as the coefficients of a correction delta_q (4 t (h - t) / h^2)^2
+// that the dense stage adds to each transfer quantity: the leading error term
+// of cubic interpolation, f^(4)(xi) t^2 (h - t)^2 / 24, has this shape, so the
+// corrected model also matches the exact one at the midpoints.  The phase
+// spline's midpoint error dphi enters as a rotation of the exact transfer
+// quantities, G e^{-i dphi}, since the model is G P e^{-i phase}.  One thread
+// per (virtual sample, detector, interval).
+__global__ void k_bump(MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= B * M.n_modes * M.n_det * (int64_t)M.J) return;
+  const int j = (int)(t % M.J);
+  const int64_t sd = t / M.J;
+  const int64_t v = sd / M.n_det;
+  float4* out = M.cbump + (size_t)t * 2;
+  if (blocks[v / M.n_modes].status != kSampleOk || M.nsp[v] < 3 || j >= M.nsp[v]) {
+    out[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    out[1] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+    return;
+  }
+  const double h = M.gh[j], tm = 0.5 * h;
+  const FF* ym = M.ym + (size_t)sd * 7 * M.J + j;
+  const FF* co = M.cphi + (size_t)t * 4;
+  const double phs = ff_to(co[0]) + tm * (ff_to(co[1]) + tm * (ff_to(co[2]) + tm * ff_to(co[3])));
+  double sn, cs;
+  sincos(ff_to(ym[(size_t)6 * M.J]) - phs, &sn, &cs);
+  const float4* cg = M.cg + (size_t)t * 8;
+  const float* alo = reinterpret_cast<const float*>(cg + 6);
+  const float* blo = M.cgb + (size_t)t * 6;
+  float dl[6];
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    double sp[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int q = 2 * ch + k;
+      const float4 c4 = cg[q];
+      sp[k] = ((double)c4.x + (double)alo[q]) +
+              tm * (((double)c4.y + (double)blo[q]) + tm * ((double)c4.z + tm * (double)c4.w));
+    }
+    const double gr = ff_to(ym[(size_t)(2 * ch) * M.J]), gi = ff_to(ym[(size_t)(2 * ch + 1) * M.J]);
+    dl[2 * ch] = (float)(gr * cs + gi * sn - sp[0]);
+    dl[2 * ch + 1] = (float)(gi * cs - gr * sn - sp[1]);
+  }
+  out[0] = make_float4(dl[0], dl[1], dl[2], dl[3]);
+  out[1] = make_float4(dl[4], dl[5], (float)h, (float)(4.0 / (h * h)));
+}
 
 // kMode 0: lnL partials; 1: lnL partials + adjoint moments; 2: write the model
 // h (unscaled, complex128 (n_det, 3, nbins)) to `model` (parity/debug path).
 // kStage: the run inputs are copied one run ahead into shared memory (pays
 // off when they stream from DRAM, and in the lnL pass; with L2-resident
 // inputs the gradient pass is faster on plain loads).
-template <int kMode, bool kStage>
+// kNM: modes summed per bin before the residual (1, or kHMModes for
+// IMRPhenomHM plans: lnL and model passes, plain loads).
+template <int kMode, bool kStage, int kNM>
 __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev M,
                                                              const SampleBlock<double>* __restrict__ blocks,
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
+  static_assert(kNM == 1 || (!kGrad && !kStage), "multi-mode dense stage: lnL and model passes, no staging");
   __shared__ double red[kMixThreads / 32][2];
   // per warp, two run buffers: the next run's inputs are copied while this one is computed
   __shared__ __align__(16) float4 rbuf[kStage ? kMixThreads / 32 : 1][kStage ? 2 : 1][kStage ? kRunBuf : 1];
@@ -1955,7 +2096,9 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   const int s = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int g = blockIdx.x * (kMixThreads / 32) + wid;  // run group
-  const int nc = M.nch[s];
+  int nc = M.nch[(size_t)s * kNM];  // runs with a live bin of any mode
+#pragma unroll
+  for (int k = 1; k < kNM; ++k) nc = max(nc, M.nch[(size_t)s * kNM + k]);
   const int64_t kcut = blocks[s].kcut;
   const int first = g * kChunkMax;
   float acc = 0.0f, comp = 0.0f;
@@ -1963,11 +2106,10 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   float xacc = 0.0f, xcomp = 0.0f;  // compensated sum of the cross term -2 Re(d^* h) w
   if (blocks[s].status == kSampleOk && first < nc) {
     for (int d = 0; d < M.n_det; ++d) {
-      const size_t sd = (size_t)s * M.n_det + d;
+      const size_t sd = (size_t)s * kNM * M.n_det + d;  // (virtual sample of mode 0, detector)
       const int xb = M.xbind[sd];
-      // ---- amplitude kink at f_peak (float-float coefficients, read past the peak only)
-      const float* KF = M.kinkF + sd * 16;
-      const float kSlope = KF[0];
+      // ---- amplitude kink (float-float coefficients, read past the kink point only)
+      const float kSlope = M.kinkF[sd * 16];  // Msec f_step, the same for every mode
       float km[12];
       bool kinked = false;
       if (kGrad) {
@@ -2000,6 +2142,8 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           cp_async16_l1(dst + 96 + lane, M.cg + (sd * M.J + M.ch_iv[c]) * 8 + lane);
         else if (lane < 11)
           cp_async16(dst + 104 + (lane - 8), M.runs + (sd * M.nchunks + c) * 3 + (lane - 8));
+        else if (lane < 13)
+          cp_async16_l1(dst + 107 + (lane - 11), M.cbump + (sd * M.J + M.ch_iv[c]) * 2 + (lane - 11));
       };
       if (kStage) {
         issue(first, 0);
@@ -2021,18 +2165,20 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           continue;
         }
         const float4* rb = kStage ? &rbuf[wid][b][0] : nullptr;
-        const float4* ra = kStage ? rb + 104 : M.runs + (sd * M.nchunks + c) * 3;
-        const float4 ra0 = ra[0], ra1 = ra[1];
-        RunPhase r;
-        r.x0 = ra0.x;
-        r.c0 = ra0.y;
-        r.s0 = ra0.z;
-        r.p1h = ra0.w;
-        r.p1l = ra1.x;
-        r.p2h = ra1.y;
-        r.p2l = ra1.z;
-        r.p3h = ra1.w;
-        r.p3l = ra[2].x;
+        RunPhase r1;  // the run's anchor (single-mode plans: loaded once per run)
+        if (kNM == 1) {
+          const float4* ra = kStage ? rb + 104 : M.runs + (sd * M.nchunks + c) * 3;
+          const float4 ra0 = ra[0], ra1 = ra[1];
+          r1.x0 = ra0.x;
+          r1.c0 = ra0.y;
+          r1.s0 = ra0.z;
+          r1.p1h = ra0.w;
+          r1.p1l = ra1.x;
+          r1.p2h = ra1.y;
+          r1.p2l = ra1.z;
+          r1.p3h = ra1.w;
+          r1.p3l = ra[2].x;
+        }
         if (kGrad && j != cur_iv) {
           if (cur_iv >= 0) flush_moments(mq, reinterpret_cast<float (*)[kMomPad]>(&msm[wid][0][0]), M.mom + (sd * M.J + cur_iv) * kNodeQ * kMoments, lane);
           cur_iv = j;
@@ -2053,61 +2199,103 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float t = pk2.w;
           const float u = (float)lane;
           const float u2 = u * u, u3 = u2 * u;
-          // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike.
-          // The phase advance is summed error-free (reductions and sums keep their
-          // roundings), its sine and cosine taken of the head and corrected to
-          // first order in the tail.
-          float del, dlo;
-          {
-            float ea, eb, ec;
-            const float a = reduce_exact_ff(r.p1h * u, &ea), b = reduce_exact_ff(r.p2h * u2, &eb),
-                        c = reduce_exact_ff(r.p3h * u3, &ec);
-            float s1, t1, s2, t2, s3, t3;
-            two_sum(a, b, s1, t1);
-            two_sum(s1, c, s2, t2);
-            two_sum(s2, fmaf(r.p1l, u, fmaf(r.p2l, u2, r.p3l * u3)), s3, t3);
-            del = s3;
-            dlo = ((ea + eb) + ec) + ((t1 + t2) + t3);
-          }
-          float sd_, cd_;
-          sincos_poly(del, &sd_, &cd_);
-          {
-            const float sdc = fmaf(dlo, cd_, sd_);
-            cd_ = fmaf(-dlo, sd_, cd_);
-            sd_ = sdc;
-          }
-          float cph = fmaf(r.c0, cd_, -(r.s0 * sd_));
-          float sph = fmaf(r.s0, cd_, r.c0 * sd_);
-          // Renormalise the rotated phasor with one Newton step for 1/|e|
-          // so that FP32 rounding leaves the model amplitude unbiased.
-          const float m2 = fmaf(cph, cph, fmaf(sph, sph, -1.0f));  // |e|^2 - 1, one rounding
-          const float corr = -0.5f * m2;
-          cph = fmaf(corr, cph, cph);
-          sph = fmaf(corr, sph, sph);
-          {
-            // TDI generation prefactor P(f): its zeros (f L = k/2) stay out of the
-            // splines; with h = G (c - i s) the factor multiplies c - i s
-            // explicit FMAs: the lnL and lnL+gradient kernels must round alike
-            const float c2 = fmaf(pk2.y, cph, pk2.z * sph);
-            const float s2 = fmaf(pk2.y, sph, -(pk2.z * cph));
-            cph = c2;
-            sph = s2;
-          }
-          const float4* G = kStage ? rb + 96 : M.cg + (sd * M.J + j) * 8;  // the interval's coefficient rows
-          const float4 gl0 = G[6], gl1 = G[7];
-          const float Glo[6] = {gl0.x, gl0.y, gl0.z, gl0.w, gl1.x, gl1.y};
-          const float xk = fmaf(kSlope, u, r.x0);
-          const float x2 = xk > 0.0f ? xk * xk : 0.0f;
-          float kink[6];
+          // the model of each channel, summed over the modes of the bin
+          float hrs[3] = {0.0f, 0.0f, 0.0f}, his[3] = {0.0f, 0.0f, 0.0f};
+          float cph = 0.0f, sph = 0.0f, xk = 0.0f, x2 = 0.0f;  // (single mode: used by the gradient)
+#pragma unroll 1
+          for (int k = 0; k < kNM; ++k) {
+            const size_t sdk = sd + (size_t)k * M.n_det;
+            RunPhase r = r1;
+            if (kNM > 1) {
+              const size_t v = (size_t)s * kNM + k;
+              if (c >= M.nch[v] || i >= M.vcut[v]) continue;  // past the mode's range
+              const float4* ra = M.runs + (sdk * M.nchunks + c) * 3;
+              const float4 ra0 = ra[0], ra1 = ra[1];
+              r.x0 = ra0.x;
+              r.c0 = ra0.y;
+              r.s0 = ra0.z;
+              r.p1h = ra0.w;
+              r.p1l = ra1.x;
+              r.p2h = ra1.y;
+              r.p2l = ra1.z;
+              r.p3h = ra1.w;
+              r.p3l = ra[2].x;
+            }
+            // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike.
+            // The phase advance is summed error-free (reductions and sums keep their
+            // roundings), its sine and cosine taken of the head and corrected to
+            // first order in the tail.
+            float del, dlo;
+            {
+              float ea, eb, ec;
+              const float a = reduce_exact_ff(r.p1h * u, &ea), b = reduce_exact_ff(r.p2h * u2, &eb),
+                          c = reduce_exact_ff(r.p3h * u3, &ec);
+              float s1, t1, s2, t2, s3, t3;
+              two_sum(a, b, s1, t1);
+              two_sum(s1, c, s2, t2);
+              two_sum(s2, fmaf(r.p1l, u, fmaf(r.p2l, u2, r.p3l * u3)), s3, t3);
+              del = s3;
+              dlo = ((ea + eb) + ec) + ((t1 + t2) + t3);
+            }
+            float sd_, cd_;
+            sincos_poly(del, &sd_, &cd_);
+            {
+              const float sdc = fmaf(dlo, cd_, sd_);
+              cd_ = fmaf(-dlo, sd_, cd_);
+              sd_ = sdc;
+            }
+            cph = fmaf(r.c0, cd_, -(r.s0 * sd_));
+            sph = fmaf(r.s0, cd_, r.c0 * sd_);
+            // Renormalise the rotated phasor with one Newton step for 1/|e|
+            // so that FP32 rounding leaves the model amplitude unbiased.
+            const float m2 = fmaf(cph, cph, fmaf(sph, sph, -1.0f));  // |e|^2 - 1, one rounding
+            const float corr = -0.5f * m2;
+            cph = fmaf(corr, cph, cph);
+            sph = fmaf(corr, sph, sph);
+            {
+              // TDI generation prefactor P(f): its zeros (f L = k/2) stay out of the
+              // splines; with h = G (c - i s) the factor multiplies c - i s
+              // explicit FMAs: the lnL and lnL+gradient kernels must round alike
+              const float c2 = fmaf(pk2.y, cph, pk2.z * sph);
+              const float s2 = fmaf(pk2.y, sph, -(pk2.z * cph));
+              cph = c2;
+              sph = s2;
+            }
+            // the interval's coefficient rows of this mode
+            const float4* G = (kNM == 1 && kStage) ? rb + 96 : M.cg + (sdk * M.J + j) * 8;
+            const float4 gl0 = G[6], gl1 = G[7];
+            const float Glo[6] = {gl0.x, gl0.y, gl0.z, gl0.w, gl1.x, gl1.y};
+            xk = fmaf(kSlope, u, r.x0);
+            x2 = xk > 0.0f ? xk * xk : 0.0f;
+            float kink[6];  // the amplitude kink and the midpoint correction of each quantity
+            {
+              const float4* BQ = (kNM == 1 && kStage) ? rb + 107 : M.cbump + (sdk * M.J + j) * 2;
+              const float4 b0 = BQ[0], b1 = BQ[1];
+              const float rr = t * (b1.z - t) * b1.w;
+              const float r2 = rr * rr;
+              kink[0] = b0.x * r2;
+              kink[1] = b0.y * r2;
+              kink[2] = b0.z * r2;
+              kink[3] = b0.w * r2;
+              kink[4] = b1.x * r2;
+              kink[5] = b1.y * r2;
+            }
+            if (xk > 0.0f) {
+              const float4* KF4 = reinterpret_cast<const float4*>(M.kinkF + sdk * 16);  // 64-byte aligned rows
+              const float4 k0 = KF4[0], k1 = KF4[1], k2 = KF4[2], k3 = KF4[3];
+              const float kfh[6] = {k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+              const float kfl[6] = {k2.x, k2.y, k2.z, k2.w, k3.x, k3.y};
 #pragma unroll
-          for (int q = 0; q < 6; ++q) kink[q] = 0.0f;
-          if (xk > 0.0f) {
-            const float4* KF4 = reinterpret_cast<const float4*>(KF);  // 64-byte aligned rows
-            const float4 k0 = KF4[0], k1 = KF4[1], k2 = KF4[2], k3 = KF4[3];
-            const float kfh[6] = {k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
-            const float kfl[6] = {k2.x, k2.y, k2.z, k2.w, k3.x, k3.y};
+              for (int q = 0; q < 6; ++q) kink[q] = fmaf(kfh[q], x2, fmaf(kfl[q], x2, kink[q]));
+            }
 #pragma unroll
-            for (int q = 0; q < 6; ++q) kink[q] = fmaf(kfh[q], x2, kfl[q] * x2);
+            for (int ch = 0; ch < 3; ++ch) {
+              const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
+              const float gr = cr.x + (kink[2 * ch] + fmaf(t, fmaf(t, fmaf(t, cr.w, cr.z), cr.y), Glo[2 * ch]));
+              const float gi = ci.x + (kink[2 * ch + 1] + fmaf(t, fmaf(t, fmaf(t, ci.w, ci.z), ci.y), Glo[2 * ch + 1]));
+              hrs[ch] += fmaf(gr, cph, gi * sph);
+              his[ch] += fmaf(gi, cph, -(gr * sph));
+            }
           }
           float term = 0.0f;  // |d - h|^2 w
           float cross = 0.0f;  // (|h|^2 - 2 Re(d^* h)) w
@@ -2117,11 +2305,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           float ag[6];
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
-            const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
-            const float gr = cr.x + (kink[2 * ch] + fmaf(t, fmaf(t, fmaf(t, cr.w, cr.z), cr.y), Glo[2 * ch]));
-            const float gi = ci.x + (kink[2 * ch + 1] + fmaf(t, fmaf(t, fmaf(t, ci.w, ci.z), ci.y), Glo[2 * ch + 1]));
-            const float hr = fmaf(gr, cph, gi * sph);
-            const float hi = fmaf(gi, cph, -(gr * sph));
+            const float hr = hrs[ch], hi = his[ch];
             const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
             const float2 dv = ch == 0 ? make_float2(pk0.x, pk0.y)
                                       : (ch == 1 ? make_float2(pk0.z, pk0.w) : make_float2(pk1.x, pk1.y));
@@ -2293,7 +2477,7 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
   const int jlo = iv_of(lo), jhi = iv_of(kcut - 1);
   const double* KC = M.kinkC + sd * 6;
   const double* wm = M.wmom + (size_t)d * P.nbins * kMomStride;
-  const FF* ym = M.ym + (size_t)sd * 6 * M.J;
+  const FF* ym = M.ym + (size_t)sd * 7 * M.J;
   double sum = 0.0, sumv = 0.0, eh = 0.0, eha = 0.0;
   for (int j = jlo + lane; j <= jhi; j += kHdThreads) {
     const int64_t e1 = M.iv_first[j], e2 = M.iv_first[j + 1];
@@ -2411,6 +2595,15 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   for (int k = 0; k < M.nblk_dense; ++k) {
     R += M.part[((size_t)s * M.nblk_dense + k) * 2];
     X += M.part[((size_t)s * M.nblk_dense + k) * 2 + 1];
+  }
+  if (M.n_modes > 1) {  // multi-mode plans: the direct sum
+    double acc = R;
+    if (M.xbin[s * M.n_modes] > 0)
+      for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
+    const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
+    lnl[s] = v;
+    if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
+    return;
   }
   for (int d = 0; d < M.n_det; ++d) {
     // sum |h|^2 w from the splines, corrected by the midpoint estimate of their error
@@ -2553,7 +2746,6 @@ static void launch_spline_fit(const MixedDev& M, int64_t B, cudaStream_t st_phas
 
 int mixed_create(PesPlan* p) {
   const PesPlanDesc& d = p->desc;
-  PES_REQUIRE(d.approximant == PES_APPROX_PHENOMD, "mixed plan: only IMRPhenomD is supported by the mixed precision path");
   PES_REQUIRE(d.n_sparse >= 8 && d.n_sparse <= 65536, "mixed plan: n_sparse must be 8..65536, got %d", d.n_sparse);
   PES_REQUIRE(d.k0 >= 1, "mixed plan: the grid must start above 0 Hz (k0 >= 1)");
   PES_REQUIRE(d.k0 + d.nbins < (int64_t)1 << 24, "mixed plan: bin indices k0 + i must stay below 2^24");
@@ -2571,7 +2763,8 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->join, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->xready, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->aux, cudaStreamNonBlocking));
-  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_tadj, &mb->ev_hd, &mb->ev_pfit})
+  for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_tadj, &mb->ev_hd, &mb->ev_pfit,
+                         &mb->ev_kink})
     PES_CHECK_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
@@ -2580,6 +2773,9 @@ int mixed_create(PesPlan* p) {
   const int64_t B = d.max_batch;
   M.J = J;
   M.n_det = nd;
+  M.n_modes = d.approximant == PES_APPROX_PHENOMHM ? kHMModes : 1;
+  M.hm = hm_blocks<double>(p);
+  const int64_t V = B * M.n_modes;  // virtual samples (sample, mode)
   if (spline_seg(J) == 32) {
     PES_CHECK_CUDA(cudaFuncSetAttribute(k_spline_fit<32, FF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)fit_smem_bytes<FF, true>(J)));
@@ -2658,13 +2854,14 @@ int mixed_create(PesPlan* p) {
   float4* sff;
   unsigned long long* cfrac;
   float2* node_ff;
-  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst;
+  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst, *vcut;
   double *xpart, *xgpart;
   double *wmom, *wtot, *dsuf, *wrow, *hdv, *rpart;
   float* cgb;
   float2* mid_ff;
   float4* tdm_ff;
   FF* ymv;
+  float4* cbump;
   SampleBlock<GradScalar>* gblk;
   double *kR, *kC;
   float* kF;
@@ -2673,32 +2870,38 @@ int mixed_create(PesPlan* p) {
   float4* pk;
   float2* ddv;
   float4* cg;
-  const size_t sd = (size_t)B * nd;
+  const size_t sd = (size_t)V * nd;  // per (virtual sample, detector)
+  // multi-mode plans: lnL only (no gradient buffers) and the direct residual
+  // sum (no split form: no weight moments)
+  const bool multi = M.n_modes > 1;
+  const size_t gsd = multi ? 1 : sd;
+  const size_t wn = multi ? 1 : (size_t)nd * n * kMomStride, wj = multi ? 1 : (size_t)nd * J * kMomStride;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) ||
-      (rc = alloc(mb, &runs, (size_t)B * nd * M.nchunks * 3)) || (rc = alloc(mb, &pk, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, B)) || (rc = alloc(mb, &nch, B)) ||
+      (rc = alloc(mb, &runs, sd * M.nchunks * 3)) || (rc = alloc(mb, &pk, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, V)) || (rc = alloc(mb, &nch, V)) || (rc = alloc(mb, &vcut, V)) ||
       (rc = alloc(mb, &yv, sd * kNodeQ * J)) || (rc = alloc(mb, &scr, sd * kNodeQ * J)) ||
       (rc = alloc(mb, &gh, J)) || (rc = alloc(mb, &ginvh, J)) || (rc = alloc(mb, &glo, J)) ||
       (rc = alloc(mb, &gup, J)) || (rc = alloc(mb, &ginvden, J)) || (rc = alloc(mb, &gcp, J)) ||
-      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &sff, (size_t)2 * B)) ||
-      (rc = alloc(mb, &cfrac, (size_t)B)) || (rc = alloc(mb, &node_ff, J)) ||
+      (rc = alloc(mb, &gf, (size_t)kGfCount * J)) || (rc = alloc(mb, &gff, (size_t)kGfCount * J)) || (rc = alloc(mb, &tdn, (size_t)nd * J)) || (rc = alloc(mb, &tdn_ff, (size_t)nd * J)) || (rc = alloc(mb, &sff, (size_t)2 * V)) ||
+      (rc = alloc(mb, &cfrac, (size_t)V)) || (rc = alloc(mb, &node_ff, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 8)) ||
-      (rc = alloc(mb, &mom, sd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, sd * kNodeQ * J)) ||
+      (rc = alloc(mb, &mom, gsd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, gsd * kNodeQ * J)) ||
       (rc = alloc(mb, &part, (size_t)B * M.nblk_dense * 2)) ||
-      (rc = alloc(mb, &wmom, (size_t)nd * n * kMomStride)) || (rc = alloc(mb, &wtot, (size_t)nd * J * kMomStride)) ||
+      (rc = alloc(mb, &wmom, wn)) || (rc = alloc(mb, &wtot, wj)) ||
       (rc = alloc(mb, &dsuf, (size_t)nd * (n + 1))) || (rc = alloc(mb, &wrow, (size_t)n)) ||
       (rc = alloc(mb, &cgb, sd * J * 6)) || (rc = alloc(mb, &hdv, sd * kHdOut)) ||
-      (rc = alloc(mb, &mid_ff, J)) || (rc = alloc(mb, &tdm_ff, (size_t)nd * J)) || (rc = alloc(mb, &ymv, sd * 6 * J)) ||
+      (rc = alloc(mb, &mid_ff, J)) || (rc = alloc(mb, &tdm_ff, (size_t)nd * J)) || (rc = alloc(mb, &ymv, sd * 7 * J)) ||
+      (rc = alloc(mb, &cbump, sd * J * 2)) ||
       (rc = alloc(mb, &rpart, (size_t)B * kRefineBlocks)) ||
-      (rc = alloc(mb, &gpart, sd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, sd)) ||
+      (rc = alloc(mb, &gpart, gsd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, gsd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
-      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, sd * 12)) || (rc = alloc(mb, &xbin, B)) || (rc = alloc(mb, &xbind, (size_t)B * nd)) ||
+      (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, gsd * 12)) || (rc = alloc(mb, &xbin, V)) || (rc = alloc(mb, &xbind, sd)) ||
       (rc = alloc(mb, &ivfirst, J + 1)) || (rc = alloc(mb, &xpart, (size_t)B * M.xblocks)) ||
       (rc = alloc(mb, &xgpart, (size_t)B * M.xblocks * 11)))
     return rc;
   PES_CHECK_CUDA(cudaMemcpy(ivfirst, ivf.data(), sizeof(int32_t) * (J + 1), cudaMemcpyHostToDevice));
-  PES_CHECK_CUDA(cudaMemset(xbin, 0, sizeof(int32_t) * B));
-  PES_CHECK_CUDA(cudaMemset(xbind, 0, sizeof(int32_t) * B * nd));
+  PES_CHECK_CUDA(cudaMemset(xbin, 0, sizeof(int32_t) * V));
+  PES_CHECK_CUDA(cudaMemset(xbind, 0, sizeof(int32_t) * sd));
   PES_CHECK_CUDA(cudaMemcpy(node_f, nf.data(), sizeof(double) * J, cudaMemcpyHostToDevice));
   {
     std::vector<float2> nff(J);
@@ -2782,6 +2985,7 @@ int mixed_create(PesPlan* p) {
   M.pk = pk;
   M.dd = ddv;
   M.nsp = nsp;
+  M.vcut = vcut;
   M.nch = nch;
   M.xbin = xbin;
   M.xbind = xbind;
@@ -2822,6 +3026,7 @@ int mixed_create(PesPlan* p) {
   M.cgb = cgb;
   M.hd = hdv;
   M.ym = ymv;
+  M.cbump = cbump;
   M.rpart = rpart;
   M.rblocks = kRefineBlocks;
   {
@@ -2844,8 +3049,8 @@ int mixed_create(PesPlan* p) {
   }
   M.mid_ff = mid_ff;
   M.tdm_ff = tdm_ff;
-  PES_CHECK_CUDA(cudaMemset(wmom, 0, sizeof(double) * nd * n * kMomStride));
-  PES_CHECK_CUDA(cudaMemset(wtot, 0, sizeof(double) * nd * J * kMomStride));
+  PES_CHECK_CUDA(cudaMemset(wmom, 0, sizeof(double) * wn));
+  PES_CHECK_CUDA(cudaMemset(wtot, 0, sizeof(double) * wj));
   PES_CHECK_CUDA(cudaMemset(dsuf, 0, sizeof(double) * nd * (n + 1)));
   // the dense-path partial buffer is not needed; gradient set-up blocks are shared
   return PES_OK;
@@ -2863,7 +3068,7 @@ void mixed_destroy(PesPlan* p) {
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
   if (p->mixed->aux) cudaStreamSynchronize(p->mixed->aux);
   for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_tadj, p->mixed->ev_hd,
-                        p->mixed->ev_pfit})
+                        p->mixed->ev_pfit, p->mixed->ev_kink})
     if (e) cudaEventDestroy(e);
   if (p->mixed->aux) cudaStreamDestroy(p->mixed->aux);
   for (void* a : p->mixed->allocs) cudaFree(a);
@@ -2886,6 +3091,7 @@ int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cud
   PES_CHECK_LAUNCH();
   suffix_sum(p->desc.nbins, M.wrow, const_cast<double*>(M.dsuf) + (size_t)det * (p->desc.nbins + 1), st);
   PES_CHECK_LAUNCH();
+  if (M.n_modes > 1) return PES_OK;  // multi-mode plans use the direct residual sum only
   k_wmoments<<<ceil_div((M.J - 1) * 6, 128), 128, 0, st>>>(p->dev, M, det, const_cast<double*>(M.wmom),
                                                             const_cast<double*>(M.wtot));
   PES_CHECK_LAUNCH();
@@ -2899,20 +3105,28 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
   k_setup<double><<<1, 64, 0, st>>>(p->dev, theta_dev, 1, 0, blocks, hm_blocks<double>(p));
   PES_CHECK_LAUNCH();
-  k_mixed_ranges<0><<<1, 64, 0, st>>>(M, blocks, 1);
-  k_mixed_ranges<1><<<1, 64, 0, st>>>(M, blocks, 1);
+  const unsigned nm = (unsigned)M.n_modes;
+  k_mixed_ranges<0><<<1, 64, 0, st>>>(p->dev, M, blocks, 1);
+  k_mixed_ranges<1><<<1, 64, 0, st>>>(p->dev, M, blocks, 1);
   PES_CHECK_LAUNCH();
   k_kink<<<1, 64, 0, st>>>(p->dev, M, G, blocks, 1);
   PES_CHECK_LAUNCH();
-  k_sparse_fwd<false><<<dim3(M.nblk_sparse, M.n_det, 1), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
+  k_sparse_fwd<false><<<dim3(M.nblk_sparse, M.n_det, nm), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   PES_CHECK_LAUNCH();
-  launch_spline_fit(M, 1, st, st);
+  launch_spline_fit(M, nm, st, st);
+  PES_CHECK_LAUNCH();
+  k_sparse_fwd<true><<<dim3(M.nblk_sparse, M.n_det, nm), kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
+  k_bump<<<(unsigned)ceil_div(nm * M.n_det * (int64_t)M.J, (int64_t)128), 128, 0, st>>>(M, blocks, 1);
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * M.n_det * 3 * p->desc.nbins, st));
-  k_run_anchors<<<dim3((unsigned)ceil_div(M.nchunks, 128), M.n_det, 1), 128, 0, st>>>(p->dev, M, blocks);
+  k_run_anchors<<<dim3((unsigned)ceil_div(M.nchunks, 128), M.n_det, nm), 128, 0, st>>>(p->dev, M, blocks);
   PES_CHECK_LAUNCH();
-  k_dense_mixed<2, false><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
-                                                                  reinterpret_cast<double2*>(out));
+  if (nm > 1)
+    k_dense_mixed<2, false, kHMModes><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(
+        p->dev, M, blocks, reinterpret_cast<double2*>(out));
+  else
+    k_dense_mixed<2, false, 1><<<dim3(M.nblk_dense, 1), kMixThreads, 0, st>>>(p->dev, M, blocks,
+                                                                     reinterpret_cast<double2*>(out));
   PES_CHECK_LAUNCH();
   k_exact<2, double><<<dim3(M.xblocks, 1), kExactThreads, 0, st>>>(p->dev, M, G, blocks,
                                                                       reinterpret_cast<double2*>(out));
@@ -2923,18 +3137,21 @@ int mixed_model(PesPlan* p, const double* theta_dev, double* out, cudaStream_t s
 int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const std::vector<int32_t>& ok,
                int64_t* out, cudaStream_t st) {
   const MixedDev& M = p->mixed->dev;
-  std::vector<int32_t> xb((size_t)B * M.n_det), ns(B);
+  const int nm = M.n_modes;
+  std::vector<int32_t> xb((size_t)B * nm * M.n_det), ns((size_t)B * nm);
   if (B > 0) {
-    PES_CHECK_CUDA(cudaMemcpy(xb.data(), M.xbind, sizeof(int32_t) * B * M.n_det, cudaMemcpyDeviceToHost));
-    PES_CHECK_CUDA(cudaMemcpy(ns.data(), M.nsp, sizeof(int32_t) * B, cudaMemcpyDeviceToHost));
+    PES_CHECK_CUDA(cudaMemcpy(xb.data(), M.xbind, sizeof(int32_t) * xb.size(), cudaMemcpyDeviceToHost));
+    PES_CHECK_CUDA(cudaMemcpy(ns.data(), M.nsp, sizeof(int32_t) * ns.size(), cudaMemcpyDeviceToHost));
   }
+  // dense and exact bins per sample (a bin sums all modes); sparse nodes per mode
   for (int64_t s = 0; s < B; ++s) {
     if (!ok[s]) continue;
     for (int d = 0; d < M.n_det; ++d) {
-      out[0] += kcut[s] - xb[(size_t)s * M.n_det + d];
-      out[1] += xb[(size_t)s * M.n_det + d];
+      out[0] += kcut[s] - xb[(size_t)s * nm * M.n_det + d];
+      out[1] += xb[(size_t)s * nm * M.n_det + d];
     }
-    if (ns[s] >= 3) out[2] += (int64_t)(ns[s] + 1) * M.n_det;
+    for (int k = 0; k < nm; ++k)
+      if (ns[(size_t)s * nm + k] >= 3) out[2] += (int64_t)(ns[(size_t)s * nm + k] + 1) * M.n_det;
   }
   (void)st;
   return PES_OK;
@@ -2945,6 +3162,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   MixedDev& M = p->mixed->dev;
   const GenArg& G = p->mixed->gen;
   SampleBlock<double>* blocks = reinterpret_cast<SampleBlock<double>*>(p->blocks);
+  const bool multi = M.n_modes > 1;
+  const int64_t V = B * M.n_modes;  // virtual samples (sample, mode)
+  PES_REQUIRE(!(grad && multi), "mixed plan: the gradient is implemented for IMRPhenomD plans only "
+                                "(the FP64 plan gives IMRPhenomHM gradients)");
   {
     ProfScope ps(p, kKSetup, st);
     k_setup<double><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, theta, B, 0, blocks,
@@ -2953,7 +3174,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKOther, st);
-    k_mixed_ranges<0><<<ceil_div(B, 64), 64, 0, st>>>(M, blocks, B);
+    k_mixed_ranges<0><<<ceil_div(V, 64), 64, 0, st>>>(p->dev, M, blocks, B);
   }
   PES_CHECK_LAUNCH();
   // side stream: the exact-bin range, the exact bins and the gradient set-up they need
@@ -2962,7 +3183,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->fork, 0));
   {
     ProfScope ps(p, kKOther, side);
-    k_mixed_ranges<1><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, side>>>(M, blocks, B);
+    k_mixed_ranges<1><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, side>>>(p->dev, M, blocks, B);
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->xready, side));
@@ -2988,36 +3209,45 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   // (the side stream's completion is recorded after the exact re-evaluation below)
   {
     ProfScope ps(p, kKSparse, st);
-    k_kink<<<ceil_div(B * (int64_t)M.n_det, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, M, G, blocks, B);
+    k_kink<<<ceil_div(V * M.n_det, p->sample_threads), p->sample_threads, 0, st>>>(p->dev, M, G, blocks, B);
+  }
+  PES_CHECK_LAUNCH();
+  cudaStream_t aux = p->mixed->aux;
+  {
+    // the exact model at the interval midpoints, beside the node values
+    PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_kink, st));
+    PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_kink, 0));
+    ProfScope ps(p, kKSparse, aux);
+    k_sparse_fwd<true><<<dim3(M.nblk_sparse, M.n_det, (unsigned)V), kSparseThreads, 0, aux>>>(p->dev, M, G, blocks);
   }
   PES_CHECK_LAUNCH();
   {
     ProfScope ps(p, kKSparse, st);
-    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)B);
+    dim3 grid(M.nblk_sparse, M.n_det, (unsigned)V);
     k_sparse_fwd<false><<<grid, kSparseThreads, 0, st>>>(p->dev, M, G, blocks);
   }
   PES_CHECK_LAUNCH();
   {
     // the phase fit here, the transfer fit on the second stream
-    cudaStream_t aux = p->mixed->aux;
     PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_nodes, st));
     PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_nodes, 0));
     ProfScope ps(p, kKSpline, st);
     ProfScope ps_aux(p, kKSpline, aux);
-    launch_spline_fit(M, B, st, aux);
+    launch_spline_fit(M, V, st, aux);
   }
   PES_CHECK_LAUNCH();
-  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tfit, p->mixed->aux));
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_pfit, st));
   {
-    // <h|h> and <d|d> of the dense ranges, beside the anchors and the dense stage
-    // (after both fits: grids beyond 64 x 32 intervals fit every quantity on the main stream)
-    cudaStream_t aux = p->mixed->aux;
-    {
-      ProfScope ps(p, kKSparse, aux);
-      k_sparse_fwd<true><<<dim3(M.nblk_sparse, M.n_det, (unsigned)B), kSparseThreads, 0, aux>>>(p->dev, M, G, blocks);
-    }
+    // the midpoint corrections, after both fits (grids beyond 64 x 32 intervals
+    // fit every quantity on the main stream)
     PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->ev_pfit, 0));
+    ProfScope ps(p, kKSpline, aux);
+    k_bump<<<(unsigned)ceil_div(V * M.n_det * (int64_t)M.J, (int64_t)128), 128, 0, aux>>>(M, blocks, B);
+  }
+  PES_CHECK_LAUNCH();
+  PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tfit, aux));
+  if (!multi) {
+    // <h|h> and <d|d> of the dense ranges, beside the anchors and the dense stage
     PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->xready, 0));
     ProfScope ps(p, kKOther, aux);
     k_hd<<<(unsigned)(B * (int64_t)M.n_det), kHdThreads, 0, aux>>>(p->dev, M, blocks, B);
@@ -3027,7 +3257,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   // the exact re-evaluation of the samples that the error estimates select,
   // on the side stream after its exact low-frequency bins
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_hd, 0));
-  {
+  if (!multi) {
     ProfScope ps(p, kKDenseFp64, side);
     k_exact<3, double><<<dim3(M.rblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
   }
@@ -3040,7 +3270,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->xready, 0));
   {
     ProfScope ps(p, kKSpline, st);
-    dim3 grid((unsigned)ceil_div(M.nchunks, 128), M.n_det, (unsigned)B);
+    dim3 grid((unsigned)ceil_div(M.nchunks, 128), M.n_det, (unsigned)V);
     k_run_anchors<<<grid, 128, 0, st>>>(p->dev, M, blocks);
   }
   PES_CHECK_LAUNCH();
@@ -3050,11 +3280,13 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     dim3 grid(M.nblk_dense, (unsigned)B);
     if (grad)
       if (p->mixed->stage_grad)
-        k_dense_mixed<1, true><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+        k_dense_mixed<1, true, 1><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
       else
-        k_dense_mixed<1, false><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+        k_dense_mixed<1, false, 1><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+    else if (multi)
+      k_dense_mixed<0, false, kHMModes><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
     else
-      k_dense_mixed<0, true><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
+      k_dense_mixed<0, true, 1><<<grid, kMixThreads, 0, st>>>(p->dev, M, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_dense, st));
@@ -3068,7 +3300,6 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   if (!grad) return PES_OK;
   // node adjoints: phase systems here, transfer systems on the second stream;
   // then the backward node stage
-  cudaStream_t aux = p->mixed->aux;
   const double ws = 4.0 * p->dev.df;
   const dim3 sgrid(M.nblk_sparse, M.n_det, (unsigned)B);
   if (spline_seg(M.J) == 32) {

@@ -903,6 +903,39 @@ PES_HD void phenomhm_eval(const PhenomDCoef<T>& c, const PhenomHMCoef<T>& h, int
   tf = c.tscale * dpsi;
 }
 
+// Mode k's amplitude kink: where its amplitude stops being C2 with the
+// largest jump of the second derivative.  (2,2): PhenomD's f_peak
+// (amp_peak_jump).  k > 0: Mf = frA, where the mapped frequency reaches the
+// mode's f_peak and the amplitude map turns linear; with A = beta A0 F(f22),
+// F(y) = y^(-7/6) Ahat(y), the jump of d^2 A / dMf^2 divided by
+// beta A0 y^(-7/6) is Rholm^2 [Ahat''] - y''_left (Ahat' - 7/6 Ahat / y) (the
+// map is C1 there, its second derivative y''_left on the Hermite side, 0
+// on the linear one).  Out: the kink's Mf, Ahat there and that jump.
+template <class T>
+PES_HD void hm_kink(const PhenomDCoef<T>& c, const PhenomHMCoef<T>& h, int k, T& mf_pk, T& ahat_pk, T& jump) {
+  if (k == 0) {
+    mf_pk = c.fpeak;
+    amp_peak_jump<T>(c, ahat_pk, jump);
+    return;
+  }
+  const HMMode<T>& md = h.md[k];
+  const double m = kHMlm[k][1];
+  const T fp = md.fpeak, x = fp - c.fRD, a = md.g3fDMeff;
+  const T D = x * x + a * a;
+  const T A = c.g1 * a / D * dexp(-c.g2 * x / a);
+  const T L1 = -c.g2 / a - 2.0 * x / D;
+  const T L2 = -2.0 * (a * a - x * x) / (D * D);
+  const T d2m = A * (L1 * L1 + L2);
+  const T d2i = 2.0 * md.dl[2] + fp * (6.0 * md.dl[3] + 12.0 * md.dl[4] * fp);
+  const T hh = md.frA - md.fiA;
+  T ypp = lift<T>(0.0);
+  if (val(hh) > 0.0)  // the Hermite blend's second derivative at its right end
+    ypp = (6.0 * (2.0 / m) * md.fiA + 2.0 * (2.0 / m) * hh - 6.0 * md.Rholm * md.frA + 4.0 * md.Rholm * hh) / (hh * hh);
+  mf_pk = md.frA;
+  ahat_pk = A;
+  jump = md.Rholm * md.Rholm * (d2m - d2i) - ypp * (A * L1 - (7.0 / 6.0) * A / fp);
+}
+
 // The modes' coefficients from the (2,2) block c (already set up from th)
 // and the remnant spin af and radiated energy erad of that set-up.
 template <class T>

@@ -14,26 +14,6 @@ constexpr int kDenseThreads = 128;
 constexpr int kDenseBinsPerThread = 4;
 constexpr int kDenseBinsPerBlock = kDenseThreads * kDenseBinsPerThread;
 
-// IMRPhenomHM container of mode k at f, time-shifted by t_c as the reference
-// does (antenna.py:435-441): hp, hc times exp(-2 pi i f t_c), tf + t_c.
-// False when the mode is above its mapped Mf = 0.2.
-template <class T>
-__device__ __forceinline__ bool hm_mode_container(const SampleBlock<T>& b, const PhenomHMCoef<T>& h, int k, double f,
-                                                  const Cx<T>& ts, Cx<T>& hp, Cx<T>& hc, T& tft) {
-  const T Mf = b.wf.Msec * f;
-  T amp, psi, tf, f22;
-  phenomhm_eval<T>(b.wf, h, k, Mf, amp, psi, tf, &f22);
-  if (val(f22) > kMfCut) return false;
-  T s, c;
-  dsincos(psi, &s, &c);
-  // h_lm = amp e^{-i psi}; hp = P h_lm, hc = i C h_lm
-  const T ap = h.md[k].P * amp, ac = h.md[k].C * amp;
-  hp = cmul(cx(ap * c, -(ap * s)), ts);
-  hc = cmul(cx(ac * s, ac * c), ts);
-  tft = tf + b.tc;
-  return true;
-}
-
 // IMRPhenomHM: the six modes' links summed per detector (antenna.py:446-458),
 // then TDI; residual sum over detectors and channels.
 template <class T>

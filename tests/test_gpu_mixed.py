@@ -1,9 +1,9 @@
 """Mixed-precision plan (FP64 sparse grid + FP32 dense bulk) against the FP64 oracle.
 
-Bar: |dlnL| <= 1e-2 against the FP64 oracle.  For templates far louder than
-the data (|lnL| >> 1e6) the FP32 bulk leaves a random model error of ~1e-7
-per bin that sums to a few 1e-9 |lnL|, so the bar is applied to the median
-and each sample is bounded by 1e-2 + 1e-8 |lnL|.  Light
+Bar: |dlnL| <= 1e-2 against the FP64 oracle, for every sample.  The plan
+adds the splines' midpoint error back per bin and re-evaluates exactly the
+samples whose estimated FP32 rounding or remaining spline error could reach
+the bar (templates far louder than the data).  Light
 systems whose lowest bins lie decades before coalescence go through the exact
 FP64 bins of the mixed plan.  The gradient is the exact gradient of the
 interpolated model, checked against the oracle's forward-mode duals to 1e-3
@@ -46,8 +46,7 @@ def test_mixed_lnl_injection_perturbed(cuda_lib, oracle, dataset):
     err = np.abs(got - want)
     assert np.all(mixed.last_status.cpu().numpy() == 0)
     assert err[0] <= 1e-2  # the injection
-    assert np.median(err) <= 1e-2, err
-    assert np.all(err <= 1e-2 + 1e-8 * np.abs(want)), err
+    assert np.all(err <= 1e-2), err
     # deterministic forward
     assert np.array_equal(got, mixed.log_likelihood_batch(thetas).cpu().numpy())
 
@@ -69,9 +68,7 @@ def test_mixed_prior_batch_cutoff(cuda_lib, oracle, network):
     got = mixed.log_likelihood_batch(thetas).cpu().numpy()
     want = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(thetas, nthreads=8)
     err = np.abs(got - want)
-    assert np.median(err) <= 1e-2, np.sort(err)[-5:]
-    # FP32 floor of the dense stage: a few 1e-9 of |lnL| for templates far louder than the data
-    assert np.all(err <= 1e-2 + 1e-8 * np.abs(want)), np.sort(err)[-5:]
+    assert np.all(err <= 1e-2), np.sort(err)[-5:]
 
 
 def test_mixed_geocentric_network(cuda_lib, oracle, dataset):
@@ -85,7 +82,7 @@ def test_mixed_geocentric_network(cuda_lib, oracle, dataset):
     w_lnl, w_grad = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(
         thetas, grad=True, nthreads=8)
     err = np.abs(lnl.cpu().numpy() - w_lnl)
-    assert np.all(err <= 1e-2 + 1e-8 * np.abs(w_lnl)), err
+    assert np.all(err <= 1e-2), err
     norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
     assert np.max(np.abs(grad.cpu().numpy() - w_grad) / norm) < 1e-3
 
@@ -139,7 +136,7 @@ def test_mixed_other_grids(cuda_lib, oracle, dataset, n_sparse):
         thetas, grad=True, nthreads=8)
     err = np.abs(lnl.cpu().numpy() - w_lnl)
     tol = 1e-2 if n_sparse >= 1024 else 5e-2  # spline error grows as (node spacing)^4
-    assert np.all(err <= tol + 1e-8 * np.abs(w_lnl)), err
+    assert np.all(err <= tol), err
     norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
     assert np.max(np.abs(grad.cpu().numpy() - w_grad) / norm) < 1e-3
 
@@ -172,8 +169,7 @@ def test_mixed_tdi2_prefactor_zero(cuda_lib, oracle):
     double zero at f L = 1/2 (0.06 Hz), where the PSD vanishes too.  The mixed
     plan keeps that factor out of its splines and applies it per bin (with the
     factor inside the splines the errors near 0.06 Hz reached |dlnL| ~ 100).
-    Over this three-decade band 1024 nodes leave a spline floor of ~1.5e-8
-    |lnL| for loud heavy templates (seen in FP64 emulation too), hence 2e-8."""
+    Every sample within 1e-2 of the oracle."""
     from pespace_gb300.inference import WhittleLikelihood
 
     grid = (2.0 ** 16, 5.0, 1e-4, 0.1)
@@ -186,8 +182,7 @@ def test_mixed_tdi2_prefactor_zero(cuda_lib, oracle):
     got = eng.log_likelihood_batch(thetas).cpu().numpy()
     want = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(thetas, nthreads=8)
     err = np.abs(got - want)
-    assert np.median(err) <= 1e-2, np.sort(err)[-5:]
-    assert np.all(err <= 1e-2 + 2e-8 * np.abs(want)), np.sort(err)[-5:]
+    assert np.all(err <= 1e-2), np.sort(err)[-5:]
 
 
 def test_mixed_edge_cases_and_status(cuda_lib, oracle, dataset):
@@ -223,7 +218,7 @@ def test_mixed_edge_cases_and_status(cuda_lib, oracle, dataset):
         got = sub.log_likelihood_batch(thetas).cpu().numpy()
         plan = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets[:1]], 1e-4, channels=chans)
         want = plan.lnl(thetas)
-        assert np.all(np.abs(got - want) <= 1e-2 + 1e-8 * np.abs(want)), (chans, got - want)
+        assert np.all(np.abs(got - want) <= 1e-2), (chans, got - want)
 
 
 def test_launch_options_and_autotune(cuda_lib, oracle, dataset):

@@ -130,3 +130,62 @@ def test_hm_container_and_six_mode_response(cuda_lib, oracle):
         got = links.cpu().numpy()
         scale = np.sum(np.abs(want), axis=0) + 1e-300
         assert np.max(np.abs(got - want) / scale) < 1e-13
+
+
+def test_hm_mixed_plan(cuda_lib, oracle, dataset):
+    """The mixed plan with the six modes as virtual samples (per-mode sparse
+    splines, kinks, anchors and midpoint corrections; the modes summed per bin
+    before the residual) against the oracle on the two-detector network:
+    |dlnL| <= 1e-2 at the injection, at perturbed points and at prior draws
+    with the cut at 1.2 times the largest ringdown frequency.  The mixed
+    gradient is refused for IMRPhenomHM (the FP64 plan gives it)."""
+    from pespace_gb300 import _lib
+    from pespace_gb300.inference import WhittleLikelihood
+
+    g, dets, th0 = dataset
+    rng = np.random.default_rng(17)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(5)] + list(random_prior_theta(rng, 10, th0[10])))
+    mixed = WhittleLikelihood(cuda_detectors(g, dets), precision="mixed", reference_frequency=1e-4,
+                              approximant="IMRPhenomHM", max_batch=16, cut_factor=1.2)
+    got = mixed.log_likelihood_batch(thetas).cpu().numpy()
+    assert np.all(mixed.last_status.cpu().numpy() == 0)
+    want = oracle_plan(oracle, g, dets, cut_factor=1.2).lnl(thetas, nthreads=8)
+    err = np.abs(got - want)
+    assert np.all(err <= 1e-2), (err, want)
+    assert np.array_equal(got, mixed.log_likelihood_batch(thetas).cpu().numpy())  # deterministic
+    with pytest.raises(_lib.PesError):
+        mixed.log_likelihood_and_grad(thetas[:2])
+
+
+def test_hm_mixed_model(cuda_lib, oracle, dataset):
+    """The mixed plan's dense six-mode model per bin against the oracle's:
+    within 1e-5 of the per-bin response scale (FP32 dense stage)."""
+    from pespace_gb300.inference import WhittleLikelihood
+
+    g, dets, th0 = dataset
+    eng = WhittleLikelihood(cuda_detectors(g, dets), precision="mixed", reference_frequency=1e-4,
+                            approximant="IMRPhenomHM", max_batch=2)
+    plan = oracle_plan(oracle, g, dets)
+    for d in range(2):
+        got = eng.model_tdi(th0, det=d).cpu().numpy()
+        want = plan.model_tdi(d, th0)
+        mag = np.sqrt(np.sum(np.abs(want) ** 2, axis=0))
+        live = mag > 1e-6 * mag.max()
+        assert np.max(np.abs(got - want)[:, live] / mag[live]) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_hm_fisher(cuda_lib, oracle, dataset, precision):
+    """IMRPhenomHM Fisher matrices (FP64 duals through the six modes, for FP64
+    and mixed plans) against the oracle's dual-number Fisher."""
+    from pespace_gb300.inference import WhittleLikelihood
+
+    g, dets, th0 = dataset
+    rng = np.random.default_rng(9)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(2)])
+    eng = WhittleLikelihood(cuda_detectors(g, dets), precision=precision, reference_frequency=1e-4,
+                            approximant="IMRPhenomHM", cut_factor=1.2, max_batch=4)
+    got = eng.fisher_matrix(thetas).cpu().numpy()
+    want = oracle_plan(oracle, g, dets, cut_factor=1.2).fisher(thetas)
+    s = np.sqrt(np.einsum("bii->bi", want))
+    assert np.max(np.abs(got - want) / (s[:, :, None] * s[:, None, :])) < 1e-9
