@@ -18,6 +18,11 @@ parameters copied from pinned host memory and lnL/gradient copied back.
     python bench.py --impl reference   # the reference's CPU path (oracle port)
     python bench.py --workload ref-shape   # the reference's published benchmark shape
     python bench.py --workload td-tdi      # time-domain TDI combination (own metric)
+    python bench.py --workload network-hm  # the higher-mode network configuration alone
+
+The default run also times the higher-mode network configuration (IMRPhenomHM,
+LISA + Taiji + TianQin, T = 2^25 s, 4096 samples, lnL through one CUDA graph)
+and reports it under "network_hm" (N = 1 only; --no-network-hm skips it).
 
 Multi-GPU (torchrun): replicas; every rank evaluates its own 1024 samples
 (weak scaling); rank 0 prints the line with the max-over-ranks step time.
@@ -50,11 +55,18 @@ WORKLOADS = {
     "network-d": (2.0 ** 25, 4.0, 3e-5, 0.1, "1.5",
                   "network-d: prior batch, LISA + Taiji + TianQin TDI1.5 AET, T=2^25 s, dt=4 s, 3354437 bins "
                   "per channel (9 channels), 2048 sparse nodes, cutoff 1.2 f_RD, IMRPhenomD (2,2)"),
+    # the higher-mode configuration: IMRPhenomHM on the three-detector network, lnL only,
+    # 4096 samples through one CUDA graph
+    "network-hm": (2.0 ** 25, 4.0, 3e-5, 0.1, "1.5",
+                   "network-hm: 4096-sample prior batch, IMRPhenomHM (6 modes), LISA + Taiji + TianQin TDI1.5 AET, "
+                   "T=2^25 s, dt=4 s, 3354437 bins per channel (9 channels), 2048 sparse nodes per mode, "
+                   "cutoff 1.2 f_RD of the highest mode, mixed precision, CUDA graph"),
     # time-domain TDI combination of six single-link series (no likelihood): its own metric
     "td-tdi": (2.0 ** 25, 4.0, None, None, "2.0",
                "td-tdi: LISA TDI2.0 AET from six single-link time series, T=2^25 s, dt=4 s, 8388609 samples"),
 }
-N_SPARSE = {"network-d": 2048}
+N_SPARSE = {"network-d": 2048, "network-hm": 2048}
+HM_METRIC = "lnL evals/s, 4096 MBHB samples, IMRPhenomHM 3-detector network, 1 GB300 (mixed, CUDA graph)"
 TD_METRIC = "TD TDI output samples/s (A/E/T from six single-link series), 1 GB300"
 LISA_ARM_M = 2.5e9
 C_SI = 299792458.0
@@ -73,6 +85,7 @@ def parse():
                     choices=["mixed", "fp64"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-network-hm", action="store_true", help="skip the higher-mode network leg")
     ap.add_argument("--workload", default="adjoint", choices=sorted(WORKLOADS))
     ap.add_argument("--n-sparse", type=int, default=None, help="sparse nodes of the mixed plan (default per workload)")
     args = ap.parse_args()
@@ -197,9 +210,11 @@ def cpu_baseline_run(n_samples, threads, precision_note, grad=True, batch=None):
     oracle.build()
     g = oracle.grid(DUR, DT, FMIN, FMAX)
     th0 = config0_theta(DUR - 86400.0)
-    # the workload's detectors: LISA, or LISA + Taiji + TianQin for network-d (seeded noise per detector)
+    # the workload's detectors: LISA, or LISA + Taiji + TianQin for the network
+    # workloads (seeded noise per detector); IMRPhenomHM for network-hm
+    approx = "IMRPhenomHM" if WORKLOAD.startswith("network-hm") else "IMRPhenomD"
     specs = [(oracle.heliocentric(2.5e9, 0.0, -math.pi / 9), "LISA_SciRDv1")]
-    if WORKLOAD.startswith("network-d"):
+    if WORKLOAD.startswith("network"):
         specs += [(oracle.heliocentric(3.0e9, 0.0, math.pi / 9), "Taiji_TDC"),
                   (oracle.geocentric(math.sqrt(3.0) * 1e8), "Tianqin_GWSpace")]
     dets = []
@@ -207,11 +222,16 @@ def cpu_baseline_run(n_samples, threads, precision_note, grad=True, batch=None):
         psd = oracle.psd(g["freqs"], "AET", False, GEN, **oracle.PSD_PRESETS[model])
         noise = oracle.noise_realization(g, psd, "AET", 2026 + k)
         dets.append((orb, GEN, np.stack([noise[c] for c in "AET"]), np.stack([psd[c] for c in "AET"])))
-    plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2)
+    plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2, approximant=approx)
     dets = [(orb, gen, data + plan.model_tdi(k, th0), psd_arr) for k, (orb, gen, data, psd_arr) in enumerate(dets)]
-    plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2)
+    plan = oracle.Plan(g, dets, 1e-4, cut_factor=1.2, approximant=approx)
     batch = BATCH if batch is None else batch
-    thetas = rank_theta(0, batch, th0[10])[stratified(batch, n_samples)]
+    if approx == "IMRPhenomHM":  # the GPU leg's batch (its own seed)
+        from pespace_gb300.workloads import prior_samples
+
+        thetas = prior_samples(np.random.default_rng(2027), batch, th0[10])[stratified(batch, n_samples)]
+    else:
+        thetas = rank_theta(0, batch, th0[10])[stratified(batch, n_samples)]
     t0 = time.perf_counter()
     plan.lnl(thetas, grad=grad, nthreads=threads)
     dt = time.perf_counter() - t0
@@ -241,6 +261,26 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     B = args.batch
+    if args.workload == "network-hm":
+        # lnL only (as the GPU leg), a few samples of its 4096 spread over the batch:
+        # each is about a minute of FP64 work per core over 3 x 3.35 M bins x 6 modes
+        B, n = 4096, max(2, threads // 4)
+        rates = []
+        for _ in range(args.warmup):
+            cpu_baseline_run(n, threads, "", grad=False, batch=B)
+        for _ in range(args.steps):
+            rates.append(cpu_baseline_run(n, threads, "", grad=False, batch=B)[0])
+        v = float(np.mean(rates))
+        line = {"impl": "reference", "metric": HM_METRIC, "value": v, "unit": "lnL evals/s", "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "batch": B},
+                "cpu_baseline": {"value": v, "unit": "lnL evals/s", "cores": threads, "kind": "port",
+                                 "sample": f"{n} of the {B} seeded samples per step (evenly spread over the batch), "
+                                           "full grid, FP64 dense IMRPhenomHM, OpenMP over samples"},
+                "e2e": {"value": v, "unit": "lnL evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     # a bounded sample of the GPU arm's seeded batch, spread evenly over it:
     # 64 of the 1024 samples (every 16th); network-d (three detectors, 3.35 M
     # bins each, about 9 s of FP64 work per sample and core) a quarter of the cores
@@ -411,6 +451,114 @@ def run_td_tdi(args):
         v, done, dt = td_cpu_baseline(arm)
         line["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": 1, "kind": "port",
                                 "sample": f"{done} output samples in 2^20-sample blocks ({dt:.1f} s, numpy)"}
+    print(json.dumps(line), flush=True)
+
+
+def network_hm_leg(steps, warmup, batch=4096, max_batch=512, check=16):
+    """The higher-mode network configuration on this GPU: the mixed IMRPhenomHM
+    plan over ``batch`` prior samples (chunks of ``max_batch``) captured in one
+    CUDA graph; lnL only.  Returns the measurements as a dict."""
+    import torch
+
+    from pespace_gb300 import _lib
+    from pespace_gb300.inference import CapturedStep, WhittleLikelihood
+    from pespace_gb300.workloads import config0_theta, network_dataset, prior_samples
+
+    T, dt, fmin, fmax, gen, desc = WORKLOADS["network-hm"]
+    th0 = config0_theta(T - 86400.0)
+    dets = network_dataset(T, dt, fmin, fmax, th0, gen, seed=2026, approximant="IMRPhenomHM")
+    eng = WhittleLikelihood(dets, precision="mixed", approximant="IMRPhenomHM", reference_frequency=1e-4,
+                            cut_factor=1.2, max_batch=max_batch, n_sparse=N_SPARSE["network-hm"])
+    theta_host = torch.as_tensor(prior_samples(np.random.default_rng(2027), batch, th0[10])).pin_memory()
+    theta = theta_host.to("cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    lib = _lib.load()
+    # one profiled (uncaptured) pass: launches and device time per kernel class, work units
+    eng.log_likelihood_batch(theta)
+    torch.cuda.synchronize()
+    n_cls = _lib.KERNEL_CLASSES
+    import ctypes
+
+    launches, dev_ms = (ctypes.c_int64 * n_cls)(), (ctypes.c_double * n_cls)()
+    lib.pes_plan_profile(eng._plan, 1)
+    lib.pes_plan_stats(eng._plan, launches, dev_ms)
+    work = {"dense_bins": 0, "fp64_bins": 0, "sparse_nodes": 0, "samples": 0}
+    for lo in range(0, batch, max_batch):
+        eng.log_likelihood_batch(theta[lo:lo + max_batch])
+        for k, v in eng.last_work(min(max_batch, batch - lo)).items():
+            work[k] += v
+    torch.cuda.synchronize()
+    lib.pes_plan_stats(eng._plan, launches, dev_ms)
+    lib.pes_plan_profile(eng._plan, 0)
+    kern = {lib.pes_kernel_class_name(k).decode(): {"launches": int(launches[k]), "ms": float(dev_ms[k])}
+            for k in range(n_cls) if launches[k]}
+    step = CapturedStep(eng, batch, grad=False)
+    for _ in range(max(3, warmup)):
+        step(theta)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    ms = []
+    with clocks:
+        for _ in range(steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            step.graph.replay()
+            e.record()
+            e.synchronize()
+            ms.append(s.elapsed_time(e))
+    mean_ms = float(np.mean(ms))
+    # end to end: parameters from pinned host memory, lnL back to the host
+    lnl_host = torch.empty(batch, dtype=torch.float64).pin_memory()
+    e2e = []
+    for _ in range(steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        step.theta.copy_(theta_host, non_blocking=True)
+        step.graph.replay()
+        lnl_host.copy_(step.lnl, non_blocking=True)
+        e.record()
+        e.synchronize()
+        e2e.append(s.elapsed_time(e))
+    got = step.lnl.clone()
+    ok = int((step.status == 0).sum().item())
+    del step, flush
+    # accuracy and speed of the FP64 plan on an evenly spread subset
+    idx = torch.as_tensor(stratified(batch, check), device="cuda")
+    ref = WhittleLikelihood(dets, precision="fp64", approximant="IMRPhenomHM", reference_frequency=1e-4,
+                            cut_factor=1.2, max_batch=len(idx))
+    sub = theta[idx]
+    want = ref.log_likelihood_batch(sub)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    ref.log_likelihood_batch(sub)
+    e.record()
+    e.synchronize()
+    ms64 = s.elapsed_time(e)
+    d = (got[idx] - want).abs()
+    return {"metric": HM_METRIC, "value": batch / (mean_ms / 1e3), "unit": "lnL evals/s", "steps": steps,
+            "warmup": max(3, warmup), "ms_per_step": mean_ms, "dtype": "f32+f64",
+            "config": {"workload": desc, "batch": batch, "max_batch": max_batch, "nbins": int(eng.desc.nbins),
+                       "detectors": 3, "modes": 6},
+            "l2": "flushed between steps (512 MB write outside the timed events)",
+            "e2e": {"value": batch / (float(np.mean(e2e)) / 1e3), "unit": "lnL evals/s",
+                    "h2d_bytes_per_step": batch * 11 * 8, "d2h_bytes_per_step": batch * 8},
+            "samples_ok": ok, "kernels": kern, "work_per_step": work,
+            "dense_bins_per_s": (work["dense_bins"] + work["fp64_bins"]) / (mean_ms / 1e3),
+            "fp64_gpu": {"value": len(idx) / (ms64 / 1e3), "unit": "lnL evals/s", "samples": len(idx),
+                         "ms": ms64},
+            "vs_fp64": (batch / (mean_ms / 1e3)) / (len(idx) / (ms64 / 1e3)),
+            "dlnl_vs_fp64": {"samples": len(idx), "max_abs": float(d.max().item()),
+                             "n_within_1e-2": int((d <= 1e-2).sum().item())},
+            "clocks": clocks.summary()}
+
+
+def run_network_hm(args):
+    line = network_hm_leg(args.steps, args.warmup)
+    line.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "data": "synthetic", "gpu_launches": sum(v["launches"] for v in line["kernels"].values())})
     print(json.dumps(line), flush=True)
 
 
@@ -613,6 +761,10 @@ def run_native(args):
             line["cpu_baseline_1core_lnl"] = {"value": v1, "unit": "lnL evals/s", "cores": 1, "kind": "port",
                                               "sample": f"{n1} of the {B} samples, full grid, FP64 dense "
                                                         f"({dt1:.1f} s)"}
+        if world == 1 and not args.no_network_hm and args.workload == "adjoint":
+            del eng
+            torch.cuda.empty_cache()
+            line["network_hm"] = network_hm_leg(3, 3)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -624,6 +776,8 @@ def main():
         run_reference(args)
     elif args.workload == "td-tdi":
         run_td_tdi(args)
+    elif args.workload == "network-hm":
+        run_network_hm(args)
     else:
         run_native(args)
 

@@ -308,13 +308,14 @@ class CapturedStep:
     The graph is recorded once on fixed device buffers (``theta``, ``lnl``,
     ``grad``, ``status``); ``__call__`` copies new parameters into ``theta``
     and replays it, which removes the per-launch host cost of the kernels and
-    event waits of a call.  The engine's measurement hooks must be off while
-    capturing.
+    event waits of a call.  A batch larger than the engine's ``max_batch``
+    is captured as consecutive calls of ``max_batch`` samples.  The engine's
+    measurement hooks must be off while capturing.
     """
 
     def __init__(self, engine, batch, grad=True):
-        if batch < 1 or batch > engine.max_batch:
-            raise ValueError(f"batch must be 1..{engine.max_batch}, got {batch}")
+        if batch < 1:
+            raise ValueError(f"batch must be at least 1, got {batch}")
         self.engine, self.batch, self.with_grad = engine, int(batch), bool(grad)
         dev = torch.device("cuda")
         self.theta = torch.zeros((batch, 11), dtype=torch.float64, device=dev)
@@ -333,13 +334,16 @@ class CapturedStep:
 
     def _launch(self):
         lib = _lib.load()
-        if self.with_grad:
-            rc = lib.pes_lnl_grad_batch(self.engine._plan, _lib.ptr(self.theta), self.batch, _lib.ptr(self.lnl),
-                                        _lib.ptr(self.grad), _lib.ptr(self.status), _lib.stream_handle())
-        else:
-            rc = lib.pes_lnl_batch(self.engine._plan, _lib.ptr(self.theta), self.batch, _lib.ptr(self.lnl),
-                                   _lib.ptr(self.status), _lib.stream_handle())
-        _lib.check(rc)
+        for lo in range(0, self.batch, self.engine.max_batch):
+            hi = min(self.batch, lo + self.engine.max_batch)
+            th, ln, st = self.theta[lo:hi], self.lnl[lo:hi], self.status[lo:hi]
+            if self.with_grad:
+                rc = lib.pes_lnl_grad_batch(self.engine._plan, _lib.ptr(th), hi - lo, _lib.ptr(ln),
+                                            _lib.ptr(self.grad[lo:hi]), _lib.ptr(st), _lib.stream_handle())
+            else:
+                rc = lib.pes_lnl_batch(self.engine._plan, _lib.ptr(th), hi - lo, _lib.ptr(ln), _lib.ptr(st),
+                                       _lib.stream_handle())
+            _lib.check(rc)
 
     def __call__(self, theta):
         """Replay on new parameters (B, 11); returns lnL (and the gradient) views of the graph's buffers."""

@@ -64,16 +64,18 @@ def lisa_dataset(duration, delta_time, fmin, fmax, theta_inj, generation="1.5", 
     return det
 
 
-def network_dataset(duration, delta_time, fmin, fmax, theta_inj, generation="1.5", seed=2026, f_ref=1e-4):
-    """Three-detector network of the higher-mode benchmark configuration, with
-    the (2,2)-mode IMRPhenomD injection: LISA-like (2.5e9 m, trailing 20 deg),
-    Taiji-like (3e9 m, leading 20 deg; OMS 8e-12, acceleration 3e-15) and
-    TianQin-like geocentric (sqrt(3) 1e8 m; OMS 1e-12, acceleration 1e-15);
-    seeded noise per detector (seed, seed + 1, seed + 2)."""
+def network_dataset(duration, delta_time, fmin, fmax, theta_inj, generation="1.5", seed=2026, f_ref=1e-4,
+                    approximant="IMRPhenomD"):
+    """Three-detector network of the higher-mode benchmark configuration:
+    LISA-like (2.5e9 m, trailing 20 deg), Taiji-like (3e9 m, leading 20 deg;
+    OMS 8e-12, acceleration 3e-15) and TianQin-like geocentric (sqrt(3) 1e8 m;
+    OMS 1e-12, acceleration 1e-15); seeded noise per detector (seed, seed + 1,
+    seed + 2) plus the injection of ``approximant`` (IMRPhenomD's (2,2) mode,
+    or the six IMRPhenomHM modes)."""
     from .detector.antenna import FDResponseModelMarset2018, InterferometerAntenna
     from .detector.orbit import KaplerianHeliocentric, KeplerianGeocentric
     from .detector.tdi import FDMichelsonConstantEqualArm, TDIChannelData
-    from .waveform import IMRPhenomD
+    from .waveform import IMRPhenomD, IMRPhenomHM
 
     specs = [("LISA", KaplerianHeliocentric(2.5e9, 0.0, -PI / 9), "LISA_SciRDv1"),
              ("Taiji", KaplerianHeliocentric(3.0e9, 0.0, PI / 9), "Taiji_TDC"),
@@ -87,7 +89,7 @@ def network_dataset(duration, delta_time, fmin, fmax, theta_inj, generation="1.5
         det = InterferometerAntenna(name, td, orbit, FDResponseModelMarset2018(),
                                     FDMichelsonConstantEqualArm(generation, True))
         td.add_into_fd_data(td.get_fd_noise_realization(seed=seed + k))
-        wf = IMRPhenomD(td.data_info.frequency_samples_array, f_ref)
+        wf = (IMRPhenomHM if approximant == "IMRPhenomHM" else IMRPhenomD)(td.data_info.frequency_samples_array, f_ref)
         det.inject_signal(wf.from_theta(th), th[6], math.asin(th[7]), th[8], th[10])
         dets.append(det)
     return tuple(dets)

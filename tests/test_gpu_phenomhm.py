@@ -159,7 +159,8 @@ def test_hm_mixed_plan(cuda_lib, oracle, dataset):
 
 def test_hm_mixed_model(cuda_lib, oracle, dataset):
     """The mixed plan's dense six-mode model per bin against the oracle's:
-    within 1e-5 of the per-bin response scale (FP32 dense stage)."""
+    within 3e-5 of the per-bin response scale (six modes, each with its FP32
+    phase and transfer rounding, summed in FP32)."""
     from pespace_gb300.inference import WhittleLikelihood
 
     g, dets, th0 = dataset
@@ -171,7 +172,7 @@ def test_hm_mixed_model(cuda_lib, oracle, dataset):
         want = plan.model_tdi(d, th0)
         mag = np.sqrt(np.sum(np.abs(want) ** 2, axis=0))
         live = mag > 1e-6 * mag.max()
-        assert np.max(np.abs(got - want)[:, live] / mag[live]) < 1e-5
+        assert np.max(np.abs(got - want)[:, live] / mag[live]) < 3e-5
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
