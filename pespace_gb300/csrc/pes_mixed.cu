@@ -67,6 +67,12 @@ struct MixedDev {
   int32_t n_modes;          // 1 (IMRPhenomD) or kHMModes (IMRPhenomHM)
   const PhenomHMCoef<double>* hm;  // [B] the samples' mode coefficients (IMRPhenomHM plans), else null
   int32_t* vcut;            // [B * n_modes] first bin past the mode's range (its mapped Mf = 0.2, or kcut)
+  // Multi-mode plans: each mode's phase is only C1 at its two phase-map
+  // corners (Mf = fiP, frP).  The jump of d^2 Psi / dMf^2 there, as
+  // Jh max(0, Mf - Mf_c)^2 (Jh half the jump), is removed from the node and
+  // midpoint phases before the fit and added back by the run anchors (runs
+  // past the corner) or per bin (the run that straddles it).
+  float4* pkink;            // [B * n_modes][2] per corner: Mf_c (hi, lo), Jh (hi, lo); null for one mode
   int32_t nchunks;
   int32_t n_det;
   int32_t nblk_dense;
@@ -124,7 +130,8 @@ struct MixedDev {
   float4* cg;
   float* mom;               // [B][n_det][J][7][4] adjoint moments (FP32 warp sums, FP32 atomics)
   float* ybar;              // [B][n_det][J][7] node adjoints (FP32: the derivative passes run in FP32)
-  double* part;             // [B][nblk_dense][2] partials: sum |d - h|^2 w (direct form), sum -2 Re(d^* h) w
+  double* part;             // [B][nblk_dense][3] partials: sum |d - h|^2 w (direct form), sum -2 Re(d^* h) w,
+                            //   sum 2 Re sum_{k<l} h_k conj(h_l) w (the modes' cross terms; 0 for one mode)
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
   double* gdir;             // [B][n_det] direct t_c term of the gradient
@@ -133,7 +140,8 @@ struct MixedDev {
   // node data before the spline fit and added back per bin.
   double* kinkR;            // [B][n_det][6] R_q
   double* kinkC;            // [B][n_det][6] C_q
-  float* kinkF;             // [B][n_det][16] Msec f_step, -, C_0..C_5 as float-float (hi x6, lo x6), -, -
+  float* kinkF;             // [B][n_det][16] Msec f_step, -, C_0..C_5 as float-float (hi x6, lo x6), the
+                            //   interval holding the kink point (multi-mode plans, else -1), -
   float* kinkM;             // [B][n_det][12] dense adjoint moments: sum A_q x^2, sum A_q x
   // The split form of the dense sum, sum |d - h|^2 w = sum |d|^2 w - 2 Re sum d^* h w
   // + sum |h|^2 w, for templates far from the data: |d|^2 w from FP64 suffix
@@ -160,11 +168,18 @@ struct MixedDev {
   // The splines' error at the midpoints, added back per bin with the shape of
   // the leading error term of cubic interpolation:
   float4* cbump;            // [B][n_det][J][2] delta_0..delta_5, h, 4 / h^2
+  // Intervals whose weight |P|^2 / S spikes (a TDI zero where the PSD's own
+  // zero does not cancel the prefactor's exactly, e.g. f L = 1 at the top of
+  // a 0.1 Hz band): there the midpoint value says nothing about the error at
+  // the few bins that carry the weight, so neither the correction nor the
+  // split form's error estimate uses it.
+  const int32_t* wspike;    // [n_det][J] 1 where max_bin W > kSpikeRatio x mean W over the interval
   int32_t rblocks;          // blocks per sample of the exact re-evaluation
   int32_t rpad;
   double* rpart;            // [B][rblocks] exact dense-range partials of re-evaluated samples
 };
 constexpr int kHdOut = 6;
+constexpr double kSpikeRatio = 8.0;
 constexpr int kMomStride = 42;  // doubles per bin (and interval) of wmom / wtot
 constexpr int kRefineBlocks = 32;  // blocks per sample of the exact re-evaluation
 
@@ -195,7 +210,7 @@ struct MixedBuffers {
   // memory when they exceed half of L2 (they then stream from DRAM)
   bool stage_grad = false;
   cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr, ev_hd = nullptr, ev_pfit = nullptr,
-              ev_kink = nullptr;
+              ev_kink = nullptr, ev_xgrad = nullptr;
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -367,6 +382,20 @@ __global__ void k_kink(PlanDev P, MixedDev M, GenArg G, const SampleBlock<double
     node_eval_mode<false, double>(P.orbit[d], M.scale, b, hm, k, D, cx(1.0, 0.0), fpk, y);
   }
   F[0] = (float)(b.wf.Msec * P.f_step);
+  F[14] = -1.0f;
+  if (hm) {
+    // Multi-mode plans carry the kink term in the coefficients of the
+    // intervals past the kink point (k_bump): far past the peak C x^2 grows
+    // to tens of times the mode's peak amplitude, and adding it back per bin
+    // in FP32 lost 1e-5 of the peak model.  Only the interval holding the
+    // kink point adds it per bin; its index in F[14].
+    int a = 0, z = M.J - 2;  // last interval starting at or below the kink point
+    while (a < z) {
+      const int mid = (a + z + 1) >> 1;
+      if (b.wf.Msec * M.node_f[mid] <= mf_pk) a = mid; else z = mid - 1;
+    }
+    F[14] = (float)a;
+  }
   for (int q = 0; q < 6; ++q) {
     R[q] = y[1 + q] / ahat;
     C[q] = 0.5 * jump * R[q];
@@ -406,7 +435,16 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse_fwd(PlanDev P, MixedD
     node_eval_mode<false, FF>(M.orbit_ff[d], M.scale_ff, sbf, M.hm ? &hmf : nullptr, k, D, D, ff_make(fn.x, fn.y),
                               y);
     const float4 pk = M.sff[2 * v + 1];  // the model's (mode's) amplitude kink point, Mf
-    const FF xk = sbf.wf.Msec * ff_make(fn.x, fn.y) - ff_make(pk.x, pk.y);
+    const FF mff = sbf.wf.Msec * ff_make(fn.x, fn.y);
+    const FF xk = mff - ff_make(pk.x, pk.y);
+    if (M.pkink) {  // the phase's corner terms
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float4 q = M.pkink[2 * v + c];
+        const FF xc = mff - ff_make(q.x, q.y);
+        if (xc.hi > 0.0f) y[0] = y[0] - ff_make(q.z, q.w) * (xc * xc);
+      }
+    }
     if (xk.hi > 0.0f) {
       const double* C = M.kinkC + vd * 6;
       const FF x2 = xk * xk;
@@ -717,6 +755,30 @@ __global__ void k_mixed_ranges(PlanDev P, MixedDev M, const SampleBlock<double>*
       kc = lo;
     }
     M.vcut[t] = (int32_t)kc;
+    if (M.pkink) {
+      // the phase's second-derivative jumps at the mode's phase-map corners:
+      // one-sided second differences of dPsi/dMf, 1e-6 of Mf_c apart
+      float4* pk = M.pkink + 2 * t;
+      for (int c = 0; c < 2; ++c) {
+        double jh = 0.0, mfc = 1.0;
+        if (b.status == kSampleOk && hm) {
+          const HMMode<double>& md = hm->md[kmode];
+          const int m = kHMlm[kmode][1];
+          mfc = c == 0 ? md.fiP : md.frP;
+          const double e = 1e-6 * mfc;
+          auto dps = [&](double x) {
+            double ps, dp;
+            hm_phase<double>(b.wf, md, m, x, ps, dp);
+            return dp;
+          };
+          const double right = (dps(mfc + 2.0 * e) - dps(mfc + e)) / e;
+          const double left = (dps(mfc - e) - dps(mfc - 2.0 * e)) / e;
+          jh = 0.5 * (right - left);
+        }
+        const FF a = ff_from(mfc), q = ff_from(jh);
+        pk[c] = make_float4(a.hi, a.lo, q.hi, q.lo);
+      }
+    }
   }
   int ns = 0, nc = 0, xb = 0;
   if (kc > 0) {
@@ -1925,6 +1987,7 @@ struct RunPhase {
   float p1h, p1l;         // per-bin increment (wrapped), head/tail
   float p2h, p2l;         // quadratic coefficient, head/tail
   float p3h, p3l;         // cubic coefficient, head/tail
+  float qx0, qj;          // multi-mode plans: the straddled phase corner (Msec f - Mf_c at the run start, Jh)
 };
 
 // Per-run phase anchors in FP64, one thread per (sample, detector, run) with a
@@ -1949,10 +2012,30 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   const FF fbf = ff_mulf(M.fstep_ff, (float)(P.k0 + kb));  // k0 + kb < 2^24: exact in FP32
   const FF t = fbf - ff_make(nfj.x, nfj.y);
   const FF ddt = dd * t;
-  const FF S0 = a + t * (b + t * (cc + ddt));
-  const FF S1 = b + t * (ff_mulf(cc, 2.0f) + ff_mulf(ddt, 3.0f));
-  const FF S2 = cc + ff_mulf(ddt, 3.0f);
+  FF S0 = a + t * (b + t * (cc + ddt));
+  FF S1 = b + t * (ff_mulf(cc, 2.0f) + ff_mulf(ddt, 3.0f));
+  FF S2 = cc + ff_mulf(ddt, 3.0f);
   const FF D = M.fstep_ff;
+  float qx0 = 0.0f, qj = 0.0f;  // the corner that the run straddles (added per bin)
+  if (M.pkink) {
+    // the phase's corner terms Jh (Msec f - Mf_c)^2: value, slope and
+    // curvature at the run start for runs past the corner
+    const FF mfb = msf * fbf;
+    const float last = (float)(M.ch_len[c] - 1) * (msf * D).hi;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float4 k4 = M.pkink[2 * s + q];
+      const FF xq = mfb - ff_make(k4.x, k4.y), jq = ff_make(k4.z, k4.w);
+      if (xq.hi >= 0.0f) {
+        S0 = S0 + jq * (xq * xq);
+        S1 = S1 + ff_mulf(jq * (xq * msf), 2.0f);
+        S2 = S2 + jq * (msf * msf);
+      } else if (xq.hi + last > 0.0f) {
+        qx0 = xq.hi;
+        qj = jq.hi;
+      }
+    }
+  }
   // anchored phase S0 + 2 pi f t_c.  f t_c reaches 1e6 cycles; its fraction is
   // (k0 + kb) frac(f_step t_c) mod 1, taken exactly in 64-bit integers and
   // read out as two 23-bit floats; the sum is wrapped in float-float (FP64
@@ -1984,7 +2067,7 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   float4* o = M.runs + (sd * M.nchunks + c) * 3;
   o[0] = make_float4(x0, fmaf(-s0f, l0, c0f), fmaf(c0f, l0, s0f), p1h);
   o[1] = make_float4(p1l, p2h, p2l, p3h);
-  o[2] = make_float4(p3l, 0.0f, 0.0f, 0.0f);
+  o[2] = make_float4(p3l, qx0, qj, 0.0f);
 }
 
 // Warp-sum of the 28 per-lane interval moments through shared memory (rows
@@ -2072,8 +2155,41 @@ __global__ void k_bump(MixedDev M, const SampleBlock<double>* __restrict__ block
     dl[2 * ch] = (float)(gr * cs + gi * sn - sp[0]);
     dl[2 * ch + 1] = (float)(gi * cs - gr * sn - sp[1]);
   }
+  if (M.wspike[(size_t)(sd % M.n_det) * M.J + j]) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) dl[q] = 0.0f;
+  }
   out[0] = make_float4(dl[0], dl[1], dl[2], dl[3]);
   out[1] = make_float4(dl[4], dl[5], (float)h, (float)(4.0 / (h * h)));
+  if (M.n_modes > 1) {
+    // the kink term C_q (X0 + Msec t)^2 of an interval past the kink point,
+    // X0 = Msec f_j - Mf_kink >= 0, folded into its coefficients (FP64 sums,
+    // value and slope kept as float-float)
+    const SampleBlock<double>& b = blocks[v / M.n_modes];
+    const float4 pk = M.sff[2 * v + 1];
+    const double X0 = b.wf.Msec * M.node_f[j] - ff_to(ff_make(pk.x, pk.y));
+    const int jk = (int)M.kinkF[(size_t)sd * 16 + 14];  // the interval holding the kink point
+    if (jk >= 0 && j > jk) {
+      const double* KC = M.kinkC + (size_t)sd * 6;
+      float4* cgw = M.cg + (size_t)t * 8;
+      float* alw = reinterpret_cast<float*>(cgw + 6);
+      float* blw = M.cgb + (size_t)t * 6;
+      const double ms = b.wf.Msec;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        float4 c4 = cgw[q];
+        const double A = ((double)c4.x + (double)alw[q]) + KC[q] * X0 * X0;
+        const double Bq = ((double)c4.y + (double)blw[q]) + 2.0 * KC[q] * X0 * ms;
+        const double Cq = (double)c4.z + KC[q] * ms * ms;
+        c4.x = (float)A;
+        c4.y = (float)Bq;
+        c4.z = (float)Cq;
+        cgw[q] = c4;
+        alw[q] = (float)(A - (double)c4.x);
+        blw[q] = (float)(Bq - (double)c4.y);
+      }
+    }
+  }
 }
 
 // kMode 0: lnL partials; 1: lnL partials + adjoint moments; 2: write the model
@@ -2089,7 +2205,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
   static_assert(kNM == 1 || (!kGrad && !kStage), "multi-mode dense stage: lnL and model passes, no staging");
-  __shared__ double red[kMixThreads / 32][2];
+  __shared__ double red[kMixThreads / 32][3];
   // per warp, two run buffers: the next run's inputs are copied while this one is computed
   __shared__ __align__(16) float4 rbuf[kStage ? kMixThreads / 32 : 1][kStage ? 2 : 1][kStage ? kRunBuf : 1];
   __shared__ float msm[kGrad ? kMixThreads / 32 : 1][kGrad ? kNodeQ * kMoments : 1][kGrad ? kMomPad : 1];
@@ -2104,6 +2220,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   float acc = 0.0f, comp = 0.0f;
   float dsh = 0.0f, dsl = 0.0f;  // float-float sum of the FP64 |d|^2/S of the weak-template bins
   float xacc = 0.0f, xcomp = 0.0f;  // compensated sum of the cross term -2 Re(d^* h) w
+  float macc = 0.0f, mcomp = 0.0f;  // multi-mode plans: compensated sum of 2 Re sum_{k<l} h_k conj(h_l) w
   if (blocks[s].status == kSampleOk && first < nc) {
     for (int d = 0; d < M.n_det; ++d) {
       const size_t sd = (size_t)s * kNM * M.n_det + d;  // (virtual sample of mode 0, detector)
@@ -2201,6 +2318,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           const float u2 = u * u, u3 = u2 * u;
           // the model of each channel, summed over the modes of the bin
           float hrs[3] = {0.0f, 0.0f, 0.0f}, his[3] = {0.0f, 0.0f, 0.0f};
+          float mx[3] = {0.0f, 0.0f, 0.0f};  // multi-mode: 2 Re h_k conj(sum of the earlier modes), per channel
           float cph = 0.0f, sph = 0.0f, xk = 0.0f, x2 = 0.0f;  // (single mode: used by the gradient)
 #pragma unroll 1
           for (int k = 0; k < kNM; ++k) {
@@ -2219,7 +2337,16 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
               r.p2h = ra1.y;
               r.p2l = ra1.z;
               r.p3h = ra1.w;
-              r.p3l = ra[2].x;
+              const float4 ra2 = ra[2];
+              r.p3l = ra2.x;
+              r.qx0 = ra2.y;
+              r.qj = ra2.z;
+            }
+            // the straddled phase corner's term (multi-mode plans), added to the advance
+            float qph = 0.0f;
+            if (kNM > 1 && r.qj != 0.0f) {
+              const float xq = fmaf(kSlope, u, r.qx0);
+              if (xq > 0.0f) qph = r.qj * (xq * xq);
             }
             // explicit FMAs on the lnL path: the lnL and lnL+gradient instantiations must round alike.
             // The phase advance is summed error-free (reductions and sums keep their
@@ -2233,7 +2360,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
               float s1, t1, s2, t2, s3, t3;
               two_sum(a, b, s1, t1);
               two_sum(s1, c, s2, t2);
-              two_sum(s2, fmaf(r.p1l, u, fmaf(r.p2l, u2, r.p3l * u3)), s3, t3);
+              two_sum(s2, fmaf(r.p1l, u, fmaf(r.p2l, u2, fmaf(r.p3l, u3, qph))), s3, t3);
               del = s3;
               dlo = ((ea + eb) + ec) + ((t1 + t2) + t3);
             }
@@ -2285,16 +2412,20 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
               const float4 k0 = KF4[0], k1 = KF4[1], k2 = KF4[2], k3 = KF4[3];
               const float kfh[6] = {k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
               const float kfl[6] = {k2.x, k2.y, k2.z, k2.w, k3.x, k3.y};
+              // multi-mode plans: intervals past the kink's own carry it in their coefficients
+              const float g = (kNM == 1 || j == (int)k3.z) ? x2 : 0.0f;
 #pragma unroll
-              for (int q = 0; q < 6; ++q) kink[q] = fmaf(kfh[q], x2, fmaf(kfl[q], x2, kink[q]));
+              for (int q = 0; q < 6; ++q) kink[q] = fmaf(kfh[q], g, fmaf(kfl[q], g, kink[q]));
             }
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
               const float4 cr = G[2 * ch], ci = G[2 * ch + 1];
               const float gr = cr.x + (kink[2 * ch] + fmaf(t, fmaf(t, fmaf(t, cr.w, cr.z), cr.y), Glo[2 * ch]));
               const float gi = ci.x + (kink[2 * ch + 1] + fmaf(t, fmaf(t, fmaf(t, ci.w, ci.z), ci.y), Glo[2 * ch + 1]));
-              hrs[ch] += fmaf(gr, cph, gi * sph);
-              his[ch] += fmaf(gi, cph, -(gr * sph));
+              const float hkr = fmaf(gr, cph, gi * sph), hki = fmaf(gi, cph, -(gr * sph));
+              if (kNM > 1) mx[ch] = fmaf(2.0f, fmaf(hkr, hrs[ch], hki * his[ch]), mx[ch]);
+              hrs[ch] += hkr;
+              his[ch] += hki;
             }
           }
           float term = 0.0f;  // |d - h|^2 w
@@ -2303,6 +2434,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
           float xdh = 0.0f;    // Re(d^* h) w
           float aphi = 0.0f;
           float ag[6];
+          float mterm = 0.0f;
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float hr = hrs[ch], hi = his[ch];
@@ -2317,6 +2449,7 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             const float dh = fmaf(dv.x, hr, dv.y * hi);
             cross = fmaf(fmaf(-2.0f, dh, h2), w, cross);
             xdh = fmaf(dh, w, xdh);
+            if (kNM > 1) mterm = fmaf(mx[ch], w, mterm);
             if (kMode == 2) model[off] = make_double2((double)hr / M.scale, (double)hi / M.scale);
             if (kGrad) {
               ag[2 * ch] = w * (er * cph - ei * sph);
@@ -2346,6 +2479,12 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
             const float tx = xacc + yx;
             xcomp = (tx - xacc) - yx;
             xacc = tx;
+          }
+          if (kNM > 1) {
+            const float ym_ = mterm - mcomp;
+            const float tm_ = macc + ym_;
+            mcomp = (tm_ - macc) - ym_;
+            macc = tm_;
           }
           if (kGrad && xk > 0.0f) {
             kinked = true;
@@ -2381,9 +2520,10 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
   }
   // deterministic reduction: lanes (float-float) -> warps (FP64) -> block partial,
   // for the direct sum and the cross-term sum
-  float vh, vl, xh, xl;
+  float vh, vl, xh, xl, mh, ml;
   two_sum(acc, -comp, vh, vl);
   two_sum(xacc, -xcomp, xh, xl);
+  two_sum(macc, -mcomp, mh, ml);
   {
     float th, tl;
     two_sum(vh, dsh, th, tl);
@@ -2396,6 +2536,8 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
     const float ol = __shfl_down_sync(0xffffffffu, vl, o);
     const float ph = __shfl_down_sync(0xffffffffu, xh, o);
     const float pl = __shfl_down_sync(0xffffffffu, xl, o);
+    const float qh = __shfl_down_sync(0xffffffffu, mh, o);
+    const float ql = __shfl_down_sync(0xffffffffu, ml, o);
     float th, tl;
     two_sum(vh, oh, th, tl);
     vh = th;
@@ -2403,17 +2545,21 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev
     two_sum(xh, ph, th, tl);
     xh = th;
     xl += tl + pl;
+    two_sum(mh, qh, th, tl);
+    mh = th;
+    ml += tl + ql;
   }
   if (lane == 0) {
     red[wid][0] = (double)vh + (double)vl;
     red[wid][1] = (double)xh + (double)xl;
+    red[wid][2] = (double)mh + (double)ml;
   }
   __syncthreads();
-  if (threadIdx.x < 2) {
+  if (threadIdx.x < 3) {
     double x = 0.0;
 #pragma unroll
     for (int w = 0; w < kMixThreads / 32; ++w) x += red[w][threadIdx.x];
-    M.part[((size_t)s * M.nblk_dense + blockIdx.x) * 2 + threadIdx.x] = x;
+    M.part[((size_t)s * M.nblk_dense + blockIdx.x) * 3 + threadIdx.x] = x;
   }
 }
 
@@ -2448,19 +2594,30 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
                                                   const SampleBlock<double>* __restrict__ blocks, int64_t B) {
   __shared__ double red[kHdThreads / 32][4];
   const int lane = threadIdx.x;
-  const int64_t sd = blockIdx.x;
-  if (sd >= B * M.n_det) return;
-  const int64_t s = sd / M.n_det;
+  const int64_t sd = blockIdx.x;  // (virtual sample, detector)
+  if (sd >= B * M.n_modes * M.n_det) return;
+  const int64_t v = sd / M.n_det;
+  const int64_t s = v / M.n_modes;
+  const int kmode = (int)(v % M.n_modes);
   const int d = (int)(sd % M.n_det);
   const SampleBlock<double>& b = blocks[s];
   double* out = M.hd + sd * kHdOut;
-  const int64_t kcut = b.kcut;
+  // sum |d|^2 w over the sample's dense range [lo, kcut); sum |h|^2 w of the
+  // mode over its own range [lo, vcut)
+  const int64_t kcut = M.vcut[v];
   const int64_t lo = M.xbind[sd];
-  if (b.status != kSampleOk || M.nsp[s] < 3 || lo >= kcut) {
+  if (b.status != kSampleOk || M.nsp[v] < 3 || lo >= kcut) {
     if (lane < kHdOut) out[lane] = 0.0;
+    if (lane == 1 && b.status == kSampleOk && lo < b.kcut) {
+      const double* ds = M.dsuf + (size_t)d * (P.nbins + 1);
+      out[1] = ds[lo] - ds[b.kcut];
+    }
     return;  // uniform per block
   }
-  const double Msec = b.wf.Msec, fpk = b.wf.fpeak;
+  // the mode's amplitude kink point; multi-mode plans carry the kink in the
+  // coefficients of the intervals after the one holding it (k_bump)
+  const double Msec = b.wf.Msec, fpk = (M.hm && kmode > 0) ? M.hm[s].md[kmode].frA : b.wf.fpeak;
+  const int jk = (int)M.kinkF[(size_t)sd * 16 + 14];
   // first bin with x = Msec f - Mf_peak > 0
   int64_t kpk = (int64_t)floor(fpk / (Msec * P.f_step)) - P.k0;
   for (int it = 0; it < 2 && kpk > 0 && Msec * ((double)(P.k0 + kpk - 1) * P.f_step) > fpk; ++it) --kpk;
@@ -2497,23 +2654,26 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
       Cc[q] = (double)c4.z;
       Dc[q] = (double)c4.w;
     }
-    // the splines' error at the midpoint (kink-free values on both sides)
+    // the splines' error at the midpoint (kink-free values on both sides, or
+    // both with the kink in a folded interval)
+    const bool folded = jk >= 0 && j > jk;
     const double h = M.gh[j], tm = 0.5 * h;
+    const double Xm = Msec * (M.node_f[j] + tm) - fpk;
     double delta[6], gm[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
       const double sp = A[q] + tm * (Bc[q] + tm * (Cc[q] + tm * Dc[q]));
-      const double ex = ff_to(ym[(size_t)q * M.J + j]);
+      const double ex = ff_to(ym[(size_t)q * M.J + j]) + (folded ? KC[q] * Xm * Xm : 0.0);
       delta[q] = ex - sp;
       gm[q] = ex;
     }
-    const double Xm = Msec * (M.node_f[j] + tm) - fpk;
-    if (Xm > 0.0) {
+    if (Xm > 0.0 && !folded) {
 #pragma unroll
       for (int q = 0; q < 6; ++q) gm[q] += KC[q] * Xm * Xm;
     }
     double Sm[42];
-    const int64_t ks = min(max(kpk, k1), k2);  // [k1, ks) before the peak, [ks, k2) past it
+    // [k1, ks) without the kink term, [ks, k2) with it (folded intervals hold it already)
+    const int64_t ks = folded ? k2 : min(max(kpk, k1), k2);
     if (ks > k1) {
 #pragma unroll
       for (int x = 0; x < 42; ++x) Sm[x] = F(ks, x) - F(k1, x);
@@ -2536,7 +2696,7 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
     }
     // first-order change of sum |h|^2 w over the interval if the splines' error
     // had the shape 16 t^2 (h - t)^2 / h^4 times its midpoint value
-    {
+    if (!M.wspike[(size_t)d * M.J + j]) {
       const double ih2 = 1.0 / (h * h);
       double e = 0.0;
 #pragma unroll
@@ -2570,7 +2730,7 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
       for (int q = 0; q < 4; ++q) t[q] += red[w][q];
     const double* ds = M.dsuf + (size_t)d * (P.nbins + 1);
     out[0] = t[0];
-    out[1] = ds[lo] - ds[kcut];
+    out[1] = ds[lo] - ds[b.kcut];
     out[2] = t[1];
     out[3] = t[2];
     out[4] = t[3];
@@ -2591,13 +2751,24 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   // dense bins: the direct sum of |d - h|^2 w, or the split form for templates
   // far from the data (residual above 2 sqrt(<h|h> <d|d>)), where the FP32
   // rounding of the model enters only the cross term
-  double R = 0.0, X = 0.0, H = 0.0, Dd = 0.0;
+  double R = 0.0, X = 0.0, H = 0.0, Dd = 0.0, Cm = 0.0;
   for (int k = 0; k < M.nblk_dense; ++k) {
-    R += M.part[((size_t)s * M.nblk_dense + k) * 2];
-    X += M.part[((size_t)s * M.nblk_dense + k) * 2 + 1];
+    R += M.part[((size_t)s * M.nblk_dense + k) * 3];
+    X += M.part[((size_t)s * M.nblk_dense + k) * 3 + 1];
+    Cm += M.part[((size_t)s * M.nblk_dense + k) * 3 + 2];
   }
-  if (M.n_modes > 1) {  // multi-mode plans: the direct sum
-    double acc = R;
+  if (M.n_modes > 1) {
+    // multi-mode plans: the split form for far templates with sum |h|^2 w =
+    // the modes' own sums (exact, from their splines) + their cross terms
+    // (dense stage); no refinement
+    for (int k = 0; k < M.n_modes; ++k)
+      for (int d = 0; d < M.n_det; ++d) {
+        const double* hv = M.hd + (((size_t)s * M.n_modes + k) * M.n_det + d) * kHdOut;
+        H += hv[0] + hv[3];
+      }
+    for (int d = 0; d < M.n_det; ++d) Dd += M.hd[((size_t)s * M.n_modes * M.n_det + d) * kHdOut + 1];
+    const double Ht = H + Cm;
+    double acc = (R > 2.0 * sqrt(fmax(Ht, 0.0) * Dd)) ? (Dd + X) + Ht : R;
     if (M.xbin[s * M.n_modes] > 0)
       for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
     const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
@@ -2673,6 +2844,28 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
 // (interval, channel) runs over the interval's bins in order, writing the
 // exclusive prefix sums of t^p W_c (p = 0..6) at every bin and the interval's
 // totals; W_c = w_c |P|^2 / scale^2 in FP64, t = f_k - f_j.
+// per interval of one detector: does the weight sum_c w_c |P|^2 spike (its
+// largest bin above kSpikeRatio times the interval's mean)?
+__global__ void k_wspike(PlanDev P, MixedDev M, int det, int32_t* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M.J) return;
+  int flag = 0;
+  if (j < M.J - 1) {
+    const int64_t k1 = M.iv_first[j], k2 = M.iv_first[j + 1];
+    double mx = 0.0, sum = 0.0;
+    for (int64_t k = k1; k < k2; ++k) {
+      const TdiFactor tf = P.tdi[(size_t)det * P.nbins + k];
+      double w = 0.0;
+      for (int c = 0; c < 3; ++c) w += P.w[((size_t)det * 3 + c) * P.nbins + k];
+      w *= tf.pre * tf.pre + tf.pim * tf.pim;
+      mx = fmax(mx, w);
+      sum += w;
+    }
+    flag = k2 > k1 && mx > kSpikeRatio * sum / (double)(k2 - k1);
+  }
+  out[(size_t)det * M.J + j] = flag;
+}
+
 __global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ wmom, double* __restrict__ wtot) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (M.J - 1) * 6) return;
@@ -2764,7 +2957,7 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaEventCreateWithFlags(&mb->xready, cudaEventDisableTiming));
   PES_CHECK_CUDA(cudaStreamCreateWithFlags(&mb->aux, cudaStreamNonBlocking));
   for (cudaEvent_t* e : {&mb->ev_nodes, &mb->ev_tfit, &mb->ev_dense, &mb->ev_tadj, &mb->ev_hd, &mb->ev_pfit,
-                         &mb->ev_kink})
+                         &mb->ev_kink, &mb->ev_xgrad})
     PES_CHECK_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   MixedDev& M = mb->dev;
   const int64_t n = d.nbins;
@@ -2854,7 +3047,7 @@ int mixed_create(PesPlan* p) {
   float4* sff;
   unsigned long long* cfrac;
   float2* node_ff;
-  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst, *vcut;
+  int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst, *vcut, *wspk;
   double *xpart, *xgpart;
   double *wmom, *wtot, *dsuf, *wrow, *hdv, *rpart;
   float* cgb;
@@ -2871,11 +3064,10 @@ int mixed_create(PesPlan* p) {
   float2* ddv;
   float4* cg;
   const size_t sd = (size_t)V * nd;  // per (virtual sample, detector)
-  // multi-mode plans: lnL only (no gradient buffers) and the direct residual
-  // sum (no split form: no weight moments)
+  // multi-mode plans: lnL only (no gradient buffers)
   const bool multi = M.n_modes > 1;
   const size_t gsd = multi ? 1 : sd;
-  const size_t wn = multi ? 1 : (size_t)nd * n * kMomStride, wj = multi ? 1 : (size_t)nd * J * kMomStride;
+  const size_t wn = (size_t)nd * n * kMomStride, wj = (size_t)nd * J * kMomStride;
   if ((rc = alloc(mb, &node_f, J)) || (rc = alloc(mb, &chb, M.nchunks)) || (rc = alloc(mb, &chl, M.nchunks)) ||
       (rc = alloc(mb, &chi, M.nchunks)) || (rc = alloc(mb, &bin_t, n)) ||
       (rc = alloc(mb, &runs, sd * M.nchunks * 3)) || (rc = alloc(mb, &pk, (size_t)nd * 3 * n)) || (rc = alloc(mb, &ddv, (size_t)nd * n)) || (rc = alloc(mb, &nsp, V)) || (rc = alloc(mb, &nch, V)) || (rc = alloc(mb, &vcut, V)) ||
@@ -2886,12 +3078,12 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &cfrac, (size_t)V)) || (rc = alloc(mb, &node_ff, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 8)) ||
       (rc = alloc(mb, &mom, gsd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, gsd * kNodeQ * J)) ||
-      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense * 2)) ||
+      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense * 3)) ||
       (rc = alloc(mb, &wmom, wn)) || (rc = alloc(mb, &wtot, wj)) ||
       (rc = alloc(mb, &dsuf, (size_t)nd * (n + 1))) || (rc = alloc(mb, &wrow, (size_t)n)) ||
       (rc = alloc(mb, &cgb, sd * J * 6)) || (rc = alloc(mb, &hdv, sd * kHdOut)) ||
       (rc = alloc(mb, &mid_ff, J)) || (rc = alloc(mb, &tdm_ff, (size_t)nd * J)) || (rc = alloc(mb, &ymv, sd * 7 * J)) ||
-      (rc = alloc(mb, &cbump, sd * J * 2)) ||
+      (rc = alloc(mb, &cbump, sd * J * 2)) || (rc = alloc(mb, &wspk, (size_t)nd * J)) ||
       (rc = alloc(mb, &rpart, (size_t)B * kRefineBlocks)) ||
       (rc = alloc(mb, &gpart, gsd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, gsd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
@@ -2986,6 +3178,12 @@ int mixed_create(PesPlan* p) {
   M.dd = ddv;
   M.nsp = nsp;
   M.vcut = vcut;
+  M.pkink = nullptr;
+  if (multi) {
+    float4* pkink = nullptr;
+    if ((rc = alloc(mb, &pkink, (size_t)V * 2))) return rc;
+    M.pkink = pkink;
+  }
   M.nch = nch;
   M.xbin = xbin;
   M.xbind = xbind;
@@ -3027,6 +3225,8 @@ int mixed_create(PesPlan* p) {
   M.hd = hdv;
   M.ym = ymv;
   M.cbump = cbump;
+  M.wspike = wspk;
+  PES_CHECK_CUDA(cudaMemset(wspk, 0, sizeof(int32_t) * nd * J));
   M.rpart = rpart;
   M.rblocks = kRefineBlocks;
   {
@@ -3068,7 +3268,7 @@ void mixed_destroy(PesPlan* p) {
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
   if (p->mixed->aux) cudaStreamSynchronize(p->mixed->aux);
   for (cudaEvent_t e : {p->mixed->ev_nodes, p->mixed->ev_tfit, p->mixed->ev_dense, p->mixed->ev_tadj, p->mixed->ev_hd,
-                        p->mixed->ev_pfit, p->mixed->ev_kink})
+                        p->mixed->ev_pfit, p->mixed->ev_kink, p->mixed->ev_xgrad})
     if (e) cudaEventDestroy(e);
   if (p->mixed->aux) cudaStreamDestroy(p->mixed->aux);
   for (void* a : p->mixed->allocs) cudaFree(a);
@@ -3091,9 +3291,10 @@ int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cud
   PES_CHECK_LAUNCH();
   suffix_sum(p->desc.nbins, M.wrow, const_cast<double*>(M.dsuf) + (size_t)det * (p->desc.nbins + 1), st);
   PES_CHECK_LAUNCH();
-  if (M.n_modes > 1) return PES_OK;  // multi-mode plans use the direct residual sum only
   k_wmoments<<<ceil_div((M.J - 1) * 6, 128), 128, 0, st>>>(p->dev, M, det, const_cast<double*>(M.wmom),
                                                             const_cast<double*>(M.wtot));
+  PES_CHECK_LAUNCH();
+  k_wspike<<<ceil_div(M.J, 128), 128, 0, st>>>(p->dev, M, det, const_cast<int32_t*>(M.wspike));
   PES_CHECK_LAUNCH();
   return PES_OK;
 }
@@ -3205,6 +3406,8 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
           p->dev, M, G, reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), nullptr);
     }
     PES_CHECK_LAUNCH();
+    // the backward node stage reads the gradient set-up
+    PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_xgrad, side));
   }
   // (the side stream's completion is recorded after the exact re-evaluation below)
   {
@@ -3246,23 +3449,32 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tfit, aux));
-  if (!multi) {
-    // <h|h> and <d|d> of the dense ranges, beside the anchors and the dense stage
+  {
+    // <h|h> and <d|d> of the dense ranges (per mode), beside the anchors and the dense stage
     PES_CHECK_CUDA(cudaStreamWaitEvent(aux, p->mixed->xready, 0));
     ProfScope ps(p, kKOther, aux);
-    k_hd<<<(unsigned)(B * (int64_t)M.n_det), kHdThreads, 0, aux>>>(p->dev, M, blocks, B);
+    k_hd<<<(unsigned)(V * M.n_det), kHdThreads, 0, aux>>>(p->dev, M, blocks, B);
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_hd, p->mixed->aux));
-  // the exact re-evaluation of the samples that the error estimates select,
-  // on the side stream after its exact low-frequency bins
+  // The exact re-evaluation of the samples that the error estimates select,
+  // on the side stream after its exact low-frequency bins: beside the dense
+  // stage for lnL calls, beside the adjoint stages (after the dense stage)
+  // for lnL+gradient calls, where it does not take SMs from the dense stage.
+  auto refine = [&]() -> int {
+    if (!multi) {
+      ProfScope ps(p, kKDenseFp64, side);
+      k_exact<3, double><<<dim3(M.rblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+    }
+    PES_CHECK_LAUNCH();
+    PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
+    return PES_OK;
+  };
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_hd, 0));
-  if (!multi) {
-    ProfScope ps(p, kKDenseFp64, side);
-    k_exact<3, double><<<dim3(M.rblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+  if (!grad) {
+    const int rc = refine();
+    if (rc != PES_OK) return rc;
   }
-  PES_CHECK_LAUNCH();
-  PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
   if (grad) {
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
     PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
@@ -3290,14 +3502,22 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_dense, st));
-  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->join, 0));
-  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_hd, 0));
+  auto finalize = [&]() -> int {
+    PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->join, 0));
+    PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_hd, 0));
+    {
+      ProfScope ps(p, kKFinalize, st);
+      k_mixed_finalize<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, M, blocks, B, lnl, status);
+    }
+    PES_CHECK_LAUNCH();
+    return PES_OK;
+  };
+  if (!grad) return finalize();
+  PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_dense, 0));
   {
-    ProfScope ps(p, kKFinalize, st);
-    k_mixed_finalize<<<ceil_div(B, 64), 64, 0, st>>>(p->dev, M, blocks, B, lnl, status);
+    const int rc = refine();
+    if (rc != PES_OK) return rc;
   }
-  PES_CHECK_LAUNCH();
-  if (!grad) return PES_OK;
   // node adjoints: phase systems here, transfer systems on the second stream;
   // then the backward node stage
   const double ws = 4.0 * p->dev.df;
@@ -3327,11 +3547,18 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_tadj, aux));
   PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_tadj, 0));
+  PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_xgrad, 0));
   {
     ProfScope ps(p, kKAdjoint, st);
     k_sparse_bwd_split<<<sgrid, kSparseThreads, 0, st>>>(p->dev, M, G, ws);
   }
   PES_CHECK_LAUNCH();
+  {
+    // the lnL sums, after the side stream's exact passes (exact-bin gradient
+    // partials, refined samples), then the gradient sums
+    const int rc = finalize();
+    if (rc != PES_OK) return rc;
+  }
   {
     ProfScope ps(p, kKFinalize, st);
     k_mixed_grad_finalize<<<ceil_div(B, 64), 64, 0, st>>>(M, B, -2.0 * p->dev.df, grad);
