@@ -61,12 +61,18 @@ WORKLOADS = {
                    "network-hm: 4096-sample prior batch, IMRPhenomHM (6 modes), LISA + Taiji + TianQin TDI1.5 AET, "
                    "T=2^25 s, dt=4 s, 3354437 bins per channel (9 channels), 2048 sparse nodes per mode, "
                    "cutoff 1.2 f_RD of the highest mode, mixed precision, CUDA graph"),
+    # SMC-style sweep: half IMRPhenomD particles on LISA (lnL, gradient, Fisher), half
+    # IMRPhenomHM particles on the three-detector network (lnL)
+    "smc-sweep": (2.0 ** 22, 8.0, 1e-4, 0.03, "1.5",
+                  "smc-sweep: 16384 particles, 8192 IMRPhenomD on LISA (T=2^22 s, 125410 bins; lnL, gradient and "
+                  "11x11 Fisher) + 8192 IMRPhenomHM on LISA + Taiji + TianQin (T=2^25 s, 3354437 bins; lnL), mixed"),
     # time-domain TDI combination of six single-link series (no likelihood): its own metric
     "td-tdi": (2.0 ** 25, 4.0, None, None, "2.0",
                "td-tdi: LISA TDI2.0 AET from six single-link time series, T=2^25 s, dt=4 s, 8388609 samples"),
 }
 N_SPARSE = {"network-d": 2048, "network-hm": 2048}
 HM_METRIC = "lnL evals/s, 4096 MBHB samples, IMRPhenomHM 3-detector network, 1 GB300 (mixed, CUDA graph)"
+SMC_METRIC = "particles/s, 16384-particle sweep (8192 IMRPhenomD lnL+grad+Fisher, 8192 IMRPhenomHM lnL), 1 GB300"
 TD_METRIC = "TD TDI output samples/s (A/E/T from six single-link series), 1 GB300"
 LISA_ARM_M = 2.5e9
 C_SI = 299792458.0
@@ -261,6 +267,11 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     B = args.batch
+    if args.workload == "smc-sweep":
+        print(json.dumps({"impl": "reference", "unavailable": "a 16384-particle sweep with Fisher matrices is hours "
+                          "of the CPU port; its halves are timed by --workload adjoint and --workload network-hm"}),
+              flush=True)
+        return
     if args.workload == "network-hm":
         # lnL only (as the GPU leg), a few samples of its 4096 spread over the batch:
         # each is about a minute of FP64 work per core over 3 x 3.35 M bins x 6 modes
@@ -555,6 +566,86 @@ def network_hm_leg(steps, warmup, batch=4096, max_batch=512, check=16):
             "clocks": clocks.summary()}
 
 
+def smc_sweep_leg(steps, warmup, n_half=8192, check=64):
+    """One SMC-style sweep per step over 2 n_half particles: the IMRPhenomD half
+    (LISA, config of the default workload) gets lnL, gradient and the 11x11
+    Fisher matrix from the mixed plan; the IMRPhenomHM half (three-detector
+    network) gets lnL from the mixed plan (its gradient and Fisher matrix are
+    the FP64 plan's, too slow for a sweep of this size: not timed here).
+    Accuracy on evenly spread subsets against the FP64 plans."""
+    import torch
+
+    from pespace_gb300.inference import WhittleLikelihood
+    from pespace_gb300.workloads import config0_theta, lisa_dataset, network_dataset, prior_samples
+
+    T1, dt1, f1, F1, g1, _ = WORKLOADS["adjoint"]
+    th1 = config0_theta(T1 - 86400.0)
+    det1 = lisa_dataset(T1, dt1, f1, F1, th1, g1, seed=2026)
+    T3, dt3, f3, F3, g3, _ = WORKLOADS["network-hm"]
+    th3 = config0_theta(T3 - 86400.0)
+    det3 = network_dataset(T3, dt3, f3, F3, th3, g3, seed=2026, approximant="IMRPhenomHM")
+    eng_d = WhittleLikelihood(det1, precision="mixed", reference_frequency=1e-4, cut_factor=1.2, max_batch=1024)
+    eng_h = WhittleLikelihood(det3, precision="mixed", approximant="IMRPhenomHM", reference_frequency=1e-4,
+                              cut_factor=1.2, max_batch=512, n_sparse=N_SPARSE["network-hm"])
+    rng = np.random.default_rng(2028)
+    th_d = torch.as_tensor(prior_samples(rng, n_half, th1[10]), device="cuda")
+    th_h = torch.as_tensor(prior_samples(rng, n_half, th3[10]), device="cuda")
+    out = {}
+
+    def sweep():
+        out["lnl_d"], out["grad_d"] = eng_d.log_likelihood_and_grad(th_d)
+        out["fisher_d"] = eng_d.fisher_matrix(th_d)
+        out["lnl_h"] = eng_h.log_likelihood_batch(th_h)
+
+    for _ in range(max(1, warmup)):
+        sweep()
+    torch.cuda.synchronize()
+    ms, parts = [], {"phenomd_lnl_grad": [], "phenomd_fisher": [], "phenomhm_lnl": []}
+    for _ in range(steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record()
+        out["lnl_d"], out["grad_d"] = eng_d.log_likelihood_and_grad(th_d)
+        ev[1].record()
+        out["fisher_d"] = eng_d.fisher_matrix(th_d)
+        ev[2].record()
+        out["lnl_h"] = eng_h.log_likelihood_batch(th_h)
+        ev[3].record()
+        ev[3].synchronize()
+        ms.append(ev[0].elapsed_time(ev[3]))
+        for k, (a, b) in zip(parts, ((0, 1), (1, 2), (2, 3))):
+            parts[k].append(ev[a].elapsed_time(ev[b]))
+    mean_ms = float(np.mean(ms))
+    # accuracy against the FP64 plans on evenly spread subsets
+    idx = torch.as_tensor(stratified(n_half, check), device="cuda")
+    ref_d = WhittleLikelihood(det1, precision="fp64", reference_frequency=1e-4, cut_factor=1.2, max_batch=len(idx))
+    d_lnl = (out["lnl_d"][idx] - ref_d.log_likelihood_batch(th_d[idx])).abs()
+    Fw = ref_d.fisher_matrix(th_d[idx])
+    sd = torch.sqrt(torch.diagonal(Fw, dim1=1, dim2=2).abs())
+    f_err = ((out["fisher_d"][idx] - Fw).abs() / (sd[:, :, None] * sd[:, None, :])).amax()
+    del ref_d
+    idx_h = idx[: check // 4]
+    ref_h = WhittleLikelihood(det3, precision="fp64", approximant="IMRPhenomHM", reference_frequency=1e-4,
+                              cut_factor=1.2, max_batch=len(idx_h))
+    d_h = (out["lnl_h"][idx_h] - ref_h.log_likelihood_batch(th_h[idx_h])).abs()
+    return {"metric": SMC_METRIC, "value": 2 * n_half / (mean_ms / 1e3), "unit": "particles/s", "steps": steps,
+            "warmup": max(1, warmup), "ms_per_step": mean_ms, "dtype": "f32+f64",
+            "config": {"workload": WORKLOADS["smc-sweep"][5], "particles": 2 * n_half},
+            "ms_per_part": {k: float(np.mean(v)) for k, v in parts.items()},
+            "not_timed": "IMRPhenomHM gradient and Fisher: FP64 plan only (no mixed multi-mode adjoint)",
+            "accuracy": {"phenomd_samples": len(idx), "phenomd_max_abs_dlnl": float(d_lnl.max().item()),
+                         "phenomd_n_within_1e-2": int((d_lnl <= 1e-2).sum().item()),
+                         "phenomd_fisher_max_rel": float(f_err.item()),
+                         "phenomhm_samples": len(idx_h), "phenomhm_max_abs_dlnl": float(d_h.max().item()),
+                         "phenomhm_n_within_1e-2": int((d_h <= 1e-2).sum().item())}}
+
+
+def run_smc_sweep(args):
+    line = smc_sweep_leg(args.steps, args.warmup)
+    line.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "data": "synthetic"})
+    print(json.dumps(line), flush=True)
+
+
 def run_network_hm(args):
     line = network_hm_leg(args.steps, args.warmup)
     line.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -778,6 +869,8 @@ def main():
         run_td_tdi(args)
     elif args.workload == "network-hm":
         run_network_hm(args)
+    elif args.workload == "smc-sweep":
+        run_smc_sweep(args)
     else:
         run_native(args)
 

@@ -5,16 +5,22 @@ call).  Its bins are compute work on data that stays in L2 (125410 bins x
 48 B per detector, three float4 rows per bin), so the bound is the FP32 pipe.  FP32 arithmetic per bin
 and detector, counted from the kernel source (FMA = 2 flops, add/mul = 1):
 
-  phase advance: three exact 2 pi reductions and the FP32 tails      38
-  FMA-only sincos of the advance                                      29
-  rotation by the run's anchor phasor and renormalisation            15
-  per channel (x3): spline value with the peak-kink term 24, model
-    rotation 6, residual 2, |d - h|^2 w 5, |h|^2 w and the cross
-    term of the weak-template form 12                       49 x 3 = 147
-  kink coordinate 3, compensated sum 4, weak-template branch 8       15
-                                                       lnL pass:    244
+  phase advance from the run's anchor, error-free: three exact
+    2 pi reductions of the split products (16 each), the products
+    and powers of the lane index 5, a two-sum chain 18, the tails'
+    polynomial 6 and their sum 5                                      82
+  FMA-only sincos of the advance 29, first-order tail correction 4   33
+  rotation by the run's anchor phasor 6, renormalisation 9, TDI
+    generation prefactor 6                                           21
+  kink coordinate 3, midpoint correction (bump shape 4, six
+    products 6)                                                      13
+  per channel (x3): spline value with the kink and midpoint terms
+    24, model rotation 6, residual 2, |d - h|^2 w 5, |h|^2 w, the
+    cross term and Re(d* h) w 14                            51 x 3 = 153
+  weak-template branch 8, compensated sums (direct 4, cross 5)      17
+                                                       lnL pass:    319
   gradient pass: per-channel adjoints 13 x 3 = 39, interval moments
-    (7 quantities x t^0..t^3) 58                              +97 = 341
+    (7 quantities x t^0..t^3) 58                              +97 = 416
 
 The per-bin kink moments of post-peak bins are not counted (a lower bound).
 The FP64 run anchors (about 30 FP64 operations per run of <= 32 bins) are
@@ -23,12 +29,12 @@ not in the FP32 count either.
 Peak: cuBLAS SGEMM 8192^3 with TF32 off, measured in bench.py (FP32 pipe).
 Traffic: DRAM bytes per dense bin measured by ncu on a 256-sample batch of
 the same workload (dram__bytes_read.sum + dram__bytes_write.sum of one
-k_dense_mixed<1> launch divided by its 19 595 338 dense bins); scaled here by
+k_dense_mixed<1> launch divided by its 19 603 667 dense bins); scaled here by
 the launch's dense bins.
 """
 
-FP32_FLOPS_PER_DENSE_BIN = {"lnl": 244, "grad": 341}
-DRAM_BYTES_PER_DENSE_BIN = 5.14  # (95.76 MB + 4.92 MB) / 19 595 338 bins, ncu --set full, 256 samples
+FP32_FLOPS_PER_DENSE_BIN = {"lnl": 319, "grad": 416}
+DRAM_BYTES_PER_DENSE_BIN = 5.61  # (102.88 MB + 7.06 MB) / 19 603 667 bins, ncu --set full, 256 samples
 
 
 def roofline(kernel_class, launches_ms, steps, work, grad, fp32_peak_tflops):

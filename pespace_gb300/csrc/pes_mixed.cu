@@ -2199,8 +2199,10 @@ __global__ void k_bump(MixedDev M, const SampleBlock<double>* __restrict__ block
 // inputs the gradient pass is faster on plain loads).
 // kNM: modes summed per bin before the residual (1, or kHMModes for
 // IMRPhenomHM plans: lnL and model passes, plain loads).
+// The gradient pass is held to 96 registers (5 blocks per SM instead of 4:
+// 2% faster on the bench workload, at a few spilled words).
 template <int kMode, bool kStage, int kNM>
-__global__ void __launch_bounds__(kMixThreads) k_dense_mixed(PlanDev P, MixedDev M,
+__global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed(PlanDev P, MixedDev M,
                                                              const SampleBlock<double>* __restrict__ blocks,
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
