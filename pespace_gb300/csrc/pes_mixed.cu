@@ -2131,29 +2131,33 @@ __global__ void k_bump(MixedDev M, const SampleBlock<double>* __restrict__ block
     out[1] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
     return;
   }
-  const double h = M.gh[j], tm = 0.5 * h;
+  // float-float on the FP32 pipes: the midpoint errors are 1e-8..1e-6 of the
+  // values, the phase error a small angle (its rotation to second order)
+  const double h = M.gh[j];
+  const FF tm = ff_from(0.5 * h);
   const FF* ym = M.ym + (size_t)sd * 7 * M.J + j;
   const FF* co = M.cphi + (size_t)t * 4;
-  const double phs = ff_to(co[0]) + tm * (ff_to(co[1]) + tm * (ff_to(co[2]) + tm * ff_to(co[3])));
-  double sn, cs;
-  sincos(ff_to(ym[(size_t)6 * M.J]) - phs, &sn, &cs);
+  const FF phs = co[0] + tm * (co[1] + tm * (co[2] + tm * co[3]));
+  const float dph = (ym[(size_t)6 * M.J] - phs).hi;
+  const float sn = dph, cs = fmaf(-0.5f * dph, dph, 1.0f);
   const float4* cg = M.cg + (size_t)t * 8;
   const float* alo = reinterpret_cast<const float*>(cg + 6);
   const float* blo = M.cgb + (size_t)t * 6;
+  const float tmf = tm.hi;
   float dl[6];
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
-    double sp[2];
+    FF sp[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int q = 2 * ch + k;
       const float4 c4 = cg[q];
-      sp[k] = ((double)c4.x + (double)alo[q]) +
-              tm * (((double)c4.y + (double)blo[q]) + tm * ((double)c4.z + tm * (double)c4.w));
+      // the value at the left node as float-float plus the (small) polynomial change
+      sp[k] = ff_addf(ff_two_sum(c4.x, alo[q]), tmf * ((c4.y + blo[q]) + tmf * fmaf(tmf, c4.w, c4.z)));
     }
-    const double gr = ff_to(ym[(size_t)(2 * ch) * M.J]), gi = ff_to(ym[(size_t)(2 * ch + 1) * M.J]);
-    dl[2 * ch] = (float)(gr * cs + gi * sn - sp[0]);
-    dl[2 * ch + 1] = (float)(gi * cs - gr * sn - sp[1]);
+    const FF gr = ym[(size_t)(2 * ch) * M.J], gi = ym[(size_t)(2 * ch + 1) * M.J];
+    dl[2 * ch] = (ff_addf(ff_mulf(gr, cs), gi.hi * sn) - sp[0]).hi;
+    dl[2 * ch + 1] = (ff_addf(ff_mulf(gi, cs), -(gr.hi * sn)) - sp[1]).hi;
   }
   if (M.wspike[(size_t)(sd % M.n_det) * M.J + j]) {
 #pragma unroll
