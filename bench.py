@@ -493,7 +493,7 @@ def network_hm_leg(steps, warmup, batch=4096, max_batch=512, check=16):
     launches, dev_ms = (ctypes.c_int64 * n_cls)(), (ctypes.c_double * n_cls)()
     lib.pes_plan_profile(eng._plan, 1)
     lib.pes_plan_stats(eng._plan, launches, dev_ms)
-    work = {"dense_bins": 0, "fp64_bins": 0, "sparse_nodes": 0, "samples": 0}
+    work = {"dense_bins": 0, "fp64_bins": 0, "sparse_nodes": 0, "samples": 0, "refined_ff": 0, "refined_exact": 0}
     for lo in range(0, batch, max_batch):
         eng.log_likelihood_batch(theta[lo:lo + max_batch])
         for k, v in eng.last_work(min(max_batch, batch - lo)).items():

@@ -244,9 +244,17 @@ const char* pes_kernel_class_name(int32_t k);
  *     when the packed dense inputs exceed 64 MB (they stream from DRAM).
  *   PES_OPT_SAMPLE_THREADS: threads per block of the per-sample kernels of
  *     the lnL calls (set-up, ranges, peak kink), 1..128 (the gradient
- *     set-up uses up to 255 registers per thread); default 8. */
+ *     set-up uses up to 255 registers per thread); default 8.
+ * One option changes results, not speed, and is not tuned:
+ *   PES_OPT_REFINE_ALL (mixed plans): 1 = every sample's dense range is
+ *     re-evaluated as the samples whose error estimates approach the
+ *     accuracy target always are: in float-float from its splines, or
+ *     exactly where the splines' own error estimate exceeds the target (a
+ *     check of those paths, and the most accurate mixed result at about
+ *     twice the dense stage's cost); 0 (default) = only those samples. */
 #define PES_OPT_DENSE_STAGE 1
 #define PES_OPT_SAMPLE_THREADS 2
+#define PES_OPT_REFINE_ALL 3
 int pes_plan_set_option(PesPlan* plan, int32_t option, int64_t value);
 int pes_plan_get_option(PesPlan* plan, int32_t option, int64_t* value /* host */);
 
@@ -269,8 +277,9 @@ int pes_fisher_batch(PesPlan* plan, const double* theta, int64_t B, double* fish
  * summed over samples and detectors; out[1]: bins evaluated directly in FP64
  * (all live bins of an fp64 plan, the exact low-frequency bins of a mixed
  * plan); out[2]: sparse-node evaluations (mixed plans); out[3]: samples in
- * the parameter domain. */
-int pes_plan_work(PesPlan* plan, int64_t B, int64_t* out /* host [4] */, void* stream);
+ * the parameter domain; out[4], out[5]: samples whose dense range a mixed
+ * plan re-evaluated in float-float from its splines, and exactly. */
+int pes_plan_work(PesPlan* plan, int64_t B, int64_t* out /* host [6] */, void* stream);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,7 @@ PES_ECUDA = 3
 PES_ETIMEOUT = 4
 PES_OPT_DENSE_STAGE = 1
 PES_OPT_SAMPLE_THREADS = 2
+PES_OPT_REFINE_ALL = 3
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 APPROX_PHENOMD = 0

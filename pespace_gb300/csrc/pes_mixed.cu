@@ -130,8 +130,9 @@ struct MixedDev {
   float4* cg;
   float* mom;               // [B][n_det][J][7][4] adjoint moments (FP32 warp sums, FP32 atomics)
   float* ybar;              // [B][n_det][J][7] node adjoints (FP32: the derivative passes run in FP32)
-  double* part;             // [B][nblk_dense][3] partials: sum |d - h|^2 w (direct form), sum -2 Re(d^* h) w,
-                            //   sum 2 Re sum_{k<l} h_k conj(h_l) w (the modes' cross terms; 0 for one mode)
+  double* part;             // [B][nblk_dense][kPartW] partials: sum |d - h|^2 w (direct form), sum -2 Re(d^* h) w,
+                            //   sum 2 Re sum_{k<l} h_k conj(h_l) w (the modes' cross terms; 0 for one mode),
+                            //   the rounding estimate (k_refine_select)
   double* gpart;            // [B][n_det][nblk_sparse][11] gradient partials
   void* gblocks;            // [B] SampleBlock<GradScalar>
   double* gdir;             // [B][n_det] direct t_c term of the gradient
@@ -148,16 +149,15 @@ struct MixedDev {
   // sums, |h|^2 w from the transfer splines' coefficients against the data's
   // weight moments (the model's squared modulus is a polynomial in t on each
   // interval), so that only the cross term carries per-bin FP32 rounding.
-  const double* wmom;       // [n_det][nbins][2][3][7] sums over the bins of k's interval before k of
-                            //   t^p W_c and of t^p V_c (W_c = w_c |P|^2 / scale^2, V_c = W_c |d_c|^2 w_c,
-                            //   t = f - f_j)
-  const double* wtot;       // [n_det][J][2][3][7] the same over each whole interval
+  const double* wmom;       // [n_det][nbins][3][7] sums over the bins of k's interval before k of
+                            //   t^p W_c (W_c = w_c |P|^2 / scale^2, t = f - f_j)
+  const double* wtot;       // [n_det][J][3][7] the same over each whole interval
   const double* dsuf;       // [n_det][nbins + 1] sum_{i >= k} sum_c |d_c|^2 w_c (FP64)
   double* wrow;             // [nbins] set-up scratch: one detector's sum_c |d_c|^2 w_c per bin
   float* cgb;               // [B][n_det][J][6] tails b - b_hi of the transfer splines' slope coefficients
-  double* hd;               // [B][n_det][kHdOut] per detector's dense range: sum |h|^2 w, sum |d|^2 w,
-                            //   sum |d|^2 |h|^2 w^2, and the splines' error estimate of sum |h|^2 w
-                            //   from the exact model at the interval midpoints (signed, absolute)
+  double* hd;               // [B][n_det][kHdOut] per detector's dense range: sum |h|^2 w, sum |d|^2 w, 0,
+                            //   and the splines' error estimate of sum |h|^2 w from the exact model at
+                            //   the interval midpoints (signed, absolute), 0
   // Samples whose FP32 or spline error could exceed the accuracy target are
   // re-evaluated exactly over their dense range: the error estimates above
   // use the exact transfer quantities at the interval midpoints.
@@ -175,12 +175,27 @@ struct MixedDev {
   // split form's error estimate uses it.
   const int32_t* wspike;    // [n_det][J] 1 where max_bin W > kSpikeRatio x mean W over the interval
   int32_t rblocks;          // blocks per sample of the exact re-evaluation
-  int32_t rpad;
+  int32_t refine_all;       // 1: every sample in the domain is re-evaluated (exactly where its spline
+                            //   estimate says so, else in float-float)
   double* rpart;            // [B][rblocks] exact dense-range partials of re-evaluated samples
+  // How each sample's dense range is re-evaluated, chosen after the dense
+  // stage from its FP32 rounding estimate (the dense stage's own sum of
+  // |d|^2 |h|^2 w^2) and its splines' error estimate (k_hd): not at all, in
+  // float-float from the same splines (rounding: k_dense_ff), or exactly
+  // (spline error, one-mode plans: k_exact<3>).
+  int32_t* rkind;           // [B] kRefineNone, kRefineFF or kRefineExact
+  double* fpart;            // [B][nblk_dense] float-float dense-range partials
+  // Float-float copies of the FP64 inputs of one bin for k_dense_ff, six rows
+  // per detector: d_A, d_E, d_T (re hi, re lo, im hi, im lo; scaled data),
+  // (w_A hi, lo, w_E hi, lo), (w_T hi, lo, P re hi, lo), (P im hi, lo, 0, 0)
+  // (w the scaled inverse PSD, 0 off the channel mask; P the TDI prefactor).
+  float4* xff;              // [n_det][6][nbins]
 };
 constexpr int kHdOut = 6;
+constexpr int kPartW = 4;  // dense partials per block: direct sum, cross term, modes' cross terms, rounding estimate
+constexpr int kRefineNone = 0, kRefineFF = 1, kRefineExact = 2;
 constexpr double kSpikeRatio = 8.0;
-constexpr int kMomStride = 42;  // doubles per bin (and interval) of wmom / wtot
+constexpr int kMomStride = 21;  // doubles per bin (and interval) of wmom / wtot
 constexpr int kRefineBlocks = 32;  // blocks per sample of the exact re-evaluation
 
 // Error-free transformation: s + e == a + b exactly (Knuth's two-sum).
@@ -1702,37 +1717,48 @@ __global__ void __launch_bounds__(kFitWarps * 32) k_spline_adjoint_staged(MixedD
 }
 
 // ------------------------------------------------------------------ exact bins
-// Error model that decides which samples are re-evaluated exactly over their
-// dense range (the bar is |dlnL| <= 1e-2 against the FP64 evaluation).  The
-// dense stage adds back the splines' midpoint error (k_bump), so what is left
-// is (a) the FP32 rounding of the model in the cross term, a sum of
-// independent per-bin errors whose spread is about 2.2e-7 sqrt(sum |d|^2 |h|^2
-// w^2) (times 2 df, in lnL), modelled as kCrossRel = 4e-7 times that root
-// sum; and (b) the part of the splines' error that the midpoint bump does not
-// capture, modelled as kSplineRel of the intervals' absolute midpoint
-// estimates of sum |h|^2 w.  A sample is refined when the two exceed
-// kRefineTarget: the unrefined ones then have a rounding spread below
-// 2.2e-3, which puts the 1e-2 bar at 4.5 of those spreads.
+// Error model that decides which samples are re-evaluated over their dense
+// range (the bar is |dlnL| <= 1e-2 against the FP64 evaluation).  The dense
+// stage adds back the splines' midpoint error (k_bump), so what is left is
+// (a) the FP32 rounding of the model in the cross term, a sum of independent
+// per-bin errors whose spread is about 2.2e-7 sqrt(sum |d|^2 |h|^2 w^2)
+// (times 2 df, in lnL), modelled as kCrossRel = 4e-7 times that root sum (for
+// several modes the root sum takes sum (|d|^2 + |h|^2) |h|^2 w^2, which also
+// bounds the modes' cross terms h_k conj(h_l) w); and (b) the part of the
+// splines' error that the midpoint bump does not capture, modelled as
+// kSplineRel of the intervals' absolute midpoint estimates of sum |h|^2 w.  A
+// sample is refined when the two exceed kRefineTarget: the unrefined ones
+// then have a rounding spread below 2.2e-3, which puts the 1e-2 bar at 4.5 of
+// those spreads.  A refined sample whose spline part alone stays within the
+// target is re-evaluated in float-float from the same splines (its rounding
+// drops out, k_dense_ff); one-mode samples above it, exactly (k_exact<3>).
 constexpr double kRefineTarget = 4e-3;
 constexpr double kCrossRel = 4e-7;
 constexpr double kSplineRel = 0.01;
 
-__device__ __forceinline__ bool refine_sample(const PlanDev& P, const MixedDev& M, int64_t s) {
-  double sv = 0.0, eha = 0.0;
-  for (int d = 0; d < M.n_det; ++d) {
-    const double* h = M.hd + ((size_t)s * M.n_det + d) * kHdOut;
-    sv += h[2];
-    eha += h[4];
+// one thread per sample, after the dense stage (its rounding sums) and k_hd
+__global__ void k_refine_select(PlanDev P, MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  int kind = kRefineNone;
+  if (blocks[s].status == kSampleOk) {
+    double sq = 0.0, eha = 0.0;
+    for (int k = 0; k < M.nblk_dense; ++k) sq += M.part[((size_t)s * M.nblk_dense + k) * kPartW + 3];
+    for (int k = 0; k < M.n_modes; ++k)
+      for (int d = 0; d < M.n_det; ++d) eha += M.hd[(((size_t)s * M.n_modes + k) * M.n_det + d) * kHdOut + 4];
+    const double er = 2.0 * P.df * kCrossRel * sqrt(fmax(sq, 0.0));
+    const double es = 2.0 * P.df * kSplineRel * eha;
+    if (M.refine_all || er + es > kRefineTarget)
+      kind = (M.n_modes == 1 && es > kRefineTarget) ? kRefineExact : kRefineFF;
   }
-  const double e = 2.0 * P.df * (kCrossRel * sqrt(fmax(sv, 0.0)) + kSplineRel * eha);
-  return e > kRefineTarget;
+  M.rkind[s] = kind;
 }
 
 // Bins [0, xbind[s][d]) of each detector evaluated directly (FP64 model and residual against the
 // FP64 data).  kMode 0: lnL partials (T = double); 1: gradient partials
 // (T = GradScalar, FP64 values with FP32 tangents); 2: write the model;
 // 3: lnL partials of bins [xbind[s][d], kcut) of the samples that
-// refine_sample selects (the exact re-evaluation of their dense range).
+// k_refine_select sends to the exact re-evaluation of their dense range.
 // grid (xblocks or rblocks, B); threads stride over the sample's exact bins.
 template <int kMode, class T>
 __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, GenArg G,
@@ -1753,7 +1779,7 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   const int nm = M.n_modes;
   const int xb = M.xbin[(size_t)s * nm];
   if (!kRefine && xb == 0) return;  // uniform per block; the finalizers skip such samples
-  if (kRefine && (blocks[s].status != kSampleOk || !refine_sample(P, M, s))) return;
+  if (kRefine && (blocks[s].status != kSampleOk || M.rkind[s] != kRefineExact)) return;
   load_block(blocks, s, sb);
   if (kFF && M.hm) load_hm(M.hm, s, hmd);
   __syncthreads();
@@ -1990,22 +2016,24 @@ struct RunPhase {
   float qx0, qj;          // multi-mode plans: the straddled phase corner (Msec f - Mf_c at the run start, Jh)
 };
 
-// Per-run phase anchors in FP64, one thread per (sample, detector, run) with a
-// live, non-exact bin: the phase spline and the 2 pi f t_c term at the run's
-// first bin, wrapped, split into an FP32 head/tail phasor and exact-product
-// FP32 heads (with tails) of the per-bin increment polynomial; and the
-// peak-kink coordinate Msec f - Mf_peak at the run start.
-__global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
-                                                      const SampleBlock<double>* __restrict__ blocks) {
-  const int s = blockIdx.z, d = blockIdx.y;  // s: virtual sample (sample, mode)
-  const int c = blockIdx.x * 128 + threadIdx.x;
-  if (blocks[s / M.n_modes].status != kSampleOk || c >= M.nch[s]) return;
-  const int kb = M.ch_begin[c];
-  if (kb < M.xbind[(size_t)s * M.n_det + d]) return;
-  const size_t sd = (size_t)s * M.n_det + d;
-  const int j = M.ch_iv[c];
-  const float4 sa = M.sff[2 * s], sbk = M.sff[2 * s + 1];
-  const FF tcf = ff_make(sa.x, sa.y), msf = ff_make(sa.z, sa.w), fpf = ff_make(sbk.x, sbk.y);
+// The phase of run c (first bin kb, interval j) of virtual sample s on
+// detector d (sd = s * n_det + d) in float-float: the phase spline plus
+// 2 pi f t_c at the run's first bin, wrapped (ph0), and the per-bin
+// increment polynomial ph1 u + ph2 u^2 + ph3 u^3 (u = bins past the first;
+// ph1 wrapped).  Past a multi-mode plan's phase corner its term is included;
+// the corner that the run straddles is returned (qk, and Msec f - Mf_c at the
+// run start and Jh in FP32) to be added per bin.
+struct AnchorFF {
+  FF ph0, ph1, ph2, ph3;
+  FF fbf;         // frequency of the run's first bin
+  float qx0, qj;  // the straddled corner (0 when none)
+  int qk;         // its index, -1 when none
+};
+__device__ __forceinline__ AnchorFF run_anchor_ff(const PlanDev& P, const MixedDev& M, int s, size_t sd, int c,
+                                                  int kb, int j) {
+  AnchorFF A;
+  const float4 sa = M.sff[2 * s];
+  const FF tcf = ff_make(sa.x, sa.y), msf = ff_make(sa.z, sa.w);
   const FF* co = M.cphi + (sd * M.J + j) * 4;
   const FF a = co[0], b = co[1], cc = co[2], dd = co[3];
   const float2 nfj = M.node_ff[j];
@@ -2016,7 +2044,9 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
   FF S1 = b + t * (ff_mulf(cc, 2.0f) + ff_mulf(ddt, 3.0f));
   FF S2 = cc + ff_mulf(ddt, 3.0f);
   const FF D = M.fstep_ff;
-  float qx0 = 0.0f, qj = 0.0f;  // the corner that the run straddles (added per bin)
+  A.qx0 = 0.0f;
+  A.qj = 0.0f;
+  A.qk = -1;
   if (M.pkink) {
     // the phase's corner terms Jh (Msec f - Mf_c)^2: value, slope and
     // curvature at the run start for runs past the corner
@@ -2031,8 +2061,9 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
         S1 = S1 + ff_mulf(jq * (xq * msf), 2.0f);
         S2 = S2 + jq * (msf * msf);
       } else if (xq.hi + last > 0.0f) {
-        qx0 = xq.hi;
-        qj = jq.hi;
+        A.qx0 = xq.hi;
+        A.qj = jq.hi;
+        A.qk = q;
       }
     }
   }
@@ -2054,20 +2085,41 @@ __global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
       ph0 = ff_from(p - (2.0 * kPi) * rint(p * (1.0 / (2.0 * kPi))));
     }
   }
-  const FF ph1 = ff_wrap_2pi(D * (S1 + tcf * (2.0 * kPi)));
-  const FF ph2 = (D * D) * S2;
-  const FF ph3 = (D * D) * (D * dd);
-  const float x0 = (msf * fbf - fpf).hi;
+  A.ph0 = ph0;
+  A.ph1 = ff_wrap_2pi(D * (S1 + tcf * (2.0 * kPi)));
+  A.ph2 = (D * D) * S2;
+  A.ph3 = (D * D) * (D * dd);
+  A.fbf = fbf;
+  return A;
+}
+
+// Per-run phase anchors, one thread per (sample, detector, run) with a live,
+// non-exact bin: the float-float anchor split into an FP32 head/tail phasor
+// and exact-product FP32 heads (with tails) of the per-bin increment
+// polynomial; and the peak-kink coordinate Msec f - Mf_peak at the run start.
+__global__ void __launch_bounds__(128) k_run_anchors(PlanDev P, MixedDev M,
+                                                      const SampleBlock<double>* __restrict__ blocks) {
+  const int s = blockIdx.z, d = blockIdx.y;  // s: virtual sample (sample, mode)
+  const int c = blockIdx.x * 128 + threadIdx.x;
+  if (blocks[s / M.n_modes].status != kSampleOk || c >= M.nch[s]) return;
+  const int kb = M.ch_begin[c];
+  if (kb < M.xbind[(size_t)s * M.n_det + d]) return;
+  const size_t sd = (size_t)s * M.n_det + d;
+  const int j = M.ch_iv[c];
+  const AnchorFF A = run_anchor_ff(P, M, s, sd, c, kb, j);
+  const float4 sa = M.sff[2 * s], sbk = M.sff[2 * s + 1];
+  const FF msf = ff_make(sa.z, sa.w), fpf = ff_make(sbk.x, sbk.y);
+  const float x0 = (msf * A.fbf - fpf).hi;
   // anchor phasor: sincos of the float head, rotated by the (tiny) tail
   float s0f, c0f;
-  sincos_poly(ph0.hi, &s0f, &c0f);
-  const float l0 = ph0.lo;
+  sincos_poly(A.ph0.hi, &s0f, &c0f);
+  const float l0 = A.ph0.lo;
   float p1l, p2l, p3l;
-  const float p1h = ff_head(ph1, 12, &p1l), p2h = ff_head(ph2, 13, &p2l), p3h = ff_head(ph3, 8, &p3l);
+  const float p1h = ff_head(A.ph1, 12, &p1l), p2h = ff_head(A.ph2, 13, &p2l), p3h = ff_head(A.ph3, 8, &p3l);
   float4* o = M.runs + (sd * M.nchunks + c) * 3;
   o[0] = make_float4(x0, fmaf(-s0f, l0, c0f), fmaf(c0f, l0, s0f), p1h);
   o[1] = make_float4(p1l, p2h, p2l, p3h);
-  o[2] = make_float4(p3l, qx0, qj, 0.0f);
+  o[2] = make_float4(p3l, A.qx0, A.qj, 0.0f);
 }
 
 // Warp-sum of the 28 per-lane interval moments through shared memory (rows
@@ -2211,7 +2263,7 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
   static_assert(kNM == 1 || (!kGrad && !kStage), "multi-mode dense stage: lnL and model passes, no staging");
-  __shared__ double red[kMixThreads / 32][3];
+  __shared__ double red[kMixThreads / 32][kPartW];
   // per warp, two run buffers: the next run's inputs are copied while this one is computed
   __shared__ __align__(16) float4 rbuf[kStage ? kMixThreads / 32 : 1][kStage ? 2 : 1][kStage ? kRunBuf : 1];
   __shared__ float msm[kGrad ? kMixThreads / 32 : 1][kGrad ? kNodeQ * kMoments : 1][kGrad ? kMomPad : 1];
@@ -2227,6 +2279,7 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
   float dsh = 0.0f, dsl = 0.0f;  // float-float sum of the FP64 |d|^2/S of the weak-template bins
   float xacc = 0.0f, xcomp = 0.0f;  // compensated sum of the cross term -2 Re(d^* h) w
   float macc = 0.0f, mcomp = 0.0f;  // multi-mode plans: compensated sum of 2 Re sum_{k<l} h_k conj(h_l) w
+  float sqa = 0.0f;  // rounding estimate: sum |d|^2 |h|^2 w^2 (several modes: (|d|^2 + |h|^2) |h|^2 w^2)
   if (blocks[s].status == kSampleOk && first < nc) {
     for (int d = 0; d < M.n_det; ++d) {
       const size_t sd = (size_t)s * kNM * M.n_det + d;  // (virtual sample of mode 0, detector)
@@ -2441,6 +2494,7 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
           float aphi = 0.0f;
           float ag[6];
           float mterm = 0.0f;
+          float sqb = 0.0f;
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float hr = hrs[ch], hi = his[ch];
@@ -2452,6 +2506,11 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
             term = fmaf(fmaf(er, er, ei * ei), w, term);
             const float h2 = fmaf(hr, hr, hi * hi);
             hh = fmaf(h2, w, hh);
+            {
+              const float hw = h2 * w;
+              const float a2 = fmaf(dv.x, dv.x, dv.y * dv.y) + (kNM > 1 ? h2 : 0.0f);
+              sqb = fmaf(a2 * hw, w, sqb);
+            }
             const float dh = fmaf(dv.x, hr, dv.y * hi);
             cross = fmaf(fmaf(-2.0f, dh, h2), w, cross);
             xdh = fmaf(dh, w, xdh);
@@ -2486,6 +2545,7 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
             xcomp = (tx - xacc) - yx;
             xacc = tx;
           }
+          sqa += sqb;
           if (kNM > 1) {
             const float ym_ = mterm - mcomp;
             const float tm_ = macc + ym_;
@@ -2555,17 +2615,179 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
     mh = th;
     ml += tl + ql;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sqa += __shfl_down_sync(0xffffffffu, sqa, o);
   if (lane == 0) {
     red[wid][0] = (double)vh + (double)vl;
     red[wid][1] = (double)xh + (double)xl;
     red[wid][2] = (double)mh + (double)ml;
+    red[wid][3] = (double)sqa;
   }
   __syncthreads();
-  if (threadIdx.x < 3) {
+  if (threadIdx.x < kPartW) {
     double x = 0.0;
 #pragma unroll
     for (int w = 0; w < kMixThreads / 32; ++w) x += red[w][threadIdx.x];
-    M.part[((size_t)s * M.nblk_dense + blockIdx.x) * 3 + threadIdx.x] = x;
+    M.part[((size_t)s * M.nblk_dense + blockIdx.x) * kPartW + threadIdx.x] = x;
+  }
+}
+
+// The float-float re-evaluation of the dense range of the samples that
+// k_refine_select sends to it (rkind == kRefineFF): the dense stage's model
+// (transfer splines with their midpoint corrections and kink, phase anchors,
+// TDI prefactor, modes summed per bin), with every step from the spline
+// coefficients to the residual |d - h|^2 w in float-float against
+// float-float copies of the FP64 data, weights and prefactor.  The per-bin
+// rounding falls from about 2e-7 of the terms to below 1e-13, so what is
+// left of the error is the splines' own.  Same grid and run groups as
+// k_dense_mixed; lane l of a warp first takes the phase anchor of the
+// group's run l of every mode (shared memory), then each run takes a bin
+// per lane.  Partials: fpart [B][nblk_dense].
+template <int kNM>
+__global__ void __launch_bounds__(kMixThreads) k_dense_ff(PlanDev P, MixedDev M,
+                                                          const SampleBlock<double>* __restrict__ blocks) {
+  __shared__ float4 anc[kMixThreads / 32][kNM][kChunkMax][2];  // ph0, ph1 | ph2, ph3 (hi, lo pairs)
+  __shared__ int ancq[kMixThreads / 32][kNM][kChunkMax];        // the straddled phase corner, -1 when none
+  __shared__ double red[kMixThreads / 32];
+  const int s = blockIdx.y;
+  if (M.rkind[s] != kRefineFF) return;  // uniform per block
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int first = (blockIdx.x * (kMixThreads / 32) + wid) * kChunkMax;
+  int nc = M.nch[(size_t)s * kNM];
+#pragma unroll
+  for (int k = 1; k < kNM; ++k) nc = max(nc, M.nch[(size_t)s * kNM + k]);
+  const int64_t kcut = blocks[s].kcut;
+  FF acc = ff_make(0.0f, 0.0f);
+  if (first < nc) {
+    const int last = min(nc, first + kChunkMax);
+    for (int d = 0; d < M.n_det; ++d) {
+      const size_t sd = (size_t)s * kNM * M.n_det + d;  // (virtual sample of mode 0, detector)
+      const int xb = M.xbind[sd];
+      {
+        const int c = first + lane;
+#pragma unroll 1
+        for (int k = 0; k < kNM; ++k) {
+          const int v = s * kNM + k;
+          float4 a0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), a1 = a0;
+          int qk = -1;
+          if (c < M.nch[v] && M.ch_begin[c] >= xb) {
+            const AnchorFF A = run_anchor_ff(P, M, v, sd + (size_t)k * M.n_det, c, M.ch_begin[c], M.ch_iv[c]);
+            a0 = make_float4(A.ph0.hi, A.ph0.lo, A.ph1.hi, A.ph1.lo);
+            a1 = make_float4(A.ph2.hi, A.ph2.lo, A.ph3.hi, A.ph3.lo);
+            qk = A.qk;
+          }
+          anc[wid][k][lane][0] = a0;
+          anc[wid][k][lane][1] = a1;
+          ancq[wid][k][lane] = qk;
+        }
+      }
+      __syncwarp();
+      for (int c = first; c < last; ++c) {
+        const int kb = M.ch_begin[c];
+        if (kb < xb) continue;  // exact bins
+        const int j = M.ch_iv[c];
+        const int64_t i = (int64_t)kb + lane;
+        if (lane >= M.ch_len[c] || i >= kcut) continue;
+        const FF f = ff_mulf(M.fstep_ff, (float)(P.k0 + i));  // k0 + i < 2^24: exact in FP32
+        const float2 nfj = M.node_ff[j];
+        const FF t = f - ff_make(nfj.x, nfj.y);
+        const float tf = t.hi, u = (float)lane;
+        FF hr[3], hi[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) hr[ch] = hi[ch] = ff_make(0.0f, 0.0f);
+#pragma unroll 1
+        for (int k = 0; k < kNM; ++k) {
+          const int v = s * kNM + k;
+          if (kNM > 1 && (c >= M.nch[v] || i >= M.vcut[v])) continue;  // past the mode's range
+          const size_t sdk = sd + (size_t)k * M.n_det;
+          const float4 a0 = anc[wid][k][c - first][0], a1 = anc[wid][k][c - first][1];
+          FF ph = ff_make(a0.x, a0.y) + ff_mulf(ff_make(a0.z, a0.w), u);
+          ph = ph + ff_mulf(ff_make(a1.x, a1.y), u * u);  // u^2, u^3 < 2^15: exact
+          ph = ph + ff_mulf(ff_make(a1.z, a1.w), u * u * u);
+          const float4 sa = M.sff[2 * v];
+          const FF msf = ff_make(sa.z, sa.w);
+          if (kNM > 1) {
+            const int qk = ancq[wid][k][c - first];
+            if (qk >= 0) {
+              const float4 k4 = M.pkink[2 * v + qk];
+              const FF xq = msf * f - ff_make(k4.x, k4.y);
+              if (xq.hi > 0.0f) ph = ph + ff_make(k4.z, k4.w) * (xq * xq);
+            }
+          }
+          FF sn, cs;
+          dsincos(ff_wrap_2pi(ph), &sn, &cs);
+          // the mode's transfer quantities on interval j: the spline (value and
+          // slope coefficients in float-float), its midpoint correction, the kink
+          const float4* G = M.cg + (sdk * M.J + j) * 8;
+          const float4 gl0 = G[6], gl1 = G[7];
+          const float alo[6] = {gl0.x, gl0.y, gl0.z, gl0.w, gl1.x, gl1.y};
+          const float* blo = M.cgb + (sdk * M.J + j) * 6;
+          const float4* BQ = M.cbump + (sdk * M.J + j) * 2;
+          const float4 b0 = BQ[0], b1 = BQ[1];
+          const float rr = tf * (b1.z - tf) * b1.w;
+          const float r2 = rr * rr;
+          const float bump[6] = {b0.x * r2, b0.y * r2, b0.z * r2, b0.w * r2, b1.x * r2, b1.y * r2};
+          const float4* KF4 = reinterpret_cast<const float4*>(M.kinkF + sdk * 16);
+          const float4 k0 = KF4[0], k1 = KF4[1], k2 = KF4[2], k3 = KF4[3];
+          bool kinked = false;
+          FF x2 = ff_make(0.0f, 0.0f);
+          if (kNM == 1 || j == (int)k3.z) {
+            const float4 sk = M.sff[2 * v + 1];
+            const FF x = msf * f - ff_make(sk.x, sk.y);
+            if (x.hi > 0.0f) {
+              kinked = true;
+              x2 = x * x;
+            }
+          }
+          const float kfh[6] = {k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+          const float kfl[6] = {k2.x, k2.y, k2.z, k2.w, k3.x, k3.y};
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            FF g[2];
+#pragma unroll
+            for (int pp = 0; pp < 2; ++pp) {
+              const int q = 2 * ch + pp;
+              const float4 c4 = G[q];
+              FF gq = ff_make(c4.x, alo[q]) + t * ff_addf(ff_make(c4.y, blo[q]), tf * fmaf(tf, c4.w, c4.z));
+              gq = ff_addf(gq, bump[q]);
+              if (kinked) gq = gq + ff_make(kfh[q], kfl[q]) * x2;
+              g[pp] = gq;
+            }
+            // G e^{-i phase} = (g0 + i g1)(cos - i sin)
+            hr[ch] = hr[ch] + (g[0] * cs + g[1] * sn);
+            hi[ch] = hi[ch] + (g[1] * cs - g[0] * sn);
+          }
+        }
+        // TDI prefactor, residual against the data, weight
+        const float4* X = M.xff + (size_t)d * 6 * P.nbins + i;
+        const float4 x3 = X[3 * (size_t)P.nbins], x4 = X[4 * (size_t)P.nbins], x5 = X[5 * (size_t)P.nbins];
+        const FF pr = ff_make(x4.z, x4.w), pim = ff_make(x5.x, x5.y);
+        const FF wch[3] = {ff_make(x3.x, x3.y), ff_make(x3.z, x3.w), ff_make(x4.x, x4.y)};
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          const float4 dv = X[(size_t)ch * P.nbins];
+          const FF er = ff_make(dv.x, dv.y) - (hr[ch] * pr - hi[ch] * pim);
+          const FF ei = ff_make(dv.z, dv.w) - (hr[ch] * pim + hi[ch] * pr);
+          acc = acc + (er * er + ei * ei) * wch[ch];
+        }
+      }
+      __syncwarp();  // the next detector's anchors overwrite this one's
+    }
+  }
+  // lanes and warps in float-float, the block partial in FP64
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, acc.hi, o);
+    const float ol = __shfl_down_sync(0xffffffffu, acc.lo, o);
+    acc = acc + ff_make(oh, ol);
+  }
+  if (lane == 0) red[wid] = ff_to(acc);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0.0;
+#pragma unroll
+    for (int w = 0; w < kMixThreads / 32; ++w) x += red[w];
+    M.fpart[(size_t)s * M.nblk_dense + blockIdx.x] = x;
   }
 }
 
@@ -2641,7 +2863,7 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
   const double* KC = M.kinkC + sd * 6;
   const double* wm = M.wmom + (size_t)d * P.nbins * kMomStride;
   const FF* ym = M.ym + (size_t)sd * 7 * M.J;
-  double sum = 0.0, sumv = 0.0, eh = 0.0, eha = 0.0;
+  double sum = 0.0, eh = 0.0, eha = 0.0;
   for (int j = jlo + lane; j <= jhi; j += kHdThreads) {
     const int64_t e1 = M.iv_first[j], e2 = M.iv_first[j + 1];
     const int64_t k1 = max(e1, lo), k2 = min(e2, kcut);
@@ -2677,14 +2899,13 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
 #pragma unroll
       for (int q = 0; q < 6; ++q) gm[q] += KC[q] * Xm * Xm;
     }
-    double Sm[42];
+    double Sm[21];
     // [k1, ks) without the kink term, [ks, k2) with it (folded intervals hold it already)
     const int64_t ks = folded ? k2 : min(max(kpk, k1), k2);
     if (ks > k1) {
 #pragma unroll
-      for (int x = 0; x < 42; ++x) Sm[x] = F(ks, x) - F(k1, x);
+      for (int x = 0; x < 21; ++x) Sm[x] = F(ks, x) - F(k1, x);
       sum += hd_piece(A, Bc, Cc, Dc, Sm);
-      sumv += hd_piece(A, Bc, Cc, Dc, Sm + 21);
     }
     if (ks < k2) {
       const double X0 = Msec * M.node_f[j] - fpk;
@@ -2696,9 +2917,8 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
         C2[q] = Cc[q] + KC[q] * Msec * Msec;
       }
 #pragma unroll
-      for (int x = 0; x < 42; ++x) Sm[x] = F(k2, x) - F(ks, x);
+      for (int x = 0; x < 21; ++x) Sm[x] = F(k2, x) - F(ks, x);
       sum += hd_piece(A2, B2, C2, Dc, Sm);
-      sumv += hd_piece(A2, B2, C2, Dc, Sm + 21);
     }
     // first-order change of sum |h|^2 w over the interval if the splines' error
     // had the shape 16 t^2 (h - t)^2 / h^4 times its midpoint value
@@ -2719,13 +2939,12 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    sumv += __shfl_xor_sync(0xffffffffu, sumv, o);
     eh += __shfl_xor_sync(0xffffffffu, eh, o);
     eha += __shfl_xor_sync(0xffffffffu, eha, o);
   }
   if ((lane & 31) == 0) {
     red[lane >> 5][0] = sum;
-    red[lane >> 5][1] = sumv;
+    red[lane >> 5][1] = 0.0;
     red[lane >> 5][2] = eh;
     red[lane >> 5][3] = eha;
   }
@@ -2759,14 +2978,14 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   // rounding of the model enters only the cross term
   double R = 0.0, X = 0.0, H = 0.0, Dd = 0.0, Cm = 0.0;
   for (int k = 0; k < M.nblk_dense; ++k) {
-    R += M.part[((size_t)s * M.nblk_dense + k) * 3];
-    X += M.part[((size_t)s * M.nblk_dense + k) * 3 + 1];
-    Cm += M.part[((size_t)s * M.nblk_dense + k) * 3 + 2];
+    R += M.part[((size_t)s * M.nblk_dense + k) * kPartW];
+    X += M.part[((size_t)s * M.nblk_dense + k) * kPartW + 1];
+    Cm += M.part[((size_t)s * M.nblk_dense + k) * kPartW + 2];
   }
   if (M.n_modes > 1) {
     // multi-mode plans: the split form for far templates with sum |h|^2 w =
     // the modes' own sums (exact, from their splines) + their cross terms
-    // (dense stage); no refinement
+    // (dense stage); refinement in float-float only
     for (int k = 0; k < M.n_modes; ++k)
       for (int d = 0; d < M.n_det; ++d) {
         const double* hv = M.hd + (((size_t)s * M.n_modes + k) * M.n_det + d) * kHdOut;
@@ -2775,6 +2994,10 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
     for (int d = 0; d < M.n_det; ++d) Dd += M.hd[((size_t)s * M.n_modes * M.n_det + d) * kHdOut + 1];
     const double Ht = H + Cm;
     double acc = (R > 2.0 * sqrt(fmax(Ht, 0.0) * Dd)) ? (Dd + X) + Ht : R;
+    if (M.rkind[s] == kRefineFF) {  // the float-float re-evaluation of the dense range
+      acc = 0.0;
+      for (int k = 0; k < M.nblk_dense; ++k) acc += M.fpart[(size_t)s * M.nblk_dense + k];
+    }
     if (M.xbin[s * M.n_modes] > 0)
       for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
     const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
@@ -2788,9 +3011,12 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
     Dd += M.hd[((size_t)s * M.n_det + d) * kHdOut + 1];
   }
   double acc = (R > 2.0 * sqrt(H * Dd)) ? (Dd + X) + H : R;
-  if (refine_sample(P, M, s)) {  // the exact re-evaluation of the dense range
+  if (M.rkind[s] == kRefineExact) {  // the exact re-evaluation of the dense range
     acc = 0.0;
     for (int k = 0; k < M.rblocks; ++k) acc += M.rpart[(size_t)s * M.rblocks + k];
+  } else if (M.rkind[s] == kRefineFF) {  // the float-float one
+    acc = 0.0;
+    for (int k = 0; k < M.nblk_dense; ++k) acc += M.fpart[(size_t)s * M.nblk_dense + k];
   }
   if (M.xbin[s] > 0)
     for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
@@ -2828,12 +3054,17 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
   if (i >= P.nbins) return;
   double dd = 0.0;
   float dr[3], di[3], wf[3];
+  FF wff[3];
+  float4* X = M.xff + (size_t)det * 6 * P.nbins + i;
   for (int ch = 0; ch < 3; ++ch) {
     const double2 v = data[ch * P.nbins + i];
-    dr[ch] = (float)(v.x * M.scale);
-    di[ch] = (float)(v.y * M.scale);
+    const FF re = ff_from(v.x * M.scale), im = ff_from(v.y * M.scale);
+    dr[ch] = re.hi;
+    di[ch] = im.hi;
+    X[(size_t)ch * P.nbins] = make_float4(re.hi, re.lo, im.hi, im.lo);
     const bool on = (P.chan_mask >> ch) & 1;
-    wf[ch] = on ? (float)(1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale)) : 0.0f;
+    wff[ch] = on ? ff_from(1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale)) : ff_make(0.0f, 0.0f);
+    wf[ch] = wff[ch].hi;
     if (on) dd += (v.x * v.x + v.y * v.y) / psd[ch * P.nbins + i];
   }
   const float hi = (float)dd;
@@ -2844,6 +3075,10 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
   pk[i] = make_float4(dr[0], di[0], dr[1], di[1]);
   pk[P.nbins + i] = make_float4(dr[2], di[2], wf[0], wf[1]);
   pk[2 * P.nbins + i] = make_float4(wf[2], (float)tf.pre, (float)tf.pim, M.bin_t[i]);
+  const FF pre = ff_from(tf.pre), pim = ff_from(tf.pim);
+  X[3 * (size_t)P.nbins] = make_float4(wff[0].hi, wff[0].lo, wff[1].hi, wff[1].lo);
+  X[4 * (size_t)P.nbins] = make_float4(wff[2].hi, wff[2].lo, pre.hi, pre.lo);
+  X[5 * (size_t)P.nbins] = make_float4(pim.hi, pim.lo, 0.0f, 0.0f);
 }
 
 // Within-interval weight moments of detector det (set-up): one thread per
@@ -2874,25 +3109,21 @@ __global__ void k_wspike(PlanDev P, MixedDev M, int det, int32_t* __restrict__ o
 
 __global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ wmom, double* __restrict__ wtot) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (M.J - 1) * 6) return;
-  const int j = t / 6, c = t % 3, v = (t % 6) / 3;  // v = 1: data-weighted moments
+  if (t >= (M.J - 1) * 3) return;
+  const int j = t / 3, c = t % 3;
   const int64_t k1 = M.iv_first[j], k2 = M.iv_first[j + 1];
   const double fj = M.node_f[j];
   const double is2 = 1.0 / (M.scale * M.scale);
   double acc[7];
 #pragma unroll
   for (int p = 0; p < 7; ++p) acc[p] = 0.0;
-  double* pm = wmom + (size_t)det * P.nbins * kMomStride + v * 21 + c * 7;
+  double* pm = wmom + (size_t)det * P.nbins * kMomStride + c * 7;
   for (int64_t k = k1; k < k2; ++k) {
     const double tk = (double)(P.k0 + k) * P.f_step - fj;
     const TdiFactor tf = P.tdi[(size_t)det * P.nbins + k];
     const size_t off = ((size_t)det * 3 + c) * P.nbins + k;
     const double w = P.w[off];
     double tp = w * (tf.pre * tf.pre + tf.pim * tf.pim) * is2;
-    if (v) {
-      const double2 dv = P.data[off];
-      tp *= (dv.x * dv.x + dv.y * dv.y) * w;
-    }
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
       pm[(size_t)k * kMomStride + p] = acc[p];
@@ -2900,7 +3131,7 @@ __global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ 
       tp *= tk;
     }
   }
-  double* tot = wtot + ((size_t)det * M.J + j) * kMomStride + v * 21 + c * 7;
+  double* tot = wtot + ((size_t)det * M.J + j) * kMomStride + c * 7;
 #pragma unroll
   for (int p = 0; p < 7; ++p) tot[p] = acc[p];
 }
@@ -3055,7 +3286,9 @@ int mixed_create(PesPlan* p) {
   float2* node_ff;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst, *vcut, *wspk;
   double *xpart, *xgpart;
-  double *wmom, *wtot, *dsuf, *wrow, *hdv, *rpart;
+  double *wmom, *wtot, *dsuf, *wrow, *hdv, *rpart, *fpart;
+  int32_t* rkind;
+  float4* xff;
   float* cgb;
   float2* mid_ff;
   float4* tdm_ff;
@@ -3084,13 +3317,14 @@ int mixed_create(PesPlan* p) {
       (rc = alloc(mb, &cfrac, (size_t)V)) || (rc = alloc(mb, &node_ff, J)) ||
       (rc = alloc(mb, &cphi, sd * J * 4)) || (rc = alloc(mb, &cg, sd * J * 8)) ||
       (rc = alloc(mb, &mom, gsd * J * kNodeQ * kMoments)) || (rc = alloc(mb, &ybar, gsd * kNodeQ * J)) ||
-      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense * 3)) ||
+      (rc = alloc(mb, &part, (size_t)B * M.nblk_dense * kPartW)) ||
       (rc = alloc(mb, &wmom, wn)) || (rc = alloc(mb, &wtot, wj)) ||
       (rc = alloc(mb, &dsuf, (size_t)nd * (n + 1))) || (rc = alloc(mb, &wrow, (size_t)n)) ||
       (rc = alloc(mb, &cgb, sd * J * 6)) || (rc = alloc(mb, &hdv, sd * kHdOut)) ||
       (rc = alloc(mb, &mid_ff, J)) || (rc = alloc(mb, &tdm_ff, (size_t)nd * J)) || (rc = alloc(mb, &ymv, sd * 7 * J)) ||
       (rc = alloc(mb, &cbump, sd * J * 2)) || (rc = alloc(mb, &wspk, (size_t)nd * J)) ||
-      (rc = alloc(mb, &rpart, (size_t)B * kRefineBlocks)) ||
+      (rc = alloc(mb, &rpart, (size_t)B * kRefineBlocks)) || (rc = alloc(mb, &rkind, (size_t)B)) ||
+      (rc = alloc(mb, &fpart, (size_t)B * M.nblk_dense)) || (rc = alloc(mb, &xff, (size_t)nd * 6 * n)) ||
       (rc = alloc(mb, &gpart, gsd * M.nblk_sparse * 11)) || (rc = alloc(mb, &gdir, gsd)) ||
       (rc = alloc(mb, &gblk, (size_t)B)) || (rc = alloc(mb, &kR, sd * 6)) || (rc = alloc(mb, &kC, sd * 6)) ||
       (rc = alloc(mb, &kF, sd * 16)) || (rc = alloc(mb, &kM, gsd * 12)) || (rc = alloc(mb, &xbin, V)) || (rc = alloc(mb, &xbind, sd)) ||
@@ -3235,6 +3469,12 @@ int mixed_create(PesPlan* p) {
   PES_CHECK_CUDA(cudaMemset(wspk, 0, sizeof(int32_t) * nd * J));
   M.rpart = rpart;
   M.rblocks = kRefineBlocks;
+  M.refine_all = 0;
+  M.rkind = rkind;
+  M.fpart = fpart;
+  M.xff = xff;
+  PES_CHECK_CUDA(cudaMemset(rkind, 0, sizeof(int32_t) * B));
+  PES_CHECK_CUDA(cudaMemset(xff, 0, sizeof(float4) * nd * 6 * n));
   {
     // interval midpoints and their TDI delay factors (the last node has no interval)
     std::vector<float2> mff(J);
@@ -3269,6 +3509,13 @@ void mixed_stage_option(PesPlan* p, int set, int64_t* value) {
     *value = p->mixed->stage_grad ? 1 : 0;
 }
 
+void mixed_refine_option(PesPlan* p, int set, int64_t* value) {
+  if (set)
+    p->mixed->dev.refine_all = *value != 0;
+  else
+    *value = p->mixed->dev.refine_all;
+}
+
 void mixed_destroy(PesPlan* p) {
   if (!p->mixed) return;
   if (p->mixed->side) cudaStreamSynchronize(p->mixed->side);
@@ -3297,7 +3544,7 @@ int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cud
   PES_CHECK_LAUNCH();
   suffix_sum(p->desc.nbins, M.wrow, const_cast<double*>(M.dsuf) + (size_t)det * (p->desc.nbins + 1), st);
   PES_CHECK_LAUNCH();
-  k_wmoments<<<ceil_div((M.J - 1) * 6, 128), 128, 0, st>>>(p->dev, M, det, const_cast<double*>(M.wmom),
+  k_wmoments<<<ceil_div((M.J - 1) * 3, 128), 128, 0, st>>>(p->dev, M, det, const_cast<double*>(M.wmom),
                                                             const_cast<double*>(M.wtot));
   PES_CHECK_LAUNCH();
   k_wspike<<<ceil_div(M.J, 128), 128, 0, st>>>(p->dev, M, det, const_cast<int32_t*>(M.wspike));
@@ -3345,10 +3592,11 @@ int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const st
                int64_t* out, cudaStream_t st) {
   const MixedDev& M = p->mixed->dev;
   const int nm = M.n_modes;
-  std::vector<int32_t> xb((size_t)B * nm * M.n_det), ns((size_t)B * nm);
+  std::vector<int32_t> xb((size_t)B * nm * M.n_det), ns((size_t)B * nm), rk((size_t)B);
   if (B > 0) {
     PES_CHECK_CUDA(cudaMemcpy(xb.data(), M.xbind, sizeof(int32_t) * xb.size(), cudaMemcpyDeviceToHost));
     PES_CHECK_CUDA(cudaMemcpy(ns.data(), M.nsp, sizeof(int32_t) * ns.size(), cudaMemcpyDeviceToHost));
+    PES_CHECK_CUDA(cudaMemcpy(rk.data(), M.rkind, sizeof(int32_t) * rk.size(), cudaMemcpyDeviceToHost));
   }
   // dense and exact bins per sample (a bin sums all modes); sparse nodes per mode
   for (int64_t s = 0; s < B; ++s) {
@@ -3359,6 +3607,8 @@ int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const st
     }
     for (int k = 0; k < nm; ++k)
       if (ns[(size_t)s * nm + k] >= 3) out[2] += (int64_t)(ns[(size_t)s * nm + k] + 1) * M.n_det;
+    out[4] += rk[s] == kRefineFF;
+    out[5] += rk[s] == kRefineExact;
   }
   (void)st;
   return PES_OK;
@@ -3467,20 +3717,33 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   // on the side stream after its exact low-frequency bins: beside the dense
   // stage for lnL calls, beside the adjoint stages (after the dense stage)
   // for lnL+gradient calls, where it does not take SMs from the dense stage.
+  // After the dense stage (its rounding sums) and k_hd: which samples to
+  // re-evaluate and how, then the re-evaluations, on the side stream (beside
+  // the adjoint stages of lnL+gradient calls).
   auto refine = [&]() -> int {
+    PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_dense, 0));
+    {
+      ProfScope ps(p, kKOther, side);
+      k_refine_select<<<ceil_div(B, 64), 64, 0, side>>>(p->dev, M, blocks, B);
+    }
+    PES_CHECK_LAUNCH();
     if (!multi) {
       ProfScope ps(p, kKDenseFp64, side);
       k_exact<3, double><<<dim3(M.rblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+    }
+    PES_CHECK_LAUNCH();
+    {
+      ProfScope ps(p, kKOther, side);
+      if (multi)
+        k_dense_ff<kHMModes><<<dim3(M.nblk_dense, (unsigned)B), kMixThreads, 0, side>>>(p->dev, M, blocks);
+      else
+        k_dense_ff<1><<<dim3(M.nblk_dense, (unsigned)B), kMixThreads, 0, side>>>(p->dev, M, blocks);
     }
     PES_CHECK_LAUNCH();
     PES_CHECK_CUDA(cudaEventRecord(p->mixed->join, side));
     return PES_OK;
   };
   PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_hd, 0));
-  if (!grad) {
-    const int rc = refine();
-    if (rc != PES_OK) return rc;
-  }
   if (grad) {
     PES_CHECK_CUDA(cudaMemsetAsync(M.mom, 0, sizeof(float) * B * M.n_det * M.J * kNodeQ * kMoments, st));
     PES_CHECK_CUDA(cudaMemsetAsync(M.kinkM, 0, sizeof(float) * B * M.n_det * 12, st));
@@ -3508,6 +3771,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_dense, st));
+  if (!grad) {
+    const int rc = refine();
+    if (rc != PES_OK) return rc;
+  }
   auto finalize = [&]() -> int {
     PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->join, 0));
     PES_CHECK_CUDA(cudaStreamWaitEvent(st, p->mixed->ev_hd, 0));
@@ -3519,7 +3786,6 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     return PES_OK;
   };
   if (!grad) return finalize();
-  PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_dense, 0));
   {
     const int rc = refine();
     if (rc != PES_OK) return rc;

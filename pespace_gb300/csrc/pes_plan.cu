@@ -510,6 +510,11 @@ int pes_plan_set_option(PesPlan* p, int32_t option, int64_t value) {
                   (long long)value);
       p->sample_threads = (int)value;
       return PES_OK;
+    case PES_OPT_REFINE_ALL:
+      PES_REQUIRE(value == 0 || value == 1, "pes_plan_set_option: PES_OPT_REFINE_ALL takes 0 or 1, got %lld",
+                  (long long)value);
+      if (p->mixed) mixed_refine_option(p, 1, &value);
+      return PES_OK;
     default:
       break;
   }
@@ -526,6 +531,10 @@ int pes_plan_get_option(PesPlan* p, int32_t option, int64_t* value) {
       return PES_OK;
     case PES_OPT_SAMPLE_THREADS:
       *value = p->sample_threads;
+      return PES_OK;
+    case PES_OPT_REFINE_ALL:
+      *value = 0;
+      if (p->mixed) mixed_refine_option(p, 0, value);
       return PES_OK;
     default:
       break;
@@ -569,7 +578,7 @@ int pes_plan_work(PesPlan* p, int64_t B, int64_t* out, void* stream) {
     ok[s] = b.status == kSampleOk;
     kcut[s] = ok[s] ? b.kcut : 0;
   }
-  for (int k = 0; k < 4; ++k) out[k] = 0;
+  for (int k = 0; k < 6; ++k) out[k] = 0;
   for (int64_t s = 0; s < B; ++s) out[3] += ok[s];
   if (p->desc.precision == PES_PRECISION_MIXED) return mixed_work(p, B, kcut, ok, out, st);
   for (int64_t s = 0; s < B; ++s) out[1] += kcut[s] * p->desc.n_det;

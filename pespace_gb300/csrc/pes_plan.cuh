@@ -267,4 +267,5 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
               cudaStream_t st);
 // read (set == 0) or write the dense stage's staging choice of the gradient pass
 void mixed_stage_option(PesPlan* p, int set, int64_t* value);
+void mixed_refine_option(PesPlan* p, int set, int64_t* value);
 }  // namespace pes

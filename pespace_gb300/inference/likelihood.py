@@ -208,6 +208,21 @@ class WhittleLikelihood:
         return out, grad
 
     @property
+    def refine_all(self):
+        """Mixed plans: True when every sample's dense range is re-evaluated
+        (``PES_OPT_REFINE_ALL``: in float-float from its splines, or exactly
+        where the splines' error estimate exceeds the target), False (the
+        default) when only the samples whose error estimates approach the
+        accuracy target are."""
+        v = ctypes.c_int64()
+        _lib.check(_lib.load().pes_plan_get_option(self._plan, _lib.PES_OPT_REFINE_ALL, ctypes.byref(v)))
+        return bool(v.value)
+
+    @refine_all.setter
+    def refine_all(self, on):
+        _lib.check(_lib.load().pes_plan_set_option(self._plan, _lib.PES_OPT_REFINE_ALL, int(bool(on))))
+
+    @property
     def launch_options(self):
         """The plan's launch options: {"dense_stage": 0 | 1, "sample_threads": n}."""
         from .autotune import OPTIONS, get_option
@@ -242,12 +257,14 @@ class WhittleLikelihood:
     def last_work(self, batch):
         """Work units of the last call on ``batch`` samples (the last chunk when the
         call was split at max_batch): dict with the bins through the FP32 dense
-        stage, the bins evaluated directly in FP64, the sparse-node evaluations
-        and the samples in the parameter domain."""
-        out = (ctypes.c_int64 * 4)()
+        stage, the bins evaluated directly in FP64, the sparse-node evaluations,
+        the samples in the parameter domain, and the samples whose dense range
+        was re-evaluated in float-float and exactly."""
+        out = (ctypes.c_int64 * 6)()
         _lib.check(_lib.load().pes_plan_work(self._plan, min(int(batch), self.max_batch), out,
                                              _lib.stream_handle()))
-        return {"dense_bins": out[0], "fp64_bins": out[1], "sparse_nodes": out[2], "samples": out[3]}
+        return {"dense_bins": out[0], "fp64_bins": out[1], "sparse_nodes": out[2], "samples": out[3],
+                "refined_ff": out[4], "refined_exact": out[5]}
 
     def log_likelihood(self, params):
         """likelihood_jax.py:207-260 call: a ``likelihood_param_type`` namedtuple

@@ -33,3 +33,15 @@ def test_reference_constructor_rejects_other_waveforms():
 
     with pytest.raises(TypeError):
         WhittleLikelihoodCuda("IMRPhenomXAS", None, ("A", "E", "T"))
+
+
+def test_option_codes_match_header():
+    import os
+    import re
+
+    from pespace_gb300 import _lib
+
+    with open(os.path.join(os.path.dirname(__file__), "..", "include", "pespace_gb300.h")) as fh:
+        codes = dict(re.findall(r"#define (PES_OPT_\w+) (\d+)", fh.read()))
+    assert set(codes) == {"PES_OPT_DENSE_STAGE", "PES_OPT_SAMPLE_THREADS", "PES_OPT_REFINE_ALL"}
+    assert all(getattr(_lib, k) == int(v) for k, v in codes.items())

@@ -1,9 +1,10 @@
 """Mixed-precision plan (FP64 sparse grid + FP32 dense bulk) against the FP64 oracle.
 
 Bar: |dlnL| <= 1e-2 against the FP64 oracle, for every sample.  The plan
-adds the splines' midpoint error back per bin and re-evaluates exactly the
-samples whose estimated FP32 rounding or remaining spline error could reach
-the bar (templates far louder than the data).  Light
+adds the splines' midpoint error back per bin and re-evaluates the dense
+range of the samples whose estimated FP32 rounding or remaining spline error
+could reach the bar (templates far louder than the data): in float-float from
+the same splines, or exactly where the spline estimate alone is too large.  Light
 systems whose lowest bins lie decades before coalescence go through the exact
 FP64 bins of the mixed plan.  The gradient is the exact gradient of the
 interpolated model, checked against the oracle's forward-mode duals to 1e-3
@@ -69,6 +70,39 @@ def test_mixed_prior_batch_cutoff(cuda_lib, oracle, network):
     want = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(thetas, nthreads=8)
     err = np.abs(got - want)
     assert np.all(err <= 1e-2), np.sort(err)[-5:]
+
+
+@pytest.mark.parametrize("network", [False, True])
+def test_mixed_float_float_refinement(cuda_lib, oracle, network):
+    """Every sample's dense range re-evaluated (the paths the samples whose
+    error estimates approach the target take: float-float from the splines,
+    exact where the splines' estimate alone is too large): within 1e-2 of the
+    oracle for every sample, the same lnL from the lnL and lnL+gradient calls,
+    and the work report counts them all."""
+    tc = DUR - 20000.0
+    th0 = config0_theta(tc)
+    dl = [lisa(oracle), taiji(oracle)] if network else [lisa(oracle)]
+    g, dets = make_dataset(oracle, DUR, DT, FMIN, FMAX, dl, th0, seed=7)
+    rng = np.random.default_rng(2026)
+    thetas = np.concatenate([th0[None], random_prior_theta(rng, 31, th0[10])])
+    mixed, _ = engines(g, dets, max_batch=32, cut_factor=1.2)
+    assert not mixed.refine_all
+    default = mixed.log_likelihood_batch(thetas).cpu().numpy()
+    mixed.refine_all = True
+    assert mixed.refine_all
+    lnl, _ = mixed.log_likelihood_and_grad(thetas)
+    got = mixed.log_likelihood_batch(thetas)
+    assert torch.equal(lnl, got)
+    work = mixed.last_work(32)
+    assert work["refined_ff"] + work["refined_exact"] == work["samples"] == 32
+    assert work["refined_ff"] >= 16
+    got = got.cpu().numpy()
+    want = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4, cut_factor=1.2).lnl(thetas, nthreads=8)
+    err = np.abs(got - want)
+    assert np.all(err <= 1e-2), np.sort(err)[-5:]
+    assert np.median(err) <= np.median(np.abs(default - want)) + 1e-6
+    mixed.refine_all = False
+    assert np.array_equal(mixed.log_likelihood_batch(thetas).cpu().numpy(), default)
 
 
 def test_mixed_geocentric_network(cuda_lib, oracle, dataset):
