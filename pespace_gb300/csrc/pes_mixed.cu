@@ -190,10 +190,45 @@ struct MixedDev {
   // (w_A hi, lo, w_E hi, lo), (w_T hi, lo, P re hi, lo), (P im hi, lo, 0, 0)
   // (w the scaled inverse PSD, 0 off the channel mask; P the TDI prefactor).
   float4* xff;              // [n_det][6][nbins]
+  // Windows about the T channel's zeros, f = n / L: there T's transfer and its
+  // PSD vanish together (S_T has sin^2(2 pi f L) sin^2(pi f L)), so the
+  // weight 1 / S_T grows as (f - n/L)^-4 and would amplify the splines'
+  // absolute error (FP32 storage, ~1e-7 of the interval's scale) into lnL
+  // errors of 1e-2 from a handful of bins.  The kZeroHalf bins on either side
+  // of each such frequency in the band are taken out of the dense stage, its
+  // split form and its refinements, and evaluated exactly (float-float model,
+  // FP64 residual, k_exact<4>; the gradient from FP64 dual numbers,
+  // k_zero_grad: FP32 tangents of T cancel there).
+  int32_t nzb[PES_MAX_DETECTORS];  // window bins of each detector
+  const int32_t* zbin;      // [n_det][kZeroMax] the window bins, ascending
+  int32_t zblocks;          // blocks per sample of the window kernels (0: no windows)
+  double* zpart;            // [B][zblocks] window lnL partials
+  double* zgpart;           // [B][zblocks][11] window gradient partials
+  void* zgblocks;           // [B] SampleBlock<Dual<11>> (one-mode plans with windows), else null
 };
+constexpr int kZeroHalf = 64;   // bins on either side of a T-channel zero
+constexpr int kZeroMax = 4096;  // window bins per detector
 constexpr int kHdOut = 6;
 constexpr int kPartW = 4;  // dense partials per block: direct sum, cross term, modes' cross terms, rounding estimate
 constexpr int kRefineNone = 0, kRefineFF = 1, kRefineExact = 2;
+
+// Is bin i of detector d in one of its T-channel zero windows (binary search
+// of the ascending window bins)?
+__device__ __forceinline__ bool in_zero_window(const MixedDev& M, int d, int64_t i) {
+  const int n = M.nzb[d];
+  if (n == 0) return false;
+  const int32_t* z = M.zbin + (size_t)d * kZeroMax;
+  if (i < z[0] || i > z[n - 1]) return false;
+  int a = 0, b = n - 1;
+  while (a < b) {
+    const int m = (a + b) >> 1;
+    if (z[m] < i)
+      a = m + 1;
+    else
+      b = m;
+  }
+  return z[a] == i;
+}
 constexpr double kSpikeRatio = 8.0;
 constexpr int kMomStride = 21;  // doubles per bin (and interval) of wmom / wtot
 constexpr int kRefineBlocks = 32;  // blocks per sample of the exact re-evaluation
@@ -226,6 +261,7 @@ struct MixedBuffers {
   bool stage_grad = false;
   cudaEvent_t ev_nodes = nullptr, ev_tfit = nullptr, ev_dense = nullptr, ev_tadj = nullptr, ev_hd = nullptr, ev_pfit = nullptr,
               ev_kink = nullptr, ev_xgrad = nullptr;
+  std::vector<int32_t> zbin_host;  // the zero windows' bins ([n_det][kZeroMax]), for the work report
 };
 
 // ------------------------------------------------------------------ sparse stage
@@ -1758,18 +1794,22 @@ __global__ void k_refine_select(PlanDev P, MixedDev M, const SampleBlock<double>
 // FP64 data).  kMode 0: lnL partials (T = double); 1: gradient partials
 // (T = GradScalar, FP64 values with FP32 tangents); 2: write the model;
 // 3: lnL partials of bins [xbind[s][d], kcut) of the samples that
-// k_refine_select sends to the exact re-evaluation of their dense range.
-// grid (xblocks or rblocks, B); threads stride over the sample's exact bins.
+// k_refine_select sends to the exact re-evaluation of their dense range
+// (without the T-channel zero windows); 4: lnL partials of the window bins
+// in [xbind[s][d], kcut) (their gradient: k_zero_grad).
+// grid (xblocks, rblocks or zblocks, B); threads stride over the bins.
 template <int kMode, class T>
 __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, GenArg G,
                                                          const SampleBlock<T>* __restrict__ blocks,
                                                          double2* __restrict__ model) {
-  constexpr int NV = kMode == 1 ? 11 : 1;
-  constexpr bool kFF = kMode != 1;  // value passes: float-float values
+  constexpr bool kGradPass = kMode == 1;
+  constexpr int NV = kGradPass ? 11 : 1;
+  constexpr bool kFF = !kGradPass;  // value passes: float-float values
   constexpr bool kRefine = kMode == 3;
-  // value passes: a float-float copy of the block; gradient pass: the split
+  constexpr bool kZero = kMode == 4;  // the T-channel zero windows
+  // value passes: a float-float copy of the block; gradient passes: the split
   // float-float block (mass/spin and response tangents)
-  using SBF = std::conditional_t<kMode == 1, ExactGradBlock, SampleBlock<FF>>;
+  using SBF = std::conditional_t<kGradPass, ExactGradBlock, SampleBlock<FF>>;
   __shared__ SampleBlock<T> sb;
   __shared__ SBF sbf;
   __shared__ double red[kExactThreads / 32][NV];
@@ -1778,7 +1818,7 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
   const int s = blockIdx.y;
   const int nm = M.n_modes;
   const int xb = M.xbin[(size_t)s * nm];
-  if (!kRefine && xb == 0) return;  // uniform per block; the finalizers skip such samples
+  if (!kRefine && !kZero && xb == 0) return;  // uniform per block; the finalizers skip such samples
   if (kRefine && (blocks[s].status != kSampleOk || M.rkind[s] != kRefineExact)) return;
   load_block(blocks, s, sb);
   if (kFF && M.hm) load_hm(M.hm, s, hmd);
@@ -1798,7 +1838,16 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
     for (int d = 0; d < M.n_det; ++d) {
       const int xbd = M.xbind[(size_t)s * nm * M.n_det + d];
       const int i0 = kRefine ? xbd : 0, i1 = kRefine ? (int)sb.kcut : xbd;
-      for (int i = i0 + blockIdx.x * kExactThreads + threadIdx.x; i < i1; i += gridDim.x * kExactThreads) {
+      const int n_it = kZero ? M.nzb[d] : i1 - i0;
+      for (int it = blockIdx.x * kExactThreads + threadIdx.x; it < n_it; it += gridDim.x * kExactThreads) {
+        int i = i0 + it;
+        if constexpr (kZero) {
+          i = M.zbin[(size_t)d * kZeroMax + it];
+          if (i < xbd || i >= (int)sb.kcut) continue;  // below: the exact low bins take it
+        }
+        if constexpr (kRefine) {
+          if (in_zero_window(M, d, i)) continue;  // the window kernel takes it
+        }
         if constexpr (kFF) {
           const FF f = ff_mulf(M.fstep_ff, (float)(P.k0 + i));  // k0 + i < 2^24: exact in FP32
           const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
@@ -1839,7 +1888,7 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
           }
           continue;
         }
-        if constexpr (kMode == 1) {
+        if constexpr (kGradPass) {
           const double f = (double)(P.k0 + i) * P.f_step;
           const TdiFactor& tdb = P.tdi[(size_t)d * P.nbins + i];
           // PhenomD with the mass/spin tangents
@@ -1926,8 +1975,91 @@ __global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, 
       M.xpart[(size_t)s * gridDim.x + blockIdx.x] = x;
     else if (kMode == 3)
       M.rpart[(size_t)s * gridDim.x + blockIdx.x] = x;
+    else if (kMode == 4)
+      M.zpart[(size_t)s * gridDim.x + blockIdx.x] = x;
     else
       M.xgpart[((size_t)s * gridDim.x + blockIdx.x) * 11 + threadIdx.x] = x;
+  }
+}
+
+// Gradient of the T-channel zero windows (one-mode plans): d/dtheta of
+// sum_c |d - h|^2 w over each window bin in [xbind, kcut) of each detector,
+// with FP64 dual numbers over the 11 parameters (near T's zero its transfer
+// is a cancellation of the links that FP32 tangents cannot resolve, and the
+// weight 1/S_T amplifies what they miss).  grid (zblocks, B).
+using ZScalar = Dual<11>;
+__device__ __forceinline__ ZScalar zero_bin_residual(const PlanDev& P, const SampleBlock<ZScalar>& b, int d,
+                                                     int64_t i) {
+  using T = ZScalar;
+  const double f = (double)(P.k0 + i) * P.f_step;
+  T amp, psi, tf;
+  phenomd_eval<T>(b.wf, b.wf.Msec * f, amp, psi, tf);
+  T sn, cs;
+  dsincos(psi, &sn, &cs);
+  const T ap = b.wf.pfac * amp, ac = b.wf.cfac * amp;
+  Cx<T> hp = cx(ap * cs, -(ap * sn));
+  Cx<T> hc = cx(-(ac * sn), -(ac * cs));
+  Cx<T> ts;
+  dsincos((-2.0 * kPi * f) * b.tc, &ts.im, &ts.re);
+  hp = cmul(hp, ts);
+  hc = cmul(hc, ts);
+  Cx<T> L[6], C[3];
+  single_links<T>(P.orbit[d], f, hp, hc, tf + b.tc, b.pol, L);
+  const TdiFactor dp = P.tdi[(size_t)d * P.nbins + i];
+  tdi_channels<T>(cx(dp.dre, dp.dim), cx(dp.pre, dp.pim), 1, L, C);
+  T sum = lift<T>(0.0);
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    if (!((P.chan_mask >> ch) & 1)) continue;
+    const size_t off = ((size_t)d * 3 + ch) * P.nbins + i;
+    const double2 dv = P.data[off];
+    const T rr = dv.x - C[ch].re, ri = dv.y - C[ch].im;
+    sum = sum + (rr * rr + ri * ri) * P.w[off];
+  }
+  return sum;
+}
+
+__global__ void __launch_bounds__(kExactThreads) k_zero_grad(PlanDev P, MixedDev M,
+                                                             const SampleBlock<ZScalar>* __restrict__ blocks) {
+  __shared__ SampleBlock<ZScalar> sb;
+  __shared__ double red[kExactThreads / 32][11];
+  const int s = blockIdx.y;
+  {
+    const int n8 = sizeof(SampleBlock<ZScalar>) / 8;
+    const double* src = reinterpret_cast<const double*>(&blocks[s]);
+    double* dst = reinterpret_cast<double*>(&sb);
+    for (int j = threadIdx.x; j < n8; j += blockDim.x) dst[j] = src[j];
+  }
+  __syncthreads();
+  double acc[11];
+#pragma unroll
+  for (int k = 0; k < 11; ++k) acc[k] = 0.0;
+  if (sb.status == kSampleOk) {
+    for (int d = 0; d < M.n_det; ++d) {
+      const int xbd = M.xbind[(size_t)s * M.n_det + d];
+      for (int it = blockIdx.x * kExactThreads + threadIdx.x; it < M.nzb[d]; it += gridDim.x * kExactThreads) {
+        const int i = M.zbin[(size_t)d * kZeroMax + it];
+        if (i < xbd || i >= (int)sb.kcut) continue;  // below: the exact low bins take it
+        const ZScalar r = zero_bin_residual(P, sb, d, i);
+#pragma unroll
+        for (int k = 0; k < 11; ++k) acc[k] += r.d[k];
+      }
+    }
+  }
+  const int wid = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 11; ++k) {
+    double x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (l == 0) red[wid][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 11) {
+    double x = 0.0;
+#pragma unroll
+    for (int w = 0; w < kExactThreads / 32; ++w) x += red[w][threadIdx.x];
+    M.zgpart[((size_t)s * gridDim.x + blockIdx.x) * 11 + threadIdx.x] = x;
   }
 }
 
@@ -3000,6 +3132,7 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
     }
     if (M.xbin[s * M.n_modes] > 0)
       for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
+    for (int k = 0; k < M.zblocks; ++k) acc += M.zpart[(size_t)s * M.zblocks + k];
     const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
     lnl[s] = v;
     if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
@@ -3020,6 +3153,7 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   }
   if (M.xbin[s] > 0)
     for (int k = 0; k < M.xblocks; ++k) acc += M.xpart[(size_t)s * M.xblocks + k];
+  for (int k = 0; k < M.zblocks; ++k) acc += M.zpart[(size_t)s * M.zblocks + k];
   const double v = -2.0 * P.df * (acc + P.suffix[b.kcut]);
   lnl[s] = v;
   if (status) status[s] = isfinite(v) ? kSampleOk : kSampleNonFinite;
@@ -3037,11 +3171,11 @@ __global__ void k_mixed_grad_finalize(MixedDev M, int64_t B, double xscale, doub
         for (int b = 0; b < M.nblk_sparse; ++b) acc += M.gpart[(((size_t)s * M.n_det + d) * M.nblk_sparse + b) * 11 + p];
         if (p == 10) acc += M.gdir[(size_t)s * M.n_det + d];
       }
-      if (exact) {
-        double x = 0.0;
+      double x = 0.0;
+      if (exact)
         for (int b = 0; b < M.xblocks; ++b) x += M.xgpart[((size_t)s * M.xblocks + b) * 11 + p];
-        acc += xscale * x;
-      }
+      for (int b = 0; b < M.zblocks; ++b) x += M.zgpart[((size_t)s * M.zblocks + b) * 11 + p];
+      acc += xscale * x;
     }
     grad[11 * s + p] = acc;
   }
@@ -3056,13 +3190,14 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
   float dr[3], di[3], wf[3];
   FF wff[3];
   float4* X = M.xff + (size_t)det * 6 * P.nbins + i;
+  const bool zw = in_zero_window(M, det, i);  // evaluated exactly: no weight in the dense stage
   for (int ch = 0; ch < 3; ++ch) {
     const double2 v = data[ch * P.nbins + i];
     const FF re = ff_from(v.x * M.scale), im = ff_from(v.y * M.scale);
     dr[ch] = re.hi;
     di[ch] = im.hi;
     X[(size_t)ch * P.nbins] = make_float4(re.hi, re.lo, im.hi, im.lo);
-    const bool on = (P.chan_mask >> ch) & 1;
+    const bool on = ((P.chan_mask >> ch) & 1) && !zw;
     wff[ch] = on ? ff_from(1.0 / (psd[ch * P.nbins + i] * M.scale * M.scale)) : ff_make(0.0f, 0.0f);
     wf[ch] = wff[ch].hi;
     if (on) dd += (v.x * v.x + v.y * v.y) / psd[ch * P.nbins + i];
@@ -3095,6 +3230,7 @@ __global__ void k_wspike(PlanDev P, MixedDev M, int det, int32_t* __restrict__ o
     const int64_t k1 = M.iv_first[j], k2 = M.iv_first[j + 1];
     double mx = 0.0, sum = 0.0;
     for (int64_t k = k1; k < k2; ++k) {
+      if (in_zero_window(M, det, k)) continue;
       const TdiFactor tf = P.tdi[(size_t)det * P.nbins + k];
       double w = 0.0;
       for (int c = 0; c < 3; ++c) w += P.w[((size_t)det * 3 + c) * P.nbins + k];
@@ -3122,7 +3258,7 @@ __global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ 
     const double tk = (double)(P.k0 + k) * P.f_step - fj;
     const TdiFactor tf = P.tdi[(size_t)det * P.nbins + k];
     const size_t off = ((size_t)det * 3 + c) * P.nbins + k;
-    const double w = P.w[off];
+    const double w = in_zero_window(M, det, k) ? 0.0 : P.w[off];
     double tp = w * (tf.pre * tf.pre + tf.pim * tf.pim) * is2;
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
@@ -3473,6 +3609,46 @@ int mixed_create(PesPlan* p) {
   M.rkind = rkind;
   M.fpart = fpart;
   M.xff = xff;
+  {
+    // the T channel's zeros f = n / L in the band (equal-arm constellations)
+    std::vector<int32_t> zb((size_t)nd * kZeroMax, 0);
+    int most = 0;
+    for (int k = 0; k < PES_MAX_DETECTORS; ++k) M.nzb[k] = 0;
+    for (int k = 0; k < nd; ++k) {
+      std::vector<int32_t> bins;
+      const double L = d.det[k].orbit.arm_sec;
+      for (int zn = 1; L > 0.0 && zn / L <= fhi + kZeroHalf * d.f_step; ++zn) {
+        const int64_t c = std::llround(zn / L / d.f_step) - d.k0;
+        for (int64_t i = c - kZeroHalf; i <= c + kZeroHalf; ++i)
+          if (i >= 0 && i < n) bins.push_back((int32_t)i);
+      }
+      std::sort(bins.begin(), bins.end());
+      bins.erase(std::unique(bins.begin(), bins.end()), bins.end());
+      PES_REQUIRE(bins.size() <= (size_t)kZeroMax,
+                  "mixed plan: detector %d has %zu bins in T-channel zero windows (at most %d)", k, bins.size(),
+                  kZeroMax);
+      std::copy(bins.begin(), bins.end(), zb.begin() + (size_t)k * kZeroMax);
+      M.nzb[k] = (int32_t)bins.size();
+      most = std::max(most, M.nzb[k]);
+    }
+    int32_t* zbin = nullptr;
+    double *zpart = nullptr, *zgpart = nullptr;
+    M.zblocks = (int32_t)std::min<int64_t>(ceil_div(most, kExactThreads), 8);
+    if ((rc = alloc(mb, &zbin, zb.size())) || (rc = alloc(mb, &zpart, (size_t)B * std::max(1, M.zblocks))) ||
+        (rc = alloc(mb, &zgpart, (size_t)B * std::max(1, M.zblocks) * 11)))
+      return rc;
+    PES_CHECK_CUDA(cudaMemcpy(zbin, zb.data(), sizeof(int32_t) * zb.size(), cudaMemcpyHostToDevice));
+    mb->zbin_host = zb;
+    M.zbin = zbin;
+    M.zgblocks = nullptr;
+    if (M.zblocks > 0 && !multi) {
+      SampleBlock<ZScalar>* zgb = nullptr;
+      if ((rc = alloc(mb, &zgb, (size_t)B))) return rc;
+      M.zgblocks = zgb;
+    }
+    M.zpart = zpart;
+    M.zgpart = zgpart;
+  }
   PES_CHECK_CUDA(cudaMemset(rkind, 0, sizeof(int32_t) * B));
   PES_CHECK_CUDA(cudaMemset(xff, 0, sizeof(float4) * nd * 6 * n));
   {
@@ -3602,8 +3778,14 @@ int mixed_work(PesPlan* p, int64_t B, const std::vector<int64_t>& kcut, const st
   for (int64_t s = 0; s < B; ++s) {
     if (!ok[s]) continue;
     for (int d = 0; d < M.n_det; ++d) {
-      out[0] += kcut[s] - xb[(size_t)s * nm * M.n_det + d];
-      out[1] += xb[(size_t)s * nm * M.n_det + d];
+      const int64_t x = xb[(size_t)s * nm * M.n_det + d];
+      int64_t zw = 0;  // window bins in [x, kcut): exact, not through the dense stage
+      for (int t = 0; t < M.nzb[d]; ++t) {
+        const int32_t i = p->mixed->zbin_host[(size_t)d * kZeroMax + t];
+        zw += i >= x && i < kcut[s];
+      }
+      out[0] += kcut[s] - x - zw;
+      out[1] += x + zw;
     }
     for (int k = 0; k < nm; ++k)
       if (ns[(size_t)s * nm + k] >= 3) out[2] += (int64_t)(ns[(size_t)s * nm + k] + 1) * M.n_det;
@@ -3649,6 +3831,11 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
     k_exact<0, double><<<dim3(M.xblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
   }
   PES_CHECK_LAUNCH();
+  if (M.zblocks > 0) {
+    ProfScope ps(p, kKDenseFp64, side);
+    k_exact<4, double><<<dim3(M.zblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
+  }
+  PES_CHECK_LAUNCH();
   if (grad) {
     {
       ProfScope ps(p, kKSetup, side);
@@ -3660,6 +3847,14 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
       ProfScope ps(p, kKDenseFp64, side);
       k_exact<1, GradScalar><<<dim3(M.xblocks, (unsigned)B), kExactThreads, 0, side>>>(
           p->dev, M, G, reinterpret_cast<const SampleBlock<GradScalar>*>(M.gblocks), nullptr);
+    }
+    PES_CHECK_LAUNCH();
+    if (M.zblocks > 0) {
+      ProfScope ps(p, kKDenseFp64, side);
+      SampleBlock<ZScalar>* zb = reinterpret_cast<SampleBlock<ZScalar>*>(M.zgblocks);
+      k_setup<ZScalar><<<ceil_div(B, p->sample_threads), p->sample_threads, 0, side>>>(p->dev, theta, B, 0, zb,
+                                                                                       nullptr);
+      k_zero_grad<<<dim3(M.zblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, zb);
     }
     PES_CHECK_LAUNCH();
     // the backward node stage reads the gradient set-up

@@ -105,6 +105,38 @@ def test_mixed_float_float_refinement(cuda_lib, oracle, network):
     assert np.array_equal(mixed.log_likelihood_batch(thetas).cpu().numpy(), default)
 
 
+def test_mixed_taiji_t_channel_zero(cuda_lib, oracle):
+    """Taiji (L = 10 s) on a band reaching 0.1 Hz holds the T channel's zero
+    f = 1/L = 0.0999 Hz, where T's transfer and its PSD vanish together and
+    1/S_T grows as (f - 1/L)^-4.  The mixed plan evaluates the bins about it
+    exactly: sources whose ringdown reaches it within 1e-2 of the oracle
+    (lnL, also with every sample refined) and within 1e-3 of the gradient
+    norm; the window bins are reported as exact bins."""
+    dur, dt = 2.0 ** 18, 4.0
+    th0 = config0_theta(dur - 20000.0)
+    th0[0] -= np.log(10.0)  # total mass 1.5e5 Msun: f_RD near 0.1 Hz
+    g, dets = make_dataset(oracle, dur, dt, 1e-4, 0.1, [taiji(oracle)], th0, seed=3)
+    rng = np.random.default_rng(19)
+    thetas = np.stack([th0] + [perturbed(th0, rng) for _ in range(7)])
+    from pespace_gb300.inference import WhittleLikelihood
+
+    mixed = WhittleLikelihood(cuda_detectors(g, dets, grid=(dur, dt, 1e-4, 0.1)), precision="mixed",
+                              reference_frequency=1e-4, max_batch=8)
+    lnl, grad = mixed.log_likelihood_and_grad(thetas)
+    work = mixed.last_work(8)
+    kcut = int(np.searchsorted(g["freqs"], 0.1, side="right"))
+    assert work["fp64_bins"] >= 8 * 64 and work["dense_bins"] + work["fp64_bins"] <= 8 * kcut
+    w_lnl, w_grad = oracle.Plan(g, [(o, gen, d, p) for _, o, gen, d, p in dets], 1e-4).lnl(
+        thetas, grad=True, nthreads=8)
+    err = np.abs(lnl.cpu().numpy() - w_lnl)
+    assert np.all(err <= 1e-2), err
+    norm = np.linalg.norm(w_grad, axis=1, keepdims=True)
+    assert np.max(np.abs(grad.cpu().numpy() - w_grad) / norm) < 1e-3
+    mixed.refine_all = True
+    err = np.abs(mixed.log_likelihood_batch(thetas).cpu().numpy() - w_lnl)
+    assert np.all(err <= 1e-2), err
+
+
 def test_mixed_geocentric_network(cuda_lib, oracle, dataset):
     """LISA + TianQin: the geocentric constellation's 3.65-day rotation makes
     most inspiral bins exact (FP64); lnL and gradient against the oracle."""
