@@ -182,7 +182,7 @@ struct MixedDev {
   // stage from its FP32 rounding estimate (the dense stage's own sum of
   // |d|^2 |h|^2 w^2) and its splines' error estimate (k_hd): not at all, in
   // float-float from the same splines (rounding: k_dense_ff), or exactly
-  // (spline error, one-mode plans: k_exact<3>).
+  // (spline error: k_exact<3>).
   int32_t* rkind;           // [B] kRefineNone, kRefineFF or kRefineExact
   double* fpart;            // [B][nblk_dense] float-float dense-range partials
   // Float-float copies of the FP64 inputs of one bin for k_dense_ff, six rows
@@ -1767,7 +1767,7 @@ __global__ void __launch_bounds__(kFitWarps * 32) k_spline_adjoint_staged(MixedD
 // then have a rounding spread below 2.2e-3, which puts the 1e-2 bar at 4.5 of
 // those spreads.  A refined sample whose spline part alone stays within the
 // target is re-evaluated in float-float from the same splines (its rounding
-// drops out, k_dense_ff); one-mode samples above it, exactly (k_exact<3>).
+// drops out, k_dense_ff); one above it, exactly (k_exact<3>).
 constexpr double kRefineTarget = 4e-3;
 constexpr double kCrossRel = 4e-7;
 constexpr double kSplineRel = 0.01;
@@ -1785,7 +1785,7 @@ __global__ void k_refine_select(PlanDev P, MixedDev M, const SampleBlock<double>
     const double er = 2.0 * P.df * kCrossRel * sqrt(fmax(sq, 0.0));
     const double es = 2.0 * P.df * kSplineRel * eha;
     if (M.refine_all || er + es > kRefineTarget)
-      kind = (M.n_modes == 1 && es > kRefineTarget) ? kRefineExact : kRefineFF;
+      kind = es > kRefineTarget ? kRefineExact : kRefineFF;
   }
   M.rkind[s] = kind;
 }
@@ -2289,6 +2289,10 @@ __device__ __forceinline__ void cp_async16_l1(void* smem, const void* gmem) {
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// bring the line holding p into L1 (no register, no completion to wait for)
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(__cvta_generic_to_global(p)));
+}
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 // One run's inputs in shared memory: the three packed rows of its (up to) 32
@@ -2388,9 +2392,10 @@ __global__ void k_bump(MixedDev M, const SampleBlock<double>* __restrict__ block
 // kNM: modes summed per bin before the residual (1, or kHMModes for
 // IMRPhenomHM plans: lnL and model passes, plain loads).
 // The gradient pass is held to 96 registers (5 blocks per SM instead of 4:
-// 2% faster on the bench workload, at a few spilled words).
+// 2% faster on the bench workload, at a few spilled words); the six-mode
+// pass to 168 (3 blocks per SM instead of 2).
 template <int kMode, bool kStage, int kNM>
-__global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed(PlanDev P, MixedDev M,
+__global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : (kNM > 1 ? 3 : 1)) k_dense_mixed(PlanDev P, MixedDev M,
                                                              const SampleBlock<double>* __restrict__ blocks,
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
@@ -2468,6 +2473,34 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : 1) k_dense_mixed
         const int j = M.ch_iv[c];
         const int kb = M.ch_begin[c];
         const int len = M.ch_len[c];
+        if (kNM > 1 && c + 1 < last) {
+          // touch the next run's inputs so that its loads hit L1: the L2 latency
+          // of the six modes' rows at the top of each run stalls the loop (the
+          // one-mode gradient pass ran 13% slower with these prefetches)
+          const int kbn = M.ch_begin[c + 1];
+          if (kbn >= xb) {
+            const int64_t in = (int64_t)kbn + lane;
+            if (lane < M.ch_len[c + 1] && in < kcut) {
+              const float4* pkd = M.pk + (size_t)d * 3 * P.nbins;
+              prefetch_l1(pkd + in);
+              prefetch_l1(pkd + P.nbins + in);
+              prefetch_l1(pkd + 2 * P.nbins + in);
+              prefetch_l1(M.dd + (size_t)d * P.nbins + in);
+            }
+            if (lane >= 32 - kNM * 3) {
+              // three lanes per mode: the run's anchor, the interval's coefficient rows and corrections
+              const int k = (31 - lane) / 3, part = (31 - lane) % 3;
+              const size_t sdk = sd + (size_t)k * M.n_det;
+              const int jn = M.ch_iv[c + 1];
+              if (part == 0)
+                prefetch_l1(M.runs + (sdk * M.nchunks + c + 1) * 3);
+              else if (part == 1)
+                prefetch_l1(M.cg + (sdk * M.J + jn) * 8);
+              else
+                prefetch_l1(M.cbump + (sdk * M.J + jn) * 2);
+            }
+          }
+        }
         if (kb < xb) {  // exact bins
           if (kStage) __syncwarp();
           continue;
@@ -3117,7 +3150,7 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
   if (M.n_modes > 1) {
     // multi-mode plans: the split form for far templates with sum |h|^2 w =
     // the modes' own sums (exact, from their splines) + their cross terms
-    // (dense stage); refinement in float-float only
+    // (dense stage)
     for (int k = 0; k < M.n_modes; ++k)
       for (int d = 0; d < M.n_det; ++d) {
         const double* hv = M.hd + (((size_t)s * M.n_modes + k) * M.n_det + d) * kHdOut;
@@ -3126,7 +3159,10 @@ __global__ void k_mixed_finalize(PlanDev P, MixedDev M, const SampleBlock<double
     for (int d = 0; d < M.n_det; ++d) Dd += M.hd[((size_t)s * M.n_modes * M.n_det + d) * kHdOut + 1];
     const double Ht = H + Cm;
     double acc = (R > 2.0 * sqrt(fmax(Ht, 0.0) * Dd)) ? (Dd + X) + Ht : R;
-    if (M.rkind[s] == kRefineFF) {  // the float-float re-evaluation of the dense range
+    if (M.rkind[s] == kRefineExact) {  // the exact re-evaluation of the dense range
+      acc = 0.0;
+      for (int k = 0; k < M.rblocks; ++k) acc += M.rpart[(size_t)s * M.rblocks + k];
+    } else if (M.rkind[s] == kRefineFF) {  // the float-float one
       acc = 0.0;
       for (int k = 0; k < M.nblk_dense; ++k) acc += M.fpart[(size_t)s * M.nblk_dense + k];
     }
@@ -3922,7 +3958,7 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
       k_refine_select<<<ceil_div(B, 64), 64, 0, side>>>(p->dev, M, blocks, B);
     }
     PES_CHECK_LAUNCH();
-    if (!multi) {
+    {
       ProfScope ps(p, kKDenseFp64, side);
       k_exact<3, double><<<dim3(M.rblocks, (unsigned)B), kExactThreads, 0, side>>>(p->dev, M, G, blocks, nullptr);
     }

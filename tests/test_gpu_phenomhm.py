@@ -153,11 +153,11 @@ def test_hm_mixed_plan(cuda_lib, oracle, dataset):
     err = np.abs(got - want)
     assert np.all(err <= 1e-2), (err, want)
     assert np.array_equal(got, mixed.log_likelihood_batch(thetas).cpu().numpy())  # deterministic
-    # every sample through the float-float re-evaluation of the six modes
+    # every sample re-evaluated (six modes: float-float from the splines, or exactly)
     mixed.refine_all = True
     ff = mixed.log_likelihood_batch(thetas).cpu().numpy()
     work = mixed.last_work(len(thetas))
-    assert work["refined_ff"] == len(thetas)
+    assert work["refined_ff"] + work["refined_exact"] == len(thetas)
     assert np.all(np.abs(ff - want) <= 1e-2), (np.abs(ff - want), want)
     mixed.refine_all = False
     with pytest.raises(_lib.PesError):
