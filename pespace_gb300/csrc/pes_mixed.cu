@@ -149,9 +149,9 @@ struct MixedDev {
   // sums, |h|^2 w from the transfer splines' coefficients against the data's
   // weight moments (the model's squared modulus is a polynomial in t on each
   // interval), so that only the cross term carries per-bin FP32 rounding.
-  const double* wmom;       // [n_det][nbins][3][7] sums over the bins of k's interval before k of
-                            //   t^p W_c (W_c = w_c |P|^2 / scale^2, t = f - f_j)
-  const double* wtot;       // [n_det][J][3][7] the same over each whole interval
+  const FF* wmom;           // [n_det][nbins][3][7] sums over the bins of k's interval j before k of
+                            //   u^p W_c (W_c = w_c |P|^2 / scale^2, u = (f - f_j) / h_j; float-float)
+  const FF* wtot;           // [n_det][J][3][7] the same over each whole interval
   const double* dsuf;       // [n_det][nbins + 1] sum_{i >= k} sum_c |d_c|^2 w_c (FP64)
   double* wrow;             // [nbins] set-up scratch: one detector's sum_c |d_c|^2 w_c per bin
   float* cgb;               // [B][n_det][J][6] tails b - b_hi of the transfer splines' slope coefficients
@@ -230,7 +230,7 @@ __device__ __forceinline__ bool in_zero_window(const MixedDev& M, int d, int64_t
   return z[a] == i;
 }
 constexpr double kSpikeRatio = 8.0;
-constexpr int kMomStride = 21;  // doubles per bin (and interval) of wmom / wtot
+constexpr int kMomStride = 21;  // moments per bin (and interval) of wmom / wtot
 constexpr int kRefineBlocks = 32;  // blocks per sample of the exact re-evaluation
 
 // Error-free transformation: s + e == a + b exactly (Knuth's two-sum).
@@ -2962,23 +2962,25 @@ __global__ void __launch_bounds__(kMixThreads) k_dense_ff(PlanDev P, MixedDev M,
 // transfer splines, re and im), plus C (X0 + Msec t)^2 past the amplitude
 // peak (X0 = Msec f_j - Mf_peak), so |h_c|^2 w_c = |G_c(t)|^2 W_c and its sum
 // over the interval's bins is sum_p g_p sum_k t_k^p W_c with g the
-// coefficients of |G_c|^2: FP64 throughout, no per-bin rounding of the model.
+// coefficients of |G_c|^2: no per-bin rounding of the model.  Float-float on
+// the FP32 pipes, in the interval's variable u = t / h (so that the moments
+// sum u^p W stay in range); in FP64 this kernel bound the FP64 pipe.
 constexpr int kHdThreads = 128;  // one block per (sample, detector), threads over its intervals
-__device__ __forceinline__ double hd_piece(const double (&A)[6], const double (&Bc)[6], const double (&Cc)[6],
-                                           const double (&Dc)[6], const double* Sm) {
-  double acc = 0.0;
+__device__ __forceinline__ FF hd_piece(const FF (&A)[6], const FF (&Bc)[6], const FF (&Cc)[6], const FF (&Dc)[6],
+                                       const FF* Sm) {
+  FF acc = ff_make(0.0f, 0.0f);
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     const int r = 2 * ch, i = 2 * ch + 1;
-    const double g0 = A[r] * A[r] + A[i] * A[i];
-    const double g1 = 2.0 * (A[r] * Bc[r] + A[i] * Bc[i]);
-    const double g2 = Bc[r] * Bc[r] + Bc[i] * Bc[i] + 2.0 * (A[r] * Cc[r] + A[i] * Cc[i]);
-    const double g3 = 2.0 * (A[r] * Dc[r] + A[i] * Dc[i] + Bc[r] * Cc[r] + Bc[i] * Cc[i]);
-    const double g4 = Cc[r] * Cc[r] + Cc[i] * Cc[i] + 2.0 * (Bc[r] * Dc[r] + Bc[i] * Dc[i]);
-    const double g5 = 2.0 * (Cc[r] * Dc[r] + Cc[i] * Dc[i]);
-    const double g6 = Dc[r] * Dc[r] + Dc[i] * Dc[i];
-    const double* m = Sm + ch * 7;
-    acc += g0 * m[0] + g1 * m[1] + g2 * m[2] + g3 * m[3] + g4 * m[4] + g5 * m[5] + g6 * m[6];
+    const FF g0 = A[r] * A[r] + A[i] * A[i];
+    const FF g1 = ff_mulf(A[r] * Bc[r] + A[i] * Bc[i], 2.0f);
+    const FF g2 = (Bc[r] * Bc[r] + Bc[i] * Bc[i]) + ff_mulf(A[r] * Cc[r] + A[i] * Cc[i], 2.0f);
+    const FF g3 = ff_mulf((A[r] * Dc[r] + A[i] * Dc[i]) + (Bc[r] * Cc[r] + Bc[i] * Cc[i]), 2.0f);
+    const FF g4 = (Cc[r] * Cc[r] + Cc[i] * Cc[i]) + ff_mulf(Bc[r] * Dc[r] + Bc[i] * Dc[i], 2.0f);
+    const FF g5 = ff_mulf(Cc[r] * Dc[r] + Cc[i] * Dc[i], 2.0f);
+    const FF g6 = Dc[r] * Dc[r] + Dc[i] * Dc[i];
+    const FF* m = Sm + ch * 7;
+    acc = acc + ((g0 * m[0] + g1 * m[1]) + (g2 * m[2] + g3 * m[3]) + (g4 * m[4] + (g5 * m[5] + g6 * m[6])));
   }
   return acc;
 }
@@ -3025,93 +3027,103 @@ __global__ void __launch_bounds__(kHdThreads) k_hd(PlanDev P, MixedDev M,
     return a;
   };
   const int jlo = iv_of(lo), jhi = iv_of(kcut - 1);
-  const double* KC = M.kinkC + sd * 6;
-  const double* wm = M.wmom + (size_t)d * P.nbins * kMomStride;
+  // the kink coefficients C_q, Msec and the kink point in float-float
+  const float* kf = M.kinkF + (size_t)sd * 16;
+  FF KC[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) KC[q] = ff_make(kf[2 + q], kf[8 + q]);
+  const float4 sa = M.sff[2 * v], sk = M.sff[2 * v + 1];
+  const FF msf = ff_make(sa.z, sa.w), fpf = ff_make(sk.x, sk.y);
+  const FF* wm = M.wmom + (size_t)d * P.nbins * kMomStride;
   const FF* ym = M.ym + (size_t)sd * 7 * M.J;
-  double sum = 0.0, eh = 0.0, eha = 0.0;
+  FF sum = ff_make(0.0f, 0.0f);
+  float eh = 0.0f, eha = 0.0f;
   for (int j = jlo + lane; j <= jhi; j += kHdThreads) {
     const int64_t e1 = M.iv_first[j], e2 = M.iv_first[j + 1];
     const int64_t k1 = max(e1, lo), k2 = min(e2, kcut);
     if (k1 >= k2) continue;
-    const double* tot = M.wtot + ((size_t)d * M.J + j) * kMomStride;
+    const FF* tot = M.wtot + ((size_t)d * M.J + j) * kMomStride;
     auto F = [&](int64_t k, int idx) { return k >= e2 ? tot[idx] : wm[(size_t)k * kMomStride + idx]; };
-    double A[6], Bc[6], Cc[6], Dc[6];
+    // the spline coefficients in the interval's own variable u = t / h (the
+    // moments are sums of u^p W): A, B h, C h^2, D h^3
+    const FF h = M.gff[j], h2 = h * h, h3 = h2 * h;
+    FF A[6], Bc[6], Cc[6], Dc[6];
     const float4* cg = M.cg + ((size_t)sd * M.J + j) * 8;
     const float* alo = reinterpret_cast<const float*>(cg + 6);
     const float* blo = M.cgb + ((size_t)sd * M.J + j) * 6;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
       const float4 c4 = cg[q];
-      A[q] = (double)c4.x + (double)alo[q];
-      Bc[q] = (double)c4.y + (double)blo[q];
-      Cc[q] = (double)c4.z;
-      Dc[q] = (double)c4.w;
+      A[q] = ff_make(c4.x, alo[q]);
+      Bc[q] = ff_make(c4.y, blo[q]) * h;
+      Cc[q] = ff_mulf(h2, c4.z);
+      Dc[q] = ff_mulf(h3, c4.w);
     }
     // the splines' error at the midpoint (kink-free values on both sides, or
     // both with the kink in a folded interval)
     const bool folded = jk >= 0 && j > jk;
-    const double h = M.gh[j], tm = 0.5 * h;
-    const double Xm = Msec * (M.node_f[j] + tm) - fpk;
-    double delta[6], gm[6];
+    const float2 nfj = M.node_ff[j];
+    const FF X0 = msf * ff_make(nfj.x, nfj.y) - fpf;
+    const FF K = msf * h;  // Msec h: x = X0 + K u
+    const FF Xm = X0 + ff_mulf(K, 0.5f);
+    const FF Xm2 = Xm * Xm;
+    float delta[6], gm[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      const double sp = A[q] + tm * (Bc[q] + tm * (Cc[q] + tm * Dc[q]));
-      const double ex = ff_to(ym[(size_t)q * M.J + j]) + (folded ? KC[q] * Xm * Xm : 0.0);
-      delta[q] = ex - sp;
-      gm[q] = ex;
+      const FF sp = A[q] + ff_mulf(Bc[q] + ff_mulf(Cc[q] + ff_mulf(Dc[q], 0.5f), 0.5f), 0.5f);
+      FF ex = ym[(size_t)q * M.J + j];
+      if (folded) ex = ex + KC[q] * Xm2;
+      delta[q] = (ex - sp).hi;
+      gm[q] = (Xm.hi > 0.0f && !folded) ? (ex + KC[q] * Xm2).hi : ex.hi;
     }
-    if (Xm > 0.0 && !folded) {
-#pragma unroll
-      for (int q = 0; q < 6; ++q) gm[q] += KC[q] * Xm * Xm;
-    }
-    double Sm[21];
+    FF Sm[21];
     // [k1, ks) without the kink term, [ks, k2) with it (folded intervals hold it already)
     const int64_t ks = folded ? k2 : min(max(kpk, k1), k2);
     if (ks > k1) {
 #pragma unroll
       for (int x = 0; x < 21; ++x) Sm[x] = F(ks, x) - F(k1, x);
-      sum += hd_piece(A, Bc, Cc, Dc, Sm);
+      sum = sum + hd_piece(A, Bc, Cc, Dc, Sm);
     }
     if (ks < k2) {
-      const double X0 = Msec * M.node_f[j] - fpk;
-      double A2[6], B2[6], C2[6];
+      // C (X0 + K u)^2 = C X0^2 + 2 C X0 K u + C K^2 u^2
+      const FF X02 = X0 * X0, X0K2 = ff_mulf(X0 * K, 2.0f), K2 = K * K;
+      FF A2[6], B2[6], C2[6];
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
-        A2[q] = A[q] + KC[q] * X0 * X0;
-        B2[q] = Bc[q] + 2.0 * KC[q] * X0 * Msec;
-        C2[q] = Cc[q] + KC[q] * Msec * Msec;
+        A2[q] = A[q] + KC[q] * X02;
+        B2[q] = Bc[q] + KC[q] * X0K2;
+        C2[q] = Cc[q] + KC[q] * K2;
       }
 #pragma unroll
       for (int x = 0; x < 21; ++x) Sm[x] = F(k2, x) - F(ks, x);
-      sum += hd_piece(A2, B2, C2, Dc, Sm);
+      sum = sum + hd_piece(A2, B2, C2, Dc, Sm);
     }
     // first-order change of sum |h|^2 w over the interval if the splines' error
-    // had the shape 16 t^2 (h - t)^2 / h^4 times its midpoint value
+    // had the shape 16 u^2 (1 - u)^2 times its midpoint value
     if (!M.wspike[(size_t)d * M.J + j]) {
-      const double ih2 = 1.0 / (h * h);
-      double e = 0.0;
+      float e = 0.0f;
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
-        const double m2 = F(k2, ch * 7 + 2) - F(k1, ch * 7 + 2), m3 = F(k2, ch * 7 + 3) - F(k1, ch * 7 + 3),
-                     m4 = F(k2, ch * 7 + 4) - F(k1, ch * 7 + 4);
-        const double bump = 16.0 * ih2 * (m2 - 2.0 * m3 / h + m4 * ih2);
-        e += 2.0 * (gm[2 * ch] * delta[2 * ch] + gm[2 * ch + 1] * delta[2 * ch + 1]) * bump;
+        const float m2 = (F(k2, ch * 7 + 2) - F(k1, ch * 7 + 2)).hi, m3 = (F(k2, ch * 7 + 3) - F(k1, ch * 7 + 3)).hi,
+                    m4 = (F(k2, ch * 7 + 4) - F(k1, ch * 7 + 4)).hi;
+        const float bump = 16.0f * (m2 - 2.0f * m3 + m4);
+        e += 2.0f * (gm[2 * ch] * delta[2 * ch] + gm[2 * ch + 1] * delta[2 * ch + 1]) * bump;
       }
       eh += e;
-      eha += fabs(e);
+      eha += fabsf(e);
     }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    sum = sum + ff_make(__shfl_xor_sync(0xffffffffu, sum.hi, o), __shfl_xor_sync(0xffffffffu, sum.lo, o));
     eh += __shfl_xor_sync(0xffffffffu, eh, o);
     eha += __shfl_xor_sync(0xffffffffu, eha, o);
   }
   if ((lane & 31) == 0) {
-    red[lane >> 5][0] = sum;
+    red[lane >> 5][0] = ff_to(sum);
     red[lane >> 5][1] = 0.0;
-    red[lane >> 5][2] = eh;
-    red[lane >> 5][3] = eha;
+    red[lane >> 5][2] = (double)eh;
+    red[lane >> 5][3] = (double)eha;
   }
   __syncthreads();
   if (lane == 0) {
@@ -3254,8 +3266,9 @@ __global__ void k_mixed_ingest(PlanDev P, MixedDev M, int det, const double2* __
 
 // Within-interval weight moments of detector det (set-up): one thread per
 // (interval, channel) runs over the interval's bins in order, writing the
-// exclusive prefix sums of t^p W_c (p = 0..6) at every bin and the interval's
-// totals; W_c = w_c |P|^2 / scale^2 in FP64, t = f_k - f_j.
+// exclusive prefix sums of u^p W_c (p = 0..6) at every bin and the interval's
+// totals; W_c = w_c |P|^2 / scale^2, u = (f_k - f_j) / h_j; summed in FP64,
+// stored as float-float.
 // per interval of one detector: does the weight sum_c w_c |P|^2 spike (its
 // largest bin above kSpikeRatio times the interval's mean)?
 __global__ void k_wspike(PlanDev P, MixedDev M, int det, int32_t* __restrict__ out) {
@@ -3279,7 +3292,7 @@ __global__ void k_wspike(PlanDev P, MixedDev M, int det, int32_t* __restrict__ o
   out[(size_t)det * M.J + j] = flag;
 }
 
-__global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ wmom, double* __restrict__ wtot) {
+__global__ void k_wmoments(PlanDev P, MixedDev M, int det, FF* __restrict__ wmom, FF* __restrict__ wtot) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (M.J - 1) * 3) return;
   const int j = t / 3, c = t % 3;
@@ -3289,23 +3302,24 @@ __global__ void k_wmoments(PlanDev P, MixedDev M, int det, double* __restrict__ 
   double acc[7];
 #pragma unroll
   for (int p = 0; p < 7; ++p) acc[p] = 0.0;
-  double* pm = wmom + (size_t)det * P.nbins * kMomStride + c * 7;
+  FF* pm = wmom + (size_t)det * P.nbins * kMomStride + c * 7;
+  const double ih = 1.0 / M.gh[j];
   for (int64_t k = k1; k < k2; ++k) {
-    const double tk = (double)(P.k0 + k) * P.f_step - fj;
+    const double tk = ((double)(P.k0 + k) * P.f_step - fj) * ih;
     const TdiFactor tf = P.tdi[(size_t)det * P.nbins + k];
     const size_t off = ((size_t)det * 3 + c) * P.nbins + k;
     const double w = in_zero_window(M, det, k) ? 0.0 : P.w[off];
     double tp = w * (tf.pre * tf.pre + tf.pim * tf.pim) * is2;
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
-      pm[(size_t)k * kMomStride + p] = acc[p];
+      pm[(size_t)k * kMomStride + p] = ff_from(acc[p]);
       acc[p] += tp;
       tp *= tk;
     }
   }
-  double* tot = wtot + ((size_t)det * M.J + j) * kMomStride + c * 7;
+  FF* tot = wtot + ((size_t)det * M.J + j) * kMomStride + c * 7;
 #pragma unroll
-  for (int p = 0; p < 7; ++p) tot[p] = acc[p];
+  for (int p = 0; p < 7; ++p) tot[p] = ff_from(acc[p]);
 }
 
 // ------------------------------------------------------------------ host side
@@ -3458,7 +3472,8 @@ int mixed_create(PesPlan* p) {
   float2* node_ff;
   int32_t *chb, *chl, *chi, *nsp, *nch, *xbin, *xbind, *ivfirst, *vcut, *wspk;
   double *xpart, *xgpart;
-  double *wmom, *wtot, *dsuf, *wrow, *hdv, *rpart, *fpart;
+  FF *wmom, *wtot;
+  double *dsuf, *wrow, *hdv, *rpart, *fpart;
   int32_t* rkind;
   float4* xff;
   float* cgb;
@@ -3707,8 +3722,8 @@ int mixed_create(PesPlan* p) {
   }
   M.mid_ff = mid_ff;
   M.tdm_ff = tdm_ff;
-  PES_CHECK_CUDA(cudaMemset(wmom, 0, sizeof(double) * wn));
-  PES_CHECK_CUDA(cudaMemset(wtot, 0, sizeof(double) * wj));
+  PES_CHECK_CUDA(cudaMemset(wmom, 0, sizeof(FF) * wn));
+  PES_CHECK_CUDA(cudaMemset(wtot, 0, sizeof(FF) * wj));
   PES_CHECK_CUDA(cudaMemset(dsuf, 0, sizeof(double) * nd * (n + 1)));
   // the dense-path partial buffer is not needed; gradient set-up blocks are shared
   return PES_OK;
@@ -3756,8 +3771,8 @@ int mixed_ingest(PesPlan* p, int det, const double* data, const double* psd, cud
   PES_CHECK_LAUNCH();
   suffix_sum(p->desc.nbins, M.wrow, const_cast<double*>(M.dsuf) + (size_t)det * (p->desc.nbins + 1), st);
   PES_CHECK_LAUNCH();
-  k_wmoments<<<ceil_div((M.J - 1) * 3, 128), 128, 0, st>>>(p->dev, M, det, const_cast<double*>(M.wmom),
-                                                            const_cast<double*>(M.wtot));
+  k_wmoments<<<ceil_div((M.J - 1) * 3, 128), 128, 0, st>>>(p->dev, M, det, const_cast<FF*>(M.wmom),
+                                                            const_cast<FF*>(M.wtot));
   PES_CHECK_LAUNCH();
   k_wspike<<<ceil_div(M.J, 128), 128, 0, st>>>(p->dev, M, det, const_cast<int32_t*>(M.wspike));
   PES_CHECK_LAUNCH();
