@@ -18,9 +18,11 @@ and detector, counted from the kernel source (FMA = 2 flops, add/mul = 1):
     24, model rotation 6, residual 2, |d - h|^2 w 5, |h|^2 w, the
     cross term and Re(d* h) w 14                            51 x 3 = 153
   weak-template branch 8, compensated sums (direct 4, cross 5)      17
-                                                       lnL pass:    319
+  rounding estimate sum |d|^2 |h|^2 w^2 (7 x 3 + 1), which chooses
+    the samples re-evaluated after the dense stage                   22
+                                                       lnL pass:    341
   gradient pass: per-channel adjoints 13 x 3 = 39, interval moments
-    (7 quantities x t^0..t^3) 58                              +97 = 416
+    (7 quantities x t^0..t^3) 58                              +97 = 438
 
 The per-bin kink moments of post-peak bins are not counted (a lower bound).
 The FP64 run anchors (about 30 FP64 operations per run of <= 32 bins) are
@@ -33,7 +35,7 @@ k_dense_mixed<1> launch divided by its 19 603 667 dense bins); scaled here by
 the launch's dense bins.
 """
 
-FP32_FLOPS_PER_DENSE_BIN = {"lnl": 319, "grad": 416}
+FP32_FLOPS_PER_DENSE_BIN = {"lnl": 341, "grad": 438}
 DRAM_BYTES_PER_DENSE_BIN = 5.61  # (102.88 MB + 7.06 MB) / 19 603 667 bins, ncu --set full, 256 samples
 
 
