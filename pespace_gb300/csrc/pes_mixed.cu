@@ -2537,6 +2537,9 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : (kNM > 1 ? 3 : 1
             pk1 = pkd[P.nbins + i];
             pk2 = pkd[2 * P.nbins + i];
           }
+          // the FP64 data norm of the weak-template form, loaded with the bin's
+          // rows so that its latency overlaps theirs (2% on the gradient pass)
+          const float2 Dn = M.dd[(size_t)d * P.nbins + i];
           const float t = pk2.w;
           const float u = (float)lane;
           const float u2 = u * u, u3 = u2 * u;
@@ -2692,11 +2695,10 @@ __global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : (kNM > 1 ? 3 : 1
           // the FP64 data (float-float): the FP32 rounding then scales with
           // |h| instead of |d|, which matters when the data hold a loud signal.
           if (hh < term) {
-            const float2 D = M.dd[(size_t)d * P.nbins + i];
             float t1, e1;
-            two_sum(dsh, D.x, t1, e1);
+            two_sum(dsh, Dn.x, t1, e1);
             dsh = t1;
-            dsl += e1 + D.y;
+            dsl += e1 + Dn.y;
             term = cross;
           }
           // compensated accumulation
