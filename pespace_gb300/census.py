@@ -36,7 +36,7 @@ the launch's dense bins.
 """
 
 FP32_FLOPS_PER_DENSE_BIN = {"lnl": 341, "grad": 438}
-DRAM_BYTES_PER_DENSE_BIN = 5.61  # (102.88 MB + 7.06 MB) / 19 603 667 bins, ncu --set full, 256 samples
+DRAM_BYTES_PER_DENSE_BIN = 5.69  # (103.32 MB + 8.18 MB) / 19 603 667 bins, ncu, 256 samples
 
 
 def roofline(kernel_class, launches_ms, steps, work, grad, fp32_peak_tflops):
