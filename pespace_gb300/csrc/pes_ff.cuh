@@ -21,8 +21,10 @@
 // the atanh series of (m - 1)/(m + 1) after extracting the binary exponent;
 // sin and cos by reduction modulo pi/2 (pi/2 split in three floats) and
 // Taylor polynomials on |r| <= pi/4 whose leading terms are in FF and whose
-// tail is in FP32; sin(x)/x by its Taylor series for |x| <= 2.  exp and atan
-// (used only past the merger joins) go through FP64.
+// tail is in FP32; sin(x)/x by its Taylor series for |x| <= 2; exp by
+// reduction modulo ln 2 and atan by reduction to |x| <= tan(pi/16), each
+// with a Taylor polynomial (the FP64 forms had each IMRPhenomHM mode's
+// node above its amplitude corner on the FP64 pipe).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -180,8 +182,67 @@ PES_HD FF dlog(const FF& x) {
   return ff_mulf(ff_from(0.69314718055994530942), (float)k) + lnm;
 }
 
-PES_HD FF dexp(const FF& x) { return ff_from(::exp(ff_to(x))); }
-PES_HD FF datan(const FF& x) { return ff_from(::atan(ff_to(x))); }
+// exp(x) = 2^k exp(r), x = k ln 2 + r with ln 2 in three parts (k * A exact
+// for |k| < 2^12) and |r| <= ln 2 / 2; exp(r) = exp(r/4)^4, exp(r/4) from its
+// Taylor series (FF Horner down to the r^4 term, the terms from r^5/5! in
+// FP32: below 4e-8 relative, truncation after r^9/9! below 1e-17).  Results
+// below the FP32 normal range lose precision (lo underflows first), as any
+// FF value does there.
+constexpr float kLn2A = 0.693115234375f;  // 2839 / 4096
+constexpr float kLn2B = 3.194618329871446e-05f;
+constexpr float kLn2C = 1.6465949697480609e-12f;
+PES_HD_OUTLINE FF dexp(const FF& x) {
+  if (!(x.hi < 88.0f)) return ff_make(x.hi != x.hi ? x.hi : INFINITY, 0.0f);
+  if (x.hi < -104.0f) return ff_make(0.0f, 0.0f);
+  const float kf = rintf(x.hi * 1.4426950408889634f);
+  FF r = ff_addf(x, -kf * kLn2A);  // exact product, FF sum
+  r = r - ff_two_prod(kf, kLn2B);
+  r = ff_addf(r, -kf * kLn2C);
+  const FF q = ff_mulf(r, 0.25f);  // exact
+  const float qf = q.hi;
+  float t = fmaf(qf, 1.0f / 362880.0f, 1.0f / 40320.0f);
+  t = fmaf(t, qf, 1.0f / 5040.0f);
+  t = fmaf(t, qf, 1.0f / 720.0f);
+  t = fmaf(t, qf, 1.0f / 120.0f);
+  FF p = ff_addf(ff_from(1.0 / 24.0), t * qf);
+  p = p * q + ff_from(1.0 / 6.0);
+  p = p * q + ff_from(0.5);
+  p = ff_addf(p * q, 1.0f);
+  p = ff_addf(p * q, 1.0f);
+  p = p * p;
+  p = p * p;
+  const int k = (int)kf;
+  return ff_make(ldexpf(p.hi, k), ldexpf(p.lo, k));
+}
+
+// atan(x): odd; for |x| > 1, pi/2 - atan(1/|x|); two halvings
+// atan(a) = 2 atan(a / (1 + sqrt(1 + a^2))) bring |a| below tan(pi/16) =
+// 0.199, where atan(a) / a = sum (-1)^n a^2n / (2n + 1) (FF Horner down to
+// the a^6 term, the terms from a^8/9 in FP32: below 3e-7 relative,
+// truncation after a^18/19 below 5e-16).
+PES_HD_OUTLINE FF datan(const FF& x) {
+  if (x.hi != x.hi) return x;
+  const bool neg = x.hi < 0.0f;
+  FF a = neg ? -x : x;
+  const bool inv = a.hi > 1.0f;
+  if (inv) a = ff_make(1.0f, 0.0f) / a;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) a = a / ff_addf(dsqrt(ff_addf(a * a, 1.0f)), 1.0f);
+  const FF z = a * a;
+  const float zf = z.hi;
+  float t = fmaf(-zf, 1.0f / 19.0f, 1.0f / 17.0f);
+  t = fmaf(-zf, t, 1.0f / 15.0f);
+  t = fmaf(-zf, t, 1.0f / 13.0f);
+  t = fmaf(-zf, t, 1.0f / 11.0f);
+  t = fmaf(-zf, t, 1.0f / 9.0f);
+  FF p = ff_addf(ff_from(-1.0 / 7.0), t * zf);
+  p = p * z + ff_from(1.0 / 5.0);
+  p = p * z + ff_from(-1.0 / 3.0);
+  p = ff_addf(p * z, 1.0f);
+  FF s = ff_mulf(a * p, 4.0f);  // exact scaling
+  if (inv) s = ff_from(1.5707963267948966) - s;
+  return neg ? -s : s;
+}
 
 // sin and cos of r, |r| <= pi/4 (FF Horner for the terms down to r^9/9! and
 // r^8/8!, FP32 for the rest: truncation and tail rounding below 1e-15).

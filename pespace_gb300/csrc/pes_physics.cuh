@@ -768,7 +768,17 @@ struct HMMode {
   T fiP, frP, aP, bP;           // phase map
   T cI0, cI1, cR0, cR1;         // C1 constants of the phase
   T fRD;                        // the mode's ringdown frequency (Mf)
+  // the mode's constants in the evaluation's scalar type (no FP64 division or
+  // conversion per node when that type is float-float): 2/m, m/2, 2 pi/m and
+  // the phase's quarter turns
+  T tm, hm, tpm, qt;
 };
+
+// a <= b and a >= b on the values (float-float compares without leaving the FP32 pipes)
+template <class T> PES_HD bool val_le(const T& a, const T& b) { return val(a) <= val(b); }
+template <class T> PES_HD bool val_ge(const T& a, const T& b) { return val(a) >= val(b); }
+PES_HD bool val_le(const FF& a, const FF& b) { return a <= b; }
+PES_HD bool val_ge(const FF& a, const FF& b) { return a >= b; }
 
 template <class T>
 struct PhenomHMCoef {
@@ -843,9 +853,9 @@ PES_HD void hm_psi_mrd(const PhenomDCoef<T>& c, const T& fdm, const T& Mf, T& ps
 template <class T>
 PES_HD void hm_phase(const PhenomDCoef<T>& c, const HMMode<T>& md, int m, const T& Mf, T& psi, T& dpsi) {
   if (Mf < md.fiP) {
-    const T f22 = (2.0 / m) * Mf;
+    const T f22 = md.tm * Mf;
     phenomd_phase<T>(c, f22, dcbrt(f22), psi, dpsi);
-    psi = (0.5 * m) * psi;
+    psi = md.hm * psi;
   } else if (Mf < md.frP) {
     const T f22 = md.aP * Mf + md.bP;
     phenomd_phase<T>(c, f22, dcbrt(f22), psi, dpsi);
@@ -873,11 +883,12 @@ PES_HD T hm_amphat(const PhenomDCoef<T>& c, const HMMode<T>& md, const T& Mf22, 
 // cubic Hermite blend of the two (values and slopes) between
 template <class T>
 PES_HD T hm_amp_map(const HMMode<T>& md, int m, const T& Mf) {
-  if (val(Mf) <= val(md.fiA)) return (2.0 / m) * Mf;
-  if (val(Mf) >= val(md.frA)) return md.Rholm * Mf;
+  (void)m;
+  if (val_le(Mf, md.fiA)) return md.tm * Mf;
+  if (val_ge(Mf, md.frA)) return md.Rholm * Mf;
   const T h = md.frA - md.fiA, s = (Mf - md.fiA) / h;
   const T s2 = s * s, s3 = s2 * s;
-  return (2.0 * s3 - 3.0 * s2 + 1.0) * ((2.0 / m) * md.fiA) + (s3 - 2.0 * s2 + s) * (h * (2.0 / m)) +
+  return (2.0 * s3 - 3.0 * s2 + 1.0) * (md.tm * md.fiA) + (s3 - 2.0 * s2 + s) * (h * md.tm) +
          (3.0 * s2 - 2.0 * s3) * (md.Rholm * md.frA) + (s3 - s2) * (h * md.Rholm);
 }
 
@@ -893,13 +904,13 @@ PES_HD void phenomhm_eval(const PhenomDCoef<T>& c, const PhenomHMCoef<T>& h, int
   const T u = dcbrt(f22);
   T beta = lift<T>(1.0);
   if (k != 0) {
-    const T fb = (val(Mf) <= val(md.fiA)) ? Mf : md.fiA * (2.0 - dexp(1.0 - Mf / md.fiA));
-    beta = hm_pn_ratio<T>(k, dcbrt((2.0 * kPi / m) * fb), h);
+    const T fb = val_le(Mf, md.fiA) ? Mf : md.fiA * (2.0 - dexp(1.0 - Mf / md.fiA));
+    beta = hm_pn_ratio<T>(k, dcbrt(md.tpm * fb), h);
   }
   amp = beta * (c.amp_scale / (f22 * dsqrt(u)) * hm_amphat<T>(c, md, f22, u));
   T dpsi;
   hm_phase<T>(c, md, m, Mf, psi, dpsi);
-  psi = psi + kHMlm[k][2] * (0.5 * kPi);
+  psi = psi + md.qt;
   tf = c.tscale * dpsi;
 }
 
@@ -955,6 +966,10 @@ PES_HD void phenomhm_setup(const T* th, const PhenomDCoef<T>& c, PhenomHMCoef<T>
   for (int k = 0; k < kHMModes; ++k) {
     HMMode<T>& md = h.md[k];
     const int l = kHMlm[k][0], m = kHMlm[k][1];
+    md.tm = lift<T>(2.0 / m);
+    md.hm = lift<T>(0.5 * m);
+    md.tpm = lift<T>(2.0 * kPi / m);
+    md.qt = lift<T>(kHMlm[k][2] * (0.5 * kPi));
     const T Yp = hm_sylm<T>(l, m, th[5]), Ym = hm_sylm<T>(l, -m, th[5]);
     const double sg = (l & 1) ? -1.0 : 1.0;
     md.P = (sg * Ym + Yp) * (1.0 / (2.0 * nrm));

@@ -15,7 +15,7 @@ int main() {
   std::mt19937_64 rng(2026);
   std::uniform_real_distribution<double> U(0.0, 1.0);
   double e_add = 0, e_mul = 0, e_div = 0, e_sqrt = 0, e_cbrt = 0, e_log = 0, e_sin = 0, e_cos = 0, e_sinc = 0,
-         e_wrap = 0, e_wrapw = 0;
+         e_wrap = 0, e_wrapw = 0, e_exp = 0, e_atan = 0;
   const long double two_pi = 6.283185307179586476925286766559L;
   for (int it = 0; it < 400000; ++it) {
     const double a = std::pow(10.0, -6.0 + 12.0 * U(rng)), b = std::pow(10.0, -6.0 + 12.0 * U(rng));
@@ -39,9 +39,13 @@ int main() {
     const long double dw = ld(ff_wrap_2pi(w)) - ld(w), dww = ld(ff_wrap_2pi_wide(ww)) - ld(ww);
     e_wrap = std::fmax(e_wrap, (double)fabsl(dw - roundl(dw / two_pi) * two_pi));
     e_wrapw = std::fmax(e_wrapw, (double)fabsl(dww - roundl(dww / two_pi) * two_pi));
+    const FF ex = ff_from(-60.0 + 80.0 * U(rng));
+    e_exp = std::fmax(e_exp, (double)(fabsl(ld(dexp(ex)) - expl(ld(ex))) / expl(ld(ex))));
+    const FF at = ff_from((U(rng) < 0.5 ? -1.0 : 1.0) * std::pow(10.0, -5.0 + 10.0 * U(rng)));
+    e_atan = std::fmax(e_atan, (double)fabsl(ld(datan(at)) - atanl(ld(at))));
   }
   std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncbrt %.3e\nlog %.3e\nsin %.3e\ncos %.3e\nsinc %.3e\n"
-              "wrap %.3e\nwrap_wide %.3e\n",
-              e_add, e_mul, e_div, e_sqrt, e_cbrt, e_log, e_sin, e_cos, e_sinc, e_wrap, e_wrapw);
+              "wrap %.3e\nwrap_wide %.3e\nexp %.3e\natan %.3e\n",
+              e_add, e_mul, e_div, e_sqrt, e_cbrt, e_log, e_sin, e_cos, e_sinc, e_wrap, e_wrapw, e_exp, e_atan);
   return 0;
 }

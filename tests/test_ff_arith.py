@@ -1,8 +1,8 @@
 """Float-float arithmetic of the node evaluations (``csrc/pes_ff.cuh``),
 compiled for the host and checked against long double: relative errors of
-+, *, /, sqrt, cbrt near 2^-46, absolute errors of log, sin, cos, sin(x)/x
-and the 2 pi wraps (moduli) near 1e-14 .. 1e-13.  The device build runs the
-same source (with a fast reciprocal estimate refined by the same Newton
++, *, /, sqrt, cbrt and exp near 2^-46, absolute errors of log, sin, cos,
+atan, sin(x)/x and the 2 pi wraps (moduli) near 1e-14 .. 1e-13.  The device
+build runs the same source (with a fast reciprocal estimate refined by the same Newton
 step); its end-to-end effect is covered by the mixed-plan parity tests."""
 
 import os
@@ -13,7 +13,7 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BOUNDS = {"add": 2e-14, "mul": 3e-14, "div": 6e-14, "sqrt": 3e-14, "cbrt": 6e-14, "log": 3e-14, "sin": 3e-14,
-          "cos": 3e-14, "sinc": 3e-14, "wrap": 1e-12, "wrap_wide": 1e-11}
+          "cos": 3e-14, "sinc": 3e-14, "wrap": 1e-12, "wrap_wide": 1e-11, "exp": 6e-14, "atan": 6e-14}
 
 
 @pytest.fixture(scope="module")
