@@ -93,13 +93,15 @@ class WhittleLikelihood:
         orthogonal A/E/T combination).  Their ``tdi_data`` must hold
         ``fd_data`` and ``fd_noise_power_density``.
     channels : subset of ("A", "E", "T").
-    precision : "fp64" (dense FP64, every bin) or "mixed" (FP64 sparse grid,
-        FP32 dense bulk).
+    precision : "fp64" (dense FP64, every bin) or "mixed" (float-float sparse
+        grid, FP32 dense bulk, the samples near the accuracy target
+        re-evaluated).
     cut_factor : per-sample model cutoff in units of the ringdown frequency
         (the largest of the modes' for IMRPhenomHM; 0 keeps the model's own
         Mf = 0.2 cut only).
     approximant : "IMRPhenomD" (the (2,2) mode) or "IMRPhenomHM" (modes
-        (2,2), (2,1), (3,3), (3,2), (4,4), (4,3); FP64 plans).
+        (2,2), (2,1), (3,3), (3,2), (4,4), (4,3); lnL, gradient and Fisher
+        matrices from FP64 plans, lnL and Fisher matrices from mixed plans).
     """
 
     APPROXIMANTS = {"IMRPhenomD": _lib.APPROX_PHENOMD, "IMRPhenomHM": _lib.APPROX_PHENOMHM}
