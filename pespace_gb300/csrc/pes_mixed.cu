@@ -1797,9 +1797,11 @@ __global__ void k_refine_select(PlanDev P, MixedDev M, const SampleBlock<double>
 // k_refine_select sends to the exact re-evaluation of their dense range
 // (without the T-channel zero windows); 4: lnL partials of the window bins
 // in [xbind[s][d], kcut) (their gradient: k_zero_grad).
-// grid (xblocks, rblocks or zblocks, B); threads stride over the bins.
+// grid (xblocks, rblocks or zblocks, B); threads stride over the bins.  The
+// value passes are held to 168 registers (3 blocks per SM instead of 2: the
+// bench step 1.5% faster).
 template <int kMode, class T>
-__global__ void __launch_bounds__(kExactThreads) k_exact(PlanDev P, MixedDev M, GenArg G,
+__global__ void __launch_bounds__(kExactThreads, kMode == 1 ? 1 : 3) k_exact(PlanDev P, MixedDev M, GenArg G,
                                                          const SampleBlock<T>* __restrict__ blocks,
                                                          double2* __restrict__ model) {
   constexpr bool kGradPass = kMode == 1;
@@ -2391,11 +2393,12 @@ __global__ void k_bump(MixedDev M, const SampleBlock<double>* __restrict__ block
 // inputs the gradient pass is faster on plain loads).
 // kNM: modes summed per bin before the residual (1, or kHMModes for
 // IMRPhenomHM plans: lnL and model passes, plain loads).
-// The gradient pass is held to 96 registers (5 blocks per SM instead of 4:
-// 2% faster on the bench workload, at a few spilled words); the six-mode
-// pass to 168 (3 blocks per SM instead of 2).
+// Every pass is held to 96 registers (5 blocks per SM, at a few spilled
+// words): the gradient pass 2% faster than at 4 blocks, the staged lnL pass
+// 6.5% (bench batch) and 17% (network, inputs from DRAM) faster than at 128
+// registers, the six-mode pass 15% faster than at 4 blocks and 2 blocks.
 template <int kMode, bool kStage, int kNM>
-__global__ void __launch_bounds__(kMixThreads, kMode == 1 ? 5 : (kNM > 1 ? 3 : 1)) k_dense_mixed(PlanDev P, MixedDev M,
+__global__ void __launch_bounds__(kMixThreads, 5) k_dense_mixed(PlanDev P, MixedDev M,
                                                              const SampleBlock<double>* __restrict__ blocks,
                                                              double2* __restrict__ model) {
   constexpr bool kGrad = kMode == 1;
