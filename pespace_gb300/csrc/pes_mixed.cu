@@ -1771,6 +1771,14 @@ __global__ void __launch_bounds__(kFitWarps * 32) k_spline_adjoint_staged(MixedD
 constexpr double kRefineTarget = 4e-3;
 constexpr double kCrossRel = 4e-7;
 constexpr double kSplineRel = 0.01;
+// Six-mode plans: the summed modes of heavy templates (dense range within the
+// lowest eighth of the grid) carry a coherent model error of up to about
+// 2e-9 of sum |h|^2 w in their merger-ringdown band, which the midpoint
+// estimate does not see (measured on the three-detector network).  Those
+// whose power puts that above the 1e-2 bar are re-evaluated exactly: few
+// samples, and few bins each.
+constexpr double kModelRelHM = 2e-9;
+constexpr double kBar = 1e-2;
 
 // one thread per sample, after the dense stage (its rounding sums) and k_hd
 __global__ void k_refine_select(PlanDev P, MixedDev M, const SampleBlock<double>* __restrict__ blocks, int64_t B) {
@@ -1778,14 +1786,20 @@ __global__ void k_refine_select(PlanDev P, MixedDev M, const SampleBlock<double>
   if (s >= B) return;
   int kind = kRefineNone;
   if (blocks[s].status == kSampleOk) {
-    double sq = 0.0, eha = 0.0;
+    double sq = 0.0, eha = 0.0, hh = 0.0;
     for (int k = 0; k < M.nblk_dense; ++k) sq += M.part[((size_t)s * M.nblk_dense + k) * kPartW + 3];
     for (int k = 0; k < M.n_modes; ++k)
-      for (int d = 0; d < M.n_det; ++d) eha += M.hd[(((size_t)s * M.n_modes + k) * M.n_det + d) * kHdOut + 4];
+      for (int d = 0; d < M.n_det; ++d) {
+        const double* hv = M.hd + (((size_t)s * M.n_modes + k) * M.n_det + d) * kHdOut;
+        eha += hv[4];
+        hh += hv[0];
+      }
     const double er = 2.0 * P.df * kCrossRel * sqrt(fmax(sq, 0.0));
     const double es = 2.0 * P.df * kSplineRel * eha;
-    if (M.refine_all || er + es > kRefineTarget)
-      kind = es > kRefineTarget ? kRefineExact : kRefineFF;
+    const bool heavy = M.n_modes > 1 && blocks[s].kcut * 8 <= P.nbins;
+    const bool loud = heavy && 2.0 * P.df * kModelRelHM * fabs(hh) > kBar;
+    if (M.refine_all || er + es > kRefineTarget || loud)
+      kind = (es > kRefineTarget || loud) ? kRefineExact : kRefineFF;
   }
   M.rkind[s] = kind;
 }
