@@ -158,9 +158,8 @@ struct MixedDev {
   double* hd;               // [B][n_det][kHdOut] per detector's dense range: sum |h|^2 w, sum |d|^2 w, 0,
                             //   and the splines' error estimate of sum |h|^2 w from the exact model at
                             //   the interval midpoints (signed, absolute), 0
-  // Samples whose FP32 or spline error could exceed the accuracy target are
-  // re-evaluated exactly over their dense range: the error estimates above
-  // use the exact transfer quantities at the interval midpoints.
+  // The splines' error estimate above (and the midpoint corrections) use the
+  // exact transfer quantities at the interval midpoints.
   const float2* mid_ff;     // [J] interval midpoints (hi, lo)
   const float4* tdm_ff;     // [n_det][J] TDI delay factor at the midpoints
   FF* ym;                   // [B][n_det][7][J] transfer quantities (rows 0-5, kink removed) and the
@@ -3978,13 +3977,10 @@ int mixed_lnl(PesPlan* p, const double* theta, int64_t B, double* lnl, double* g
   }
   PES_CHECK_LAUNCH();
   PES_CHECK_CUDA(cudaEventRecord(p->mixed->ev_hd, p->mixed->aux));
-  // The exact re-evaluation of the samples that the error estimates select,
-  // on the side stream after its exact low-frequency bins: beside the dense
-  // stage for lnL calls, beside the adjoint stages (after the dense stage)
-  // for lnL+gradient calls, where it does not take SMs from the dense stage.
   // After the dense stage (its rounding sums) and k_hd: which samples to
-  // re-evaluate and how, then the re-evaluations, on the side stream (beside
-  // the adjoint stages of lnL+gradient calls).
+  // re-evaluate and how, then the re-evaluations, on the side stream after
+  // its exact low-frequency bins (beside the adjoint stages of lnL+gradient
+  // calls, where they do not take SMs from the dense stage).
   auto refine = [&]() -> int {
     PES_CHECK_CUDA(cudaStreamWaitEvent(side, p->mixed->ev_dense, 0));
     {
