@@ -627,11 +627,29 @@ def smc_sweep_leg(steps, warmup, n_half=8192, check=64):
     ref_h = WhittleLikelihood(det3, precision="fp64", approximant="IMRPhenomHM", reference_frequency=1e-4,
                               cut_factor=1.2, max_batch=len(idx_h))
     d_h = (out["lnl_h"][idx_h] - ref_h.log_likelihood_batch(th_h[idx_h])).abs()
+    # what the IMRPhenomHM half's gradient and Fisher matrices cost from the
+    # FP64 plan (the only plan that gives the six-mode gradient), on a few
+    # particles: the reason they are not in the timed sweep
+    few = th_h[idx_h[:4]]
+    ref_h.log_likelihood_and_grad(few[:1])
+    ref_h.fisher_matrix(few[:1])
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    ref_h.log_likelihood_and_grad(few)
+    ev[1].record()
+    ref_h.fisher_matrix(few)
+    ev[2].record()
+    ev[2].synchronize()
+    g_ms, f_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    hm_fp64 = {"particles": len(few), "lnl_grad_ms": g_ms, "fisher_ms": f_ms,
+               "sweep_half_s_at_this_rate": n_half * (g_ms + f_ms) / len(few) / 1e3}
     return {"metric": SMC_METRIC, "value": 2 * n_half / (mean_ms / 1e3), "unit": "particles/s", "steps": steps,
             "warmup": max(1, warmup), "ms_per_step": mean_ms, "dtype": "f32+f64",
             "config": {"workload": WORKLOADS["smc-sweep"][5], "particles": 2 * n_half},
             "ms_per_part": {k: float(np.mean(v)) for k, v in parts.items()},
             "not_timed": "IMRPhenomHM gradient and Fisher: FP64 plan only (no mixed multi-mode adjoint)",
+            "phenomhm_grad_fisher_fp64": hm_fp64,
             "accuracy": {"phenomd_samples": len(idx), "phenomd_max_abs_dlnl": float(d_lnl.max().item()),
                          "phenomd_n_within_1e-2": int((d_lnl <= 1e-2).sum().item()),
                          "phenomd_fisher_max_rel": float(f_err.item()),
